@@ -1,0 +1,188 @@
+"""Generate the golden fixtures in this folder from the reference itself.
+
+Builds oracle/_ref/ref_driver -- the reference's own AProductCore.cpp,
+DDAModel.cpp, tools.cpp, ... compiled unchanged from /root/reference with the
+CPU stand-ins for cuFFT and the CUDA runtime in oracle/ref_shim -- and runs it
+on seeded inputs.  Each fixture stores its inputs and the reference's outputs:
+
+  ldr.npz          LDR_inter (AProductCore.cpp:588-623) at a set of offsets
+  aprod_*.npz      Aproduct / Aproductwithalb (AProductCore.cpp:697-758,
+                   DDAModel.cpp:577-586) of seeded vectors
+  solve_*.npz      bicgstab + update_E_in_structure (DDAModel.cpp:131-260,
+                   567-575): ITERATION, the printed Error, P, Einternal
+
+Run from the repository root:  python tests/golden/make_golden.py
+It needs /root/reference, so it runs in the development container only; the
+fixtures it writes are committed and travel with the tests.
+"""
+from __future__ import annotations
+
+import math
+import os
+import re
+import struct
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "topo-dda-forwin64_gb300"))
+from tdda import lattice  # noqa: E402
+
+DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+
+
+def build_driver():
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+
+
+def write_input(path, mode, Nx, Ny, Nz, R, d, lam, nback, material, nK, E0, nE0, max_it, max_err,
+                diel_old, vecs):
+    R = np.ascontiguousarray(R, np.int32).reshape(-1)
+    N = R.size // 3
+    material = np.asarray(material, np.complex128)
+    with open(path, "wb") as f:
+        f.write(struct.pack("<5i", mode, Nx, Ny, Nz, N))
+        f.write(struct.pack("<3d", d, lam, nback))
+        f.write(struct.pack("<i", material.size))
+        f.write(material.astype("<c16").tobytes())
+        f.write(np.asarray(nK, "<f8").tobytes())
+        f.write(struct.pack("<d", E0))
+        f.write(np.asarray(nE0, "<f8").tobytes())
+        f.write(struct.pack("<id", max_it, max_err))
+        f.write(R.astype("<i4").tobytes())
+        f.write(np.asarray(diel_old, "<f8").tobytes())
+        f.write(struct.pack("<i", len(vecs)))
+        for v in vecs:
+            f.write(np.asarray(v).astype("<c16" if mode != 2 else "<f8").tobytes())
+
+
+def run(mode, **kw):
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+        write_input(fin, mode, **kw)
+        pr = subprocess.run([DRIVER, fin, fout], capture_output=True, text=True, check=True)
+        with open(fout, "rb") as f:
+            raw = f.read()
+    return raw, pr.stdout
+
+
+def case_kw(w: lattice.Workload, inc=None, max_it=10000, max_err=1e-5):
+    inc = inc or w.incidences[0]
+    return dict(Nx=w.Nx, Ny=w.Ny, Nz=w.Nz, R=w.R, d=w.d, lam=w.lam, nback=w.nback,
+                material=w.material, nK=inc.nK, E0=inc.E0, nE0=inc.nE0, max_it=max_it,
+                max_err=max_err, diel_old=w.diel_old)
+
+
+def inputs_dict(w: lattice.Workload, inc=None):
+    inc = inc or w.incidences[0]
+    return dict(box=np.array([w.Nx, w.Ny, w.Nz], np.int32), R=w.R, d=w.d, lam=w.lam, nback=w.nback,
+                material=w.material, nK=inc.nK, E0=inc.E0, nE0=inc.nE0, diel_old=w.diel_old)
+
+
+def small_workload(name, Nx, Ny, Nz, seed, em=4.0 + 0.1j, d=10.0, lam=500.0, keep=1.0,
+                   shuffle=False):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    R = lattice.bulk(Nx, Ny, Nz).reshape(-1, 3)
+    if keep < 1.0:
+        R = R[rng.random(R.shape[0]) < keep]
+    if shuffle:
+        R = R[rng.permutation(R.shape[0])]
+    rho = rng.random(R.shape[0])
+    return lattice.Workload(name=name, Nx=Nx, Ny=Ny, Nz=Nz, d=d, lam=lam,
+                            material=np.array([1.0 + 0j, em]), rho=rho,
+                            R=np.ascontiguousarray(R.ravel(), np.int32),
+                            incidences=[lattice.XPOL_Z])
+
+
+def rand_vec(n, seed):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex128)
+
+
+def gen_ldr():
+    pts = np.array([[10, 0, 0], [0, 0, 0], [0, 10, 0], [0, 0, 10], [10, 20, -30], [-50, 30, 70],
+                    [3.5, -7.25, 11.0], [190, -190, 90], [-10, -10, -10], [400, 0, 0]], np.float64)
+    w = small_workload("ldr", 2, 2, 2, 7)
+    raw, _ = run(2, **case_kw(w), vecs=list(pts))
+    K = struct.unpack_from("<d", raw, 0)[0]
+    vals = np.frombuffer(raw, "<c16", offset=8).reshape(-1, 6)
+    np.savez(os.path.join(HERE, "ldr.npz"), lam=w.lam, K=K, points=pts, tensors=vals)
+    print("ldr: K=%.12g xx(10,0,0)=%s" % (K, vals[0, 0]))
+
+
+def gen_aprod(name, w: lattice.Workload, nvec, seed):
+    N = w.N
+    vecs = [rand_vec(3 * N, seed + v) for v in range(nvec)]
+    raw, _ = run(0, **case_kw(w), vecs=vecs)
+    off = 0
+    Rout = np.frombuffer(raw, "<i4", count=3 * N, offset=off)
+    off += 12 * N
+    al = np.frombuffer(raw, "<c16", count=3 * N, offset=off)
+    off += 48 * N
+    ys, yws = [], []
+    for _ in range(nvec):
+        ys.append(np.frombuffer(raw, "<c16", count=3 * N, offset=off))
+        off += 48 * N
+        yws.append(np.frombuffer(raw, "<c16", count=3 * N, offset=off))
+        off += 48 * N
+    assert np.array_equal(Rout, w.R), "reference reordered the dipoles"
+    np.savez_compressed(os.path.join(HERE, f"aprod_{name}.npz"), **inputs_dict(w), al=al, b=np.array(vecs),
+             y=np.array(ys), y_alb=np.array(yws))
+    print(f"aprod_{name}: N={N} |y|={np.linalg.norm(ys[0]):.6g}")
+
+
+def gen_solve(name, w: lattice.Workload, inc=None, P0=None, Ein=None, max_it=10000, max_err=1e-5):
+    N = w.N
+    vecs = []
+    if P0 is not None:
+        vecs.append(P0)
+    if Ein is not None:
+        vecs.append(Ein)
+    raw, out = run(1, **case_kw(w, inc, max_it, max_err), vecs=vecs)
+    off = 12 * N
+    al = np.frombuffer(raw, "<c16", count=3 * N, offset=off)
+    off += 48 * N
+    it = struct.unpack_from("<i", raw, off)[0]
+    off += 4
+    P = np.frombuffer(raw, "<c16", count=3 * N, offset=off)
+    off += 48 * N
+    Ein_out = np.frombuffer(raw, "<c16", count=3 * N, offset=off)
+    m = re.findall(r"Error:\s*([-+0-9.eE]+)", out)
+    err = float(m[-1]) if m else float("nan")
+    extra = {}
+    if P0 is not None:
+        extra["P0"] = P0
+    if Ein is not None:
+        extra["E_rhs"] = Ein
+    np.savez_compressed(os.path.join(HERE, f"solve_{name}.npz"), **inputs_dict(w, inc), iterations=it,
+             error=err, P=P, Einternal=Ein_out, max_it=max_it, max_err=max_err, **extra)
+    print(f"solve_{name}: N={N} iterations={it} error={err:.6g} P[0]={P[0]}")
+
+
+def main():
+    build_driver()
+    gen_ldr()
+    gen_aprod("box6x5x4", small_workload("box6x5x4", 6, 5, 4, 11), 2, 100)
+    gen_aprod("sparse8x7x5", small_workload("sparse8x7x5", 8, 7, 5, 12, keep=0.6, shuffle=True), 1, 200)
+    gen_aprod("box14x12x8", small_workload("box14x12x8", 14, 12, 8, 13, em=6.25 + 0.05j, lam=600.0), 1, 300)
+    # the plain FP64 parity workload: 20x20x10, rho~U[0,1], eps_m=4+0.1i, x-pol along +z, tol 1e-5
+    gen_solve("cfg1", lattice.config(1))
+    # the same workload solved to 1e-10: the regime where solutions of two implementations
+    # that differ only in rounding agree to ~1e-10 (at 1e-5 they differ by O(1e-5))
+    gen_solve("cfg1_tight", lattice.config(1), max_err=1e-10)
+    # oblique incidence on a sparse, shuffled lattice with a real-valued material
+    ws = small_workload("sparse10x9x6", 10, 9, 6, 14, em=2.25 + 0j, keep=0.7, shuffle=True)
+    th = math.radians(30.0)
+    inc = lattice.Incidence(np.array([math.sin(th), 0.0, math.cos(th)]), lattice.n_e_perp_in_xz(th))
+    gen_solve("sparse10x9x6", ws, inc)
+    # warm start + a replaced right-hand side (the adjoint's change_E / InitializeP)
+    wa = small_workload("adj8x8x4", 8, 8, 4, 15)
+    gen_solve("adj8x8x4", wa, P0=0.01 * rand_vec(3 * wa.N, 400), Ein=rand_vec(3 * wa.N, 500))
+
+
+if __name__ == "__main__":
+    main()
