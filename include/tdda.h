@@ -1,0 +1,156 @@
+/*
+ * tdda.h -- C ABI of the GB300-native DDA solve path (libtdda.so).
+ *
+ * The library replaces the FFT-accelerated interaction product and the
+ * BiCGSTAB solve of Topo-DDA (AProductCore / DDAModel).  Every entry point
+ * below names the reference interface it stands in for.  Plain C types only:
+ * complex vectors are interleaved doubles (re, im) -- the storage of
+ * std::complex<double> and Eigen::VectorXcd -- and dipole vectors are AoS
+ * [x, y, z] per dipole in the order of R, as in the reference.
+ *
+ * Conventions
+ *   - every function returns a tdda_status; nothing throws across the ABI;
+ *   - calls are synchronous (the result is ready when the call returns), like
+ *     the reference; each core owns one CUDA stream;
+ *   - handles are not thread-safe; models that share a core must not be used
+ *     from two threads at once (the reference shares one core's scratch
+ *     between models the same way, EvoDDAModel.h:14);
+ *   - `mem` says whether a vector argument is host or device memory.
+ */
+#ifndef TDDA_H_
+#define TDDA_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TDDA_ABI_VERSION 1
+
+typedef enum tdda_status {
+    TDDA_OK = 0,
+    TDDA_ERR_INVALID_ARGUMENT = 1,
+    TDDA_ERR_CUDA = 2,
+    TDDA_ERR_OUT_OF_MEMORY = 3,
+    TDDA_ERR_UNSUPPORTED = 4,
+    TDDA_NOT_CONVERGED = 5, /* iteration limit reached (DDAModel.cpp:256-259) */
+    TDDA_BREAKDOWN = 6,     /* r0.rl == 0 stop (DDAModel.cpp:193-216) */
+    TDDA_ERR_NAN = 7,       /* a BiCGSTAB scalar became NaN or infinite */
+    TDDA_ERR_NO_DEVICE = 8
+} tdda_status;
+
+typedef enum tdda_method { TDDA_METHOD_LDR = 0, TDDA_METHOD_FCD = 1 } tdda_method;
+typedef enum tdda_memory { TDDA_MEM_HOST = 0, TDDA_MEM_DEVICE = 1 } tdda_memory;
+typedef enum tdda_precision {
+    TDDA_FP64 = 0,       /* complex128 FFT convolution and Krylov vectors */
+    TDDA_FP32_REFINE = 1 /* complex64 FFT and Krylov vectors, FP64 dots, scalars and an outer
+                            FP64 residual with iterative refinement */
+} tdda_precision;
+typedef enum tdda_field {
+    TDDA_FIELD_P = 0,
+    TDDA_FIELD_E = 1,
+    TDDA_FIELD_AL = 2,
+    TDDA_FIELD_DIEL = 3,
+    TDDA_FIELD_EINTERNAL = 4
+} tdda_field;
+
+typedef struct tdda_core_desc {
+    int Nx, Ny, Nz;          /* lattice box (CoreStructure get_Nx/Ny/Nz) */
+    int N;                   /* number of dipoles */
+    const int* R;            /* 3N lattice indices, host memory (CoreStructure get_R) */
+    double d;                /* lattice spacing */
+    double lam;              /* vacuum wavelength */
+    double nback;            /* background refractive index */
+    const double* material;  /* nmat complex permittivities (re, im), host memory */
+    int nmat;
+    int method;              /* TDDA_METHOD_LDR */
+    int max_rhs;             /* right-hand sides a batched solve may carry (>= 1) */
+    int device;              /* CUDA device ordinal */
+} tdda_core_desc;
+
+typedef struct tdda_solve_info {
+    int status;            /* tdda_status of this right-hand side */
+    int iterations;        /* ITERATION as DDAModel::get_ITERATION reports it */
+    double error;          /* |r| / |E| of the recursive residual at the end */
+    double true_residual;  /* |E - A P| / |E| recomputed in FP64 (mixed precision only, else -1) */
+    int outer_iterations;  /* refinement steps (mixed precision only, else 0) */
+    int inner_iterations;  /* FP32 BiCGSTAB iterations summed over refinement steps */
+} tdda_solve_info;
+
+typedef struct tdda_core_s tdda_core;
+typedef struct tdda_model_s tdda_model;
+
+/* library ------------------------------------------------------------- */
+int tdda_abi_version(void);
+/* message of the last error on this thread ("" if none) */
+const char* tdda_last_error(void);
+/* number of visible CUDA devices (0 without a GPU; never fails) */
+int tdda_device_count(void);
+
+/* core: one lattice at one wavelength ---------------------------------- */
+/* Replaces AProductCore::AProductCore(CStr, lam, material, nback, method)
+ * (AProductCore.h:51, AProductCore.cpp:12-249): material normalisation,
+ * Green tensor on the padded grid, its spectrum -- all on the device. */
+tdda_status tdda_core_create(const tdda_core_desc* desc, tdda_core** out);
+/* Replaces AProductCore::~AProductCore (AProductCore.cpp:538-558). */
+tdda_status tdda_core_destroy(tdda_core* core);
+/* AProductCore::get_K / get_material (AProductCore.h:72,75) and the FFT grid
+ * chosen per axis.  Any output pointer may be NULL. */
+tdda_status tdda_core_info(const tdda_core* core, double* K, int* grid3, double* material_norm);
+/* y = A_offdiag b, 3N complex (AProductCore::Aproduct, AProductCore.h:56,
+ * AProductCore.cpp:697-758).  precision TDDA_FP32_REFINE runs the complex64
+ * convolution once (no refinement) for error studies. */
+tdda_status tdda_aproduct(tdda_core* core, int precision, const double* b, double* y, int mem);
+/* The LDR interaction tensor at offset (x, y, z) in the units of d
+ * (AProductCore::LDR_inter, AProductCore.h:80): out12 = xx, xy, xz, yy, yz,
+ * zz as (re, im).  Host arithmetic, as in the reference. */
+tdda_status tdda_core_ldr_inter(const tdda_core* core, double x, double y, double z, double* out12);
+
+/* model: incident field, polarisability and solve state ----------------- */
+/* Replaces DDAModel::DDAModel(Core, n_K, E0, n_E0) (DDAModel.h:34,
+ * DDAModel.cpp:12-69).  diel_old: the core structure's 3N densities
+ * (CoreStructure get_diel_old), host memory. */
+tdda_status tdda_model_create(tdda_core* core, const double* nK, double E0, const double* nE0,
+                              const double* diel_old, tdda_model** out);
+tdda_status tdda_model_destroy(tdda_model* model);
+/* DDAModel::UpdateAlpha (DDAModel.cpp:470-487) for new 3N densities. */
+tdda_status tdda_model_update_alpha(tdda_model* model, const double* diel_old);
+/* DDAModel::UpdateAlphaSingle (DDAModel.cpp:489-528) after the density of
+ * dipole idx became `value` (CoreStructure::UpdateStrSingle). */
+tdda_status tdda_model_update_alpha_single(tdda_model* model, int idx, double value);
+/* DDAModel::change_E / reset_E / InitializeP (DDAModel.cpp:453-468, 731-733). */
+tdda_status tdda_model_change_E(tdda_model* model, const double* E, int mem);
+tdda_status tdda_model_reset_E(tdda_model* model);
+tdda_status tdda_model_initialize_P(tdda_model* model, const double* P, int mem);
+/* y = A b + al b (DDAModel::Aproductwithalb, DDAModel.cpp:577-586). */
+tdda_status tdda_model_aproduct_with_alb(tdda_model* model, const double* b, double* y, int mem);
+/* DDAModel::bicgstab(MAX_ITERATION, MAX_ERROR) (DDAModel.cpp:131-260), FP64.
+ * info may be NULL. */
+tdda_status tdda_model_bicgstab(tdda_model* model, int max_it, double max_err, tdda_solve_info* info);
+/* The same solve in mixed precision with FP64 refinement to max_err. */
+tdda_status tdda_model_solve_mixed(tdda_model* model, int max_it, double max_err, tdda_solve_info* info);
+/* DDAModel::update_E_in_structure (DDAModel.cpp:567-575). */
+tdda_status tdda_model_update_E_in_structure(tdda_model* model);
+/* DDAModel::get_P / get_Einternal / get_al (DDAModel.h:50-56) and E, diel:
+ * copies 3N complex into out. */
+tdda_status tdda_model_get(const tdda_model* model, int field, double* out, int mem);
+/* DDAModel::get_ITERATION (DDAModel.h:59). */
+int tdda_model_iterations(const tdda_model* model);
+
+/* batched solve: n models on one core, one launch per pass -------------- */
+/* The forward and adjoint solves of EvoDDAModel::EvoOptimization
+ * (EvoDDAModel.cpp:435-436, 596-600), or several incidences on one lattice,
+ * solved together.  n <= max_rhs of the core.  infos may be NULL. */
+tdda_status tdda_solve_batch(tdda_model* const* models, int n, int precision, int max_it, double max_err,
+                             tdda_solve_info* infos);
+
+/* FFT engine ------------------------------------------------------------ */
+/* In-place unnormalised 3-D complex128 FFT of a device array (n0, n1, n2),
+ * last index fastest, sign -1 forward / +1 inverse, each n 7-smooth; the
+ * engine the A-product runs on (cufftExecZ2Z's role, AProductCore.cpp:719). */
+tdda_status tdda_fft3d(double* data, int n0, int n1, int n2, int sign);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,214 @@
+"""CUDA product path against the oracle and the reference's golden outputs.
+
+Every call goes through libtdda's C ABI.  Tolerances:
+  * FFT engine / A-product, FP64: 1e-12 relative (norm-wise) -- rounding of two FFTs;
+  * A-product, FP32 convolution: 1e-5 relative;
+  * FP64 solve at the reference's tolerance 1e-5: converged, |E - A P|/|E| <= 1e-5 checked
+    with the oracle, P and Einternal within 2e-4 of the reference's and the iteration
+    count within 15% -- the reference's own solve moves by O(1e-5) and several
+    iterations under a rounding-level change of its product (test_oracle_golden.py);
+  * FP64 solve at 1e-10: P and Einternal within 1e-9 of the reference's run at 1e-10.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+import tdda
+from conftest import golden, rel
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if tdda.device_count() < 1:
+        pytest.skip("no CUDA device")
+
+
+def _core(g, **kw):
+    Nx, Ny, Nz = (int(v) for v in g["box"])
+    return tdda.AProductCore(Nx, Ny, Nz, g["R"], float(g["d"]), float(g["lam"]), g["material"],
+                             float(g["nback"]), **kw)
+
+
+def _ocore(g, **kw):
+    Nx, Ny, Nz = (int(v) for v in g["box"])
+    return O.OracleCore(Nx, Ny, Nz, g["R"], float(g["d"]), float(g["lam"]), g["material"], float(g["nback"]), **kw)
+
+
+@pytest.mark.parametrize("shape", [(8, 12, 10), (40, 40, 20), (5, 7, 3), (1, 16, 9), (64, 30, 14), (21, 1, 1)])
+def test_fft_engine_matches_numpy(shape):
+    torch = pytest.importorskip("torch")
+    rng = np.random.Generator(np.random.PCG64(sum(shape)))
+    a = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    for sign, ref in ((-1, np.fft.fftn(a)), (+1, np.fft.ifftn(a) * a.size)):
+        t = torch.from_numpy(a.copy()).to("cuda")
+        torch.cuda.synchronize()
+        tdda.fft3d_device(t.data_ptr(), *shape, sign)
+        out = t.cpu().numpy()
+        assert rel(out, ref) <= 1e-14
+
+
+def test_core_reports_reference_quantities():
+    g = golden("aprod_box6x5x4.npz")
+    c = _core(g)
+    oc = _ocore(g)
+    assert c.get_K() == oc.K
+    assert np.array_equal(c.get_material(), oc.material)  # 1.0 -> 1.01 (AProductCore.cpp:21-23)
+    assert c.grid == (12, 9, 7)  # smallest 7-smooth lengths >= 2N-1
+    t = c.LDR_inter(10.0, 0.0, 0.0)
+    assert t[0, 0] == pytest.approx(-2.01573e-3 - 1.32085e-6j, rel=1e-5)
+
+
+@pytest.mark.parametrize("name", ["box6x5x4", "sparse8x7x5", "box14x12x8"])
+def test_aproduct_matches_reference(name):
+    g = golden(f"aprod_{name}.npz")
+    c = _core(g)
+    Nx, Ny, Nz = (int(v) for v in g["box"])
+    m = tdda.DDAModel(c, g["nK"], float(g["E0"]), g["nE0"], g["diel_old"])
+    assert rel(m.get_al(), g["al"]) <= 1e-15
+    for b, y, yw in zip(g["b"], g["y"], g["y_alb"]):
+        assert rel(c.Aproduct(b), y) <= 1e-12
+        assert rel(m.Aproductwithalb(b), yw) <= 1e-12
+        assert rel(c.Aproduct(b, precision=tdda.FP32_REFINE), y) <= 1e-5
+
+
+def test_aproduct_equals_direct_sum_on_odd_boxes():
+    rng = np.random.Generator(np.random.PCG64(77))
+    for (Nx, Ny, Nz) in ((5, 3, 7), (1, 1, 6), (9, 2, 1), (4, 4, 4)):
+        R = tdda.lattice.bulk(Nx, Ny, Nz)
+        c = tdda.AProductCore(Nx, Ny, Nz, R, 7.0, 480.0, np.array([1.0, 2.25]))
+        b = rng.standard_normal(R.size) + 1j * rng.standard_normal(R.size)
+        yd = O.aproduct_direct(R, 7.0, c.K, b)
+        assert rel(c.Aproduct(b), yd) <= 1e-12
+
+
+def test_aproduct_config_shapes_against_oracle():
+    rng = np.random.Generator(np.random.PCG64(3))
+    for idx in (1, 2):
+        w = tdda.lattice.config(idx)
+        c = tdda.AProductCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material)
+        oc = O.OracleCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material, grid=c.grid, pruned=True)
+        b = rng.standard_normal(w.R.size) + 1j * rng.standard_normal(w.R.size)
+        y = oc.Aproduct(b)
+        assert rel(c.Aproduct(b), y) <= 1e-12
+        assert rel(c.Aproduct(b, precision=tdda.FP32_REFINE), y) <= 1e-5
+
+
+def _model(g, core):
+    m = tdda.DDAModel(core, g["nK"], float(g["E0"]), g["nE0"], g["diel_old"])
+    if "P0" in g:
+        m.InitializeP(g["P0"])
+    if "E_rhs" in g:
+        m.change_E(g["E_rhs"])
+    return m
+
+
+def _true_residual(g, P, E):
+    oc = _ocore(g)
+    om = O.OracleModel(oc, g["nK"], float(g["E0"]), g["nE0"], g["diel_old"])
+    return rel(om.Aproductwithalb(P), E)
+
+
+@pytest.mark.parametrize("name", ["cfg1", "sparse10x9x6", "adj8x8x4"])
+def test_fp64_solve_matches_reference_at_its_tolerance(name):
+    g = golden(f"solve_{name}.npz")
+    c = _core(g)
+    m = _model(g, c)
+    info = m.bicgstab(int(g["max_it"]), float(g["max_err"]))
+    m.update_E_in_structure()
+    assert info["status"] == tdda.OK
+    assert info["error"] <= float(g["max_err"])
+    it_ref = int(g["iterations"])
+    assert abs(m.get_ITERATION() - it_ref) <= max(1, int(0.15 * it_ref))
+    assert _true_residual(g, m.get_P(), m.get_E()) <= 1.5 * float(g["max_err"])
+    assert rel(m.get_P(), g["P"]) <= 2e-4
+    assert rel(m.get_Einternal(), g["Einternal"]) <= 2e-4
+
+
+def test_fp64_solve_matches_reference_to_1e9_at_tight_tolerance():
+    g = golden("solve_cfg1_tight.npz")
+    c = _core(g)
+    m = _model(g, c)
+    info = m.bicgstab(int(g["max_it"]), float(g["max_err"]))
+    m.update_E_in_structure()
+    assert info["status"] == tdda.OK
+    assert rel(m.get_P(), g["P"]) <= 1e-9
+    assert rel(m.get_Einternal(), g["Einternal"]) <= 1e-9
+
+
+def test_mixed_precision_reaches_tolerance_with_fp64_residual():
+    g = golden("solve_cfg1.npz")
+    c = _core(g)
+    m = _model(g, c)
+    info = m.solve_mixed(10000, 1e-5)
+    m.update_E_in_structure()
+    assert info["status"] == tdda.OK and info["outer_iterations"] >= 1
+    assert info["true_residual"] <= 1e-5
+    assert _true_residual(g, m.get_P(), m.get_E()) <= 1e-5
+    assert rel(m.get_P(), g["P"]) <= 2e-4
+
+
+def test_batch_equals_alone():
+    w = tdda.lattice.config(1)
+    incs = [tdda.lattice.XPOL_Z,
+            tdda.lattice.Incidence(np.array([0.0, 0.0, 1.0]), np.array([0.0, 1.0, 0.0])),
+            tdda.lattice.Incidence(np.array([np.sin(0.5), 0.0, np.cos(0.5)]), tdda.lattice.n_e_perp_in_xz(0.5))]
+    for prec in (tdda.FP64, tdda.FP32_REFINE):
+        core = tdda.AProductCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material, max_rhs=4)
+        alone = []
+        for inc in incs:
+            m = tdda.DDAModel(core, inc.nK, 1.0, inc.nE0, w.diel_old)
+            info = m.bicgstab(10000, 1e-5) if prec == tdda.FP64 else m.solve_mixed(10000, 1e-5)
+            alone.append((m.get_P(), info))
+        ms = [tdda.DDAModel(core, inc.nK, 1.0, inc.nE0, w.diel_old) for inc in incs]
+        infos = tdda.solve_batch(ms, prec, 10000, 1e-5)
+        for m, info, (P, ia) in zip(ms, infos, alone):
+            assert info["status"] == tdda.OK
+            assert info["iterations"] == ia["iterations"]
+            assert np.array_equal(m.get_P(), P)
+
+
+def test_zero_rhs_breaks_down_like_the_reference():
+    """E = 0: r0.rl = 0 at the first loop iteration, ITERATION = 1 (DDAModel.cpp:193-215)."""
+    g = golden("aprod_box6x5x4.npz")
+    c = _core(g)
+    m = tdda.DDAModel(c, g["nK"], float(g["E0"]), g["nE0"], g["diel_old"])
+    m.change_E(np.zeros(3 * c.N, np.complex128))
+    info = m.bicgstab(100, 1e-5)
+    oc = _ocore(g)
+    om = O.OracleModel(oc, g["nK"], float(g["E0"]), g["nE0"], g["diel_old"])
+    om.change_E(np.zeros(3 * c.N, np.complex128))
+    assert om.bicgstab(100, 1e-5) == O.BREAKDOWN and om.ITERATION == 1
+    assert info["status"] == tdda.BREAKDOWN and m.get_ITERATION() == 1
+
+
+def test_iteration_limit_keeps_previous_iteration_count():
+    """Non-convergence leaves ITERATION at its previous value (DDAModel.cpp:256-259)."""
+    g = golden("solve_cfg1.npz")
+    c = _core(g)
+    m = _model(g, c)
+    info = m.bicgstab(3, 1e-5)
+    assert info["status"] == tdda.NOT_CONVERGED and m.get_ITERATION() == 0
+    m2 = _model(g, c)
+    m2.bicgstab(10000, 1e-5)
+    it = m2.get_ITERATION()
+    m2.bicgstab(2, 1e-12)
+    assert m2.get_ITERATION() == it
+
+
+def test_update_alpha_matches_oracle():
+    g = golden("aprod_box6x5x4.npz")
+    c = _core(g)
+    m = tdda.DDAModel(c, g["nK"], float(g["E0"]), g["nE0"], g["diel_old"])
+    d2 = np.clip(g["diel_old"] * 0.5 + 0.25, 0, 1)
+    m.UpdateAlpha(d2)
+    om = O.OracleModel(_ocore(g), g["nK"], float(g["E0"]), g["nE0"], d2)
+    assert rel(m.get_al(), om.al) <= 1e-15
+    m.UpdateAlphaSingle(3, 1.0)
+    d3 = d2.copy()
+    d3[9:12] = 1.0
+    om.UpdateAlpha(d3)
+    assert rel(m.get_al(), om.al) <= 1e-15
+    m.reset_E()
+    assert rel(m.get_E(), om.E) <= 1e-15

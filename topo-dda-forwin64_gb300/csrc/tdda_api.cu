@@ -1,0 +1,1023 @@
+// tdda_api.cu -- implementation of the C ABI in include/tdda.h.
+//
+// Host responsibilities: argument checks, the FFT plan per axis, the
+// incident field and polarisabilities (O(N), host FP64 std::complex exactly
+// as DDAModel.cpp:47-63 / tools.cpp:617-630), device memory, and the solve
+// drivers.  Every O(grid) operation runs on the device (tdda_kernels.cu).
+// One BiCGSTAB iteration (11 kernels) is captured once per core, precision
+// and batch width as a CUDA graph and replayed; the host reads the solver
+// status every few iterations.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/tdda.h"
+#include "tdda_internal.cuh"
+
+using tdda::AxisPlan;
+using tdda::Geom;
+using tdda::RhsVecs;
+using tdda::SolveState;
+using cd = std::complex<double>;
+
+namespace {
+
+thread_local std::string g_err;
+
+void set_err(const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+}
+
+tdda_status cuda_fail(cudaError_t e, const char* what) {
+    set_err("%s: %s", what, cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? TDDA_ERR_OUT_OF_MEMORY : TDDA_ERR_CUDA;
+}
+
+#define TDDA_CK(call)                                                   \
+    do {                                                                \
+        cudaError_t e_ = (call);                                        \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);             \
+    } while (0)
+
+constexpr double kPi = 3.14159265358979323846264338327950288;
+constexpr int kChunk = 4;        // iterations between status reads
+constexpr int kMaxOuter = 10;    // refinement steps of the mixed solve
+
+bool smooth7(int m) {
+    for (int p : {2, 3, 5, 7})
+        while (m % p == 0) m /= p;
+    return m == 1;
+}
+int smooth_size(int n) {
+    int m = std::max(1, n);
+    while (!smooth7(m)) m++;
+    return m;
+}
+
+// radix plan: 8s and 4s (no lone 2 unless the power of two is 2), then 3, 5, 7
+bool make_plan(int M, AxisPlan* ap) {
+    std::memset(ap, 0, sizeof(*ap));
+    ap->M = M;
+    int m = M, a = 0;
+    while (m % 2 == 0) { m /= 2; a++; }
+    std::vector<int> r;
+    while (a >= 3 && a != 4) { r.push_back(8); a -= 3; }
+    while (a >= 2) { r.push_back(4); a -= 2; }
+    if (a == 1) r.push_back(2);
+    for (int p : {3, 5, 7})
+        while (m % p == 0) { r.push_back(p); m /= p; }
+    if (m != 1 || (int)r.size() > tdda::kMaxStages) return false;
+    ap->nstages = (int)r.size();
+    ap->rmin = 8;
+    for (size_t i = 0; i < r.size(); i++) {
+        ap->radix[i] = r[i];
+        ap->rmin = std::min(ap->rmin, r[i]);
+    }
+    if (r.empty()) ap->rmin = 1;
+    return true;
+}
+
+void twiddles(int M, std::vector<double2>& w64, std::vector<float2>& w32) {
+    w64.resize(M);
+    w32.resize(M);
+    for (int m = 0; m < M; m++) {
+        long double a = 2.0L * 3.141592653589793238462643383279502884L * (long double)m / (long double)M;
+        double c = (double)std::cos(a), s = -(double)std::sin(a);
+        w64[m] = make_double2(c, s);
+        w32[m] = make_float2((float)c, (float)s);
+    }
+}
+
+// AProductCore::LDR_inter (AProductCore.cpp:588-623), host FP64
+void ldr_host(double K, double x, double y, double z, cd out[6]) {
+    using namespace std::complex_literals;
+    double xs = x * x, ys = y * y, zs = z * z;
+    double rn = std::sqrt(xs + ys + zs);
+    if (rn == 0.0) {
+        for (int l = 0; l < 6; l++) out[l] = 0.0;
+        return;
+    }
+    double xy = x * y, yz = y * z, zx = z * x;
+    double rsq = rn * rn, rcu = rn * rn * rn;
+    cd c1 = 1i * K * rn;
+    c1 = std::exp(c1) / rcu;
+    cd c2 = (1.0 - K * rn * 1i);
+    c2 = c2 / rsq;
+    cd c3 = K * K - 3.0 * c2;
+    out[0] = c1 * (c2 * (rsq - 3 * xs) - K * K * (ys + zs));
+    out[1] = c1 * (xy * c3);
+    out[2] = c1 * (zx * c3);
+    out[3] = c1 * (c2 * (rsq - 3 * ys) - K * K * (zs + xs));
+    out[4] = c1 * (yz * c3);
+    out[5] = c1 * (c2 * (rsq - 3 * zs) - K * K * (xs + ys));
+}
+
+// Get_Alpha, LDR (tools.cpp:617-630)
+cd get_alpha(double K, double d, cd diel, const double nE0[3], const double nK[3]) {
+    using namespace std::complex_literals;
+    const double b1 = -1.891531, b2 = 0.1648469, b3 = -1.7700004;
+    cd a1 = (3 * std::pow(d, 3) / (4 * kPi)) * (diel - 1.0) / (diel + 2.0);
+    cd result = 0.0 + (2.0 / 3.0) * std::pow(K * d, 3) * 1.0i;
+    double S = std::pow(nE0[0] * nK[0], 2) + std::pow(nE0[1] * nK[1], 2) + std::pow(nE0[2] * nK[2], 2);
+    result = 1.0 + (a1 / std::pow(d, 3)) * ((b1 + diel * b2 + diel * b3 * S) * std::pow(K * d, 2) - result);
+    return a1 / result;
+}
+
+template <typename T> struct Graphs {
+    cudaGraphExec_t iter[65] = {};  // one iteration, by batch width
+};
+
+}  // namespace
+
+struct tdda_core_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    Geom g{};
+    int N = 0, nmat = 0, max_rhs = 1, method = 0, maxblk = 1;
+    double d = 0, lam = 0, nback = 1, K = 0;
+    std::vector<cd> material;  // normalised
+    std::vector<int> R;
+    int* cellmap = nullptr;
+    double2* green64 = nullptr;
+    float2* green32 = nullptr;
+    double2* tw64[3] = {nullptr, nullptr, nullptr};
+    float2* tw32[3] = {nullptr, nullptr, nullptr};
+    double2* grid64 = nullptr;
+    float2* grid32 = nullptr;
+    double2 *vin64 = nullptr, *vout64 = nullptr;
+    float2 *vin32 = nullptr, *vout32 = nullptr;
+    RhsVecs<double>* rhs64 = nullptr;  // device, max_rhs + 1 entries (last: plain products)
+    RhsVecs<float>* rhs32 = nullptr;
+    SolveState* st64 = nullptr;        // device, max_rhs
+    SolveState* st32 = nullptr;
+    SolveState* hst = nullptr;         // pinned host, max_rhs
+    double* part = nullptr;
+    unsigned int* cnt = nullptr;
+    Graphs<double> g64;
+    Graphs<float> g32;
+    std::vector<void*> allocs;
+};
+
+struct tdda_model_s {
+    tdda_core* core = nullptr;
+    double nK[3] = {0, 0, 0}, nE0[3] = {0, 0, 0}, E0 = 1;
+    std::vector<double> diel_old;
+    // FP64 state: P, E, al, diel, Einternal and the Krylov vectors
+    double2 *P = nullptr, *E = nullptr, *al = nullptr, *diel = nullptr, *Ein = nullptr;
+    double2 *r = nullptr, *r0 = nullptr, *p = nullptr, *u = nullptr, *t = nullptr, *Ap = nullptr, *At = nullptr;
+    // FP32 Krylov vectors of the mixed solve (allocated on first use)
+    float2 *fP = nullptr, *fE = nullptr, *fal = nullptr, *fr = nullptr, *fr0 = nullptr, *fp = nullptr, *fu = nullptr,
+           *ft = nullptr, *fAp = nullptr, *fAt = nullptr;
+    std::vector<void*> allocs;
+    bool P_zero = true;
+    int ITERATION = 0;
+    double Error = 0.0;
+};
+
+namespace {
+
+template <typename T> tdda_status dalloc(std::vector<void*>& list, T** p, size_t count) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, sizeof(T) * std::max<size_t>(count, 1));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    list.push_back(q);
+    *p = (T*)q;
+    return TDDA_OK;
+}
+
+#define TDDA_TRY(call)                         \
+    do {                                       \
+        tdda_status s_ = (call);               \
+        if (s_ != TDDA_OK) return s_;          \
+    } while (0)
+
+void free_all(std::vector<void*>& list) {
+    for (void* q : list) cudaFree(q);
+    list.clear();
+}
+
+cudaMemcpyKind kind_in(int mem) { return mem == TDDA_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice; }
+cudaMemcpyKind kind_out(int mem) { return mem == TDDA_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost; }
+
+RhsVecs<double> vecs64(tdda_core* c, tdda_model* m, int slot) {
+    RhsVecs<double> v{};
+    v.P = m->P; v.E = m->E; v.r = m->r; v.r0 = m->r0; v.p = m->p; v.u = m->u; v.t = m->t;
+    v.Ap = m->Ap; v.At = m->At; v.al = m->al;
+    v.st = c->st64 + slot;
+    v.part = c->part + (size_t)slot * tdda::kPartSlots * c->maxblk;
+    v.cnt = c->cnt + (size_t)slot * tdda::kCounters;
+    return v;
+}
+RhsVecs<float> vecs32(tdda_core* c, tdda_model* m, int slot) {
+    RhsVecs<float> v{};
+    v.P = m->fP; v.E = m->fE; v.r = m->fr; v.r0 = m->fr0; v.p = m->fp; v.u = m->fu; v.t = m->ft;
+    v.Ap = m->fAp; v.At = m->fAt; v.al = m->fal;
+    v.st = c->st32 + slot;
+    v.part = c->part + (size_t)slot * tdda::kPartSlots * c->maxblk;
+    v.cnt = c->cnt + (size_t)slot * tdda::kCounters;
+    return v;
+}
+
+// incident field and polarisability of a model (DDAModel.cpp:47-63)
+tdda_status model_upload_fields(tdda_model* m, bool field_E, bool field_al) {
+    tdda_core* c = m->core;
+    const int N = c->N;
+    std::vector<cd> buf(3 * (size_t)N), buf2(3 * (size_t)N);
+    if (field_E) {
+        using namespace std::complex_literals;
+        for (int i = 0; i < N; i++) {
+            const double ph = c->K * c->d *
+                              (m->nK[0] * c->R[3 * i] + m->nK[1] * c->R[3 * i + 1] + m->nK[2] * c->R[3 * i + 2]);
+            for (int j = 0; j < 3; j++) buf[3 * i + j] = m->E0 * m->nE0[j] * (std::cos(ph) + std::sin(ph) * 1i);
+        }
+        TDDA_CK(cudaMemcpyAsync(m->E, buf.data(), sizeof(cd) * buf.size(), cudaMemcpyHostToDevice, c->stream));
+        TDDA_CK(cudaStreamSynchronize(c->stream));
+    }
+    if (field_al) {
+        for (int i = 0; i < 3 * N; i++) {
+            const double v = m->diel_old[i];
+            int lf = (int)std::floor(v);
+            int ln = lf + 1;
+            if (lf >= 1) ln = lf;
+            if (lf < 0 || lf >= c->nmat || ln >= c->nmat) {
+                set_err("density %g of entry %d is outside the material table", v, i);
+                return TDDA_ERR_INVALID_ARGUMENT;
+            }
+            cd eps = c->material[lf] + (v - double(lf)) * (c->material[ln] - c->material[lf]);
+            buf[i] = eps;
+            buf2[i] = 1.0 / get_alpha(c->K, c->d, eps, m->nE0, m->nK);
+        }
+        TDDA_CK(cudaMemcpyAsync(m->diel, buf.data(), sizeof(cd) * buf.size(), cudaMemcpyHostToDevice, c->stream));
+        TDDA_CK(cudaMemcpyAsync(m->al, buf2.data(), sizeof(cd) * buf2.size(), cudaMemcpyHostToDevice, c->stream));
+        if (m->fal) TDDA_CK(tdda::launch_to_f32(3 * N, m->al, m->fal, c->stream));
+        TDDA_CK(cudaStreamSynchronize(c->stream));
+    }
+    return TDDA_OK;
+}
+
+tdda_status model_alloc_f32(tdda_model* m) {
+    if (m->fP) return TDDA_OK;
+    const size_t n3 = 3 * (size_t)m->core->N;
+    float2** v[] = {&m->fP, &m->fE, &m->fal, &m->fr, &m->fr0, &m->fp, &m->fu, &m->ft, &m->fAp, &m->fAt};
+    for (float2** q : v) TDDA_TRY(dalloc(m->allocs, q, n3));
+    TDDA_CK(tdda::launch_to_f32((int)n3, m->al, m->fal, m->core->stream));
+    return TDDA_OK;
+}
+
+template <typename T> struct Prec;
+template <> struct Prec<double> {
+    static RhsVecs<double>* rhs(tdda_core* c) { return c->rhs64; }
+    static SolveState* st(tdda_core* c) { return c->st64; }
+    static const double2* green(tdda_core* c) { return c->green64; }
+    static double2* grid(tdda_core* c) { return c->grid64; }
+    static const double2* tw(tdda_core* c, int a) { return c->tw64[a]; }
+    static cudaGraphExec_t& graph(tdda_core* c, int n) { return c->g64.iter[n]; }
+};
+template <> struct Prec<float> {
+    static RhsVecs<float>* rhs(tdda_core* c) { return c->rhs32; }
+    static SolveState* st(tdda_core* c) { return c->st32; }
+    static const float2* green(tdda_core* c) { return c->green32; }
+    static float2* grid(tdda_core* c) { return c->grid32; }
+    static const float2* tw(tdda_core* c, int a) { return c->tw32[a]; }
+    static cudaGraphExec_t& graph(tdda_core* c, int n) { return c->g32.iter[n]; }
+};
+
+template <typename T>
+cudaError_t aprod(tdda_core* c, int src, int snk, int n, const RhsVecs<T>* rhs) {
+    return tdda::launch_aproduct<T>(c->g, src, snk, n, rhs, Prec<T>::green(c), Prec<T>::tw(c, 0), Prec<T>::tw(c, 1),
+                                    Prec<T>::tw(c, 2), c->cellmap, Prec<T>::grid(c), c->stream);
+}
+
+template <typename T> cudaError_t enqueue_iteration(tdda_core* c, int n) {
+    const RhsVecs<T>* rhs = Prec<T>::rhs(c);
+    cudaError_t e;
+    if ((e = aprod<T>(c, tdda::SRC_PUPD, tdda::SNK_AP, n, rhs))) return e;  // p, Ap, alpha
+    if ((e = aprod<T>(c, tdda::SRC_TUPD, tdda::SNK_AT, n, rhs))) return e;  // t, At, zeta
+    return tdda::launch_update<T>(c->g, n, rhs, 0, c->stream);              // u, P, r, rho, beta
+}
+
+template <typename T> tdda_status get_iteration_graph(tdda_core* c, int n, cudaGraphExec_t* out) {
+    cudaGraphExec_t& ex = Prec<T>::graph(c, n);
+    if (!ex) {
+        cudaGraph_t gr = nullptr;
+        TDDA_CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = enqueue_iteration<T>(c, n);
+        cudaError_t e2 = cudaStreamEndCapture(c->stream, &gr);
+        if (e != cudaSuccess) return cuda_fail(e, "capture of one BiCGSTAB iteration");
+        if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&ex, gr, 0);
+        cudaGraphDestroy(gr);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    }
+    *out = ex;
+    return TDDA_OK;
+}
+
+// BiCGSTAB on n right-hand sides whose RhsVecs<T> and states are uploaded.
+// DDAModel.cpp:164-255.  p_zero: every P is zero, so r = E without a product.
+template <typename T> tdda_status krylov(tdda_core* c, int n, bool p_zero, int max_it) {
+    const RhsVecs<T>* rhs = Prec<T>::rhs(c);
+    if (p_zero) {
+        TDDA_CK(tdda::launch_residual_is_rhs<T>(c->g, n, rhs, c->stream));
+    } else {
+        TDDA_CK(tdda::launch_solve_begin<T>(c->g, n, rhs, c->stream));
+        TDDA_CK(aprod<T>(c, tdda::SRC_P, tdda::SNK_RES, n, rhs));  // r = r0 = p = E - A P
+    }
+    TDDA_CK(aprod<T>(c, tdda::SRC_IN, tdda::SNK_AP, n, rhs));    // Ap0, alpha
+    TDDA_CK(aprod<T>(c, tdda::SRC_TUPD, tdda::SNK_AT, n, rhs));  // t, At0, zeta
+    TDDA_CK(tdda::launch_update<T>(c->g, n, rhs, 1, c->stream));
+    cudaGraphExec_t ex;
+    TDDA_TRY(get_iteration_graph<T>(c, n, &ex));
+    int done_it = 0;
+    for (;;) {
+        TDDA_CK(cudaMemcpyAsync(c->hst, Prec<T>::st(c), sizeof(SolveState) * n, cudaMemcpyDeviceToHost, c->stream));
+        TDDA_CK(cudaStreamSynchronize(c->stream));
+        bool running = false;
+        for (int i = 0; i < n; i++) running |= c->hst[i].status == tdda::ST_RUNNING;
+        if (!running || done_it > max_it) break;
+        for (int k = 0; k < kChunk; k++) TDDA_CK(cudaGraphLaunch(ex, c->stream));
+        done_it += kChunk;
+    }
+    return TDDA_OK;
+}
+
+tdda_status status_of(const SolveState& s) {
+    switch (s.status) {
+        case tdda::ST_CONVERGED: return TDDA_OK;
+        case tdda::ST_BREAKDOWN: return TDDA_BREAKDOWN;
+        case tdda::ST_MAXITER: return TDDA_NOT_CONVERGED;
+        case tdda::ST_NAN: return TDDA_ERR_NAN;
+        default: return TDDA_ERR_CUDA;
+    }
+}
+
+SolveState fresh_state(double tol, int max_it, int iterations) {
+    SolveState s;
+    std::memset(&s, 0, sizeof(s));
+    s.tol = tol;
+    s.max_it = max_it;
+    s.iterations = iterations;
+    s.status = tdda::ST_RUNNING;
+    return s;
+}
+
+tdda_status check_batch(tdda_model* const* ms, int n) {
+    if (!ms || n < 1) {
+        set_err("empty batch");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    tdda_core* c = ms[0] ? ms[0]->core : nullptr;
+    if (!c) {
+        set_err("null model");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    if (n > c->max_rhs) {
+        set_err("batch of %d exceeds the core's max_rhs %d", n, c->max_rhs);
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    for (int i = 0; i < n; i++) {
+        if (!ms[i] || ms[i]->core != c) {
+            set_err("models of a batch must share one core");
+            return TDDA_ERR_INVALID_ARGUMENT;
+        }
+        for (int j = 0; j < i; j++)
+            if (ms[j] == ms[i]) {
+                set_err("a model appears twice in a batch");
+                return TDDA_ERR_INVALID_ARGUMENT;
+            }
+    }
+    return TDDA_OK;
+}
+
+tdda_status solve_fp64(tdda_model* const* ms, int n, int max_it, double tol, tdda_solve_info* infos) {
+    tdda_core* c = ms[0]->core;
+    std::vector<RhsVecs<double>> hv(n);
+    bool p_zero = true;
+    for (int i = 0; i < n; i++) {
+        hv[i] = vecs64(c, ms[i], i);
+        c->hst[i] = fresh_state(tol, max_it, ms[i]->ITERATION);
+        p_zero &= ms[i]->P_zero;
+    }
+    TDDA_CK(cudaMemcpyAsync(c->rhs64, hv.data(), sizeof(RhsVecs<double>) * n, cudaMemcpyHostToDevice, c->stream));
+    TDDA_CK(cudaMemcpyAsync(c->st64, c->hst, sizeof(SolveState) * n, cudaMemcpyHostToDevice, c->stream));
+    if (max_it <= 0) {
+        // the reference still runs its three initial products and the update
+        TDDA_TRY(krylov<double>(c, n, p_zero, 0));
+    } else {
+        TDDA_TRY(krylov<double>(c, n, p_zero, max_it));
+    }
+    tdda_status worst = TDDA_OK;
+    for (int i = 0; i < n; i++) {
+        const SolveState& s = c->hst[i];
+        tdda_model* m = ms[i];
+        m->P_zero = false;
+        tdda_status st = status_of(s);
+        if (s.status == tdda::ST_CONVERGED || s.status == tdda::ST_BREAKDOWN) {
+            m->ITERATION = s.iterations;
+            m->Error = s.error;
+        }
+        if (infos) {
+            infos[i].status = st;
+            infos[i].iterations = m->ITERATION;
+            infos[i].error = s.error;
+            infos[i].true_residual = -1.0;
+            infos[i].outer_iterations = 0;
+            infos[i].inner_iterations = s.it;
+        }
+        if (st != TDDA_OK && worst == TDDA_OK) worst = st;
+    }
+    return worst;
+}
+
+// Mixed precision: FP32 BiCGSTAB on the FP64 residual, FP64 accumulation of
+// the correction, FP64 residual check, until |E - A P| / |E| <= tol.
+tdda_status solve_mixed(tdda_model* const* ms, int n, int max_it, double tol, tdda_solve_info* infos) {
+    tdda_core* c = ms[0]->core;
+    for (int i = 0; i < n; i++) TDDA_TRY(model_alloc_f32(ms[i]));
+    std::vector<RhsVecs<double>> h64(n);
+    std::vector<RhsVecs<float>> h32(n);
+    std::vector<int> done(n, 0), inner(n, 0), outer(n, 0);
+    std::vector<double> Enorm(n, 0.0), res(n, 1.0), prev_res(n, 1e300);
+    std::vector<tdda_status> stat(n, TDDA_NOT_CONVERGED);
+    for (int i = 0; i < n; i++) {
+        h64[i] = vecs64(c, ms[i], i);
+        h32[i] = vecs32(c, ms[i], i);
+    }
+    TDDA_CK(cudaMemcpyAsync(c->rhs64, h64.data(), sizeof(RhsVecs<double>) * n, cudaMemcpyHostToDevice, c->stream));
+    TDDA_CK(cudaMemcpyAsync(c->rhs32, h32.data(), sizeof(RhsVecs<float>) * n, cudaMemcpyHostToDevice, c->stream));
+    for (int outer_it = 0; outer_it <= kMaxOuter; outer_it++) {
+        // FP64 residual r = E - (A P + al P) of the right-hand sides still open
+        for (int i = 0; i < n; i++) {
+            c->hst[i] = fresh_state(tol, 0, 0);
+            if (done[i]) c->hst[i].status = tdda::ST_CONVERGED;
+        }
+        TDDA_CK(cudaMemcpyAsync(c->st64, c->hst, sizeof(SolveState) * n, cudaMemcpyHostToDevice, c->stream));
+        TDDA_CK(tdda::launch_solve_begin<double>(c->g, n, c->rhs64, c->stream));
+        TDDA_CK(aprod<double>(c, tdda::SRC_P, tdda::SNK_RES, n, c->rhs64));
+        TDDA_CK(cudaMemcpyAsync(c->hst, c->st64, sizeof(SolveState) * n, cudaMemcpyDeviceToHost, c->stream));
+        TDDA_CK(cudaStreamSynchronize(c->stream));
+        bool open = false;
+        for (int i = 0; i < n; i++) {
+            if (done[i]) continue;
+            const SolveState& s = c->hst[i];
+            if (s.status == tdda::ST_NAN) {
+                done[i] = 1;
+                stat[i] = TDDA_ERR_NAN;
+                continue;
+            }
+            Enorm[i] = s.Enorm;
+            res[i] = Enorm[i] > 0 ? std::sqrt(s.rnorm2) / Enorm[i] : 0.0;
+            if (!std::isfinite(res[i])) {
+                done[i] = 1;
+                stat[i] = TDDA_ERR_NAN;
+            } else if (res[i] <= tol) {
+                done[i] = 1;
+                stat[i] = TDDA_OK;
+            } else if (outer_it == kMaxOuter || inner[i] >= max_it || res[i] >= prev_res[i]) {
+                done[i] = 1;
+                stat[i] = TDDA_NOT_CONVERGED;
+            } else {
+                open = true;
+            }
+            prev_res[i] = res[i];
+        }
+        if (!open) break;
+        // FP32 correction: A d = r, d0 = 0, to a relative tolerance that brings
+        // the true residual under tol with margin
+        for (int i = 0; i < n; i++) {
+            tdda_model* m = ms[i];
+            double tin = std::min(0.5, std::max(2e-6, 0.5 * tol / std::max(res[i], 1e-300)));
+            c->hst[i] = fresh_state(tin, max_it - inner[i], 0);
+            if (done[i]) {
+                c->hst[i].status = tdda::ST_CONVERGED;
+                continue;
+            }
+            TDDA_CK(tdda::launch_to_f32(3 * c->N, m->r, m->fE, c->stream));
+            TDDA_CK(tdda::launch_zero<float>(3LL * c->N, m->fP, c->stream));
+        }
+        TDDA_CK(cudaMemcpyAsync(c->st32, c->hst, sizeof(SolveState) * n, cudaMemcpyHostToDevice, c->stream));
+        TDDA_TRY(krylov<float>(c, n, true, max_it));
+        for (int i = 0; i < n; i++) {
+            if (done[i]) continue;
+            const SolveState& s = c->hst[i];
+            inner[i] += s.it;
+            outer[i] += 1;
+            if (s.status == tdda::ST_NAN) {
+                done[i] = 1;
+                stat[i] = TDDA_ERR_NAN;
+                continue;
+            }
+            TDDA_CK(tdda::launch_accumulate(3 * c->N, ms[i]->fP, ms[i]->P, c->stream));
+        }
+    }
+    TDDA_CK(cudaStreamSynchronize(c->stream));
+    tdda_status worst = TDDA_OK;
+    for (int i = 0; i < n; i++) {
+        tdda_model* m = ms[i];
+        m->P_zero = false;
+        if (stat[i] == TDDA_OK) {
+            m->ITERATION = inner[i];
+            m->Error = res[i];
+        }
+        if (infos) {
+            infos[i].status = stat[i];
+            infos[i].iterations = inner[i];
+            infos[i].error = res[i];
+            infos[i].true_residual = res[i];
+            infos[i].outer_iterations = outer[i];
+            infos[i].inner_iterations = inner[i];
+        }
+        if (stat[i] != TDDA_OK && worst == TDDA_OK) worst = stat[i];
+    }
+    return worst;
+}
+
+tdda_status set_device(int dev) {
+    cudaError_t e = cudaSetDevice(dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    return TDDA_OK;
+}
+
+}  // namespace
+
+// ======================================================================= ABI
+extern "C" {
+
+int tdda_abi_version(void) { return TDDA_ABI_VERSION; }
+const char* tdda_last_error(void) { return g_err.c_str(); }
+int tdda_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+tdda_status tdda_core_create(const tdda_core_desc* desc, tdda_core** out) {
+    g_err.clear();
+    if (!desc || !out) {
+        set_err("null argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    if (desc->Nx < 1 || desc->Ny < 1 || desc->Nz < 1 || desc->N < 1 || !desc->R || desc->nmat < 1 ||
+        !desc->material || !(desc->d > 0) || !(desc->lam > 0) || !(desc->nback > 0) || desc->max_rhs < 1 ||
+        desc->max_rhs > 64) {
+        set_err("invalid core description");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    if (desc->method != TDDA_METHOD_LDR) {
+        set_err("only the LDR interaction tensor is built (FCD needs the Si/Ci tables)");
+        return TDDA_ERR_UNSUPPORTED;
+    }
+    if ((long long)desc->Nx * desc->Ny * desc->Nz > (1LL << 28)) {
+        set_err("lattice box too large");
+        return TDDA_ERR_UNSUPPORTED;
+    }
+    if (tdda_device_count() < 1) {
+        set_err("no CUDA device");
+        return TDDA_ERR_NO_DEVICE;
+    }
+    tdda_status s = set_device(desc->device);
+    if (s != TDDA_OK) return s;
+    tdda_core* c = new tdda_core_s();
+    c->device = desc->device;
+    c->N = desc->N;
+    c->nmat = desc->nmat;
+    c->max_rhs = desc->max_rhs;
+    c->method = desc->method;
+    c->d = desc->d;
+    c->lam = desc->lam;
+    c->nback = desc->nback;
+    c->K = 2 * kPi / (c->lam / c->nback);  // AProductCore.cpp:17
+    c->material.resize(c->nmat);
+    for (int i = 0; i < c->nmat; i++) {  // AProductCore.cpp:19-24
+        cd m(desc->material[2 * i], desc->material[2 * i + 1]);
+        m = m / (c->nback * c->nback);
+        if (std::sqrt(std::norm(m)) <= 1.01) m = m + 0.01;
+        c->material[i] = m;
+    }
+    c->R.assign(desc->R, desc->R + 3 * (size_t)desc->N);
+    Geom& g = c->g;
+    g.Nx = desc->Nx;
+    g.Ny = desc->Ny;
+    g.Nz = desc->Nz;
+    g.N = desc->N;
+    std::vector<int> cellmap((size_t)g.Nx * g.Ny * g.Nz, -1);
+    for (int i = 0; i < g.N; i++) {
+        int x = c->R[3 * i], y = c->R[3 * i + 1], z = c->R[3 * i + 2];
+        if (x < 0 || x >= g.Nx || y < 0 || y >= g.Ny || z < 0 || z >= g.Nz) {
+            set_err("dipole %d at (%d,%d,%d) lies outside the %dx%dx%d box", i, x, y, z, g.Nx, g.Ny, g.Nz);
+            delete c;
+            return TDDA_ERR_INVALID_ARGUMENT;
+        }
+        int& cell = cellmap[((size_t)x * g.Ny + y) * g.Nz + z];
+        if (cell >= 0) {
+            set_err("dipoles %d and %d occupy the same lattice site", cell, i);
+            delete c;
+            return TDDA_ERR_INVALID_ARGUMENT;
+        }
+        cell = i;
+    }
+    // FFT length per axis: smallest 7-smooth >= 2N-1 (the reference's
+    // 2N-1, AProductCore.cpp:41-43, gives the same linear convolution)
+    int Ms[3] = {smooth_size(2 * g.Nx - 1), smooth_size(2 * g.Ny - 1), smooth_size(2 * g.Nz - 1)};
+    AxisPlan* plans[3] = {&g.px, &g.py, &g.pz};
+    for (int a = 0; a < 3; a++) {
+        if (!make_plan(Ms[a], plans[a])) {
+            set_err("no radix plan for FFT length %d", Ms[a]);
+            delete c;
+            return TDDA_ERR_UNSUPPORTED;
+        }
+    }
+    g.Hx = g.px.M / 2 + 1;
+    g.Hy = g.py.M / 2 + 1;
+    g.Hz = g.pz.M / 2 + 1;
+    g.sy = g.pz.M;
+    g.sx = (long long)g.py.M * g.pz.M;
+    g.sc = (long long)g.Nx * g.sx;
+    g.sb = 3 * g.sc;
+    if (tdda::max_pass_smem(g) > tdda::kMaxPassSmem) {
+        set_err("FFT grid %dx%dx%d needs more shared memory per tile than a block has", g.px.M, g.py.M, g.pz.M);
+        delete c;
+        return TDDA_ERR_UNSUPPORTED;
+    }
+    c->maxblk = tdda::max_blocks_per_rhs(g);
+
+#define TDDA_CORE_TRY(call)          \
+    do {                             \
+        tdda_status s_ = (call);     \
+        if (s_ != TDDA_OK) {         \
+            tdda_core_destroy(c);    \
+            return s_;               \
+        }                            \
+    } while (0)
+#define TDDA_CORE_CK(call)                                     \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) {                               \
+            tdda_status s_ = cuda_fail(e_, #call);             \
+            tdda_core_destroy(c);                              \
+            return s_;                                         \
+        }                                                      \
+    } while (0)
+
+    TDDA_CORE_CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    const size_t n3 = 3 * (size_t)g.N;
+    const long long H6 = 6LL * g.Hx * g.Hy * g.Hz;
+    const long long Mfull = (long long)g.px.M * g.py.M * g.pz.M;
+    TDDA_CORE_TRY(dalloc(c->allocs, &c->cellmap, cellmap.size()));
+    TDDA_CORE_TRY(dalloc(c->allocs, &c->green64, (size_t)H6));
+    TDDA_CORE_TRY(dalloc(c->allocs, &c->green32, (size_t)H6));
+    for (int a = 0; a < 3; a++) {
+        TDDA_CORE_TRY(dalloc(c->allocs, &c->tw64[a], (size_t)plans[a]->M));
+        TDDA_CORE_TRY(dalloc(c->allocs, &c->tw32[a], (size_t)plans[a]->M));
+    }
+    TDDA_CORE_TRY(dalloc(c->allocs, &c->grid64, (size_t)(g.sb * c->max_rhs)));
+    TDDA_CORE_TRY(dalloc(c->allocs, &c->grid32, (size_t)(g.sb * c->max_rhs)));
+    TDDA_CORE_TRY(dalloc(c->allocs, &c->vin64, n3));
+    TDDA_CORE_TRY(dalloc(c->allocs, &c->vout64, n3));
+    TDDA_CORE_TRY(dalloc(c->allocs, &c->vin32, n3));
+    TDDA_CORE_TRY(dalloc(c->allocs, &c->vout32, n3));
+    TDDA_CORE_TRY(dalloc(c->allocs, &c->rhs64, (size_t)c->max_rhs + 1));
+    TDDA_CORE_TRY(dalloc(c->allocs, &c->rhs32, (size_t)c->max_rhs + 1));
+    TDDA_CORE_TRY(dalloc(c->allocs, &c->st64, (size_t)c->max_rhs));
+    TDDA_CORE_TRY(dalloc(c->allocs, &c->st32, (size_t)c->max_rhs));
+    TDDA_CORE_TRY(dalloc(c->allocs, &c->part, (size_t)c->max_rhs * tdda::kPartSlots * c->maxblk));
+    TDDA_CORE_TRY(dalloc(c->allocs, &c->cnt, (size_t)c->max_rhs * tdda::kCounters));
+    TDDA_CORE_CK(cudaMallocHost((void**)&c->hst, sizeof(SolveState) * c->max_rhs));
+    TDDA_CORE_CK(cudaMemsetAsync(c->cnt, 0, sizeof(unsigned int) * c->max_rhs * tdda::kCounters, c->stream));
+    TDDA_CORE_CK(cudaMemcpyAsync(c->cellmap, cellmap.data(), sizeof(int) * cellmap.size(), cudaMemcpyHostToDevice,
+                                 c->stream));
+    for (int a = 0; a < 3; a++) {
+        std::vector<double2> w64;
+        std::vector<float2> w32;
+        twiddles(plans[a]->M, w64, w32);
+        TDDA_CORE_CK(cudaMemcpyAsync(c->tw64[a], w64.data(), sizeof(double2) * w64.size(), cudaMemcpyHostToDevice,
+                                     c->stream));
+        TDDA_CORE_CK(cudaMemcpyAsync(c->tw32[a], w32.data(), sizeof(float2) * w32.size(), cudaMemcpyHostToDevice,
+                                     c->stream));
+        TDDA_CORE_CK(cudaStreamSynchronize(c->stream));
+    }
+    // plain-product slots (the entry after the batch slots)
+    RhsVecs<double> p64{};
+    p64.p = c->vin64;
+    p64.Ap = c->vout64;
+    RhsVecs<float> p32{};
+    p32.p = c->vin32;
+    p32.Ap = c->vout32;
+    TDDA_CORE_CK(cudaMemcpyAsync(c->rhs64 + c->max_rhs, &p64, sizeof(p64), cudaMemcpyHostToDevice, c->stream));
+    TDDA_CORE_CK(cudaMemcpyAsync(c->rhs32 + c->max_rhs, &p32, sizeof(p32), cudaMemcpyHostToDevice, c->stream));
+    TDDA_CORE_CK(tdda::configure_kernels());
+    // Green spectrum (AProductCore.cpp:53-229), on a temporary full grid
+    double2* full6 = nullptr;
+    TDDA_CORE_CK(cudaMallocAsync((void**)&full6, sizeof(double2) * 6 * (size_t)Mfull, c->stream));
+    cudaError_t ge = tdda::launch_green(g, c->K, c->d, c->tw64[0], c->tw64[1], c->tw64[2], full6, c->green64,
+                                        c->green32, c->stream);
+    cudaError_t fe = cudaFreeAsync(full6, c->stream);
+    TDDA_CORE_CK(ge);
+    TDDA_CORE_CK(fe);
+    TDDA_CORE_CK(cudaStreamSynchronize(c->stream));
+#undef TDDA_CORE_TRY
+#undef TDDA_CORE_CK
+    *out = c;
+    return TDDA_OK;
+}
+
+tdda_status tdda_core_destroy(tdda_core* c) {
+    if (!c) return TDDA_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto& e : c->g64.iter)
+        if (e) cudaGraphExecDestroy(e);
+    for (auto& e : c->g32.iter)
+        if (e) cudaGraphExecDestroy(e);
+    free_all(c->allocs);
+    if (c->hst) cudaFreeHost(c->hst);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return TDDA_OK;
+}
+
+tdda_status tdda_core_info(const tdda_core* c, double* K, int* grid3, double* material_norm) {
+    if (!c) {
+        set_err("null core");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    if (K) *K = c->K;
+    if (grid3) {
+        grid3[0] = c->g.px.M;
+        grid3[1] = c->g.py.M;
+        grid3[2] = c->g.pz.M;
+    }
+    if (material_norm)
+        for (int i = 0; i < c->nmat; i++) {
+            material_norm[2 * i] = c->material[i].real();
+            material_norm[2 * i + 1] = c->material[i].imag();
+        }
+    return TDDA_OK;
+}
+
+tdda_status tdda_core_ldr_inter(const tdda_core* c, double x, double y, double z, double* out12) {
+    if (!c || !out12) {
+        set_err("null argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    cd t[6];
+    ldr_host(c->K, x, y, z, t);
+    for (int l = 0; l < 6; l++) {
+        out12[2 * l] = t[l].real();
+        out12[2 * l + 1] = t[l].imag();
+    }
+    return TDDA_OK;
+}
+
+tdda_status tdda_aproduct(tdda_core* c, int precision, const double* b, double* y, int mem) {
+    if (!c || !b || !y || (precision != TDDA_FP64 && precision != TDDA_FP32_REFINE)) {
+        set_err("invalid argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    TDDA_TRY(set_device(c->device));
+    const size_t n3 = 3 * (size_t)c->N;
+    TDDA_CK(cudaMemcpyAsync(c->vin64, b, sizeof(double2) * n3, kind_in(mem), c->stream));
+    if (precision == TDDA_FP64) {
+        TDDA_CK(aprod<double>(c, tdda::SRC_IN, tdda::SNK_OUT, 1, c->rhs64 + c->max_rhs));
+    } else {
+        TDDA_CK(tdda::launch_to_f32((int)n3, c->vin64, c->vin32, c->stream));
+        TDDA_CK(aprod<float>(c, tdda::SRC_IN, tdda::SNK_OUT, 1, c->rhs32 + c->max_rhs));
+        TDDA_CK(tdda::launch_zero<double>((long long)n3, c->vout64, c->stream));
+        TDDA_CK(tdda::launch_accumulate((int)n3, c->vout32, c->vout64, c->stream));
+    }
+    TDDA_CK(cudaMemcpyAsync(y, c->vout64, sizeof(double2) * n3, kind_out(mem), c->stream));
+    TDDA_CK(cudaStreamSynchronize(c->stream));
+    return TDDA_OK;
+}
+
+tdda_status tdda_model_create(tdda_core* c, const double* nK, double E0, const double* nE0, const double* diel_old,
+                              tdda_model** out) {
+    if (!c || !nK || !nE0 || !diel_old || !out) {
+        set_err("null argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    TDDA_TRY(set_device(c->device));
+    tdda_model* m = new tdda_model_s();
+    m->core = c;
+    for (int j = 0; j < 3; j++) {
+        m->nK[j] = nK[j];
+        m->nE0[j] = nE0[j];
+    }
+    m->E0 = E0;
+    const size_t n3 = 3 * (size_t)c->N;
+    m->diel_old.assign(diel_old, diel_old + n3);
+    double2** v[] = {&m->P, &m->E, &m->al, &m->diel, &m->Ein, &m->r, &m->r0, &m->p, &m->u, &m->t, &m->Ap, &m->At};
+    for (double2** q : v) {
+        tdda_status s = dalloc(m->allocs, q, n3);
+        if (s != TDDA_OK) {
+            tdda_model_destroy(m);
+            return s;
+        }
+    }
+    cudaError_t e = cudaMemsetAsync(m->P, 0, sizeof(double2) * n3, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(m->Ein, 0, sizeof(double2) * n3, c->stream);
+    if (e != cudaSuccess) {
+        tdda_model_destroy(m);
+        return cuda_fail(e, "cudaMemsetAsync");
+    }
+    tdda_status s = model_upload_fields(m, true, true);
+    if (s != TDDA_OK) {
+        tdda_model_destroy(m);
+        return s;
+    }
+    *out = m;
+    return TDDA_OK;
+}
+
+tdda_status tdda_model_destroy(tdda_model* m) {
+    if (!m) return TDDA_OK;
+    cudaSetDevice(m->core->device);
+    cudaStreamSynchronize(m->core->stream);
+    free_all(m->allocs);
+    delete m;
+    return TDDA_OK;
+}
+
+tdda_status tdda_model_update_alpha(tdda_model* m, const double* diel_old) {
+    if (!m || !diel_old) {
+        set_err("null argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    TDDA_TRY(set_device(m->core->device));
+    std::vector<double> keep = m->diel_old;
+    m->diel_old.assign(diel_old, diel_old + 3 * (size_t)m->core->N);
+    tdda_status s = model_upload_fields(m, false, true);
+    if (s != TDDA_OK) m->diel_old = keep;
+    return s;
+}
+
+tdda_status tdda_model_update_alpha_single(tdda_model* m, int idx, double value) {
+    if (!m || idx < 0 || idx >= m->core->N) {
+        set_err("invalid argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    std::vector<double> d = m->diel_old;
+    d[3 * (size_t)idx] = d[3 * (size_t)idx + 1] = d[3 * (size_t)idx + 2] = value;
+    return tdda_model_update_alpha(m, d.data());
+}
+
+tdda_status tdda_model_change_E(tdda_model* m, const double* E, int mem) {
+    if (!m || !E) {
+        set_err("null argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    TDDA_TRY(set_device(m->core->device));
+    TDDA_CK(cudaMemcpyAsync(m->E, E, sizeof(double2) * 3 * (size_t)m->core->N, kind_in(mem), m->core->stream));
+    TDDA_CK(cudaStreamSynchronize(m->core->stream));
+    return TDDA_OK;
+}
+
+tdda_status tdda_model_reset_E(tdda_model* m) {
+    if (!m) {
+        set_err("null model");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    TDDA_TRY(set_device(m->core->device));
+    return model_upload_fields(m, true, false);
+}
+
+tdda_status tdda_model_initialize_P(tdda_model* m, const double* P, int mem) {
+    if (!m || !P) {
+        set_err("null argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    TDDA_TRY(set_device(m->core->device));
+    TDDA_CK(cudaMemcpyAsync(m->P, P, sizeof(double2) * 3 * (size_t)m->core->N, kind_in(mem), m->core->stream));
+    TDDA_CK(cudaStreamSynchronize(m->core->stream));
+    m->P_zero = false;
+    return TDDA_OK;
+}
+
+tdda_status tdda_model_aproduct_with_alb(tdda_model* m, const double* b, double* y, int mem) {
+    if (!m || !b || !y) {
+        set_err("null argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    tdda_core* c = m->core;
+    TDDA_TRY(set_device(c->device));
+    const size_t n3 = 3 * (size_t)c->N;
+    RhsVecs<double> v{};
+    v.p = c->vin64;
+    v.Ap = c->vout64;
+    v.al = m->al;
+    TDDA_CK(cudaMemcpyAsync(c->rhs64 + c->max_rhs, &v, sizeof(v), cudaMemcpyHostToDevice, c->stream));
+    TDDA_CK(cudaMemcpyAsync(c->vin64, b, sizeof(double2) * n3, kind_in(mem), c->stream));
+    TDDA_CK(aprod<double>(c, tdda::SRC_IN, tdda::SNK_ALB, 1, c->rhs64 + c->max_rhs));
+    TDDA_CK(cudaMemcpyAsync(y, c->vout64, sizeof(double2) * n3, kind_out(mem), c->stream));
+    v.al = nullptr;
+    TDDA_CK(cudaMemcpyAsync(c->rhs64 + c->max_rhs, &v, sizeof(v), cudaMemcpyHostToDevice, c->stream));
+    TDDA_CK(cudaStreamSynchronize(c->stream));
+    return TDDA_OK;
+}
+
+tdda_status tdda_solve_batch(tdda_model* const* ms, int n, int precision, int max_it, double max_err,
+                             tdda_solve_info* infos) {
+    g_err.clear();
+    TDDA_TRY(check_batch(ms, n));
+    if (!(max_err >= 0) || (precision != TDDA_FP64 && precision != TDDA_FP32_REFINE)) {
+        set_err("invalid tolerance or precision");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    TDDA_TRY(set_device(ms[0]->core->device));
+    if (precision == TDDA_FP64) return solve_fp64(ms, n, max_it, max_err, infos);
+    return solve_mixed(ms, n, max_it, max_err, infos);
+}
+
+tdda_status tdda_model_bicgstab(tdda_model* m, int max_it, double max_err, tdda_solve_info* info) {
+    return tdda_solve_batch(&m, 1, TDDA_FP64, max_it, max_err, info);
+}
+
+tdda_status tdda_model_solve_mixed(tdda_model* m, int max_it, double max_err, tdda_solve_info* info) {
+    return tdda_solve_batch(&m, 1, TDDA_FP32_REFINE, max_it, max_err, info);
+}
+
+tdda_status tdda_model_update_E_in_structure(tdda_model* m) {
+    if (!m) {
+        set_err("null model");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    TDDA_TRY(set_device(m->core->device));
+    TDDA_CK(tdda::launch_einternal(3 * m->core->N, m->al, m->P, m->diel, m->Ein, m->core->stream));
+    TDDA_CK(cudaStreamSynchronize(m->core->stream));
+    return TDDA_OK;
+}
+
+tdda_status tdda_model_get(const tdda_model* m, int field, double* out, int mem) {
+    if (!m || !out) {
+        set_err("null argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    const double2* src = field == TDDA_FIELD_P ? m->P
+                         : field == TDDA_FIELD_E ? m->E
+                         : field == TDDA_FIELD_AL ? m->al
+                         : field == TDDA_FIELD_DIEL ? m->diel
+                         : field == TDDA_FIELD_EINTERNAL ? m->Ein
+                                                         : nullptr;
+    if (!src) {
+        set_err("unknown field %d", field);
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    TDDA_TRY(set_device(m->core->device));
+    TDDA_CK(cudaMemcpyAsync(out, src, sizeof(double2) * 3 * (size_t)m->core->N, kind_out(mem), m->core->stream));
+    TDDA_CK(cudaStreamSynchronize(m->core->stream));
+    return TDDA_OK;
+}
+
+int tdda_model_iterations(const tdda_model* m) { return m ? m->ITERATION : -1; }
+
+tdda_status tdda_fft3d(double* data, int n0, int n1, int n2, int sign) {
+    AxisPlan p[3];
+    int n[3] = {n0, n1, n2};
+    if (!data || (sign != -1 && sign != 1)) {
+        set_err("invalid argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    for (int a = 0; a < 3; a++)
+        if (n[a] < 1 || !make_plan(n[a], &p[a]) || n[a] > 2048) {
+            set_err("FFT length %d is not supported", n[a]);
+            return TDDA_ERR_UNSUPPORTED;
+        }
+    std::vector<void*> tmp;
+    double2* tw[3];
+    for (int a = 0; a < 3; a++) {
+        std::vector<double2> w64;
+        std::vector<float2> w32;
+        twiddles(n[a], w64, w32);
+        tdda_status s = dalloc(tmp, &tw[a], (size_t)n[a]);
+        if (s != TDDA_OK) {
+            free_all(tmp);
+            return s;
+        }
+        cudaMemcpy(tw[a], w64.data(), sizeof(double2) * n[a], cudaMemcpyHostToDevice);
+    }
+    cudaError_t e = tdda::configure_kernels();
+    if (e == cudaSuccess) e = tdda::launch_fft3d_f64((double2*)data, p[0], p[1], p[2], tw[0], tw[1], tw[2], sign, 0);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    free_all(tmp);
+    if (e != cudaSuccess) return cuda_fail(e, "tdda_fft3d");
+    return TDDA_OK;
+}
+
+}  // extern "C"

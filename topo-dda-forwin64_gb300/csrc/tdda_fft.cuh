@@ -1,0 +1,249 @@
+// tdda_fft.cuh -- complex helpers and the shared-memory Stockham FFT used by
+// every pass of the A-product (sm_103a; float and double instantiations).
+//
+// A pass kernel stages a tile of L independent lines of length M in shared
+// memory (line l at s + l*ls, element m at + m*ms) and calls smem_fft().  Each
+// radix-R stage maps butterfly j of every line (Stockham autosort, span Ns):
+//     k = j mod Ns,  v[r] = x[j + r M/R] * W^(r k M/(Ns R)),  V = DFT_R(v),
+//     y[(j-k) R + k + q Ns] = V[q]
+// from one shared buffer to the other (ping-pong), one barrier per stage.
+// The radix-2/3/4/5/7/8 butterflies are written from the DFT definition; the
+// twiddle table W[m] = exp(-2 pi i m / M) is computed on the host in extended
+// precision and staged into shared memory by the kernel.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace tdda {
+
+template <typename T> struct cplx_t;
+template <> struct cplx_t<float> { typedef float2 type; };
+template <> struct cplx_t<double> { typedef double2 type; };
+
+template <typename T> using cx = typename cplx_t<T>::type;
+
+template <typename T> __host__ __device__ __forceinline__ cx<T> mk(T re, T im) {
+    cx<T> c;
+    c.x = re;
+    c.y = im;
+    return c;
+}
+template <typename T> __device__ __forceinline__ cx<T> cadd(cx<T> a, cx<T> b) { return mk<T>(a.x + b.x, a.y + b.y); }
+template <typename T> __device__ __forceinline__ cx<T> csub(cx<T> a, cx<T> b) { return mk<T>(a.x - b.x, a.y - b.y); }
+template <typename T> __device__ __forceinline__ cx<T> cmul(cx<T> a, cx<T> b) {
+    return mk<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// conj(a) * b
+template <typename T> __device__ __forceinline__ cx<T> cmulc(cx<T> a, cx<T> b) {
+    return mk<T>(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+template <typename T> __device__ __forceinline__ cx<T> cscale(cx<T> a, T s) { return mk<T>(a.x * s, a.y * s); }
+// multiply by (sign * i): sign = -1 gives -i (forward), +1 gives +i (inverse)
+template <int SIGN, typename T> __device__ __forceinline__ cx<T> cmul_i(cx<T> a) {
+    return SIGN < 0 ? mk<T>(a.y, -a.x) : mk<T>(-a.y, a.x);
+}
+template <typename T> __device__ __forceinline__ cx<T> czero() { return mk<T>(T(0), T(0)); }
+
+// Up to 8 radix stages per axis (M <= 8^8 is far beyond any lattice here).
+constexpr int kMaxStages = 8;
+
+struct AxisPlan {
+    int M;                  // FFT length
+    int nstages;
+    int radix[kMaxStages];  // applied first to last
+    int rmin;               // smallest radix (bounds butterflies per stage)
+};
+
+// ---------------------------------------------------------------- butterflies
+// In-place DFT of v[0..R-1]: V[q] = sum_r v[r] exp(SIGN 2 pi i r q / R).
+template <int R, int SIGN, typename T> struct Bfly;
+
+template <int SIGN, typename T> struct Bfly<2, SIGN, T> {
+    static __device__ __forceinline__ void run(cx<T>* v) {
+        cx<T> a = v[0], b = v[1];
+        v[0] = cadd<T>(a, b);
+        v[1] = csub<T>(a, b);
+    }
+};
+
+template <int SIGN, typename T> struct Bfly<4, SIGN, T> {
+    static __device__ __forceinline__ void run(cx<T>* v) {
+        cx<T> t0 = cadd<T>(v[0], v[2]);
+        cx<T> t1 = csub<T>(v[0], v[2]);
+        cx<T> t2 = cadd<T>(v[1], v[3]);
+        cx<T> t3 = cmul_i<SIGN, T>(csub<T>(v[1], v[3]));
+        v[0] = cadd<T>(t0, t2);
+        v[2] = csub<T>(t0, t2);
+        v[1] = cadd<T>(t1, t3);
+        v[3] = csub<T>(t1, t3);
+    }
+};
+
+template <int SIGN, typename T> struct Bfly<8, SIGN, T> {
+    // split into even / odd 4-point DFTs, combine with W8^q
+    static __device__ __forceinline__ void run(cx<T>* v) {
+        const T h = T(0.70710678118654752440084436210484904);  // sqrt(1/2)
+        cx<T> e[4] = {v[0], v[2], v[4], v[6]};
+        cx<T> o[4] = {v[1], v[3], v[5], v[7]};
+        Bfly<4, SIGN, T>::run(e);
+        Bfly<4, SIGN, T>::run(o);
+        // W8^1 = (1 + SIGN i) sqrt(1/2), W8^2 = SIGN i, W8^3 = (-1 + SIGN i) sqrt(1/2)
+        cx<T> o1 = mk<T>((o[1].x - T(SIGN) * o[1].y) * h, (o[1].y + T(SIGN) * o[1].x) * h);
+        cx<T> o2 = cmul_i<SIGN, T>(o[2]);
+        cx<T> o3 = mk<T>((-o[3].x - T(SIGN) * o[3].y) * h, (-o[3].y + T(SIGN) * o[3].x) * h);
+        v[0] = cadd<T>(e[0], o[0]);
+        v[4] = csub<T>(e[0], o[0]);
+        v[1] = cadd<T>(e[1], o1);
+        v[5] = csub<T>(e[1], o1);
+        v[2] = cadd<T>(e[2], o2);
+        v[6] = csub<T>(e[2], o2);
+        v[3] = cadd<T>(e[3], o3);
+        v[7] = csub<T>(e[3], o3);
+    }
+};
+
+// odd prime radices: V[q] = v0 + sum_{r=1}^{(R-1)/2} [ c_{rq} (v_r + v_{R-r}) + SIGN i s_{rq} (v_r - v_{R-r}) ]
+// with c_m = cos(2 pi m / R), s_m = sin(2 pi m / R)
+template <int R> struct OddConst;
+template <> struct OddConst<3> {
+    static __device__ __forceinline__ double c(int m) { return m % 3 == 0 ? 1.0 : -0.5; }
+    static __device__ __forceinline__ double s(int m) {
+        int k = m % 3;
+        return k == 0 ? 0.0 : (k == 1 ? 0.86602540378443864676372317075293618 : -0.86602540378443864676372317075293618);
+    }
+};
+template <> struct OddConst<5> {
+    static __device__ __forceinline__ double c(int m) {
+        int k = m % 5;
+        return k == 0 ? 1.0 : (k == 1 || k == 4) ? 0.30901699437494742410229341718281906 : -0.80901699437494742410229341718281906;
+    }
+    static __device__ __forceinline__ double s(int m) {
+        int k = m % 5;
+        const double s1 = 0.95105651629515357211643933337938214, s2 = 0.58778525229247312916870595463907277;
+        return k == 0 ? 0.0 : k == 1 ? s1 : k == 2 ? s2 : k == 3 ? -s2 : -s1;
+    }
+};
+template <> struct OddConst<7> {
+    static __device__ __forceinline__ double c(int m) {
+        int k = m % 7;
+        const double c1 = 0.62348980185873353052500488400423981, c2 = -0.22252093395631440428890256449679476,
+                     c3 = -0.90096886790241912623610231950744505;
+        return k == 0 ? 1.0 : (k == 1 || k == 6) ? c1 : (k == 2 || k == 5) ? c2 : c3;
+    }
+    static __device__ __forceinline__ double s(int m) {
+        int k = m % 7;
+        const double s1 = 0.78183148246802980870844452667405775, s2 = 0.97492791218182360701813168299393122,
+                     s3 = 0.43388373911755812047576833284835875;
+        return k == 0 ? 0.0 : k == 1 ? s1 : k == 2 ? s2 : k == 3 ? s3 : k == 4 ? -s3 : k == 5 ? -s2 : -s1;
+    }
+};
+
+template <int R, int SIGN, typename T> struct BflyOdd {
+    static __device__ __forceinline__ void run(cx<T>* v) {
+        constexpr int H = (R - 1) / 2;
+        cx<T> sp[H], sm[H];
+#pragma unroll
+        for (int r = 1; r <= H; r++) {
+            sp[r - 1] = cadd<T>(v[r], v[R - r]);
+            sm[r - 1] = csub<T>(v[r], v[R - r]);
+        }
+        cx<T> out[R];
+        cx<T> s0 = v[0];
+#pragma unroll
+        for (int r = 0; r < H; r++) s0 = cadd<T>(s0, sp[r]);
+        out[0] = s0;
+#pragma unroll
+        for (int q = 1; q <= H; q++) {
+            cx<T> re = v[0];
+            cx<T> im = czero<T>();
+#pragma unroll
+            for (int r = 1; r <= H; r++) {
+                const T c = T(OddConst<R>::c(r * q));
+                const T s = T(OddConst<R>::s(r * q));
+                re = mk<T>(re.x + c * sp[r - 1].x, re.y + c * sp[r - 1].y);
+                im = mk<T>(im.x + s * sm[r - 1].x, im.y + s * sm[r - 1].y);
+            }
+            cx<T> rot = cmul_i<SIGN, T>(im);  // SIGN i * im
+            out[q] = cadd<T>(re, rot);
+            out[R - q] = csub<T>(re, rot);
+        }
+#pragma unroll
+        for (int q = 0; q < R; q++) v[q] = out[q];
+    }
+};
+template <int SIGN, typename T> struct Bfly<3, SIGN, T> : BflyOdd<3, SIGN, T> {};
+template <int SIGN, typename T> struct Bfly<5, SIGN, T> : BflyOdd<5, SIGN, T> {};
+template <int SIGN, typename T> struct Bfly<7, SIGN, T> : BflyOdd<7, SIGN, T> {};
+
+// ----------------------------------------------------------------- one stage
+// Out-of-place (ping-pong) stage: reads x, writes y, then a barrier.  Each
+// thread loops over butterflies, holding one radix-R butterfly in registers.
+// nvalid: inputs with index >= nvalid are zero (first stage only); nout:
+// outputs with index >= nout are not stored (last stage only).
+template <int R, int SIGN, typename T>
+__device__ __forceinline__ void fft_stage(const cx<T>* __restrict__ x, cx<T>* __restrict__ y, int L, int ls, int ms,
+                                          int M, int Ns, const cx<T>* tw, int nvalid, int nout) {
+    const int m = M / R;
+    const int nb = L * m;
+    const int twstep = M / (Ns * R);
+    for (int w = threadIdx.x; w < nb; w += blockDim.x) {
+        const int j = w / L;
+        const int l = w - j * L;
+        const cx<T>* xb = x + l * ls;
+        cx<T> v[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int idx = j + r * m;
+            v[r] = idx < nvalid ? xb[idx * ms] : czero<T>();
+        }
+        const int k = j % Ns;
+        if (Ns > 1) {
+#pragma unroll
+            for (int r = 1; r < R; r++) {
+                cx<T> t = tw[r * k * twstep];
+                if (SIGN > 0) t.y = -t.y;
+                v[r] = cmul<T>(v[r], t);
+            }
+        }
+        Bfly<R, SIGN, T>::run(v);
+        cx<T>* yb = y + l * ls;
+        const int ob = (j - k) * R + k;
+#pragma unroll
+        for (int q = 0; q < R; q++) {
+            const int idx = ob + q * Ns;
+            if (idx < nout) yb[idx * ms] = v[q];
+        }
+    }
+    __syncthreads();
+}
+
+// Full transform of the L lines held in buffer a (b is scratch of the same
+// shape).  SIGN = -1 forward, +1 inverse; unnormalised.  Returns the buffer
+// that holds the result.
+template <int SIGN, typename T>
+__device__ __forceinline__ cx<T>* smem_fft(cx<T>* a, cx<T>* b, int L, int ls, int ms, const AxisPlan& ap,
+                                           const cx<T>* tw, int nvalid, int nout) {
+    int Ns = 1;
+    const int M = ap.M;
+    for (int st = 0; st < ap.nstages; st++) {
+        const int R = ap.radix[st];
+        const int nv = st == 0 ? nvalid : M;
+        const int no = st == ap.nstages - 1 ? nout : M;
+        switch (R) {
+            case 2: fft_stage<2, SIGN, T>(a, b, L, ls, ms, M, Ns, tw, nv, no); break;
+            case 3: fft_stage<3, SIGN, T>(a, b, L, ls, ms, M, Ns, tw, nv, no); break;
+            case 4: fft_stage<4, SIGN, T>(a, b, L, ls, ms, M, Ns, tw, nv, no); break;
+            case 5: fft_stage<5, SIGN, T>(a, b, L, ls, ms, M, Ns, tw, nv, no); break;
+            case 7: fft_stage<7, SIGN, T>(a, b, L, ls, ms, M, Ns, tw, nv, no); break;
+            default: fft_stage<8, SIGN, T>(a, b, L, ls, ms, M, Ns, tw, nv, no); break;
+        }
+        Ns *= R;
+        cx<T>* t = a;
+        a = b;
+        b = t;
+    }
+    return a;
+}
+
+}  // namespace tdda

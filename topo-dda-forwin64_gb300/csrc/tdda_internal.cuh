@@ -1,0 +1,135 @@
+// tdda_internal.cuh -- device data layout and kernel launchers shared by the
+// C-ABI implementation (tdda_api.cu) and the kernels (tdda_kernels.cu).
+//
+// HBM layout of one core (one lattice at one wavelength):
+//   cellmap   int32 [Nx][Ny][Nz]          dipole index of each cell, -1 if empty
+//   green64   double2 [Hy][Hz][Hx][6]     folded Green spectrum / (Mx My Mz)
+//   green32   float2  [Hy][Hz][Hx][6]     the same rounded to FP32 (mixed path)
+//   tw{x,y,z} double2/float2 [M]          exp(-2 pi i m / M)
+//   grid      cx<T> [nrhs][3][Nx][My][Mz]  FFT work grid (x kept to the lattice)
+// with H = M/2 + 1 per axis (the tensor components are even or odd in each
+// axis, so the spectrum at M-k equals +/- the spectrum at k).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "tdda_fft.cuh"
+
+namespace tdda {
+
+struct Geom {
+    int Nx, Ny, Nz;    // lattice box
+    int N;             // dipoles
+    AxisPlan px, py, pz;
+    int Hx, Hy, Hz;    // folded Green extents
+    long long sy, sx, sc, sb;  // grid strides (y, x, component, rhs) in elements
+};
+
+// solver status values (mirrored in include/tdda.h)
+enum : int { ST_RUNNING = 0, ST_CONVERGED = 1, ST_BREAKDOWN = 2, ST_MAXITER = 3, ST_NAN = 4 };
+
+// FP64 scalars of one BiCGSTAB right-hand side (DDAModel.cpp:153-156, 186-255)
+struct SolveState {
+    double2 alpha, beta, zeta;
+    double2 rho;       // r0 . r      (current residual)
+    double2 rho_prev;  // r0 . rl     (previous residual)
+    double rnorm2;     // |r|^2
+    double Enorm;      // |E|
+    double tol;
+    double error;      // |r| / |E| at the end
+    int status;
+    int it;            // completed loop iterations
+    int max_it;
+    int iterations;    // ITERATION as the reference reports it
+};
+
+// per right-hand side: the vectors of one solve (AoS [x,y,z] per dipole)
+template <typename T> struct RhsVecs {
+    cx<T>* P;
+    cx<T>* E;
+    cx<T>* r;
+    cx<T>* r0;
+    cx<T>* p;
+    cx<T>* u;
+    cx<T>* t;
+    cx<T>* Ap;
+    cx<T>* At;
+    const cx<T>* al;
+    SolveState* st;
+    double* part;        // reduction partials, kPartSlots x maxblk doubles
+    unsigned int* cnt;   // last-block counters, kCounters
+};
+constexpr int kPartSlots = 4;
+constexpr int kCounters = 8;
+
+// what the first z-pass transforms (the fused vector update of the solver)
+enum SrcMode : int {
+    SRC_IN = 0,      // v = in
+    SRC_PUPD = 1,    // p = r + beta (p - u)         (DDAModel.cpp:219)
+    SRC_TUPD = 2,    // t = r - alpha Ap             (DDAModel.cpp:222)
+    SRC_P = 3,       // v = P                        (DDAModel.cpp:164)
+};
+// what the last z-pass does with A v
+enum SnkMode : int {
+    SNK_OUT = 0,     // out = A v
+    SNK_ALB = 1,     // out = A v + al v             (DDAModel.cpp:577-586)
+    SNK_AP = 2,      // Ap = A p + al p, alpha = (r0.r) / (r0.Ap)
+    SNK_AT = 3,      // At = A t + al t, zeta = (At.t) / (At.At)
+    SNK_RES = 4,     // r = r0 = p = E - (A P + al P), rho = r0.r   (DDAModel.cpp:164-168)
+};
+
+// -------------------------------------------------------------- launchers
+// All launchers enqueue on `stream` and return cudaGetLastError().
+
+// Green spectrum: LDR tensor on the full grid, 3-D forward FFT, fold, scale.
+cudaError_t launch_green(const Geom& g, double K, double d, const double2* tw64x, const double2* tw64y,
+                         const double2* tw64z, double2* full6 /* 6*Mx*My*Mz scratch */, double2* green64,
+                         float2* green32, cudaStream_t stream);
+
+// One A-product over nrhs right-hand sides.  rhs[] lives in device memory.
+// For SRC_IN with SNK_OUT / SNK_ALB the vectors used are rhs[b].p (input)
+// and rhs[b].Ap (output); SNK_RES reads P and E and writes r, r0, p.
+template <typename T>
+cudaError_t launch_aproduct(const Geom& g, int src, int snk, int nrhs, const RhsVecs<T>* rhs,
+                            const cx<T>* green, const cx<T>* twx, const cx<T>* twy, const cx<T>* twz,
+                            const int* cellmap, cx<T>* grid, cudaStream_t stream);
+
+// u = zeta Ap; z = zeta r - alpha u; P += alpha p + z; r = t - zeta At;
+// rho_prev = rho; rho = r0.r; convergence / breakdown / iteration limit;
+// beta for the next iteration.  is_init marks the step after the three
+// initial products (DDAModel.cpp:177-182), which checks no convergence.
+template <typename T>
+cudaError_t launch_update(const Geom& g, int nrhs, const RhsVecs<T>* rhs, int is_init, cudaStream_t stream);
+
+// |E| of every right-hand side into st->Enorm, and reset of the state.
+template <typename T>
+cudaError_t launch_solve_begin(const Geom& g, int nrhs, const RhsVecs<T>* rhs, cudaStream_t stream);
+
+// When P = 0 the initial residual is E: r = r0 = p = E, rho = r0.r.
+template <typename T>
+cudaError_t launch_residual_is_rhs(const Geom& g, int nrhs, const RhsVecs<T>* rhs, cudaStream_t stream);
+
+// Einternal = al P / ((2 + eps) / 3)       (DDAModel.cpp:567-575)
+cudaError_t launch_einternal(int n3, const double2* al, const double2* P, const double2* diel, double2* Ein,
+                             cudaStream_t stream);
+
+// mixed precision helpers: dst32 = (float) src64 ; P64 += (double) d32 ; zero
+cudaError_t launch_to_f32(int n3, const double2* src, float2* dst, cudaStream_t stream);
+cudaError_t launch_accumulate(int n3, const float2* d, double2* P, cudaStream_t stream);
+template <typename T> cudaError_t launch_zero(long long n, cx<T>* v, cudaStream_t stream);
+
+// generic in-place 3-D FFT of a contiguous (n0, n1, n2) double2 array
+cudaError_t launch_fft3d_f64(double2* data, const AxisPlan& p0, const AxisPlan& p1, const AxisPlan& p2,
+                             const double2* tw0, const double2* tw1, const double2* tw2, int sign,
+                             cudaStream_t stream);
+
+int max_blocks_per_rhs(const Geom& g);
+// largest dynamic shared memory any pass kernel needs for this geometry
+size_t max_pass_smem(const Geom& g);
+constexpr size_t kMaxPassSmem = 200 * 1024;
+
+// raise the dynamic shared-memory limit of every pass kernel (once per device,
+// outside any stream capture)
+cudaError_t configure_kernels();
+
+}  // namespace tdda

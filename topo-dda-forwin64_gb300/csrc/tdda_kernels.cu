@@ -1,0 +1,826 @@
+// tdda_kernels.cu -- sm_103a kernels of the DDA solve path.
+//
+//   K0  green      LDR tensor on the padded grid (AProductCore.cpp:53-194,
+//                  588-623), forward 3-D FFT, fold to the octant, scale 1/M
+//   K1  zfwd       gather the dipole vector onto the grid (+ the fused
+//                  BiCGSTAB vector update), z-axis forward FFT, pruned input
+//   K2  ypass      y-axis forward FFT over the x < Nx planes, pruned input
+//   K3  xpass      x-axis forward FFT, symmetric 3x3 spectral product with
+//                  the six Green components (kernel.cu:74-85), inverse x FFT,
+//                  pruned output
+//   K4  ypass      y-axis inverse FFT, pruned output
+//   K5  zinv       z-axis inverse FFT, pruned output, scatter to dipoles,
+//                  + al*v and the fused dot products of the solver
+//   K6  update     BiCGSTAB vector update and dots (DDAModel.cpp:225-232)
+// The pass structure replaces the reference's host scatter, H2D copy, six
+// cuFFT calls, three element-wise kernels and D2H copy per product
+// (AProductCore.cpp:697-758).  All reductions are deterministic: fixed
+// per-block trees and a fixed-order sum of block partials by the last block.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "tdda_internal.cuh"
+
+namespace tdda {
+
+namespace {
+
+constexpr int kNT = 256;  // threads of every pass and vector kernel
+
+__host__ __device__ inline int iclamp(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+__host__ __device__ inline int floor_pow2(int v) {
+    int p = 1;
+    while (p * 2 <= v) p *= 2;
+    return p;
+}
+
+__host__ __device__ inline int pad_odd(int m) { return (m % 2 == 0) ? m + 1 : m; }
+
+// Tiles are sized so that the two ping-pong buffers of a block stay within
+// kSmemBudget (two resident blocks per SM at the largest grids).
+constexpr int kSmemBudget = 96 * 1024;
+
+// lines of a z-pass tile: 3 components x LZ (x, y) columns
+template <typename T> __host__ __device__ inline int z_lines(const AxisPlan& pz) {
+    const int per = 2 * 3 * pad_odd(pz.M) * (int)sizeof(cx<T>);
+    return iclamp((kSmemBudget - pz.M * (int)sizeof(cx<T>)) / per, 1, 16);
+}
+// z-tile of a y-pass
+template <typename T> __host__ __device__ inline int y_tile(const AxisPlan& py) {
+    const int per = 2 * py.M * (int)sizeof(cx<T>);
+    return iclamp(floor_pow2((kSmemBudget - py.M * (int)sizeof(cx<T>)) / per), 1, 16);
+}
+// z-tile of the x-pass (3 components per z)
+template <typename T> __host__ __device__ inline int x_tile(const AxisPlan& px) {
+    const int per = 2 * 3 * px.M * (int)sizeof(cx<T>);
+    return iclamp(floor_pow2((kSmemBudget - px.M * (int)sizeof(cx<T>)) / per), 1, 16);
+}
+// lines of a generic row FFT and z-tile of a generic column FFT (FP64)
+__host__ __device__ inline int row_lines(const AxisPlan& p) {
+    return iclamp((kSmemBudget - p.M * 16) / (2 * pad_odd(p.M) * 16), 1, 32);
+}
+__host__ __device__ inline int col_tile(const AxisPlan& p) {
+    return iclamp(floor_pow2((kSmemBudget - p.M * 16) / (2 * p.M * 16)), 1, 16);
+}
+
+template <typename T> __device__ __forceinline__ cx<T> ld(const cx<T>* p) { return *p; }
+
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
+    // Smith's algorithm (R. L. Smith, CACM 5(8), 1962)
+    if (fabs(b.x) >= fabs(b.y)) {
+        double r = b.y / b.x, den = b.x + b.y * r;
+        return make_double2((a.x + a.y * r) / den, (a.y - a.x * r) / den);
+    }
+    double r = b.x / b.y, den = b.x * r + b.y;
+    return make_double2((a.x * r + a.y) / den, (a.y * r - a.x) / den);
+}
+__device__ __forceinline__ double2 dmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ bool finite2(double2 a) { return isfinite(a.x) && isfinite(a.y); }
+
+template <typename T> __device__ __forceinline__ cx<T> from_d(double2 a) { return mk<T>(T(a.x), T(a.y)); }
+
+// ------------------------------------------------------------ reductions
+// Block-wide sum of NV doubles with a fixed tree; the result is valid in
+// thread 0.  sred must hold NV * 32 doubles.
+template <int NV> __device__ __forceinline__ void block_sum(double (&v)[NV], double* sred) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++)
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) sred[k * 32 + warp] = v[k];
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            v[k] = lane < nw ? sred[k * 32 + lane] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+        }
+    }
+}
+
+// Publish this block's partials; the last block of the grid (for this
+// right-hand side) sums all partials in block order and returns true in
+// every thread of that block, with the totals in tot (valid in thread 0).
+template <int NV>
+__device__ bool last_block_total(double (&v)[NV], double* part, int nblk, int bid, unsigned int* cnt, double* sred,
+                                 double (&tot)[NV]) {
+    __shared__ int s_last;
+    block_sum<NV>(v, sred);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) part[k * nblk + bid] = v[k];
+        __threadfence();
+        unsigned int prev = atomicAdd(cnt, 1u);
+        s_last = (prev == (unsigned int)(nblk - 1));
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        double a = 0.0;
+        for (int i = threadIdx.x; i < nblk; i += blockDim.x) a += __ldcg(part + k * nblk + i);
+        tot[k] = a;
+    }
+    block_sum<NV>(tot, sred);
+    if (threadIdx.x == 0) *cnt = 0u;
+    return true;
+}
+
+__device__ __forceinline__ bool rhs_done(const SolveState* st) {
+    return st != nullptr && *((volatile const int*)&st->status) != ST_RUNNING;
+}
+
+template <typename T> __device__ __forceinline__ void stage_tw(cx<T>* stw, const cx<T>* tw, int M) {
+    for (int i = threadIdx.x; i < M; i += blockDim.x) stw[i] = tw[i];
+}
+
+// ================================================================ K1 zfwd
+template <typename T, int SRC>
+__global__ void __launch_bounds__(kNT) k_zfwd(Geom g, const RhsVecs<T>* __restrict__ rhs,
+                                              const cx<T>* __restrict__ twz, const int* __restrict__ cellmap,
+                                              cx<T>* __restrict__ grid) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int b = blockIdx.y;
+    const RhsVecs<T> R = rhs[b];
+    if (rhs_done(R.st)) return;
+    const int Mz = g.pz.M, Nz = g.Nz;
+    const int LZ = z_lines<T>(g.pz), MzP = pad_odd(Mz);
+    cx<T>* stw = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* s = stw + Mz;
+    cx<T>* s2 = s + 3 * LZ * MzP;
+    stage_tw<T>(stw, twz, Mz);
+    const int nlines = g.Nx * g.Ny;
+    const int l0 = blockIdx.x * LZ;
+    const int nl = min(LZ, nlines - l0);
+
+    cx<T> beta, alpha;
+    if (SRC == SRC_PUPD) beta = from_d<T>(R.st->beta);
+    if (SRC == SRC_TUPD) alpha = from_d<T>(R.st->alpha);
+    const cx<T>* src = SRC == SRC_IN ? R.p : R.P;
+    for (int e = threadIdx.x; e < nl * Nz; e += blockDim.x) {
+        const int line = e / Nz, z = e - (e / Nz) * Nz;
+        const int i = cellmap[(long long)(l0 + line) * Nz + z];
+        cx<T> v[3];
+        if (i >= 0) {
+            const long long o = 3LL * i;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                if (SRC == SRC_PUPD) {
+                    cx<T> pc = R.p[o + c], uc = R.u[o + c], rc = R.r[o + c];
+                    v[c] = cadd<T>(rc, cmul<T>(beta, csub<T>(pc, uc)));
+                    R.p[o + c] = v[c];
+                } else if (SRC == SRC_TUPD) {
+                    cx<T> rc = R.r[o + c], ac = R.Ap[o + c];
+                    v[c] = csub<T>(rc, cmul<T>(alpha, ac));
+                    R.t[o + c] = v[c];
+                } else {
+                    v[c] = src[o + c];
+                }
+            }
+        } else {
+            v[0] = v[1] = v[2] = czero<T>();
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) s[(c * LZ + line) * MzP + z] = v[c];
+    }
+    __syncthreads();
+    const cx<T>* res = smem_fft<-1, T>(s, s2, 3 * LZ, MzP, 1, g.pz, stw, Nz, Mz);
+    cx<T>* gb = grid + (long long)b * g.sb;
+    for (int e = threadIdx.x; e < 3 * nl * Mz; e += blockDim.x) {
+        const int cl = e / Mz, z = e - (e / Mz) * Mz;
+        const int c = cl / nl, line = cl - (cl / nl) * nl;
+        const int l = l0 + line, x = l / g.Ny, y = l - (l / g.Ny) * g.Ny;
+        gb[c * g.sc + x * g.sx + y * g.sy + z] = res[(c * LZ + line) * MzP + z];
+    }
+}
+
+// ================================================================ K2/K4 ypass
+template <typename T, int SIGN>
+__global__ void __launch_bounds__(kNT) k_ypass(Geom g, const RhsVecs<T>* __restrict__ rhs,
+                                               const cx<T>* __restrict__ twy, cx<T>* __restrict__ grid) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int b = blockIdx.z;
+    if (rhs_done(rhs[b].st)) return;
+    const int My = g.py.M, Mz = g.pz.M;
+    const int ZT = y_tile<T>(g.py);
+    const int nzt = (Mz + ZT - 1) / ZT;
+    const int x = blockIdx.x / nzt, z0 = (blockIdx.x - x * nzt) * ZT;
+    const int c = blockIdx.y;
+    const int zn = min(ZT, Mz - z0);
+    cx<T>* stw = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* s = stw + My;
+    cx<T>* s2 = s + My * ZT;
+    stage_tw<T>(stw, twy, My);
+    cx<T>* gp = grid + (long long)b * g.sb + c * g.sc + (long long)x * g.sx + z0;
+    const int nin = SIGN < 0 ? g.Ny : My;
+    const int nout = SIGN < 0 ? My : g.Ny;
+    for (int e = threadIdx.x; e < nin * ZT; e += blockDim.x) {
+        const int y = e / ZT, zl = e - (e / ZT) * ZT;
+        if (zl < zn) s[y * ZT + zl] = gp[(long long)y * g.sy + zl];
+    }
+    __syncthreads();
+    const cx<T>* res = smem_fft<SIGN, T>(s, s2, ZT, 1, ZT, g.py, stw, nin, nout);
+    for (int e = threadIdx.x; e < nout * ZT; e += blockDim.x) {
+        const int y = e / ZT, zl = e - (e / ZT) * ZT;
+        if (zl < zn) gp[(long long)y * g.sy + zl] = res[y * ZT + zl];
+    }
+}
+
+// ================================================================ K3 xpass
+// folding of a spectral index and the parity of each tensor component:
+// xx, yy, zz even in all axes; xy odd in x,y; xz odd in x,z; yz odd in y,z
+__device__ __forceinline__ int fold(int k, int M) { return 2 * k > M ? M - k : k; }
+
+template <typename T>
+__global__ void __launch_bounds__(kNT) k_xpass(Geom g, const RhsVecs<T>* __restrict__ rhs,
+                                                const cx<T>* __restrict__ green, const cx<T>* __restrict__ twx,
+                                                cx<T>* __restrict__ grid) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int b = blockIdx.y;
+    if (rhs_done(rhs[b].st)) return;
+    const int Mx = g.px.M, My = g.py.M, Mz = g.pz.M, Nx = g.Nx;
+    const int ZT = x_tile<T>(g.px);
+    const int nzt = (Mz + ZT - 1) / ZT;
+    const int y = blockIdx.x / nzt, z0 = (blockIdx.x - y * nzt) * ZT;
+    const int zn = min(ZT, Mz - z0);
+    const int W = 3 * ZT;  // elements per x in shared memory
+    cx<T>* stw = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* s = stw + Mx;
+    cx<T>* s2 = s + Mx * W;
+    stage_tw<T>(stw, twx, Mx);
+    cx<T>* gp = grid + (long long)b * g.sb + (long long)y * g.sy + z0;
+    for (int e = threadIdx.x; e < Nx * W; e += blockDim.x) {
+        const int x = e / W, r = e - (e / W) * W;
+        const int c = r / ZT, zl = r - (r / ZT) * ZT;
+        if (zl < zn) s[e] = gp[c * g.sc + (long long)x * g.sx + zl];
+        else s[e] = czero<T>();
+    }
+    __syncthreads();
+    cx<T>* res = smem_fft<-1, T>(s, s2, W, 1, W, g.px, stw, Nx, Mx);
+
+    // spectral product: C = A b with the symmetric 3x3 Green tensor
+    const int fy = fold(y, My);
+    const bool uy = 2 * y > My;
+    for (int e = threadIdx.x; e < Mx * ZT; e += blockDim.x) {
+        const int kx = e / ZT, zl = e - (e / ZT) * ZT;
+        const int z = z0 + zl;
+        if (zl >= zn) continue;
+        const int fx = fold(kx, Mx), fz = fold(z, Mz);
+        const bool ux = 2 * kx > Mx, uz = 2 * z > Mz;
+        const cx<T>* gg = green + (((long long)fy * g.Hz + fz) * g.Hx + fx) * 6;
+        cx<T> a0 = gg[0], a1 = gg[1], a2 = gg[2], a3 = gg[3], a4 = gg[4], a5 = gg[5];
+        if (ux != uy) a1 = mk<T>(-a1.x, -a1.y);  // xy: odd in x and y
+        if (ux != uz) a2 = mk<T>(-a2.x, -a2.y);  // xz: odd in x and z
+        if (uy != uz) a4 = mk<T>(-a4.x, -a4.y);  // yz: odd in y and z
+        cx<T>* p = res + kx * W + zl;
+        const cx<T> bx = p[0], by = p[ZT], bz = p[2 * ZT];
+        p[0] = cadd<T>(cadd<T>(cmul<T>(a0, bx), cmul<T>(a1, by)), cmul<T>(a2, bz));
+        p[ZT] = cadd<T>(cadd<T>(cmul<T>(a1, bx), cmul<T>(a3, by)), cmul<T>(a4, bz));
+        p[2 * ZT] = cadd<T>(cadd<T>(cmul<T>(a2, bx), cmul<T>(a4, by)), cmul<T>(a5, bz));
+    }
+    __syncthreads();
+    const cx<T>* out = smem_fft<+1, T>(res, res == s ? s2 : s, W, 1, W, g.px, stw, Mx, Nx);
+    for (int e = threadIdx.x; e < Nx * W; e += blockDim.x) {
+        const int x = e / W, r = e - (e / W) * W;
+        const int c = r / ZT, zl = r - (r / ZT) * ZT;
+        if (zl < zn) gp[c * g.sc + (long long)x * g.sx + zl] = out[e];
+    }
+}
+
+// ================================================================ K5 zinv
+template <typename T, int SRC, int SNK>
+__global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restrict__ rhs,
+                                              const cx<T>* __restrict__ twz, const int* __restrict__ cellmap,
+                                              cx<T>* __restrict__ grid) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ double sred[4 * 32];
+    const int b = blockIdx.y;
+    const RhsVecs<T> R = rhs[b];
+    if (rhs_done(R.st)) return;
+    const int Mz = g.pz.M, Nz = g.Nz;
+    const int LZ = z_lines<T>(g.pz), MzP = pad_odd(Mz);
+    cx<T>* stw = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* s = stw + Mz;
+    cx<T>* s2 = s + 3 * LZ * MzP;
+    stage_tw<T>(stw, twz, Mz);
+    const int nlines = g.Nx * g.Ny;
+    const int l0 = blockIdx.x * LZ;
+    const int nl = min(LZ, nlines - l0);
+    const cx<T>* gb = grid + (long long)b * g.sb;
+    for (int e = threadIdx.x; e < 3 * nl * Mz; e += blockDim.x) {
+        const int cl = e / Mz, z = e - (e / Mz) * Mz;
+        const int c = cl / nl, line = cl - (cl / nl) * nl;
+        const int l = l0 + line, x = l / g.Ny, y = l - (l / g.Ny) * g.Ny;
+        s[(c * LZ + line) * MzP + z] = gb[c * g.sc + x * g.sx + y * g.sy + z];
+    }
+    __syncthreads();
+    const cx<T>* res = smem_fft<+1, T>(s, s2, 3 * LZ, MzP, 1, g.pz, stw, Mz, Nz);
+
+    // scatter to the dipoles, fused diagonal term and dot products
+    const cx<T>* vsrc = (SRC == SRC_TUPD) ? R.t : (SRC == SRC_P ? R.P : R.p);
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int e = threadIdx.x; e < nl * Nz; e += blockDim.x) {
+        const int line = e / Nz, z = e - (e / Nz) * Nz;
+        const int i = cellmap[(long long)(l0 + line) * Nz + z];
+        if (i < 0) continue;
+        const long long o = 3LL * i;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            cx<T> val = res[(c * LZ + line) * MzP + z];
+            if (SNK == SNK_OUT) {
+                R.Ap[o + c] = val;
+                continue;
+            }
+            const cx<T> vv = vsrc[o + c];
+            const cx<T> w = cadd<T>(val, cmul<T>(vv, R.al[o + c]));
+            if (SNK == SNK_ALB) {
+                R.Ap[o + c] = w;
+            } else if (SNK == SNK_AP) {
+                R.Ap[o + c] = w;
+                const cx<T> q = R.r0[o + c];  // r0 . Ap
+                acc[0] += (double)q.x * (double)w.x + (double)q.y * (double)w.y;
+                acc[1] += (double)q.x * (double)w.y - (double)q.y * (double)w.x;
+            } else if (SNK == SNK_AT) {
+                R.At[o + c] = w;
+                const cx<T> tt = vv;  // At . t and At . At
+                acc[0] += (double)w.x * (double)tt.x + (double)w.y * (double)tt.y;
+                acc[1] += (double)w.x * (double)tt.y - (double)w.y * (double)tt.x;
+                acc[2] += (double)w.x * (double)w.x + (double)w.y * (double)w.y;
+            } else if (SNK == SNK_RES) {
+                const cx<T> res = csub<T>(R.E[o + c], w);
+                R.r[o + c] = res;
+                R.r0[o + c] = res;
+                R.p[o + c] = res;
+                acc[0] += (double)res.x * (double)res.x + (double)res.y * (double)res.y;
+            }
+        }
+    }
+    if (SNK == SNK_OUT || SNK == SNK_ALB) return;
+    double tot[4];
+    const int nblk = gridDim.x;
+    const int slot = SNK == SNK_AP ? 0 : (SNK == SNK_AT ? 1 : 2);
+    if (!last_block_total<4>(acc, R.part, nblk, blockIdx.x, R.cnt + slot, sred, tot)) return;
+    if (threadIdx.x != 0) return;
+    SolveState* st = R.st;
+    if (SNK == SNK_AP) {
+        double2 r0Ap = make_double2(tot[0], tot[1]);
+        st->alpha = cdiv(st->rho, r0Ap);  // DDAModel.cpp:221
+    } else if (SNK == SNK_AT) {
+        st->zeta = cdiv(make_double2(tot[0], tot[1]), make_double2(tot[2], 0.0));  // DDAModel.cpp:225
+    } else {
+        st->rho = make_double2(tot[0], 0.0);  // r0 . r with r0 = r
+        st->rnorm2 = tot[0];
+    }
+}
+
+// ================================================================ K6 update
+template <typename T>
+__global__ void __launch_bounds__(kNT) k_update(int n3, const RhsVecs<T>* __restrict__ rhs, int is_init) {
+    __shared__ double sred[4 * 32];
+    const int b = blockIdx.y;
+    const RhsVecs<T> R = rhs[b];
+    if (rhs_done(R.st)) return;
+    const cx<T> alpha = from_d<T>(R.st->alpha), zeta = from_d<T>(R.st->zeta);
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x) {
+        const cx<T> Ap = R.Ap[e], r = R.r[e], p = R.p[e], t = R.t[e], At = R.At[e], r0 = R.r0[e];
+        cx<T> P = R.P[e];
+        const cx<T> u = cmul<T>(zeta, Ap);                              // u = zeta Ap
+        const cx<T> z = csub<T>(cmul<T>(zeta, r), cmul<T>(alpha, u));  // z = zeta r - alpha u
+        P = cadd<T>(cadd<T>(P, cmul<T>(alpha, p)), z);                 // P = P + alpha p + z
+        const cx<T> rn = csub<T>(t, cmul<T>(zeta, At));                // r = t - zeta At
+        R.u[e] = u;
+        R.P[e] = P;
+        R.r[e] = rn;
+        acc[0] += (double)r0.x * (double)rn.x + (double)r0.y * (double)rn.y;
+        acc[1] += (double)r0.x * (double)rn.y - (double)r0.y * (double)rn.x;
+        acc[2] += (double)rn.x * (double)rn.x + (double)rn.y * (double)rn.y;
+    }
+    double tot[4];
+    if (!last_block_total<4>(acc, R.part, gridDim.x, blockIdx.x, R.cnt + 3, sred, tot)) return;
+    if (threadIdx.x != 0) return;
+    SolveState* st = R.st;
+    st->rho_prev = st->rho;
+    st->rho = make_double2(tot[0], tot[1]);
+    st->rnorm2 = tot[2];
+    const double err = sqrt(tot[2]) / st->Enorm;
+    if (!is_init) {
+        st->it += 1;
+        if (err <= st->tol) {  // DDAModel.cpp:232-235
+            st->status = ST_CONVERGED;
+            st->iterations = st->it;
+            st->error = err;
+            return;
+        }
+    }
+    if (st->it >= st->max_it) {  // the loop of DDAModel.cpp:186 ends
+        st->status = ST_MAXITER;
+        st->error = err;
+        return;
+    }
+    if (st->rho_prev.x == 0.0 && st->rho_prev.y == 0.0) {  // DDAModel.cpp:193-215
+        st->status = ST_BREAKDOWN;
+        st->iterations = st->it + 1;
+        st->error = err;
+        return;
+    }
+    // beta = (alpha / zeta) * (r0 . r) / (r0 . rl)      DDAModel.cpp:218
+    st->beta = cdiv(dmul(cdiv(st->alpha, st->zeta), st->rho), st->rho_prev);
+    // the reference would iterate on NaN up to the limit; stop and report it
+    if (!finite2(st->rho) || !isfinite(err) || !finite2(st->beta)) {
+        st->status = ST_NAN;
+        st->error = err;
+    }
+}
+
+// |E| of each right-hand side
+template <typename T>
+__global__ void __launch_bounds__(kNT) k_solve_begin(int n3, const RhsVecs<T>* __restrict__ rhs, int resid_is_rhs) {
+    __shared__ double sred[4 * 32];
+    const int b = blockIdx.y;
+    const RhsVecs<T> R = rhs[b];
+    if (rhs_done(R.st)) return;
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x) {
+        const cx<T> v = R.E[e];
+        acc[0] += (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+        if (resid_is_rhs) {
+            R.r[e] = v;
+            R.r0[e] = v;
+            R.p[e] = v;
+        }
+    }
+    double tot[4];
+    if (!last_block_total<4>(acc, R.part, gridDim.x, blockIdx.x, R.cnt + 4, sred, tot)) return;
+    if (threadIdx.x != 0) return;
+    R.st->Enorm = sqrt(tot[0]);
+    if (resid_is_rhs) {
+        R.st->rho = make_double2(tot[0], 0.0);
+        R.st->rnorm2 = tot[0];
+    }
+}
+
+// ================================================================ K0 green
+__global__ void k_green_real(Geom g, double K, double d, double2* __restrict__ full6) {
+    const int Mx = g.px.M, My = g.py.M, Mz = g.pz.M;
+    const long long M = (long long)Mx * My * Mz;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < M; e += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(e % Mz);
+        const int j = (int)((e / Mz) % My);
+        const int i = (int)(e / ((long long)Mz * My));
+        // signed lattice offset of each grid index (AProductCore.cpp:53-194)
+        int ox = i < g.Nx ? i : (i > Mx - g.Nx ? i - Mx : INT32_MIN);
+        int oy = j < g.Ny ? j : (j > My - g.Ny ? j - My : INT32_MIN);
+        int oz = k < g.Nz ? k : (k > Mz - g.Nz ? k - Mz : INT32_MIN);
+        double2 t[6];
+#pragma unroll
+        for (int l = 0; l < 6; l++) t[l] = make_double2(0.0, 0.0);
+        if (ox != INT32_MIN && oy != INT32_MIN && oz != INT32_MIN) {
+            // LDR_inter (AProductCore.cpp:588-623); r = 0 gives the zero tensor
+            const double x = d * ox, y = d * oy, z = d * oz;
+            const double xs = x * x, ys = y * y, zs = z * z;
+            const double rn = sqrt(xs + ys + zs);
+            if (rn != 0.0) {
+                const double rsq = rn * rn, rcu = rn * rn * rn;
+                double sn, cs;
+                sincos(K * rn, &sn, &cs);
+                const double2 c1 = make_double2(cs / rcu, sn / rcu);        // e^{iKr} / r^3
+                const double2 c2 = make_double2(1.0 / rsq, -(K * rn) / rsq);  // (1 - iKr) / r^2
+                const double2 c3 = make_double2(K * K - 3.0 * c2.x, -3.0 * c2.y);
+                double2 v[6];
+                v[0] = make_double2(c2.x * (rsq - 3 * xs) - K * K * (ys + zs), c2.y * (rsq - 3 * xs));
+                v[1] = make_double2(x * y * c3.x, x * y * c3.y);
+                v[2] = make_double2(z * x * c3.x, z * x * c3.y);
+                v[3] = make_double2(c2.x * (rsq - 3 * ys) - K * K * (zs + xs), c2.y * (rsq - 3 * ys));
+                v[4] = make_double2(y * z * c3.x, y * z * c3.y);
+                v[5] = make_double2(c2.x * (rsq - 3 * zs) - K * K * (xs + ys), c2.y * (rsq - 3 * zs));
+#pragma unroll
+                for (int l = 0; l < 6; l++) t[l] = dmul(c1, v[l]);
+            }
+        }
+#pragma unroll
+        for (int l = 0; l < 6; l++) full6[l * M + e] = t[l];
+    }
+}
+
+// fold the spectrum to the octant, scale by 1/M, write FP64 and FP32 copies
+__global__ void k_green_fold(Geom g, const double2* __restrict__ full6, double2* __restrict__ green64,
+                             float2* __restrict__ green32) {
+    const int Mx = g.px.M, My = g.py.M, Mz = g.pz.M;
+    const long long M = (long long)Mx * My * Mz;
+    const long long H = (long long)g.Hx * g.Hy * g.Hz;
+    const double inv = 1.0 / (double)M;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < H * 6; e += (long long)gridDim.x * blockDim.x) {
+        const int l = (int)(e % 6);
+        const long long q = e / 6;
+        const int fx = (int)(q % g.Hx);
+        const int fz = (int)((q / g.Hx) % g.Hz);
+        const int fy = (int)(q / ((long long)g.Hx * g.Hz));
+        const double2 v = full6[l * M + ((long long)fx * My + fy) * Mz + fz];
+        const double2 w = make_double2(v.x * inv, v.y * inv);
+        green64[e] = w;
+        green32[e] = make_float2((float)w.x, (float)w.y);
+    }
+}
+
+// ------------------------------------------------------- generic FFT passes
+// rows: nrows contiguous lines of length M
+__global__ void __launch_bounds__(kNT) k_fft_rows(double2* __restrict__ data, long long nrows, AxisPlan p,
+                                                  const double2* __restrict__ tw, int sign) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int M = p.M;
+    const int L = row_lines(p);
+    const int MP = pad_odd(M);
+    double2* stw = reinterpret_cast<double2*>(smem_raw);
+    double2* s = stw + M;
+    double2* s2 = s + L * MP;
+    stage_tw<double>(stw, tw, M);
+    const long long r0 = (long long)blockIdx.x * L;
+    const int nl = (int)min((long long)L, nrows - r0);
+    for (int e = threadIdx.x; e < nl * M; e += blockDim.x) {
+        const int line = e / M, m = e - (e / M) * M;
+        s[line * MP + m] = data[(r0 + line) * M + m];
+    }
+    __syncthreads();
+    const double2* res = sign < 0 ? smem_fft<-1, double>(s, s2, L, MP, 1, p, stw, M, M)
+                                  : smem_fft<+1, double>(s, s2, L, MP, 1, p, stw, M, M);
+    for (int e = threadIdx.x; e < nl * M; e += blockDim.x) {
+        const int line = e / M, m = e - (e / M) * M;
+        data[(r0 + line) * M + m] = res[line * MP + m];
+    }
+}
+
+// columns: element m of line (o, t) at off(o) + t + m*ms, t in [0, ninner)
+// contiguous; off(o) = (o / o1) * s1 + (o % o1) * s2
+__global__ void __launch_bounds__(kNT) k_fft_cols(double2* __restrict__ data, int nouter, int o1, long long s1,
+                                                  long long s2, long long ms, int ninner, AxisPlan p,
+                                                  const double2* __restrict__ tw, int sign) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int M = p.M;
+    const int ZT = col_tile(p);
+    const int nt = (ninner + ZT - 1) / ZT;
+    const int o = blockIdx.x / nt, t0 = (blockIdx.x - o * nt) * ZT;
+    const int zn = min(ZT, ninner - t0);
+    double2* stw = reinterpret_cast<double2*>(smem_raw);
+    double2* s = stw + M;
+    double2* sb2 = s + M * ZT;
+    stage_tw<double>(stw, tw, M);
+    double2* base = data + (long long)(o / o1) * s1 + (long long)(o % o1) * s2 + t0;
+    for (int e = threadIdx.x; e < M * ZT; e += blockDim.x) {
+        const int m = e / ZT, zl = e - (e / ZT) * ZT;
+        s[e] = zl < zn ? base[m * ms + zl] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    const double2* res = sign < 0 ? smem_fft<-1, double>(s, sb2, ZT, 1, ZT, p, stw, M, M)
+                                  : smem_fft<+1, double>(s, sb2, ZT, 1, ZT, p, stw, M, M);
+    for (int e = threadIdx.x; e < M * ZT; e += blockDim.x) {
+        const int m = e / ZT, zl = e - (e / ZT) * ZT;
+        if (zl < zn) base[m * ms + zl] = res[e];
+    }
+}
+
+// ------------------------------------------------------------ small kernels
+__global__ void k_einternal(int n3, const double2* al, const double2* P, const double2* diel, double2* Ein) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x) {
+        const double2 lf = make_double2((2.0 + diel[e].x) / 3.0, diel[e].y / 3.0);
+        Ein[e] = cdiv(dmul(al[e], P[e]), lf);
+    }
+}
+__global__ void k_to_f32(int n3, const double2* src, float2* dst) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x)
+        dst[e] = make_float2((float)src[e].x, (float)src[e].y);
+}
+__global__ void k_accumulate(int n3, const float2* d, double2* P) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x)
+        P[e] = make_double2(P[e].x + (double)d[e].x, P[e].y + (double)d[e].y);
+}
+template <typename T> __global__ void k_zero(long long n, cx<T>* v) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        v[e] = czero<T>();
+}
+
+int grid1d(long long n, int nt) {
+    long long b = (n + nt - 1) / nt;
+    if (b > 152 * 16) b = 152 * 16;  // 16 resident blocks per SM on 152 SMs at most
+    return (int)(b < 1 ? 1 : b);
+}
+
+template <typename T> size_t zsmem(const Geom& g) {
+    return sizeof(cx<T>) * (size_t)(g.pz.M + 2 * 3 * z_lines<T>(g.pz) * pad_odd(g.pz.M));
+}
+template <typename T> size_t ysmem(const Geom& g) {
+    return sizeof(cx<T>) * (size_t)(g.py.M + 2 * g.py.M * y_tile<T>(g.py));
+}
+template <typename T> size_t xsmem(const Geom& g) {
+    return sizeof(cx<T>) * (size_t)(g.px.M + 2 * g.px.M * 3 * x_tile<T>(g.px));
+}
+size_t rowsmem(const AxisPlan& p) { return sizeof(double2) * (size_t)(p.M + 2 * row_lines(p) * pad_odd(p.M)); }
+size_t colsmem(const AxisPlan& p) { return sizeof(double2) * (size_t)(p.M + 2 * p.M * col_tile(p)); }
+
+
+constexpr int kMaxSmem = 200 * 1024;  // leaves room for the static reduction buffers
+
+template <typename T> cudaError_t configure_t() {
+    cudaError_t e = cudaSuccess;
+    auto set = [&](const void* k) {
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
+    };
+    set((const void*)k_zfwd<T, SRC_IN>);
+    set((const void*)k_zfwd<T, SRC_PUPD>);
+    set((const void*)k_zfwd<T, SRC_TUPD>);
+    set((const void*)k_zfwd<T, SRC_P>);
+    set((const void*)k_ypass<T, -1>);
+    set((const void*)k_ypass<T, +1>);
+    set((const void*)k_xpass<T>);
+    set((const void*)k_zinv<T, SRC_IN, SNK_OUT>);
+    set((const void*)k_zinv<T, SRC_IN, SNK_ALB>);
+    set((const void*)k_zinv<T, SRC_PUPD, SNK_AP>);
+    set((const void*)k_zinv<T, SRC_TUPD, SNK_AT>);
+    set((const void*)k_zinv<T, SRC_P, SNK_RES>);
+    return e;
+}
+
+}  // namespace
+
+cudaError_t configure_kernels() {
+    cudaError_t e = configure_t<double>();
+    if (e == cudaSuccess) e = configure_t<float>();
+    if (e == cudaSuccess) e = cudaFuncSetAttribute((const void*)k_fft_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute((const void*)k_fft_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
+    return e;
+}
+
+size_t max_pass_smem(const Geom& g) {
+    size_t m = 0;
+    m = std::max(m, zsmem<double>(g));
+    m = std::max(m, ysmem<double>(g));
+    m = std::max(m, xsmem<double>(g));
+    m = std::max(m, rowsmem(g.pz));
+    m = std::max(m, colsmem(g.py));
+    m = std::max(m, colsmem(g.px));
+    return m;  // the FP32 tiles are never larger than the FP64 ones
+}
+
+int max_blocks_per_rhs(const Geom& g) {
+    const int lz = z_lines<float>(g.pz) > z_lines<double>(g.pz) ? z_lines<double>(g.pz) : z_lines<float>(g.pz);
+    int nz = (g.Nx * g.Ny + lz - 1) / lz;
+    int nv = grid1d(3LL * g.N, kNT);
+    return nz > nv ? nz : nv;
+}
+
+// ------------------------------------------------------------------ launchers
+namespace {
+cudaError_t fft_rows(double2* data, long long nrows, const AxisPlan& p, const double2* tw, int sign,
+                     cudaStream_t stream) {
+    const int L = row_lines(p);
+    k_fft_rows<<<(unsigned)((nrows + L - 1) / L), kNT, rowsmem(p), stream>>>(data, nrows, p, tw, sign);
+    return cudaGetLastError();
+}
+cudaError_t fft_cols(double2* data, int nouter, int o1, long long s1, long long s2, long long ms, int ninner,
+                     const AxisPlan& p, const double2* tw, int sign, cudaStream_t stream) {
+    const int ZT = col_tile(p);
+    const int nt = (ninner + ZT - 1) / ZT;
+    k_fft_cols<<<(unsigned)(nouter * nt), kNT, colsmem(p), stream>>>(data, nouter, o1, s1, s2, ms, ninner, p, tw,
+                                                                      sign);
+    return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t launch_green(const Geom& g, double K, double d, const double2* twx, const double2* twy, const double2* twz,
+                         double2* full6, double2* green64, float2* green32, cudaStream_t stream) {
+    const int Mx = g.px.M, My = g.py.M, Mz = g.pz.M;
+    const long long M = (long long)Mx * My * Mz;
+    k_green_real<<<grid1d(M, kNT), kNT, 0, stream>>>(g, K, d, full6);
+    cudaError_t err = cudaGetLastError();
+    // the six components form a (6 Mx, My, Mz) array for the z and y axes;
+    // the x axis runs over the outer pairs (component, y)
+    if (!err) err = fft_rows(full6, 6LL * Mx * My, g.pz, twz, -1, stream);
+    if (!err) err = fft_cols(full6, 6 * Mx, 6 * Mx, 0, (long long)My * Mz, Mz, Mz, g.py, twy, -1, stream);
+    if (!err) err = fft_cols(full6, 6 * My, My, M, Mz, (long long)My * Mz, Mz, g.px, twx, -1, stream);
+    if (err) return err;
+    const long long H6 = 6LL * g.Hx * g.Hy * g.Hz;
+    k_green_fold<<<grid1d(H6, kNT), kNT, 0, stream>>>(g, full6, green64, green32);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fft3d_f64(double2* data, const AxisPlan& p0, const AxisPlan& p1, const AxisPlan& p2,
+                             const double2* tw0, const double2* tw1, const double2* tw2, int sign,
+                             cudaStream_t stream) {
+    const int n0 = p0.M, n1 = p1.M, n2 = p2.M;
+    cudaError_t err = fft_rows(data, (long long)n0 * n1, p2, tw2, sign, stream);
+    if (!err) err = fft_cols(data, n0, n0, 0, (long long)n1 * n2, n2, n2, p1, tw1, sign, stream);
+    if (!err) err = fft_cols(data, n1, n1, 0, n2, (long long)n1 * n2, n2, p0, tw0, sign, stream);
+    return err;
+}
+
+template <typename T>
+cudaError_t launch_aproduct(const Geom& g, int src, int snk, int nrhs, const RhsVecs<T>* rhs, const cx<T>* green,
+                            const cx<T>* twx, const cx<T>* twy, const cx<T>* twz, const int* cellmap, cx<T>* grid,
+                            cudaStream_t stream) {
+    cudaError_t err;
+    const int LZ = z_lines<T>(g.pz);
+    const dim3 gz((g.Nx * g.Ny + LZ - 1) / LZ, nrhs);
+    const size_t smz = zsmem<T>(g);
+    // K1
+    switch (src) {
+        case SRC_IN:
+            k_zfwd<T, SRC_IN><<<gz, kNT, smz, stream>>>(g, rhs, twz, cellmap, grid);
+            break;
+        case SRC_PUPD:
+            k_zfwd<T, SRC_PUPD><<<gz, kNT, smz, stream>>>(g, rhs, twz, cellmap, grid);
+            break;
+        case SRC_TUPD:
+            k_zfwd<T, SRC_TUPD><<<gz, kNT, smz, stream>>>(g, rhs, twz, cellmap, grid);
+            break;
+        default:
+            k_zfwd<T, SRC_P><<<gz, kNT, smz, stream>>>(g, rhs, twz, cellmap, grid);
+            break;
+    }
+    if ((err = cudaGetLastError())) return err;
+    // K2
+    const int YT = y_tile<T>(g.py);
+    const dim3 gy(g.Nx * ((g.pz.M + YT - 1) / YT), 3, nrhs);
+    const size_t smy = ysmem<T>(g);
+    k_ypass<T, -1><<<gy, kNT, smy, stream>>>(g, rhs, twy, grid);
+    if ((err = cudaGetLastError())) return err;
+    // K3
+    const int XT = x_tile<T>(g.px);
+    const dim3 gx(g.py.M * ((g.pz.M + XT - 1) / XT), nrhs);
+    const size_t smx = xsmem<T>(g);
+    k_xpass<T><<<gx, kNT, smx, stream>>>(g, rhs, green, twx, grid);
+    if ((err = cudaGetLastError())) return err;
+    // K4
+    k_ypass<T, +1><<<gy, kNT, smy, stream>>>(g, rhs, twy, grid);
+    if ((err = cudaGetLastError())) return err;
+    // K5
+#define TDDA_ZINV(S, K) k_zinv<T, S, K><<<gz, kNT, smz, stream>>>(g, rhs, twz, cellmap, grid)
+    if (snk == SNK_OUT) TDDA_ZINV(SRC_IN, SNK_OUT);
+    else if (snk == SNK_ALB) TDDA_ZINV(SRC_IN, SNK_ALB);
+    else if (snk == SNK_AP) TDDA_ZINV(SRC_PUPD, SNK_AP);
+    else if (snk == SNK_AT) TDDA_ZINV(SRC_TUPD, SNK_AT);
+    else TDDA_ZINV(SRC_P, SNK_RES);
+#undef TDDA_ZINV
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_update(const Geom& g, int nrhs, const RhsVecs<T>* rhs, int is_init, cudaStream_t stream) {
+    const dim3 gr(grid1d(3LL * g.N, kNT), nrhs);
+    k_update<T><<<gr, kNT, 0, stream>>>(3 * g.N, rhs, is_init);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_solve_begin(const Geom& g, int nrhs, const RhsVecs<T>* rhs, cudaStream_t stream) {
+    const dim3 gr(grid1d(3LL * g.N, kNT), nrhs);
+    k_solve_begin<T><<<gr, kNT, 0, stream>>>(3 * g.N, rhs, 0);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_residual_is_rhs(const Geom& g, int nrhs, const RhsVecs<T>* rhs, cudaStream_t stream) {
+    const dim3 gr(grid1d(3LL * g.N, kNT), nrhs);
+    k_solve_begin<T><<<gr, kNT, 0, stream>>>(3 * g.N, rhs, 1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_einternal(int n3, const double2* al, const double2* P, const double2* diel, double2* Ein,
+                             cudaStream_t stream) {
+    k_einternal<<<grid1d(n3, kNT), kNT, 0, stream>>>(n3, al, P, diel, Ein);
+    return cudaGetLastError();
+}
+cudaError_t launch_to_f32(int n3, const double2* src, float2* dst, cudaStream_t stream) {
+    k_to_f32<<<grid1d(n3, kNT), kNT, 0, stream>>>(n3, src, dst);
+    return cudaGetLastError();
+}
+cudaError_t launch_accumulate(int n3, const float2* d, double2* P, cudaStream_t stream) {
+    k_accumulate<<<grid1d(n3, kNT), kNT, 0, stream>>>(n3, d, P);
+    return cudaGetLastError();
+}
+template <typename T> cudaError_t launch_zero(long long n, cx<T>* v, cudaStream_t stream) {
+    k_zero<T><<<grid1d(n, kNT), kNT, 0, stream>>>(n, v);
+    return cudaGetLastError();
+}
+
+#define TDDA_INST(T)                                                                                               \
+    template cudaError_t launch_aproduct<T>(const Geom&, int, int, int, const RhsVecs<T>*, const cx<T>*,          \
+                                            const cx<T>*, const cx<T>*, const cx<T>*, const int*, cx<T>*,         \
+                                            cudaStream_t);                                                         \
+    template cudaError_t launch_update<T>(const Geom&, int, const RhsVecs<T>*, int, cudaStream_t);                 \
+    template cudaError_t launch_solve_begin<T>(const Geom&, int, const RhsVecs<T>*, cudaStream_t);                 \
+    template cudaError_t launch_residual_is_rhs<T>(const Geom&, int, const RhsVecs<T>*, cudaStream_t);             \
+    template cudaError_t launch_zero<T>(long long, cx<T>*, cudaStream_t);
+TDDA_INST(float)
+TDDA_INST(double)
+#undef TDDA_INST
+
+}  // namespace tdda

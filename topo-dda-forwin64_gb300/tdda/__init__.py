@@ -1,0 +1,331 @@
+"""Python binding of libtdda (the C ABI in include/tdda.h), shaped like the reference.
+
+``AProductCore`` and ``DDAModel`` keep the method names and argument meaning of the
+reference's classes (AProductCore.h:51-80, DDAModel.h:34-74) so that tests and
+benchmarks read like the reference's own call sequence (main.cpp:245-251):
+
+    core = AProductCore(Nx, Ny, Nz, R, d, lam, material, nback)
+    model = DDAModel(core, n_K, E0, n_E0, diel_old)
+    model.bicgstab(MAX_ITERATION, MAX_ERROR)
+    model.update_E_in_structure()
+    P, Ein = model.get_P(), model.get_Einternal()
+
+Every call goes through the CUDA library; there is no CPU path.  Loading fails
+loudly when libtdda.so has not been built (``python topo-dda-forwin64_gb300/build.py``).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import lattice  # noqa: F401
+
+_PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(_PKG, "libtdda.so")
+
+OK, ERR_INVALID_ARGUMENT, ERR_CUDA, ERR_OUT_OF_MEMORY, ERR_UNSUPPORTED = 0, 1, 2, 3, 4
+NOT_CONVERGED, BREAKDOWN, ERR_NAN, ERR_NO_DEVICE = 5, 6, 7, 8
+STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "cuda error", 3: "out of memory", 4: "unsupported",
+                5: "not converged", 6: "breakdown", 7: "nan", 8: "no device"}
+FP64, FP32_REFINE = 0, 1
+MEM_HOST, MEM_DEVICE = 0, 1
+FIELD_P, FIELD_E, FIELD_AL, FIELD_DIEL, FIELD_EINTERNAL = 0, 1, 2, 3, 4
+METHODS = {"LDR": 0, "FCD": 1}
+
+# every entry point declared in include/tdda.h
+EXPORTS = [
+    "tdda_abi_version", "tdda_last_error", "tdda_device_count", "tdda_core_create", "tdda_core_destroy",
+    "tdda_core_info", "tdda_aproduct", "tdda_core_ldr_inter", "tdda_model_create", "tdda_model_destroy",
+    "tdda_model_update_alpha", "tdda_model_update_alpha_single", "tdda_model_change_E", "tdda_model_reset_E",
+    "tdda_model_initialize_P", "tdda_model_aproduct_with_alb", "tdda_model_bicgstab", "tdda_model_solve_mixed",
+    "tdda_model_update_E_in_structure", "tdda_model_get", "tdda_model_iterations", "tdda_solve_batch",
+    "tdda_fft3d",
+]
+
+
+class TddaError(RuntimeError):
+    def __init__(self, status: int, where: str, message: str):
+        super().__init__(f"{where}: {STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class CoreDesc(ctypes.Structure):
+    _fields_ = [("Nx", ctypes.c_int), ("Ny", ctypes.c_int), ("Nz", ctypes.c_int), ("N", ctypes.c_int),
+                ("R", ctypes.POINTER(ctypes.c_int)), ("d", ctypes.c_double), ("lam", ctypes.c_double),
+                ("nback", ctypes.c_double), ("material", ctypes.POINTER(ctypes.c_double)),
+                ("nmat", ctypes.c_int), ("method", ctypes.c_int), ("max_rhs", ctypes.c_int),
+                ("device", ctypes.c_int)]
+
+
+class SolveInfo(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("iterations", ctypes.c_int), ("error", ctypes.c_double),
+                ("true_residual", ctypes.c_double), ("outer_iterations", ctypes.c_int),
+                ("inner_iterations", ctypes.c_int)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_LIB = None
+
+
+def load() -> ctypes.CDLL:
+    """Load libtdda.so; raise if it is missing (the product has no fallback)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with topo-dda-forwin64_gb300/build.py")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, dp, ip, i, d = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int), \
+        ctypes.c_int, ctypes.c_double
+    sig = {
+        "tdda_abi_version": (i, []),
+        "tdda_last_error": (ctypes.c_char_p, []),
+        "tdda_device_count": (i, []),
+        "tdda_core_create": (i, [ctypes.POINTER(CoreDesc), ctypes.POINTER(vp)]),
+        "tdda_core_destroy": (i, [vp]),
+        "tdda_core_info": (i, [vp, dp, ip, dp]),
+        "tdda_aproduct": (i, [vp, i, vp, vp, i]),
+        "tdda_core_ldr_inter": (i, [vp, d, d, d, dp]),
+        "tdda_model_create": (i, [vp, dp, d, dp, dp, ctypes.POINTER(vp)]),
+        "tdda_model_destroy": (i, [vp]),
+        "tdda_model_update_alpha": (i, [vp, dp]),
+        "tdda_model_update_alpha_single": (i, [vp, i, d]),
+        "tdda_model_change_E": (i, [vp, vp, i]),
+        "tdda_model_reset_E": (i, [vp]),
+        "tdda_model_initialize_P": (i, [vp, vp, i]),
+        "tdda_model_aproduct_with_alb": (i, [vp, vp, vp, i]),
+        "tdda_model_bicgstab": (i, [vp, i, d, ctypes.POINTER(SolveInfo)]),
+        "tdda_model_solve_mixed": (i, [vp, i, d, ctypes.POINTER(SolveInfo)]),
+        "tdda_model_update_E_in_structure": (i, [vp]),
+        "tdda_model_get": (i, [vp, i, vp, i]),
+        "tdda_model_iterations": (i, [vp]),
+        "tdda_solve_batch": (i, [ctypes.POINTER(vp), i, i, i, d, ctypes.POINTER(SolveInfo)]),
+        "tdda_fft3d": (i, [vp, i, i, i, i]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _LIB = L
+    return L
+
+
+def device_count() -> int:
+    return load().tdda_device_count()
+
+
+def _check(st: int, where: str, allowed=(OK,)):
+    if st not in allowed:
+        raise TddaError(st, where, load().tdda_last_error().decode())
+    return st
+
+
+def _c128(a, n=None) -> np.ndarray:
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.complex128).reshape(-1))
+    if n is not None and a.size != n:
+        raise ValueError(f"expected {n} complex entries, got {a.size}")
+    return a
+
+
+def _ptr(a: np.ndarray):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class AProductCore:
+    """The interaction operator of one lattice at one wavelength (AProductCore.h:12-81)."""
+
+    def __init__(self, Nx, Ny, Nz, R, d, lam, material, nback=1.0, method="LDR", max_rhs=1, device=0):
+        L = load()
+        self.R = np.ascontiguousarray(np.asarray(R, dtype=np.int32).reshape(-1))
+        self.N = self.R.size // 3
+        self.Nx, self.Ny, self.Nz = int(Nx), int(Ny), int(Nz)
+        self.d, self.lam, self.nback = float(d), float(lam), float(nback)
+        mat = _c128(material)
+        self._mat = mat
+        desc = CoreDesc(self.Nx, self.Ny, self.Nz, self.N,
+                        self.R.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), self.d, self.lam, self.nback,
+                        _dptr(mat.view(np.float64)), mat.size, METHODS[method], int(max_rhs), int(device))
+        h = ctypes.c_void_p()
+        _check(L.tdda_core_create(ctypes.byref(desc), ctypes.byref(h)), "tdda_core_create")
+        self.h = h
+        self.max_rhs = int(max_rhs)
+        K = ctypes.c_double()
+        g = (ctypes.c_int * 3)()
+        mn = np.zeros(mat.size, np.complex128)
+        _check(L.tdda_core_info(h, ctypes.byref(K), g, _dptr(mn.view(np.float64))), "tdda_core_info")
+        self.K = K.value
+        self.grid = tuple(g)
+        self.material = mn
+
+    def get_N(self): return self.N
+    def get_Nx(self): return self.Nx
+    def get_Ny(self): return self.Ny
+    def get_Nz(self): return self.Nz
+    def get_R(self): return self.R
+    def get_d(self): return self.d
+    def get_lam(self): return self.lam
+    def get_K(self): return self.K
+    def get_material(self): return self.material
+    def get_nback(self): return self.nback
+
+    def Aproduct(self, b, precision: int = FP64) -> np.ndarray:
+        """y = A_offdiag b (AProductCore.cpp:697-758); host arrays in and out."""
+        b = _c128(b, 3 * self.N)
+        y = np.empty_like(b)
+        _check(load().tdda_aproduct(self.h, precision, _ptr(b), _ptr(y), MEM_HOST), "tdda_aproduct")
+        return y
+
+    def Aproduct_device(self, b_ptr: int, y_ptr: int, precision: int = FP64):
+        _check(load().tdda_aproduct(self.h, precision, ctypes.c_void_p(b_ptr), ctypes.c_void_p(y_ptr),
+                                    MEM_DEVICE), "tdda_aproduct")
+
+    def LDR_inter(self, x, y, z) -> np.ndarray:
+        out = np.zeros(6, np.complex128)
+        _check(load().tdda_core_ldr_inter(self.h, x, y, z, _dptr(out.view(np.float64))), "tdda_core_ldr_inter")
+        a = out
+        return np.array([[a[0], a[1], a[2]], [a[1], a[3], a[4]], [a[2], a[4], a[5]]])
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().tdda_core_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DDAModel:
+    """Incident field, polarisability and solve of one right-hand side (DDAModel.h:6-75)."""
+
+    def __init__(self, core: AProductCore, n_K, E0, n_E0, diel_old):
+        self.core = core
+        self.n3 = 3 * core.N
+        nK = np.ascontiguousarray(n_K, np.float64)
+        nE = np.ascontiguousarray(n_E0, np.float64)
+        diel = np.ascontiguousarray(diel_old, np.float64)
+        if diel.size != self.n3:
+            raise ValueError("diel_old must hold 3N densities")
+        h = ctypes.c_void_p()
+        _check(load().tdda_model_create(core.h, _dptr(nK), float(E0), _dptr(nE), _dptr(diel), ctypes.byref(h)),
+               "tdda_model_create")
+        self.h = h
+        self.last_info = None
+
+    def _get(self, field: int) -> np.ndarray:
+        out = np.empty(self.n3, np.complex128)
+        _check(load().tdda_model_get(self.h, field, _ptr(out), MEM_HOST), "tdda_model_get")
+        return out
+
+    def get_P(self): return self._get(FIELD_P)
+    def get_E(self): return self._get(FIELD_E)
+    def get_al(self): return self._get(FIELD_AL)
+    def get_diel(self): return self._get(FIELD_DIEL)
+    def get_Einternal(self): return self._get(FIELD_EINTERNAL)
+    def get_ITERATION(self) -> int: return load().tdda_model_iterations(self.h)
+
+    def UpdateAlpha(self, diel_old):
+        diel = np.ascontiguousarray(diel_old, np.float64)
+        _check(load().tdda_model_update_alpha(self.h, _dptr(diel)), "tdda_model_update_alpha")
+
+    def UpdateAlphaSingle(self, idx: int, value: float):
+        _check(load().tdda_model_update_alpha_single(self.h, int(idx), float(value)), "UpdateAlphaSingle")
+
+    def change_E(self, E):
+        E = _c128(E, self.n3)
+        _check(load().tdda_model_change_E(self.h, _ptr(E), MEM_HOST), "tdda_model_change_E")
+
+    def reset_E(self):
+        _check(load().tdda_model_reset_E(self.h), "tdda_model_reset_E")
+
+    def InitializeP(self, P):
+        P = _c128(P, self.n3)
+        _check(load().tdda_model_initialize_P(self.h, _ptr(P), MEM_HOST), "tdda_model_initialize_P")
+
+    def Aproductwithalb(self, b) -> np.ndarray:
+        b = _c128(b, self.n3)
+        y = np.empty_like(b)
+        _check(load().tdda_model_aproduct_with_alb(self.h, _ptr(b), _ptr(y), MEM_HOST), "Aproductwithalb")
+        return y
+
+    def bicgstab(self, MAX_ITERATION: int, MAX_ERROR: float) -> dict:
+        """FP64 BiCGSTAB (DDAModel.cpp:131-260).  Returns the solve info; a breakdown or a
+        reached iteration limit is reported in info['status'], as the reference only prints."""
+        info = SolveInfo()
+        load().tdda_model_bicgstab(self.h, int(MAX_ITERATION), float(MAX_ERROR), ctypes.byref(info))
+        _check(info.status, "bicgstab", allowed=(OK, NOT_CONVERGED, BREAKDOWN))
+        self.last_info = info.as_dict()
+        return self.last_info
+
+    def solve_mixed(self, MAX_ITERATION: int, MAX_ERROR: float) -> dict:
+        """FP32 BiCGSTAB with FP64 refinement to MAX_ERROR."""
+        info = SolveInfo()
+        load().tdda_model_solve_mixed(self.h, int(MAX_ITERATION), float(MAX_ERROR), ctypes.byref(info))
+        _check(info.status, "solve_mixed", allowed=(OK, NOT_CONVERGED, BREAKDOWN))
+        self.last_info = info.as_dict()
+        return self.last_info
+
+    def update_E_in_structure(self):
+        _check(load().tdda_model_update_E_in_structure(self.h), "update_E_in_structure")
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().tdda_model_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def solve_batch(models, precision: int = FP64, max_it: int = 10000, tol: float = 1e-5) -> list:
+    """Solve several models of one core in one batched pass per kernel."""
+    n = len(models)
+    arr = (ctypes.c_void_p * n)(*[m.h.value for m in models])
+    infos = (SolveInfo * n)()
+    st = load().tdda_solve_batch(arr, n, int(precision), int(max_it), float(tol), infos)
+    _check(st, "tdda_solve_batch", allowed=(OK, NOT_CONVERGED, BREAKDOWN))
+    out = [infos[k].as_dict() for k in range(n)]
+    for m, o in zip(models, out):
+        m.last_info = o
+    return out
+
+
+def fft3d_device(ptr: int, n0: int, n1: int, n2: int, sign: int):
+    """In-place complex128 3-D FFT of device memory at ptr (the engine's own FFT)."""
+    _check(load().tdda_fft3d(ctypes.c_void_p(ptr), n0, n1, n2, sign), "tdda_fft3d")
+
+
+@dataclass
+class Solved:
+    P: np.ndarray
+    Einternal: np.ndarray
+    info: dict
+
+
+def solve_workload(w, precision: int = FP64, inc=None, tol=None, max_it=None) -> Solved:
+    """One solve of a lattice.Workload through the reference-shaped API."""
+    inc = inc or w.incidences[0]
+    core = AProductCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material, w.nback)
+    model = DDAModel(core, inc.nK, inc.E0, inc.nE0, w.diel_old)
+    tol = w.tol if tol is None else tol
+    max_it = w.max_it if max_it is None else max_it
+    info = model.bicgstab(max_it, tol) if precision == FP64 else model.solve_mixed(max_it, tol)
+    model.update_E_in_structure()
+    out = Solved(model.get_P(), model.get_Einternal(), info)
+    model.close()
+    core.close()
+    return out
