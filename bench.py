@@ -1,0 +1,392 @@
+"""Benchmark of the DDA solve hot path: converged solves/s at rel. residual 1e-5.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (one step = one converged solve): the mixed-precision single-solve lattice
+64x64x16 dipoles (65,536; FFT grid 128x128x32), d = 10 nm, lambda = 600 nm, rho ~ U[0,1]
+seeded then 3x3x3 box filtered, eps_m = 6.25+0.05i, x-polarised plane wave along +z,
+LDR polarisability, BiCGSTAB to |r|/|E| <= 1e-5.  Data are seeded synthetic (no dataset).
+
+ours       FP32 FFT convolution + Krylov vectors, FP64 dots / scalars, FP64 residual
+           with iterative refinement (value); the plain FP64 solve of the same lattice is
+           timed beside it (fp64).  Inputs are resident in HBM in the device-timed region;
+           `e2e` is the same solve through the C ABI with host buffers.
+reference  the reference's solve path run on the host cores (the oracle port of
+           AProductCore::Aproduct + DDAModel::bicgstab, all host threads, one solve per
+           thread), a bounded sample scaled to solves/s.
+
+Multi-GPU: the solve does not shard; N ranks run N independent replicas (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "topo-dda-forwin64_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from tdda import lattice  # noqa: E402
+
+METRIC = "solves/s & p99 latency, FP32+refine vs FP64 plain, same GB300, rel.res 1e-5"
+UNIT = "solves/s"
+TOL = 1e-5
+MAX_IT = 10000
+WORKLOAD = "mixed-precision single solve 64x64x16 (cfg 2)"
+# iteration count of the oracle's FP64 BiCGSTAB on this lattice run to convergence
+# (tol 1e-5); scales the bounded CPU sample to a full solve
+ORACLE_FP64_ITERATIONS_CFG2 = 29
+
+
+# --------------------------------------------------------------------------- helpers
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")), \
+        int(os.environ.get("WORLD_SIZE", "1"))
+
+
+class Dist:
+    """Barrier and max-reduction over ranks (torch.distributed when WORLD_SIZE > 1)."""
+
+    def __init__(self):
+        self.rank, self.local_rank, self.world = env_rank()
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi SM clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def pass_bytes(grid, Nx, Ny, Nz, N, s):
+    """Algorithmic bytes of the five A-product passes for one right-hand side.
+
+    Pass model of the survey's canonical count, on the grid (Mx, My, Mz) actually used:
+    the z-forward pass reads the 3N vector and writes 3 Nx Ny Mz grid entries, the
+    y-forward pass reads those and writes 3 Nx My Mz, the x pass reads and writes
+    3 Nx My Mz and reads the six Green components on the full grid (6 Mx My Mz,
+    the canonical count; the folded layout actually stores 6 Hx Hy Hz), the inverse
+    passes mirror the forward ones.  s = bytes per complex entry."""
+    Mx, My, Mz = grid
+    zf = 3 * N + 3 * Nx * Ny * Mz
+    yf = 3 * Nx * Ny * Mz + 3 * Nx * My * Mz
+    xp = 2 * 3 * Nx * My * Mz + 6 * Mx * My * Mz
+    return [zf * s, yf * s, xp * s, yf * s, zf * s]
+
+
+PASS_NAMES = ["k_zfwd", "k_ypass(fwd)", "k_xpass", "k_ypass(inv)", "k_zinv"]
+
+
+# ------------------------------------------------------------------ CPU baseline
+class CpuBaseline:
+    """Bounded sample of the reference's solve path on the host cores: `threads`
+    independent solves of the workload (one per thread, the oracle's FP64 restatement of
+    AProductCore::Aproduct + DDAModel::bicgstab, FFT grid pruned to the lattice), each
+    stopped after its 3 initial products and `iters` BiCGSTAB iterations.  The time of a
+    full solve is that sample scaled by the product count (3 + 2 * iterations) of the
+    oracle's converged FP64 solve of the same lattice.  The operators (Green spectra) are
+    built once, outside the sample, as the GPU path builds its core once."""
+
+    def __init__(self, w, threads: int):
+        import oracle as O
+
+        self.O = O
+        self.w = w
+        self.threads = threads
+        grid = tuple(lattice.smooth_size(2 * n - 1) for n in (w.Nx, w.Ny, w.Nz))
+        inc = w.incidences[0]
+        self.cores = [O.OracleCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material, grid=grid, pruned=True)
+                      for _ in range(threads)]
+        self.models = [O.OracleModel(c, inc.nK, inc.E0, inc.nE0, w.diel_old) for c in self.cores]
+        self.zero = np.zeros(3 * w.N, np.complex128)
+
+    def sample(self, iters: int) -> dict:
+        for m in self.models:
+            m.InitializeP(self.zero)
+
+        def run(k):
+            self.models[k].bicgstab(iters, TOL)  # ctypes releases the GIL for the call
+
+        th = [threading.Thread(target=run, args=(k,)) for k in range(self.threads)]
+        t0 = time.perf_counter()
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        wall = time.perf_counter() - t0
+        full_its = ORACLE_FP64_ITERATIONS_CFG2
+        scale = (3 + 2 * full_its) / (3 + 2 * iters)
+        return {"value": self.threads / (wall * scale), "unit": UNIT, "cores": self.threads, "kind": "port",
+                "sample": (f"{self.threads} threads x one solve each of the same lattice, stopped after 3 "
+                           f"initial products + {iters} BiCGSTAB iterations ({wall:.2f} s wall), scaled to "
+                           f"the {full_its}-iteration converged FP64 solve of this lattice"),
+                "sample_wall_s": wall}
+
+
+def run_reference(args, dist: Dist):
+    """The reference's CPU solve path timed on the host cores (rank 0 only)."""
+    if dist.rank != 0:
+        return
+    w = lattice.config(2)
+    threads = os.cpu_count() or 1
+    iters = max(1, args.cpu_iters)
+    cpu = CpuBaseline(w, threads)
+    for _ in range(args.warmup):
+        cpu.sample(1)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r = cpu.sample(iters)
+        vals.append(r["value"])
+    total = time.perf_counter() - t0
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+            "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "lattice": [w.Nx, w.Ny, w.Nz], "dipoles": w.N, "tol": TOL,
+                       "grid": [lattice.smooth_size(2 * n - 1) for n in (w.Nx, w.Ny, w.Nz)]},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": r["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------- ours
+def pinned_c128(n: int) -> np.ndarray:
+    import torch
+    return torch.zeros(n, dtype=torch.complex128, pin_memory=True).numpy()
+
+
+def run_ours(args, dist: Dist):
+    import torch
+
+    import tdda
+
+    dev = dist.local_rank
+    torch.cuda.set_device(dev)
+    w = lattice.config(2)
+    inc = w.incidences[0]
+    n3 = 3 * w.N
+    core = tdda.AProductCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material, w.nback, max_rhs=1, device=dev)
+    model = tdda.DDAModel(core, inc.nK, inc.E0, inc.nE0, w.diel_old)
+    stream = torch.cuda.ExternalStream(core.stream(), device=dev)
+    zero = pinned_c128(n3)
+    P_host = pinned_c128(n3)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")  # > 129 MB of L2
+
+    def flush_l2():
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+
+    def solve(prec):
+        model.InitializeP(zero)  # P = 0, as a fresh DDAModel starts (DDAModel.cpp:42)
+        flush_l2()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        info = model.solve_mixed(MAX_IT, TOL) if prec == tdda.FP32_REFINE else model.bicgstab(MAX_IT, TOL)
+        e1.record(stream)
+        e1.synchronize()
+        if info["status"] != tdda.OK:
+            raise RuntimeError(f"solve did not converge: {info}")
+        return e0.elapsed_time(e1), info
+
+    for _ in range(args.warmup):
+        solve(tdda.FP32_REFINE)
+    dist.barrier()
+    torch.cuda.synchronize(dev)
+    l0 = tdda.kernel_launches()
+    with Clocks(dev) as ck:
+        runs = [solve(tdda.FP32_REFINE) for _ in range(args.steps)]
+    launches = tdda.kernel_launches() - l0
+    ms = [r[0] for r in runs]
+    info = runs[-1][1]
+    t_max = dist.max(sum(ms))
+    value = dist.world * args.steps / (t_max / 1000.0)
+
+    # the plain FP64 solve of the same lattice, same timing rules
+    k64 = max(3, min(args.steps, args.fp64_steps))
+    solve(tdda.FP64)
+    r64 = [solve(tdda.FP64) for _ in range(k64)]
+    ms64 = [r[0] for r in r64]
+    fp64_value = dist.world * k64 / (dist.max(sum(ms64)) / 1000.0)
+
+    # end to end through the C ABI with host buffers: new densities in, P out
+    rho_host = np.ascontiguousarray(w.diel_old)
+    h2d = (2 * n3 + n3) * 16  # al and eps uploaded by UpdateAlpha, P0 by InitializeP
+    d2h = n3 * 16             # P
+    for _ in range(1):
+        model.UpdateAlpha(rho_host)
+    e2e_s = []
+    for _ in range(args.steps):
+        flush_l2()
+        t0 = time.perf_counter()
+        model.UpdateAlpha(rho_host)
+        model.InitializeP(zero)
+        model.solve_mixed(MAX_IT, TOL)
+        model._get(tdda.FIELD_P, out=P_host)
+        e2e_s.append(time.perf_counter() - t0)
+    e2e_value = dist.world * args.steps / dist.max(sum(e2e_s))
+
+    # roofline of the dominant pass kernel (per-pass CUDA events on the core's stream)
+    prof32 = core.profile_aproduct(tdda.FP32_REFINE, 1, 20)
+    prof64 = core.profile_aproduct(tdda.FP64, 1, 5)
+    n32 = 2 * info["inner_iterations"] + 2 * info["outer_iterations"]   # FP32 products per solve
+    n64 = info["outer_iterations"] + 1                                  # FP64 residual products
+    shares = [(n32 * t, "fp32", k) for k, t in enumerate(prof32)] + [(n64 * t, "fp64", k) for k, t in enumerate(prof64)]
+    _, prec, k = max(shares)
+    s = 8 if prec == "fp32" else 16
+    bytes_k = pass_bytes(core.grid, w.Nx, w.Ny, w.Nz, w.N, s)[k]
+    t_k = (prof32 if prec == "fp32" else prof64)[k]
+    peaks = measured_peaks()
+    achieved = bytes_k / (t_k * 1e-3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(tf):
+        with open(tf) as f:
+            traffic = json.load(f).get(f"{PASS_NAMES[k]}:{prec}")
+
+    cpu = None
+    if dist.rank == 0:
+        base = CpuBaseline(w, args.cpu_threads or (os.cpu_count() or 1))
+        cpu = base.sample(args.cpu_iters)
+        cpu.pop("sample_wall_s", None)
+    clocks = ck.summary()
+    if dist.rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64/f64", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "lattice": [w.Nx, w.Ny, w.Nz], "dipoles": w.N,
+                       "grid": list(core.grid), "tol": TOL, "precision": "FP32+refine",
+                       "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{dist.world}"},
+            "latency_ms": {"p50": float(np.percentile(ms, 50)), "p99": float(np.percentile(ms, 99))},
+            "solve": {"inner_iterations": info["inner_iterations"], "outer_iterations": info["outer_iterations"],
+                      "true_residual": info["true_residual"]},
+            "fp64": {"value": fp64_value, "unit": UNIT, "steps": k64,
+                     "latency_ms": {"p50": float(np.percentile(ms64, 50)), "p99": float(np.percentile(ms64, 99))},
+                     "iterations": r64[-1][1]["iterations"], "speedup_fp32_refine": value / fp64_value},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": {"kernel": f"{PASS_NAMES[k]} ({prec})", "bound": "hbm", "achieved": achieved,
+                         "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+                         "peak_source": peaks["source"], "algorithmic_bytes": bytes_k, "avg_ms": t_k,
+                         "traffic": traffic,
+                         "pass_ms_fp32": prof32, "pass_ms_fp64": prof64},
+            "gpu_launches": launches,
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--fp64-steps", type=int, default=5)
+    ap.add_argument("--cpu-iters", type=int, default=4)
+    ap.add_argument("--cpu-threads", type=int, default=0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

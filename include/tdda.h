@@ -149,6 +149,17 @@ tdda_status tdda_solve_batch(tdda_model* const* models, int n, int precision, in
  * engine the A-product runs on (cufftExecZ2Z's role, AProductCore.cpp:719). */
 tdda_status tdda_fft3d(double* data, int n0, int n1, int n2, int sign);
 
+/* measurement hooks (no counterpart in the reference) ------------------- */
+/* The CUDA stream (cudaStream_t) all work of this core runs on. */
+tdda_status tdda_core_stream(const tdda_core* core, void** stream);
+/* Kernels this library has launched in this process (graph replays included). */
+unsigned long long tdda_kernel_launches(void);
+/* Average device time in ms of each of the five A-product passes (z forward,
+ * y forward, x forward + spectral product + x inverse, y inverse, z inverse)
+ * over `reps` plain products of nrhs right-hand sides, timed with CUDA events
+ * on the core's stream. */
+tdda_status tdda_profile_aproduct(tdda_core* core, int precision, int nrhs, int reps, double* ms5);
+
 #ifdef __cplusplus
 }
 #endif

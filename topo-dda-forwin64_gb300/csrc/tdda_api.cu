@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <complex>
 #include <cstdarg>
@@ -49,6 +50,19 @@ tdda_status cuda_fail(cudaError_t e, const char* what) {
     do {                                                                \
         cudaError_t e_ = (call);                                        \
         if (e_ != cudaSuccess) return cuda_fail(e_, #call);             \
+    } while (0)
+
+// kernels launched by this library (graph replays included); a stream
+// capture records launches without running them, so it does not count
+std::atomic<unsigned long long> g_launches{0};
+thread_local bool t_capturing = false;
+inline void count_launches(int n) {
+    if (!t_capturing) g_launches += (unsigned long long)n;
+}
+#define TDDA_CK1(call)          \
+    do {                        \
+        count_launches(1);      \
+        TDDA_CK(call);          \
     } while (0)
 
 constexpr double kPi = 3.14159265358979323846264338327950288;
@@ -181,6 +195,7 @@ struct tdda_model_s {
     float2 *fP = nullptr, *fE = nullptr, *fal = nullptr, *fr = nullptr, *fr0 = nullptr, *fp = nullptr, *fu = nullptr,
            *ft = nullptr, *fAp = nullptr, *fAt = nullptr;
     std::vector<void*> allocs;
+    cd* stage = nullptr;  // pinned host staging, 2 x 3N complex
     bool P_zero = true;
     int ITERATION = 0;
     double Error = 0.0;
@@ -234,7 +249,9 @@ RhsVecs<float> vecs32(tdda_core* c, tdda_model* m, int slot) {
 tdda_status model_upload_fields(tdda_model* m, bool field_E, bool field_al) {
     tdda_core* c = m->core;
     const int N = c->N;
-    std::vector<cd> buf(3 * (size_t)N), buf2(3 * (size_t)N);
+    cd* buf = m->stage;
+    cd* buf2 = m->stage + 3 * (size_t)N;
+    const size_t bytes = sizeof(cd) * 3 * (size_t)N;
     if (field_E) {
         using namespace std::complex_literals;
         for (int i = 0; i < N; i++) {
@@ -242,10 +259,11 @@ tdda_status model_upload_fields(tdda_model* m, bool field_E, bool field_al) {
                               (m->nK[0] * c->R[3 * i] + m->nK[1] * c->R[3 * i + 1] + m->nK[2] * c->R[3 * i + 2]);
             for (int j = 0; j < 3; j++) buf[3 * i + j] = m->E0 * m->nE0[j] * (std::cos(ph) + std::sin(ph) * 1i);
         }
-        TDDA_CK(cudaMemcpyAsync(m->E, buf.data(), sizeof(cd) * buf.size(), cudaMemcpyHostToDevice, c->stream));
+        TDDA_CK(cudaMemcpyAsync(m->E, buf, bytes, cudaMemcpyHostToDevice, c->stream));
         TDDA_CK(cudaStreamSynchronize(c->stream));
     }
     if (field_al) {
+        TDDA_CK(cudaStreamSynchronize(c->stream));  // the staging buffer is free again
         for (int i = 0; i < 3 * N; i++) {
             const double v = m->diel_old[i];
             int lf = (int)std::floor(v);
@@ -259,9 +277,9 @@ tdda_status model_upload_fields(tdda_model* m, bool field_E, bool field_al) {
             buf[i] = eps;
             buf2[i] = 1.0 / get_alpha(c->K, c->d, eps, m->nE0, m->nK);
         }
-        TDDA_CK(cudaMemcpyAsync(m->diel, buf.data(), sizeof(cd) * buf.size(), cudaMemcpyHostToDevice, c->stream));
-        TDDA_CK(cudaMemcpyAsync(m->al, buf2.data(), sizeof(cd) * buf2.size(), cudaMemcpyHostToDevice, c->stream));
-        if (m->fal) TDDA_CK(tdda::launch_to_f32(3 * N, m->al, m->fal, c->stream));
+        TDDA_CK(cudaMemcpyAsync(m->diel, buf, bytes, cudaMemcpyHostToDevice, c->stream));
+        TDDA_CK(cudaMemcpyAsync(m->al, buf2, bytes, cudaMemcpyHostToDevice, c->stream));
+        if (m->fal) TDDA_CK1(tdda::launch_to_f32(3 * N, m->al, m->fal, c->stream));
         TDDA_CK(cudaStreamSynchronize(c->stream));
     }
     return TDDA_OK;
@@ -272,7 +290,7 @@ tdda_status model_alloc_f32(tdda_model* m) {
     const size_t n3 = 3 * (size_t)m->core->N;
     float2** v[] = {&m->fP, &m->fE, &m->fal, &m->fr, &m->fr0, &m->fp, &m->fu, &m->ft, &m->fAp, &m->fAt};
     for (float2** q : v) TDDA_TRY(dalloc(m->allocs, q, n3));
-    TDDA_CK(tdda::launch_to_f32((int)n3, m->al, m->fal, m->core->stream));
+    TDDA_CK1(tdda::launch_to_f32((int)n3, m->al, m->fal, m->core->stream));
     return TDDA_OK;
 }
 
@@ -295,9 +313,10 @@ template <> struct Prec<float> {
 };
 
 template <typename T>
-cudaError_t aprod(tdda_core* c, int src, int snk, int n, const RhsVecs<T>* rhs) {
+cudaError_t aprod(tdda_core* c, int src, int snk, int n, const RhsVecs<T>* rhs, cudaEvent_t* ev = nullptr) {
+    count_launches(5);
     return tdda::launch_aproduct<T>(c->g, src, snk, n, rhs, Prec<T>::green(c), Prec<T>::tw(c, 0), Prec<T>::tw(c, 1),
-                                    Prec<T>::tw(c, 2), c->cellmap, Prec<T>::grid(c), c->stream);
+                                    Prec<T>::tw(c, 2), c->cellmap, Prec<T>::grid(c), c->stream, ev);
 }
 
 template <typename T> cudaError_t enqueue_iteration(tdda_core* c, int n) {
@@ -305,6 +324,7 @@ template <typename T> cudaError_t enqueue_iteration(tdda_core* c, int n) {
     cudaError_t e;
     if ((e = aprod<T>(c, tdda::SRC_PUPD, tdda::SNK_AP, n, rhs))) return e;  // p, Ap, alpha
     if ((e = aprod<T>(c, tdda::SRC_TUPD, tdda::SNK_AT, n, rhs))) return e;  // t, At, zeta
+    count_launches(1);
     return tdda::launch_update<T>(c->g, n, rhs, 0, c->stream);              // u, P, r, rho, beta
 }
 
@@ -313,7 +333,9 @@ template <typename T> tdda_status get_iteration_graph(tdda_core* c, int n, cudaG
     if (!ex) {
         cudaGraph_t gr = nullptr;
         TDDA_CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        t_capturing = true;
         cudaError_t e = enqueue_iteration<T>(c, n);
+        t_capturing = false;
         cudaError_t e2 = cudaStreamEndCapture(c->stream, &gr);
         if (e != cudaSuccess) return cuda_fail(e, "capture of one BiCGSTAB iteration");
         if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
@@ -330,14 +352,14 @@ template <typename T> tdda_status get_iteration_graph(tdda_core* c, int n, cudaG
 template <typename T> tdda_status krylov(tdda_core* c, int n, bool p_zero, int max_it) {
     const RhsVecs<T>* rhs = Prec<T>::rhs(c);
     if (p_zero) {
-        TDDA_CK(tdda::launch_residual_is_rhs<T>(c->g, n, rhs, c->stream));
+        TDDA_CK1(tdda::launch_residual_is_rhs<T>(c->g, n, rhs, c->stream));
     } else {
-        TDDA_CK(tdda::launch_solve_begin<T>(c->g, n, rhs, c->stream));
+        TDDA_CK1(tdda::launch_solve_begin<T>(c->g, n, rhs, c->stream));
         TDDA_CK(aprod<T>(c, tdda::SRC_P, tdda::SNK_RES, n, rhs));  // r = r0 = p = E - A P
     }
     TDDA_CK(aprod<T>(c, tdda::SRC_IN, tdda::SNK_AP, n, rhs));    // Ap0, alpha
     TDDA_CK(aprod<T>(c, tdda::SRC_TUPD, tdda::SNK_AT, n, rhs));  // t, At0, zeta
-    TDDA_CK(tdda::launch_update<T>(c->g, n, rhs, 1, c->stream));
+    TDDA_CK1(tdda::launch_update<T>(c->g, n, rhs, 1, c->stream));
     cudaGraphExec_t ex;
     TDDA_TRY(get_iteration_graph<T>(c, n, &ex));
     int done_it = 0;
@@ -347,7 +369,10 @@ template <typename T> tdda_status krylov(tdda_core* c, int n, bool p_zero, int m
         bool running = false;
         for (int i = 0; i < n; i++) running |= c->hst[i].status == tdda::ST_RUNNING;
         if (!running || done_it > max_it) break;
-        for (int k = 0; k < kChunk; k++) TDDA_CK(cudaGraphLaunch(ex, c->stream));
+        for (int k = 0; k < kChunk; k++) {
+            count_launches(11);
+            TDDA_CK(cudaGraphLaunch(ex, c->stream));
+        }
         done_it += kChunk;
     }
     return TDDA_OK;
@@ -464,7 +489,7 @@ tdda_status solve_mixed(tdda_model* const* ms, int n, int max_it, double tol, td
             if (done[i]) c->hst[i].status = tdda::ST_CONVERGED;
         }
         TDDA_CK(cudaMemcpyAsync(c->st64, c->hst, sizeof(SolveState) * n, cudaMemcpyHostToDevice, c->stream));
-        TDDA_CK(tdda::launch_solve_begin<double>(c->g, n, c->rhs64, c->stream));
+        TDDA_CK1(tdda::launch_solve_begin<double>(c->g, n, c->rhs64, c->stream));
         TDDA_CK(aprod<double>(c, tdda::SRC_P, tdda::SNK_RES, n, c->rhs64));
         TDDA_CK(cudaMemcpyAsync(c->hst, c->st64, sizeof(SolveState) * n, cudaMemcpyDeviceToHost, c->stream));
         TDDA_CK(cudaStreamSynchronize(c->stream));
@@ -504,8 +529,8 @@ tdda_status solve_mixed(tdda_model* const* ms, int n, int max_it, double tol, td
                 c->hst[i].status = tdda::ST_CONVERGED;
                 continue;
             }
-            TDDA_CK(tdda::launch_to_f32(3 * c->N, m->r, m->fE, c->stream));
-            TDDA_CK(tdda::launch_zero<float>(3LL * c->N, m->fP, c->stream));
+            TDDA_CK1(tdda::launch_to_f32(3 * c->N, m->r, m->fE, c->stream));
+            TDDA_CK1(tdda::launch_zero<float>(3LL * c->N, m->fP, c->stream));
         }
         TDDA_CK(cudaMemcpyAsync(c->st32, c->hst, sizeof(SolveState) * n, cudaMemcpyHostToDevice, c->stream));
         TDDA_TRY(krylov<float>(c, n, true, max_it));
@@ -519,7 +544,7 @@ tdda_status solve_mixed(tdda_model* const* ms, int n, int max_it, double tol, td
                 stat[i] = TDDA_ERR_NAN;
                 continue;
             }
-            TDDA_CK(tdda::launch_accumulate(3 * c->N, ms[i]->fP, ms[i]->P, c->stream));
+            TDDA_CK1(tdda::launch_accumulate(3 * c->N, ms[i]->fP, ms[i]->P, c->stream));
         }
     }
     TDDA_CK(cudaStreamSynchronize(c->stream));
@@ -725,6 +750,7 @@ tdda_status tdda_core_create(const tdda_core_desc* desc, tdda_core** out) {
     // Green spectrum (AProductCore.cpp:53-229), on a temporary full grid
     double2* full6 = nullptr;
     TDDA_CORE_CK(cudaMallocAsync((void**)&full6, sizeof(double2) * 6 * (size_t)Mfull, c->stream));
+    count_launches(5);
     cudaError_t ge = tdda::launch_green(g, c->K, c->d, c->tw64[0], c->tw64[1], c->tw64[2], full6, c->green64,
                                         c->green32, c->stream);
     cudaError_t fe = cudaFreeAsync(full6, c->stream);
@@ -796,10 +822,10 @@ tdda_status tdda_aproduct(tdda_core* c, int precision, const double* b, double* 
     if (precision == TDDA_FP64) {
         TDDA_CK(aprod<double>(c, tdda::SRC_IN, tdda::SNK_OUT, 1, c->rhs64 + c->max_rhs));
     } else {
-        TDDA_CK(tdda::launch_to_f32((int)n3, c->vin64, c->vin32, c->stream));
+        TDDA_CK1(tdda::launch_to_f32((int)n3, c->vin64, c->vin32, c->stream));
         TDDA_CK(aprod<float>(c, tdda::SRC_IN, tdda::SNK_OUT, 1, c->rhs32 + c->max_rhs));
-        TDDA_CK(tdda::launch_zero<double>((long long)n3, c->vout64, c->stream));
-        TDDA_CK(tdda::launch_accumulate((int)n3, c->vout32, c->vout64, c->stream));
+        TDDA_CK1(tdda::launch_zero<double>((long long)n3, c->vout64, c->stream));
+        TDDA_CK1(tdda::launch_accumulate((int)n3, c->vout32, c->vout64, c->stream));
     }
     TDDA_CK(cudaMemcpyAsync(y, c->vout64, sizeof(double2) * n3, kind_out(mem), c->stream));
     TDDA_CK(cudaStreamSynchronize(c->stream));
@@ -831,7 +857,13 @@ tdda_status tdda_model_create(tdda_core* c, const double* nK, double E0, const d
             return s;
         }
     }
-    cudaError_t e = cudaMemsetAsync(m->P, 0, sizeof(double2) * n3, c->stream);
+    cudaError_t e = cudaMallocHost((void**)&m->stage, 2 * sizeof(cd) * n3);
+    if (e != cudaSuccess) {
+        m->stage = nullptr;
+        tdda_model_destroy(m);
+        return cuda_fail(e, "cudaMallocHost");
+    }
+    e = cudaMemsetAsync(m->P, 0, sizeof(double2) * n3, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(m->Ein, 0, sizeof(double2) * n3, c->stream);
     if (e != cudaSuccess) {
         tdda_model_destroy(m);
@@ -851,6 +883,7 @@ tdda_status tdda_model_destroy(tdda_model* m) {
     cudaSetDevice(m->core->device);
     cudaStreamSynchronize(m->core->stream);
     free_all(m->allocs);
+    if (m->stage) cudaFreeHost(m->stage);
     delete m;
     return TDDA_OK;
 }
@@ -904,9 +937,12 @@ tdda_status tdda_model_initialize_P(tdda_model* m, const double* P, int mem) {
         return TDDA_ERR_INVALID_ARGUMENT;
     }
     TDDA_TRY(set_device(m->core->device));
-    TDDA_CK(cudaMemcpyAsync(m->P, P, sizeof(double2) * 3 * (size_t)m->core->N, kind_in(mem), m->core->stream));
+    const size_t n = 6 * (size_t)m->core->N;
+    TDDA_CK(cudaMemcpyAsync(m->P, P, sizeof(double) * n, kind_in(mem), m->core->stream));
+    bool zero = mem == TDDA_MEM_HOST;
+    for (size_t i = 0; zero && i < n; i++) zero = P[i] == 0.0;
     TDDA_CK(cudaStreamSynchronize(m->core->stream));
-    m->P_zero = false;
+    m->P_zero = zero;  // A 0 = 0 exactly, so the solve may skip its first product
     return TDDA_OK;
 }
 
@@ -959,7 +995,7 @@ tdda_status tdda_model_update_E_in_structure(tdda_model* m) {
         return TDDA_ERR_INVALID_ARGUMENT;
     }
     TDDA_TRY(set_device(m->core->device));
-    TDDA_CK(tdda::launch_einternal(3 * m->core->N, m->al, m->P, m->diel, m->Ein, m->core->stream));
+    TDDA_CK1(tdda::launch_einternal(3 * m->core->N, m->al, m->P, m->diel, m->Ein, m->core->stream));
     TDDA_CK(cudaStreamSynchronize(m->core->stream));
     return TDDA_OK;
 }
@@ -1013,11 +1049,66 @@ tdda_status tdda_fft3d(double* data, int n0, int n1, int n2, int sign) {
         cudaMemcpy(tw[a], w64.data(), sizeof(double2) * n[a], cudaMemcpyHostToDevice);
     }
     cudaError_t e = tdda::configure_kernels();
+    count_launches(3);
     if (e == cudaSuccess) e = tdda::launch_fft3d_f64((double2*)data, p[0], p[1], p[2], tw[0], tw[1], tw[2], sign, 0);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     free_all(tmp);
     if (e != cudaSuccess) return cuda_fail(e, "tdda_fft3d");
     return TDDA_OK;
+}
+
+tdda_status tdda_core_stream(const tdda_core* c, void** stream) {
+    if (!c || !stream) {
+        set_err("null argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    *stream = (void*)c->stream;
+    return TDDA_OK;
+}
+
+unsigned long long tdda_kernel_launches(void) { return g_launches.load(); }
+
+tdda_status tdda_profile_aproduct(tdda_core* c, int precision, int nrhs, int reps, double* ms5) {
+    if (!c || !ms5 || reps < 1 || nrhs < 1 || nrhs > c->max_rhs ||
+        (precision != TDDA_FP64 && precision != TDDA_FP32_REFINE)) {
+        set_err("invalid argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    TDDA_TRY(set_device(c->device));
+    // nrhs plain products on the core's input / output vectors (the same
+    // vectors for every right-hand side: the passes read and write the
+    // grid slot of each right-hand side separately)
+    std::vector<RhsVecs<double>> h64(nrhs, RhsVecs<double>{});
+    std::vector<RhsVecs<float>> h32(nrhs, RhsVecs<float>{});
+    for (int i = 0; i < nrhs; i++) {
+        h64[i].p = c->vin64;
+        h64[i].Ap = c->vout64;
+        h32[i].p = c->vin32;
+        h32[i].Ap = c->vout32;
+    }
+    TDDA_CK(cudaMemcpyAsync(c->rhs64, h64.data(), sizeof(RhsVecs<double>) * nrhs, cudaMemcpyHostToDevice, c->stream));
+    TDDA_CK(cudaMemcpyAsync(c->rhs32, h32.data(), sizeof(RhsVecs<float>) * nrhs, cudaMemcpyHostToDevice, c->stream));
+    cudaEvent_t ev[6];
+    for (auto& e : ev) TDDA_CK(cudaEventCreate(&e));
+    double acc[5] = {0, 0, 0, 0, 0};
+    tdda_status st = TDDA_OK;
+    for (int r = 0; r < reps + 1 && st == TDDA_OK; r++) {  // the first run is a warm-up
+        cudaError_t e = precision == TDDA_FP64 ? aprod<double>(c, tdda::SRC_IN, tdda::SNK_OUT, nrhs, c->rhs64, ev)
+                                               : aprod<float>(c, tdda::SRC_IN, tdda::SNK_OUT, nrhs, c->rhs32, ev);
+        if (e == cudaSuccess) e = cudaEventSynchronize(ev[5]);
+        if (e != cudaSuccess) {
+            st = cuda_fail(e, "profiled A-product");
+            break;
+        }
+        for (int k = 0; k < 5 && r > 0; k++) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+            acc[k] += ms;
+        }
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    for (int k = 0; k < 5; k++) ms5[k] = acc[k] / reps;
+    return st;
 }
 
 }  // extern "C"

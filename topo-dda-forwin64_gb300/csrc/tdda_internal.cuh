@@ -87,12 +87,13 @@ cudaError_t launch_green(const Geom& g, double K, double d, const double2* tw64x
                          float2* green32, cudaStream_t stream);
 
 // One A-product over nrhs right-hand sides.  rhs[] lives in device memory.
+// ev, when given, holds 6 events recorded before K1..K5 and after K5.
 // For SRC_IN with SNK_OUT / SNK_ALB the vectors used are rhs[b].p (input)
 // and rhs[b].Ap (output); SNK_RES reads P and E and writes r, r0, p.
 template <typename T>
 cudaError_t launch_aproduct(const Geom& g, int src, int snk, int nrhs, const RhsVecs<T>* rhs,
                             const cx<T>* green, const cx<T>* twx, const cx<T>* twy, const cx<T>* twz,
-                            const int* cellmap, cx<T>* grid, cudaStream_t stream);
+                            const int* cellmap, cx<T>* grid, cudaStream_t stream, cudaEvent_t* ev = nullptr);
 
 // u = zeta Ap; z = zeta r - alpha u; P += alpha p + z; r = t - zeta At;
 // rho_prev = rho; rho = r0.r; convergence / breakdown / iteration limit;

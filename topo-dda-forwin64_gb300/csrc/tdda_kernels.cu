@@ -725,8 +725,9 @@ cudaError_t launch_fft3d_f64(double2* data, const AxisPlan& p0, const AxisPlan& 
 template <typename T>
 cudaError_t launch_aproduct(const Geom& g, int src, int snk, int nrhs, const RhsVecs<T>* rhs, const cx<T>* green,
                             const cx<T>* twx, const cx<T>* twy, const cx<T>* twz, const int* cellmap, cx<T>* grid,
-                            cudaStream_t stream) {
+                            cudaStream_t stream, cudaEvent_t* ev) {
     cudaError_t err;
+    if (ev) cudaEventRecord(ev[0], stream);
     const int LZ = z_lines<T>(g.pz);
     const dim3 gz((g.Nx * g.Ny + LZ - 1) / LZ, nrhs);
     const size_t smz = zsmem<T>(g);
@@ -746,21 +747,25 @@ cudaError_t launch_aproduct(const Geom& g, int src, int snk, int nrhs, const Rhs
             break;
     }
     if ((err = cudaGetLastError())) return err;
+    if (ev) cudaEventRecord(ev[1], stream);
     // K2
     const int YT = y_tile<T>(g.py);
     const dim3 gy(g.Nx * ((g.pz.M + YT - 1) / YT), 3, nrhs);
     const size_t smy = ysmem<T>(g);
     k_ypass<T, -1><<<gy, kNT, smy, stream>>>(g, rhs, twy, grid);
     if ((err = cudaGetLastError())) return err;
+    if (ev) cudaEventRecord(ev[2], stream);
     // K3
     const int XT = x_tile<T>(g.px);
     const dim3 gx(g.py.M * ((g.pz.M + XT - 1) / XT), nrhs);
     const size_t smx = xsmem<T>(g);
     k_xpass<T><<<gx, kNT, smx, stream>>>(g, rhs, green, twx, grid);
     if ((err = cudaGetLastError())) return err;
+    if (ev) cudaEventRecord(ev[3], stream);
     // K4
     k_ypass<T, +1><<<gy, kNT, smy, stream>>>(g, rhs, twy, grid);
     if ((err = cudaGetLastError())) return err;
+    if (ev) cudaEventRecord(ev[4], stream);
     // K5
 #define TDDA_ZINV(S, K) k_zinv<T, S, K><<<gz, kNT, smz, stream>>>(g, rhs, twz, cellmap, grid)
     if (snk == SNK_OUT) TDDA_ZINV(SRC_IN, SNK_OUT);
@@ -769,6 +774,7 @@ cudaError_t launch_aproduct(const Geom& g, int src, int snk, int nrhs, const Rhs
     else if (snk == SNK_AT) TDDA_ZINV(SRC_TUPD, SNK_AT);
     else TDDA_ZINV(SRC_P, SNK_RES);
 #undef TDDA_ZINV
+    if (ev) cudaEventRecord(ev[5], stream);
     return cudaGetLastError();
 }
 
@@ -814,7 +820,7 @@ template <typename T> cudaError_t launch_zero(long long n, cx<T>* v, cudaStream_
 #define TDDA_INST(T)                                                                                               \
     template cudaError_t launch_aproduct<T>(const Geom&, int, int, int, const RhsVecs<T>*, const cx<T>*,          \
                                             const cx<T>*, const cx<T>*, const cx<T>*, const int*, cx<T>*,         \
-                                            cudaStream_t);                                                         \
+                                            cudaStream_t, cudaEvent_t*);                                           \
     template cudaError_t launch_update<T>(const Geom&, int, const RhsVecs<T>*, int, cudaStream_t);                 \
     template cudaError_t launch_solve_begin<T>(const Geom&, int, const RhsVecs<T>*, cudaStream_t);                 \
     template cudaError_t launch_residual_is_rhs<T>(const Geom&, int, const RhsVecs<T>*, cudaStream_t);             \

@@ -42,7 +42,7 @@ EXPORTS = [
     "tdda_model_update_alpha", "tdda_model_update_alpha_single", "tdda_model_change_E", "tdda_model_reset_E",
     "tdda_model_initialize_P", "tdda_model_aproduct_with_alb", "tdda_model_bicgstab", "tdda_model_solve_mixed",
     "tdda_model_update_E_in_structure", "tdda_model_get", "tdda_model_iterations", "tdda_solve_batch",
-    "tdda_fft3d",
+    "tdda_fft3d", "tdda_core_stream", "tdda_kernel_launches", "tdda_profile_aproduct",
 ]
 
 
@@ -106,6 +106,9 @@ def load() -> ctypes.CDLL:
         "tdda_model_iterations": (i, [vp]),
         "tdda_solve_batch": (i, [ctypes.POINTER(vp), i, i, i, d, ctypes.POINTER(SolveInfo)]),
         "tdda_fft3d": (i, [vp, i, i, i, i]),
+        "tdda_core_stream": (i, [vp, ctypes.POINTER(vp)]),
+        "tdda_kernel_launches": (ctypes.c_ulonglong, []),
+        "tdda_profile_aproduct": (i, [vp, i, i, i, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -117,6 +120,11 @@ def load() -> ctypes.CDLL:
 
 def device_count() -> int:
     return load().tdda_device_count()
+
+
+def kernel_launches() -> int:
+    """Kernels libtdda has launched in this process."""
+    return int(load().tdda_kernel_launches())
 
 
 def _check(st: int, where: str, allowed=(OK,)):
@@ -188,6 +196,19 @@ class AProductCore:
         _check(load().tdda_aproduct(self.h, precision, ctypes.c_void_p(b_ptr), ctypes.c_void_p(y_ptr),
                                     MEM_DEVICE), "tdda_aproduct")
 
+    def stream(self) -> int:
+        """The cudaStream_t of this core (for events recorded on it)."""
+        p = ctypes.c_void_p()
+        _check(load().tdda_core_stream(self.h, ctypes.byref(p)), "tdda_core_stream")
+        return p.value or 0
+
+    def profile_aproduct(self, precision: int = FP32_REFINE, nrhs: int = 1, reps: int = 10) -> list:
+        """Average ms of the five passes of one A-product (CUDA events on the core stream)."""
+        out = (ctypes.c_double * 5)()
+        _check(load().tdda_profile_aproduct(self.h, int(precision), int(nrhs), int(reps), out),
+               "tdda_profile_aproduct")
+        return list(out)
+
     def LDR_inter(self, x, y, z) -> np.ndarray:
         out = np.zeros(6, np.complex128)
         _check(load().tdda_core_ldr_inter(self.h, x, y, z, _dptr(out.view(np.float64))), "tdda_core_ldr_inter")
@@ -223,8 +244,11 @@ class DDAModel:
         self.h = h
         self.last_info = None
 
-    def _get(self, field: int) -> np.ndarray:
-        out = np.empty(self.n3, np.complex128)
+    def _get(self, field: int, out: np.ndarray = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(self.n3, np.complex128)
+        elif out.dtype != np.complex128 or out.size != self.n3 or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous complex128 array of 3N entries")
         _check(load().tdda_model_get(self.h, field, _ptr(out), MEM_HOST), "tdda_model_get")
         return out
 
