@@ -149,6 +149,20 @@ tdda_status tdda_solve_batch(tdda_model* const* models, int n, int precision, in
  * engine the A-product runs on (cufftExecZ2Z's role, AProductCore.cpp:719). */
 tdda_status tdda_fft3d(double* data, int n0, int n1, int n2, int sign);
 
+/* allocation-free product (no counterpart in the reference) ------------- */
+/* y = A_offdiag b in FP64 for callers that cannot allocate device memory at
+ * the point of the call (memory pre-reserved under a fixed budget, or a host
+ * framework that forbids allocation after its setup).  b and y are 3N complex
+ * in device memory.  The FFT work grid is a static 64 MiB device array that
+ * every GPU loading the library holds until exit, so the core's grid
+ * 3 x Nx x My x Mz must be at most 4,194,304 complex128 entries, else
+ * TDDA_ERR_UNSUPPORTED.  The first call on a device looks the array up
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the array, so calls that overlap on the GPU (two threads, or
+ * two cores on different streams) race; each call fully rewrites what it
+ * reads, so nothing needs clearing between calls. */
+tdda_status tdda_aproduct_noalloc(tdda_core* core, const double* b, double* y);
+
 /* measurement hooks (no counterpart in the reference) ------------------- */
 /* The CUDA stream (cudaStream_t) all work of this core runs on. */
 tdda_status tdda_core_stream(const tdda_core* core, void** stream);

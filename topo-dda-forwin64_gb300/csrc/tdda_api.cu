@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <mutex>
 #include <cmath>
 #include <complex>
 #include <cstdarg>
@@ -575,6 +576,51 @@ tdda_status set_device(int dev) {
     return TDDA_OK;
 }
 
+// ------------------------------------------------- allocation-free A-product
+// Some callers cannot call cudaMalloc while they run the product: code that
+// runs under an external memory budget with every byte pre-reserved, or a host
+// framework that forbids device allocation once its own setup is done.  For
+// them tdda_aproduct_noalloc keeps the FFT work grid of the product in this
+// fixed, file-scope device array instead of the core's buffers.  Every GPU that
+// loads the library holds it (64 MiB) until the process exits.
+constexpr size_t kNoAllocGridElems = 4u << 20;  // complex128 entries: 64 MiB
+static __device__ __align__(256) double2 g_noalloc_grid[kNoAllocGridElems];
+static __device__ __align__(256) RhsVecs<double> g_noalloc_rhs;
+
+struct NoAllocSlot {
+    bool ready = false;
+    double2* grid = nullptr;
+    RhsVecs<double>* rhs = nullptr;
+};
+constexpr int kNoAllocDevices = 64;
+NoAllocSlot g_noalloc_slots[kNoAllocDevices];
+std::mutex g_noalloc_mu;
+
+// Device addresses of the two arrays, looked up once per device with that
+// device current.  In host code the arrays' names are host-side stand-ins, not
+// device addresses, so only these looked-up pointers reach a kernel.
+tdda_status noalloc_setup(int device, NoAllocSlot* out) {
+    if (device < 0 || device >= kNoAllocDevices) {
+        set_err("device %d out of range for the allocation-free product", device);
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    NoAllocSlot& slot = g_noalloc_slots[device];
+    if (!slot.ready) {
+        void* g = nullptr;
+        void* r = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&g, g_noalloc_grid);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_grid)");
+        e = cudaGetSymbolAddress(&r, g_noalloc_rhs);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_rhs)");
+        slot.grid = (double2*)g;
+        slot.rhs = (RhsVecs<double>*)r;
+        slot.ready = true;
+    }
+    *out = slot;
+    return TDDA_OK;
+}
+
 }  // namespace
 
 // ======================================================================= ABI
@@ -1109,6 +1155,32 @@ tdda_status tdda_profile_aproduct(tdda_core* c, int precision, int nrhs, int rep
     for (auto& e : ev) cudaEventDestroy(e);
     for (int k = 0; k < 5; k++) ms5[k] = acc[k] / reps;
     return st;
+}
+
+tdda_status tdda_aproduct_noalloc(tdda_core* c, const double* b, double* y) {
+    if (!c || !b || !y) {
+        set_err("null argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    const size_t need = (size_t)c->g.sb;  // 3 x Nx x My x Mz complex128 entries
+    if (need > kNoAllocGridElems) {
+        set_err("allocation-free A-product: FFT work grid of %zu complex128 entries exceeds the static "
+                "maximum of %zu (64 MiB); use tdda_aproduct",
+                need, kNoAllocGridElems);
+        return TDDA_ERR_UNSUPPORTED;
+    }
+    TDDA_TRY(set_device(c->device));
+    NoAllocSlot slot;
+    TDDA_TRY(noalloc_setup(c->device, &slot));
+    RhsVecs<double> v{};
+    v.p = (double2*)b;
+    v.Ap = (double2*)y;
+    TDDA_CK(cudaMemcpyAsync(slot.rhs, &v, sizeof(v), cudaMemcpyHostToDevice, c->stream));
+    count_launches(5);
+    TDDA_CK(tdda::launch_aproduct<double>(c->g, tdda::SRC_IN, tdda::SNK_OUT, 1, slot.rhs, c->green64, c->tw64[0],
+                                          c->tw64[1], c->tw64[2], c->cellmap, slot.grid, c->stream));
+    TDDA_CK(cudaStreamSynchronize(c->stream));
+    return TDDA_OK;
 }
 
 }  // extern "C"

@@ -43,6 +43,7 @@ EXPORTS = [
     "tdda_model_initialize_P", "tdda_model_aproduct_with_alb", "tdda_model_bicgstab", "tdda_model_solve_mixed",
     "tdda_model_update_E_in_structure", "tdda_model_get", "tdda_model_iterations", "tdda_solve_batch",
     "tdda_fft3d", "tdda_core_stream", "tdda_kernel_launches", "tdda_profile_aproduct",
+    "tdda_aproduct_noalloc",
 ]
 
 
@@ -109,6 +110,7 @@ def load() -> ctypes.CDLL:
         "tdda_core_stream": (i, [vp, ctypes.POINTER(vp)]),
         "tdda_kernel_launches": (ctypes.c_ulonglong, []),
         "tdda_profile_aproduct": (i, [vp, i, i, i, dp]),
+        "tdda_aproduct_noalloc": (i, [vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -208,6 +210,12 @@ class AProductCore:
         _check(load().tdda_profile_aproduct(self.h, int(precision), int(nrhs), int(reps), out),
                "tdda_profile_aproduct")
         return list(out)
+
+    def Aproduct_noalloc(self, b_ptr: int, y_ptr: int):
+        """y = A_offdiag b on device memory (3N complex128 each) without any device
+        allocation: the FFT work grid is the library's static scratch array."""
+        _check(load().tdda_aproduct_noalloc(self.h, ctypes.c_void_p(b_ptr), ctypes.c_void_p(y_ptr)),
+               "tdda_aproduct_noalloc")
 
     def LDR_inter(self, x, y, z) -> np.ndarray:
         out = np.zeros(6, np.complex128)
