@@ -300,7 +300,7 @@ def run_ours(args, dist: Dist):
 
     # end to end through the C ABI with host buffers: new densities in, P out
     rho_host = np.ascontiguousarray(w.diel_old)
-    h2d = (2 * n3 + n3) * 16  # al and eps uploaded by UpdateAlpha, P0 by InitializeP
+    h2d = n3 * 8 + n3 * 16    # the 3N densities uploaded by UpdateAlpha, P0 by InitializeP
     d2h = n3 * 16             # P
     for _ in range(1):
         model.UpdateAlpha(rho_host)

@@ -2,6 +2,7 @@
 
 Every call goes through libtdda's C ABI.  Tolerances:
   * FFT engine / A-product, FP64: 1e-12 relative (norm-wise) -- rounding of two FFTs;
+  * polarisability al: 1e-14 (device FP64 complex division against the host's);
   * A-product, FP32 convolution: 1e-5 relative;
   * FP64 solve at the reference's tolerance 1e-5: converged, |E - A P|/|E| <= 1e-5 checked
     with the oracle, P and Einternal within 2e-4 of the reference's and the iteration
@@ -66,7 +67,7 @@ def test_aproduct_matches_reference(name):
     c = _core(g)
     Nx, Ny, Nz = (int(v) for v in g["box"])
     m = tdda.DDAModel(c, g["nK"], float(g["E0"]), g["nE0"], g["diel_old"])
-    assert rel(m.get_al(), g["al"]) <= 1e-15
+    assert rel(m.get_al(), g["al"]) <= 1e-14  # device FP64 complex division vs the host's
     for b, y, yw in zip(g["b"], g["y"], g["y_alb"]):
         assert rel(c.Aproduct(b), y) <= 1e-12
         assert rel(m.Aproductwithalb(b), yw) <= 1e-12
@@ -204,11 +205,12 @@ def test_update_alpha_matches_oracle():
     d2 = np.clip(g["diel_old"] * 0.5 + 0.25, 0, 1)
     m.UpdateAlpha(d2)
     om = O.OracleModel(_ocore(g), g["nK"], float(g["E0"]), g["nE0"], d2)
-    assert rel(m.get_al(), om.al) <= 1e-15
+    assert rel(m.get_al(), om.al) <= 1e-14
+    assert rel(m.get_diel(), om.diel) <= 1e-15
     m.UpdateAlphaSingle(3, 1.0)
     d3 = d2.copy()
     d3[9:12] = 1.0
     om.UpdateAlpha(d3)
-    assert rel(m.get_al(), om.al) <= 1e-15
+    assert rel(m.get_al(), om.al) <= 1e-14
     m.reset_E()
     assert rel(m.get_E(), om.E) <= 1e-15

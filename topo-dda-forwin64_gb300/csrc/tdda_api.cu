@@ -96,9 +96,12 @@ bool make_plan(int M, AxisPlan* ap) {
     if (m != 1 || (int)r.size() > tdda::kMaxStages) return false;
     ap->nstages = (int)r.size();
     ap->rmin = 8;
+    int span = 1;
     for (size_t i = 0; i < r.size(); i++) {
         ap->radix[i] = r[i];
         ap->rmin = std::min(ap->rmin, r[i]);
+        ap->ns[i] = tdda::fastdiv_make((unsigned)span);
+        span *= r[i];
     }
     if (r.empty()) ap->rmin = 1;
     return true;
@@ -137,17 +140,6 @@ void ldr_host(double K, double x, double y, double z, cd out[6]) {
     out[3] = c1 * (c2 * (rsq - 3 * ys) - K * K * (zs + xs));
     out[4] = c1 * (yz * c3);
     out[5] = c1 * (c2 * (rsq - 3 * zs) - K * K * (xs + ys));
-}
-
-// Get_Alpha, LDR (tools.cpp:617-630)
-cd get_alpha(double K, double d, cd diel, const double nE0[3], const double nK[3]) {
-    using namespace std::complex_literals;
-    const double b1 = -1.891531, b2 = 0.1648469, b3 = -1.7700004;
-    cd a1 = (3 * std::pow(d, 3) / (4 * kPi)) * (diel - 1.0) / (diel + 2.0);
-    cd result = 0.0 + (2.0 / 3.0) * std::pow(K * d, 3) * 1.0i;
-    double S = std::pow(nE0[0] * nK[0], 2) + std::pow(nE0[1] * nK[1], 2) + std::pow(nE0[2] * nK[2], 2);
-    result = 1.0 + (a1 / std::pow(d, 3)) * ((b1 + diel * b2 + diel * b3 * S) * std::pow(K * d, 2) - result);
-    return a1 / result;
 }
 
 template <typename T> struct Graphs {
@@ -191,12 +183,13 @@ struct tdda_model_s {
     std::vector<double> diel_old;
     // FP64 state: P, E, al, diel, Einternal and the Krylov vectors
     double2 *P = nullptr, *E = nullptr, *al = nullptr, *diel = nullptr, *Ein = nullptr;
+    double* dold = nullptr;  // the 3N densities on the device
     double2 *r = nullptr, *r0 = nullptr, *p = nullptr, *u = nullptr, *t = nullptr, *Ap = nullptr, *At = nullptr;
     // FP32 Krylov vectors of the mixed solve (allocated on first use)
     float2 *fP = nullptr, *fE = nullptr, *fal = nullptr, *fr = nullptr, *fr0 = nullptr, *fp = nullptr, *fu = nullptr,
            *ft = nullptr, *fAp = nullptr, *fAt = nullptr;
     std::vector<void*> allocs;
-    cd* stage = nullptr;  // pinned host staging, 2 x 3N complex
+    cd* stage = nullptr;  // pinned host staging, 3N complex
     bool P_zero = true;
     int ITERATION = 0;
     double Error = 0.0;
@@ -251,7 +244,6 @@ tdda_status model_upload_fields(tdda_model* m, bool field_E, bool field_al) {
     tdda_core* c = m->core;
     const int N = c->N;
     cd* buf = m->stage;
-    cd* buf2 = m->stage + 3 * (size_t)N;
     const size_t bytes = sizeof(cd) * 3 * (size_t)N;
     if (field_E) {
         using namespace std::complex_literals;
@@ -264,23 +256,30 @@ tdda_status model_upload_fields(tdda_model* m, bool field_E, bool field_al) {
         TDDA_CK(cudaStreamSynchronize(c->stream));
     }
     if (field_al) {
-        TDDA_CK(cudaStreamSynchronize(c->stream));  // the staging buffer is free again
+        // eps and al on the device (DDAModel.cpp:54-63, tools.cpp:617-630); the
+        // density range is checked here so that the kernel never indexes
+        // outside the material table
         for (int i = 0; i < 3 * N; i++) {
             const double v = m->diel_old[i];
-            int lf = (int)std::floor(v);
-            int ln = lf + 1;
-            if (lf >= 1) ln = lf;
-            if (lf < 0 || lf >= c->nmat || ln >= c->nmat) {
+            const int lf = (int)std::floor(v);
+            const int ln = lf >= 1 ? lf : lf + 1;
+            if (!(v == v) || lf < 0 || lf >= c->nmat || ln >= c->nmat) {
                 set_err("density %g of entry %d is outside the material table", v, i);
                 return TDDA_ERR_INVALID_ARGUMENT;
             }
-            cd eps = c->material[lf] + (v - double(lf)) * (c->material[ln] - c->material[lf]);
-            buf[i] = eps;
-            buf2[i] = 1.0 / get_alpha(c->K, c->d, eps, m->nE0, m->nK);
         }
-        TDDA_CK(cudaMemcpyAsync(m->diel, buf, bytes, cudaMemcpyHostToDevice, c->stream));
-        TDDA_CK(cudaMemcpyAsync(m->al, buf2, bytes, cudaMemcpyHostToDevice, c->stream));
-        if (m->fal) TDDA_CK1(tdda::launch_to_f32(3 * N, m->al, m->fal, c->stream));
+        tdda::AlphaParams ap;
+        std::memset(&ap, 0, sizeof(ap));
+        ap.a1c = 3 * std::pow(c->d, 3) / (4 * kPi);
+        ap.d3 = std::pow(c->d, 3);
+        ap.Kd2 = std::pow(c->K * c->d, 2);
+        ap.rad = (2.0 / 3.0) * std::pow(c->K * c->d, 3);
+        ap.S = std::pow(m->nE0[0] * m->nK[0], 2) + std::pow(m->nE0[1] * m->nK[1], 2) + std::pow(m->nE0[2] * m->nK[2], 2);
+        ap.nmat = c->nmat;
+        for (int k = 0; k < c->nmat; k++) ap.mat[k] = make_double2(c->material[k].real(), c->material[k].imag());
+        TDDA_CK(cudaMemcpyAsync(m->dold, m->diel_old.data(), sizeof(double) * 3 * (size_t)N, cudaMemcpyHostToDevice,
+                                c->stream));
+        TDDA_CK1(tdda::launch_model_alpha(3 * N, m->dold, ap, m->diel, m->al, m->fal, c->stream));
         TDDA_CK(cudaStreamSynchronize(c->stream));
     }
     return TDDA_OK;
@@ -477,9 +476,11 @@ tdda_status solve_mixed(tdda_model* const* ms, int n, int max_it, double tol, td
     std::vector<int> done(n, 0), inner(n, 0), outer(n, 0);
     std::vector<double> Enorm(n, 0.0), res(n, 1.0), prev_res(n, 1e300);
     std::vector<tdda_status> stat(n, TDDA_NOT_CONVERGED);
+    bool all_p_zero = true;
     for (int i = 0; i < n; i++) {
         h64[i] = vecs64(c, ms[i], i);
         h32[i] = vecs32(c, ms[i], i);
+        all_p_zero &= ms[i]->P_zero;
     }
     TDDA_CK(cudaMemcpyAsync(c->rhs64, h64.data(), sizeof(RhsVecs<double>) * n, cudaMemcpyHostToDevice, c->stream));
     TDDA_CK(cudaMemcpyAsync(c->rhs32, h32.data(), sizeof(RhsVecs<float>) * n, cudaMemcpyHostToDevice, c->stream));
@@ -490,8 +491,13 @@ tdda_status solve_mixed(tdda_model* const* ms, int n, int max_it, double tol, td
             if (done[i]) c->hst[i].status = tdda::ST_CONVERGED;
         }
         TDDA_CK(cudaMemcpyAsync(c->st64, c->hst, sizeof(SolveState) * n, cudaMemcpyHostToDevice, c->stream));
-        TDDA_CK1(tdda::launch_solve_begin<double>(c->g, n, c->rhs64, c->stream));
-        TDDA_CK(aprod<double>(c, tdda::SRC_P, tdda::SNK_RES, n, c->rhs64));
+        if (outer_it == 0 && all_p_zero) {
+            // P = 0: the residual is E exactly (A 0 = 0), no product needed
+            TDDA_CK1(tdda::launch_residual_is_rhs<double>(c->g, n, c->rhs64, c->stream));
+        } else {
+            TDDA_CK1(tdda::launch_solve_begin<double>(c->g, n, c->rhs64, c->stream));
+            TDDA_CK(aprod<double>(c, tdda::SRC_P, tdda::SNK_RES, n, c->rhs64));
+        }
         TDDA_CK(cudaMemcpyAsync(c->hst, c->st64, sizeof(SolveState) * n, cudaMemcpyDeviceToHost, c->stream));
         TDDA_CK(cudaStreamSynchronize(c->stream));
         bool open = false;
@@ -649,6 +655,10 @@ tdda_status tdda_core_create(const tdda_core_desc* desc, tdda_core** out) {
         desc->max_rhs > 64) {
         set_err("invalid core description");
         return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    if (desc->nmat > tdda::kMaxMaterials) {
+        set_err("at most %d materials", tdda::kMaxMaterials);
+        return TDDA_ERR_UNSUPPORTED;
     }
     if (desc->method != TDDA_METHOD_LDR) {
         set_err("only the LDR interaction tensor is built (FCD needs the Si/Ci tables)");
@@ -903,7 +913,14 @@ tdda_status tdda_model_create(tdda_core* c, const double* nK, double E0, const d
             return s;
         }
     }
-    cudaError_t e = cudaMallocHost((void**)&m->stage, 2 * sizeof(cd) * n3);
+    {
+        tdda_status s = dalloc(m->allocs, &m->dold, n3);
+        if (s != TDDA_OK) {
+            tdda_model_destroy(m);
+            return s;
+        }
+    }
+    cudaError_t e = cudaMallocHost((void**)&m->stage, sizeof(cd) * n3);
     if (e != cudaSuccess) {
         m->stage = nullptr;
         tdda_model_destroy(m);

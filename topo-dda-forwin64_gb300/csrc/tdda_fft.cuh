@@ -48,11 +48,26 @@ template <typename T> __device__ __forceinline__ cx<T> czero() { return mk<T>(T(
 // Up to 8 radix stages per axis (M <= 8^8 is far beyond any lattice here).
 constexpr int kMaxStages = 8;
 
+// Exact unsigned division by a fixed divisor d via a 32x32 multiply-high:
+// q = umulhi(n, ceil(2^32 / d)) equals floor(n / d) whenever n * d < 2^32,
+// which every index here satisfies (n < 2^20, d <= 2^11).
+struct FastDiv {
+    unsigned d, m;  // m = 0 encodes d = 1
+};
+__host__ __device__ inline FastDiv fastdiv_make(unsigned d) {
+    FastDiv f;
+    f.d = d;
+    f.m = d <= 1 ? 0u : (unsigned)(((1ull << 32) + d - 1) / d);
+    return f;
+}
+__device__ __forceinline__ unsigned fastdiv(unsigned n, FastDiv f) { return f.m ? __umulhi(n, f.m) : n; }
+
 struct AxisPlan {
     int M;                  // FFT length
     int nstages;
     int radix[kMaxStages];  // applied first to last
-    int rmin;               // smallest radix (bounds butterflies per stage)
+    int rmin;               // smallest radix
+    FastDiv ns[kMaxStages]; // division by the span Ns of each stage
 };
 
 // ---------------------------------------------------------------- butterflies
@@ -182,13 +197,14 @@ template <int SIGN, typename T> struct Bfly<7, SIGN, T> : BflyOdd<7, SIGN, T> {}
 // nvalid: inputs with index >= nvalid are zero (first stage only); nout:
 // outputs with index >= nout are not stored (last stage only).
 template <int R, int SIGN, typename T>
-__device__ __forceinline__ void fft_stage(const cx<T>* __restrict__ x, cx<T>* __restrict__ y, int L, int ls, int ms,
-                                          int M, int Ns, const cx<T>* tw, int nvalid, int nout) {
+__device__ __forceinline__ void fft_stage(const cx<T>* __restrict__ x, cx<T>* __restrict__ y, int L, FastDiv fl,
+                                          int ls, int ms, int M, int Ns, FastDiv fns, const cx<T>* tw, int nvalid,
+                                          int nout) {
     const int m = M / R;
     const int nb = L * m;
     const int twstep = M / (Ns * R);
     for (int w = threadIdx.x; w < nb; w += blockDim.x) {
-        const int j = w / L;
+        const int j = (int)fastdiv((unsigned)w, fl);
         const int l = w - j * L;
         const cx<T>* xb = x + l * ls;
         cx<T> v[R];
@@ -197,7 +213,7 @@ __device__ __forceinline__ void fft_stage(const cx<T>* __restrict__ x, cx<T>* __
             const int idx = j + r * m;
             v[r] = idx < nvalid ? xb[idx * ms] : czero<T>();
         }
-        const int k = j % Ns;
+        const int k = j - (int)fastdiv((unsigned)j, fns) * Ns;
         if (Ns > 1) {
 #pragma unroll
             for (int r = 1; r < R; r++) {
@@ -226,17 +242,19 @@ __device__ __forceinline__ cx<T>* smem_fft(cx<T>* a, cx<T>* b, int L, int ls, in
                                            const cx<T>* tw, int nvalid, int nout) {
     int Ns = 1;
     const int M = ap.M;
+    const FastDiv fl = fastdiv_make((unsigned)L);
     for (int st = 0; st < ap.nstages; st++) {
         const int R = ap.radix[st];
         const int nv = st == 0 ? nvalid : M;
         const int no = st == ap.nstages - 1 ? nout : M;
+        const FastDiv fns = ap.ns[st];
         switch (R) {
-            case 2: fft_stage<2, SIGN, T>(a, b, L, ls, ms, M, Ns, tw, nv, no); break;
-            case 3: fft_stage<3, SIGN, T>(a, b, L, ls, ms, M, Ns, tw, nv, no); break;
-            case 4: fft_stage<4, SIGN, T>(a, b, L, ls, ms, M, Ns, tw, nv, no); break;
-            case 5: fft_stage<5, SIGN, T>(a, b, L, ls, ms, M, Ns, tw, nv, no); break;
-            case 7: fft_stage<7, SIGN, T>(a, b, L, ls, ms, M, Ns, tw, nv, no); break;
-            default: fft_stage<8, SIGN, T>(a, b, L, ls, ms, M, Ns, tw, nv, no); break;
+            case 2: fft_stage<2, SIGN, T>(a, b, L, fl, ls, ms, M, Ns, fns, tw, nv, no); break;
+            case 3: fft_stage<3, SIGN, T>(a, b, L, fl, ls, ms, M, Ns, fns, tw, nv, no); break;
+            case 4: fft_stage<4, SIGN, T>(a, b, L, fl, ls, ms, M, Ns, fns, tw, nv, no); break;
+            case 5: fft_stage<5, SIGN, T>(a, b, L, fl, ls, ms, M, Ns, fns, tw, nv, no); break;
+            case 7: fft_stage<7, SIGN, T>(a, b, L, fl, ls, ms, M, Ns, fns, tw, nv, no); break;
+            default: fft_stage<8, SIGN, T>(a, b, L, fl, ls, ms, M, Ns, fns, tw, nv, no); break;
         }
         Ns *= R;
         cx<T>* t = a;

@@ -110,6 +110,21 @@ cudaError_t launch_solve_begin(const Geom& g, int nrhs, const RhsVecs<T>* rhs, c
 template <typename T>
 cudaError_t launch_residual_is_rhs(const Geom& g, int nrhs, const RhsVecs<T>* rhs, cudaStream_t stream);
 
+// eps by linear interpolation in the material table and al = 1 / alpha_LDR(eps)
+// for 3N densities (DDAModel.cpp:54-63, tools.cpp:617-630), FP64.
+constexpr int kMaxMaterials = 16;
+struct AlphaParams {
+    double a1c;   // 3 d^3 / (4 pi)
+    double d3;    // d^3
+    double Kd2;   // (K d)^2
+    double rad;   // (2/3) (K d)^3
+    double S;     // sum_i (nE0_i nK_i)^2
+    int nmat;
+    double2 mat[kMaxMaterials];
+};
+cudaError_t launch_model_alpha(int n3, const double* diel_old, const AlphaParams& ap, double2* diel, double2* al,
+                               float2* fal, cudaStream_t stream);
+
 // Einternal = al P / ((2 + eps) / 3)       (DDAModel.cpp:567-575)
 cudaError_t launch_einternal(int n3, const double2* al, const double2* P, const double2* diel, double2* Ein,
                              cudaStream_t stream);

@@ -85,25 +85,26 @@ __device__ __forceinline__ bool finite2(double2 a) { return isfinite(a.x) && isf
 template <typename T> __device__ __forceinline__ cx<T> from_d(double2 a) { return mk<T>(T(a.x), T(a.y)); }
 
 // ------------------------------------------------------------ reductions
-// Block-wide sum of NV doubles with a fixed tree; the result is valid in
-// thread 0.  sred must hold NV * 32 doubles.
+// Block-wide sum of NV doubles in a fixed order; the result is valid in
+// thread 0.  sred must hold NV * blockDim.x doubles.  The partials go through
+// shared memory and one warp adds them: on GB300 every FP64 warp instruction
+// occupies the narrow FP64 pipe for many cycles, so one warp summing the block
+// costs far less than a shuffle tree run by every warp.
 template <int NV> __device__ __forceinline__ void block_sum(double (&v)[NV], double* sred) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nt = blockDim.x;
 #pragma unroll
-    for (int k = 0; k < NV; k++)
-        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
-    __syncthreads();
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < NV; k++) sred[k * 32 + warp] = v[k];
+    for (int k = 0; k < NV; k++) sred[k * nt + threadIdx.x] = v[k];
     __syncthreads();
     if (warp == 0) {
 #pragma unroll
         for (int k = 0; k < NV; k++) {
-            v[k] = lane < nw ? sred[k * 32 + lane] : 0.0;
-            for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+            double a = 0.0;
+            for (int i = lane; i < nt; i += 32) a += sred[k * nt + i];
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+            v[k] = a;
         }
     }
+    __syncthreads();
 }
 
 // Publish this block's partials; the last block of the grid (for this
@@ -302,7 +303,7 @@ __global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restri
                                               const cx<T>* __restrict__ twz, const int* __restrict__ cellmap,
                                               cx<T>* __restrict__ grid) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ double sred[4 * 32];
+    __shared__ double sred[4 * kNT];
     const int b = blockIdx.y;
     const RhsVecs<T> R = rhs[b];
     if (rhs_done(R.st)) return;
@@ -385,7 +386,7 @@ __global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restri
 // ================================================================ K6 update
 template <typename T>
 __global__ void __launch_bounds__(kNT) k_update(int n3, const RhsVecs<T>* __restrict__ rhs, int is_init) {
-    __shared__ double sred[4 * 32];
+    __shared__ double sred[4 * kNT];
     const int b = blockIdx.y;
     const RhsVecs<T> R = rhs[b];
     if (rhs_done(R.st)) return;
@@ -445,7 +446,7 @@ __global__ void __launch_bounds__(kNT) k_update(int n3, const RhsVecs<T>* __rest
 // |E| of each right-hand side
 template <typename T>
 __global__ void __launch_bounds__(kNT) k_solve_begin(int n3, const RhsVecs<T>* __restrict__ rhs, int resid_is_rhs) {
-    __shared__ double sred[4 * 32];
+    __shared__ double sred[4 * kNT];
     const int b = blockIdx.y;
     const RhsVecs<T> R = rhs[b];
     if (rhs_done(R.st)) return;
@@ -588,6 +589,37 @@ __global__ void __launch_bounds__(kNT) k_fft_cols(double2* __restrict__ data, in
     }
 }
 
+// ------------------------------------------------------------ polarisability
+__device__ __forceinline__ double2 dadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 dscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+
+__global__ void k_model_alpha(int n3, const double* __restrict__ diel_old, AlphaParams ap, double2* __restrict__ diel,
+                              double2* __restrict__ al, float2* __restrict__ fal) {
+    const double b1 = -1.891531, b2 = 0.1648469, b3 = -1.7700004;  // LDR coefficients (tools.cpp:618-620)
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x) {
+        const double v = diel_old[e];
+        int lf = (int)floor(v);
+        int ln = lf + 1;
+        if (lf >= 1) ln = lf;
+        lf = lf < 0 ? 0 : (lf >= ap.nmat ? ap.nmat - 1 : lf);  // the host checked the range
+        ln = ln >= ap.nmat ? ap.nmat - 1 : ln;
+        const double2 mf = ap.mat[lf], mn = ap.mat[ln];
+        const double w = v - (double)lf;
+        const double2 eps = make_double2(mf.x + w * (mn.x - mf.x), mf.y + w * (mn.y - mf.y));
+        // a1 = (3 d^3 / (4 pi)) (eps - 1) / (eps + 2)
+        const double2 a1 = cdiv(dscale(make_double2(eps.x - 1.0, eps.y), ap.a1c), make_double2(eps.x + 2.0, eps.y));
+        // result = 1 + (a1 / d^3) ((b1 + eps b2 + eps b3 S) (K d)^2 - i (2/3)(K d)^3)
+        const double2 q = dadd(dadd(make_double2(b1, 0.0), dscale(eps, b2)), dscale(dscale(eps, b3), ap.S));
+        const double2 t = make_double2(q.x * ap.Kd2, q.y * ap.Kd2 - ap.rad);
+        const double2 res = dadd(make_double2(1.0, 0.0), dmul(make_double2(a1.x / ap.d3, a1.y / ap.d3), t));
+        const double2 alpha = cdiv(a1, res);
+        const double2 inv = cdiv(make_double2(1.0, 0.0), alpha);
+        diel[e] = eps;
+        al[e] = inv;
+        if (fal) fal[e] = make_float2((float)inv.x, (float)inv.y);
+    }
+}
+
 // ------------------------------------------------------------ small kernels
 __global__ void k_einternal(int n3, const double2* al, const double2* P, const double2* diel, double2* Ein) {
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x) {
@@ -611,6 +643,13 @@ template <typename T> __global__ void k_zero(long long n, cx<T>* v) {
 int grid1d(long long n, int nt) {
     long long b = (n + nt - 1) / nt;
     if (b > 152 * 16) b = 152 * 16;  // 16 resident blocks per SM on 152 SMs at most
+    return (int)(b < 1 ? 1 : b);
+}
+// reductions over a vector: four entries per thread keeps the FP64 block
+// sums few while leaving enough threads to cover memory latency
+int grid_reduce(long long n) {
+    long long b = (n + 4LL * kNT - 1) / (4LL * kNT);
+    if (b > 152 * 8) b = 152 * 8;
     return (int)(b < 1 ? 1 : b);
 }
 
@@ -673,7 +712,7 @@ size_t max_pass_smem(const Geom& g) {
 int max_blocks_per_rhs(const Geom& g) {
     const int lz = z_lines<float>(g.pz) > z_lines<double>(g.pz) ? z_lines<double>(g.pz) : z_lines<float>(g.pz);
     int nz = (g.Nx * g.Ny + lz - 1) / lz;
-    int nv = grid1d(3LL * g.N, kNT);
+    int nv = grid_reduce(3LL * g.N);
     return nz > nv ? nz : nv;
 }
 
@@ -780,21 +819,21 @@ cudaError_t launch_aproduct(const Geom& g, int src, int snk, int nrhs, const Rhs
 
 template <typename T>
 cudaError_t launch_update(const Geom& g, int nrhs, const RhsVecs<T>* rhs, int is_init, cudaStream_t stream) {
-    const dim3 gr(grid1d(3LL * g.N, kNT), nrhs);
+    const dim3 gr(grid_reduce(3LL * g.N), nrhs);
     k_update<T><<<gr, kNT, 0, stream>>>(3 * g.N, rhs, is_init);
     return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_solve_begin(const Geom& g, int nrhs, const RhsVecs<T>* rhs, cudaStream_t stream) {
-    const dim3 gr(grid1d(3LL * g.N, kNT), nrhs);
+    const dim3 gr(grid_reduce(3LL * g.N), nrhs);
     k_solve_begin<T><<<gr, kNT, 0, stream>>>(3 * g.N, rhs, 0);
     return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_residual_is_rhs(const Geom& g, int nrhs, const RhsVecs<T>* rhs, cudaStream_t stream) {
-    const dim3 gr(grid1d(3LL * g.N, kNT), nrhs);
+    const dim3 gr(grid_reduce(3LL * g.N), nrhs);
     k_solve_begin<T><<<gr, kNT, 0, stream>>>(3 * g.N, rhs, 1);
     return cudaGetLastError();
 }
@@ -802,6 +841,11 @@ cudaError_t launch_residual_is_rhs(const Geom& g, int nrhs, const RhsVecs<T>* rh
 cudaError_t launch_einternal(int n3, const double2* al, const double2* P, const double2* diel, double2* Ein,
                              cudaStream_t stream) {
     k_einternal<<<grid1d(n3, kNT), kNT, 0, stream>>>(n3, al, P, diel, Ein);
+    return cudaGetLastError();
+}
+cudaError_t launch_model_alpha(int n3, const double* diel_old, const AlphaParams& ap, double2* diel, double2* al,
+                               float2* fal, cudaStream_t stream) {
+    k_model_alpha<<<grid1d(n3, kNT), kNT, 0, stream>>>(n3, diel_old, ap, diel, al, fal);
     return cudaGetLastError();
 }
 cudaError_t launch_to_f32(int n3, const double2* src, float2* dst, cudaStream_t stream) {
