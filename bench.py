@@ -244,6 +244,55 @@ def pinned_c128(n: int) -> np.ndarray:
     return torch.zeros(n, dtype=torch.complex128, pin_memory=True).numpy()
 
 
+def time_batch(tdda, torch, w, incs, precision, steps, dev, flush_l2):
+    """Solve len(incs) right-hand sides of one lattice in one batched solve per step."""
+    core = tdda.AProductCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material, w.nback, max_rhs=len(incs), device=dev)
+    models = [tdda.DDAModel(core, inc.nK, inc.E0, inc.nE0, w.diel_old) for inc in incs]
+    stream = torch.cuda.ExternalStream(core.stream(), device=dev)
+    zero = pinned_c128(3 * w.N)
+
+    def step():
+        for m in models:
+            m.InitializeP(zero)
+        flush_l2()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        infos = tdda.solve_batch(models, precision, MAX_IT, TOL)
+        e1.record(stream)
+        e1.synchronize()
+        if any(i["status"] != tdda.OK for i in infos):
+            raise RuntimeError(f"batched solve did not converge: {infos}")
+        return e0.elapsed_time(e1), infos
+
+    step()
+    runs = [step() for _ in range(steps)]
+    ms = [r[0] for r in runs]
+    infos = runs[-1][1]
+    n32 = 2 * max(i["inner_iterations"] for i in infos) + 2 * max(i["outer_iterations"] for i in infos)
+    prof = core.profile_aproduct(precision, len(incs), 5)
+    out = {"rhs": len(incs), "value": len(incs) * steps / (sum(ms) / 1000.0), "unit": UNIT, "steps": steps,
+           "ms_per_batch": sum(ms) / steps, "iterations": [i["iterations"] for i in infos],
+           "pass_ms": prof, "grid": list(core.grid)}
+    for m in models:
+        m.close()
+    core.close()
+    return out, prof, n32
+
+
+def batched_roofline(w, grid, prof, nrhs, s, peak):
+    """Roofline of the x pass (the largest) for nrhs right-hand sides: the Green tensor is
+    read once per launch, the grid once per right-hand side."""
+    Mx, My, Mz = grid
+    grid_bytes = 2 * 3 * w.Nx * My * Mz * s * nrhs
+    green_bytes = 6 * Mx * My * Mz * s
+    b = grid_bytes + green_bytes
+    t = prof[2]
+    ach = b / (t * 1e-3) / 1e9
+    return {"kernel": "k_xpass", "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+            "algorithmic_bytes": b, "avg_ms": t}
+
+
 def run_ours(args, dist: Dist):
     import torch
 
@@ -333,6 +382,18 @@ def run_ours(args, dist: Dist):
         with open(tf) as f:
             traffic = json.load(f).get(f"{PASS_NAMES[k]}:{prec}")
 
+    # batched right-hand sides: the 96x96x24 lattice with its 8 incidences in one solve
+    batched = None
+    if not args.no_batched:
+        w3 = lattice.config(3)
+        b32, prof_b, _ = time_batch(tdda, torch, w3, w3.incidences, tdda.FP32_REFINE, args.batched_steps, dev, flush_l2)
+        b32["roofline"] = batched_roofline(w3, tuple(b32["grid"]), prof_b, len(w3.incidences), 8, peaks["hbm_gbs"])
+        b64, _, _ = time_batch(tdda, torch, w3, w3.incidences, tdda.FP64, 1, dev, flush_l2)
+        batched = {"workload": "batched 8 RHS 96x96x24 (cfg 3)", "dipoles": w3.N, "fp32_refine": b32,
+                   "fp64": {"value": b64["value"], "unit": UNIT, "iterations": b64["iterations"],
+                            "ms_per_batch": b64["ms_per_batch"]},
+                   "speedup_fp32_refine": b32["value"] / b64["value"]}
+
     cpu = None
     if dist.rank == 0:
         base = CpuBaseline(w, args.cpu_threads or (os.cpu_count() or 1))
@@ -359,11 +420,26 @@ def run_ours(args, dist: Dist):
                          "peak_source": peaks["source"], "algorithmic_bytes": bytes_k, "avg_ms": t_k,
                          "traffic": traffic,
                          "pass_ms_fp32": prof32, "pass_ms_fp64": prof64},
+            "batched": batched,
             "gpu_launches": launches,
             "clocks": clocks,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
+
+
+def run_aprod_only(args):
+    """Only A-products of one workload (for profiler captures): --aprod-only CFG runs
+    `--reps` plain products of all of the workload's right-hand sides at once."""
+    import tdda
+
+    w = lattice.config(args.aprod_only)
+    nrhs = len(w.incidences)
+    core = tdda.AProductCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material, w.nback, max_rhs=nrhs)
+    prec = tdda.FP64 if args.aprod_precision == "fp64" else tdda.FP32_REFINE
+    ms = core.profile_aproduct(prec, nrhs, args.reps)
+    print(json.dumps({"aprod_only": f"cfg{args.aprod_only}", "rhs": nrhs, "grid": list(core.grid),
+                      "precision": args.aprod_precision, "pass_ms": ms}), flush=True)
 
 
 def main():
@@ -375,9 +451,17 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=5)
     ap.add_argument("--cpu-iters", type=int, default=4)
     ap.add_argument("--cpu-threads", type=int, default=0)
+    ap.add_argument("--batched-steps", type=int, default=3)
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--aprod-only", type=int, default=0)
+    ap.add_argument("--aprod-precision", choices=["fp32", "fp64"], default="fp32")
+    ap.add_argument("--reps", type=int, default=3)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.aprod_only:
+        run_aprod_only(args)
+        return
     dist = Dist()
     try:
         if args.impl == "reference":

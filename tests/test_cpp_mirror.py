@@ -1,0 +1,62 @@
+"""The C++ drop-in (topo-dda-forwin64_gb300/cpp/tdda.hpp) used with the reference's call sequence.
+
+tests/cpp/mirror_solve.cpp builds a structure with the reference CoreStructure's getters,
+constructs AProductCore / DDAModel, runs bicgstab + update_E_in_structure and dumps the
+results; here they are compared with the oracle.  Compiling is a CPU test; running is a
+GPU test.
+"""
+import math
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle as O
+import tdda
+from conftest import ROOT, rel
+
+SRC = os.path.join(ROOT, "tests", "cpp", "mirror_solve.cpp")
+PKG = os.path.join(ROOT, "topo-dda-forwin64_gb300")
+
+
+def _build(tmp_path) -> str:
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    exe = str(tmp_path / "mirror_solve")
+    subprocess.run([cxx, "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), SRC, "-o", exe, "-L", PKG,
+                    "-ltdda", f"-Wl,-rpath,{PKG}"], check=True, capture_output=True, text=True)
+    return exe
+
+
+def test_mirror_header_compiles_against_the_abi(tmp_path):
+    tdda.load()  # libtdda.so must exist to link
+    assert os.path.exists(_build(tmp_path))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol,bound", [(0, 1e-10, 1e-9), (1, 1e-5, 1e-4)])
+def test_mirror_solve_matches_oracle(tmp_path, precision, tol, bound):
+    if tdda.device_count() < 1:
+        pytest.skip("no CUDA device")
+    exe = _build(tmp_path)
+    Nx, Ny, Nz, d, lam, em = 9, 8, 6, 10.0, 520.0, 4.0 + 0.1j
+    out = str(tmp_path / "out.bin")
+    r = subprocess.run([exe, str(Nx), str(Ny), str(Nz), str(d), str(lam), str(em.real), str(em.imag), repr(tol),
+                        str(precision), out], check=True, capture_output=True, text=True)
+    N = Nx * Ny * Nz
+    raw = open(out, "rb").read()
+    it = int(np.frombuffer(raw, "<i4", count=1)[0])
+    P = np.frombuffer(raw, "<c16", count=3 * N, offset=4)
+    Ein = np.frombuffer(raw, "<c16", count=3 * N, offset=4 + 48 * N)
+    rho = np.array([0.5 + 0.5 * math.sin(0.37 * i) for i in range(N)])
+    R = tdda.lattice.bulk(Nx, Ny, Nz)
+    oc = O.OracleCore(Nx, Ny, Nz, R, d, lam, np.array([1.0, em]))
+    om = O.OracleModel(oc, [0, 0, 1], 1.0, [1, 0, 0], np.repeat(rho, 3))
+    assert om.bicgstab(100000, 1e-12) == O.CONVERGED
+    om.update_E_in_structure()
+    assert it > 0, r.stdout
+    assert rel(P, om.P) <= bound
+    assert rel(Ein, om.Einternal) <= bound

@@ -1,0 +1,248 @@
+// tdda.hpp -- C++ drop-in for the reference's AProductCore / DDAModel solve path.
+//
+// Header-only, over the C ABI of libtdda (include/tdda.h).  The classes keep
+// the reference's constructor arguments, method names and call sequence
+// (AProductCore.h:51-80, DDAModel.h:34-74), so the reference's callers
+// (main.cpp:245-251, EvoDDAModel.cpp:433-457, 596-610) compile against them:
+//
+//     tdda::AProductCore Core(&CStr, lam, material, nback, "LDR");
+//     tdda::DDAModel TestModel(&Core, n_K, E0, n_E0);
+//     TestModel.bicgstab(MAX_ITERATION_DDA, MAX_ERROR);
+//     TestModel.update_E_in_structure();
+//
+// Type parameters keep it independent of Eigen:
+//   * the structure (CStr) may be any class with the reference CoreStructure's
+//     getters get_N/get_Nx/get_Ny/get_Nz/get_d, get_R() -> pointer to an
+//     integer vector and get_diel_old() -> pointer to a double vector (the
+//     reference's own CoreStructure qualifies, CoreStructure.h:44-52);
+//   * complex vectors are any contiguous container of std::complex<double>
+//     with data()/size() and a size constructor (Eigen::VectorXcd,
+//     std::vector<std::complex<double>>), chosen by DDAModelT's parameter.
+//
+// Behaviour matches the reference where it is observable: the material is
+// normalised and a vacuum permittivity bumped to 1.01 (AProductCore.cpp:19-24);
+// bicgstab prints its progress when verbose and leaves get_ITERATION()
+// unchanged when it does not converge (DDAModel.cpp:256-259); an unknown
+// method string throws std::invalid_argument (AProductCore.cpp:567-569).  CUDA
+// or argument errors, which the reference never checks, throw
+// std::runtime_error.  The FCD tensor is not built and is rejected.
+#pragma once
+
+#include <array>
+#include <complex>
+#include <cstdio>
+#include <functional>
+#include <iostream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "tdda.h"
+
+namespace tdda {
+
+using cplx = std::complex<double>;
+
+inline void check(tdda_status st, const char* where) {
+    if (st != TDDA_OK) throw std::runtime_error(std::string(where) + ": " + tdda_last_error());
+}
+
+template <class V> inline const double* dptr(const V& v) { return reinterpret_cast<const double*>(v.data()); }
+template <class V> inline double* dptr(V& v) { return reinterpret_cast<double*>(v.data()); }
+
+class AProductCore {
+   public:
+    // AProductCore(CoreStructure*, double lam, VectorXcd material, double nback, string method)
+    template <class CStrT, class MatVec>
+    AProductCore(CStrT* CStr, double lam, const MatVec& material, double nback, const std::string& method,
+                 int max_rhs = 1, int device = 0)
+        : lam_(lam), nback_(nback) {
+        if (method != "LDR" && method != "FCD")
+            throw std::invalid_argument("\"" + method + "\" is not a valid polarizabiliy calculation method.");
+        N_ = CStr->get_N();
+        Nx_ = CStr->get_Nx();
+        Ny_ = CStr->get_Ny();
+        Nz_ = CStr->get_Nz();
+        d_ = CStr->get_d();
+        const auto* R = CStr->get_R();
+        R_.resize(3 * (size_t)N_);
+        for (size_t i = 0; i < R_.size(); i++) R_[i] = (int)(*R)(i);
+        diel_old_ = [CStr](std::vector<double>& out) {
+            const auto* dv = CStr->get_diel_old();
+            out.resize((size_t)dv->size());
+            for (size_t i = 0; i < out.size(); i++) out[i] = (*dv)(i);
+        };
+        std::vector<double> mat(2 * (size_t)material.size());
+        for (size_t i = 0; i < (size_t)material.size(); i++) {
+            mat[2 * i] = std::real(material[i]);
+            mat[2 * i + 1] = std::imag(material[i]);
+        }
+        tdda_core_desc desc;
+        desc.Nx = Nx_;
+        desc.Ny = Ny_;
+        desc.Nz = Nz_;
+        desc.N = N_;
+        desc.R = R_.data();
+        desc.d = d_;
+        desc.lam = lam;
+        desc.nback = nback;
+        desc.material = mat.data();
+        desc.nmat = (int)material.size();
+        desc.method = method == "LDR" ? TDDA_METHOD_LDR : TDDA_METHOD_FCD;
+        desc.max_rhs = max_rhs;
+        desc.device = device;
+        check(tdda_core_create(&desc, &h_), "AProductCore");
+        material_.resize(material.size());
+        check(tdda_core_info(h_, &K_, grid_.data(), reinterpret_cast<double*>(material_.data())), "AProductCore");
+    }
+    AProductCore(const AProductCore&) = delete;
+    AProductCore& operator=(const AProductCore&) = delete;
+    ~AProductCore() { tdda_core_destroy(h_); }
+
+    // VectorXcd Aproduct(VectorXcd& b)     AProductCore.cpp:697-758
+    template <class V> V Aproduct(const V& b) {
+        V y(b.size());
+        check(tdda_aproduct(h_, TDDA_FP64, dptr(b), dptr(y), TDDA_MEM_HOST), "Aproduct");
+        return y;
+    }
+    // Matrix3cd LDR_inter(double x, double y, double z)     AProductCore.cpp:588-623
+    std::array<std::array<cplx, 3>, 3> LDR_inter(double x, double y, double z) const {
+        double t[12];
+        check(tdda_core_ldr_inter(h_, x, y, z, t), "LDR_inter");
+        cplx a[6];
+        for (int l = 0; l < 6; l++) a[l] = cplx(t[2 * l], t[2 * l + 1]);
+        return {{{a[0], a[1], a[2]}, {a[1], a[3], a[4]}, {a[2], a[4], a[5]}}};
+    }
+    std::array<std::array<cplx, 3>, 3> A_dic_generator(double x, double y, double z) const {
+        return LDR_inter(x, y, z);
+    }
+
+    int get_N() const { return N_; }
+    int get_Nx() const { return Nx_; }
+    int get_Ny() const { return Ny_; }
+    int get_Nz() const { return Nz_; }
+    double get_d() const { return d_; }
+    double get_lam() const { return lam_; }
+    double get_K() const { return K_; }
+    double get_nback() const { return nback_; }
+    const std::vector<cplx>* get_material() const { return &material_; }
+    const std::vector<int>* get_R() const { return &R_; }
+    std::array<int, 3> grid() const { return grid_; }
+    tdda_core* handle() const { return h_; }
+    // the structure's current densities (CoreStructure::get_diel_old)
+    void read_diel_old(std::vector<double>& out) const { diel_old_(out); }
+
+   private:
+    tdda_core* h_ = nullptr;
+    int N_ = 0, Nx_ = 0, Ny_ = 0, Nz_ = 0;
+    double d_ = 0, lam_ = 0, nback_ = 1, K_ = 0;
+    std::vector<int> R_;
+    std::vector<cplx> material_;
+    std::array<int, 3> grid_{{0, 0, 0}};
+    std::function<void(std::vector<double>&)> diel_old_;
+};
+
+// DDAModel over a complex vector type VectorXcd (Eigen::VectorXcd or
+// std::vector<std::complex<double>>).
+template <class VectorXcd = std::vector<cplx>> class DDAModelT {
+   public:
+    // DDAModel(AProductCore*, Vector3d n_K, double E0, Vector3d n_E0, bool verbose = true)
+    template <class V3>
+    DDAModelT(AProductCore* Core, const V3& n_K, double E0, const V3& n_E0, bool verbose = true)
+        : core_(Core), E0_(E0), verbose_(verbose) {
+        for (int j = 0; j < 3; j++) {
+            nK_[j] = n_K[j];
+            nE0_[j] = n_E0[j];
+        }
+        std::vector<double> diel;
+        Core->read_diel_old(diel);
+        check(tdda_model_create(Core->handle(), nK_, E0, nE0_, diel.data(), &h_), "DDAModel");
+        n3_ = 3 * (size_t)Core->get_N();
+        P_ = VectorXcd(n3_);
+        Einternal_ = VectorXcd(n3_);
+        al_ = VectorXcd(n3_);
+        fetch(TDDA_FIELD_AL, al_);
+    }
+    DDAModelT(const DDAModelT&) = delete;
+    DDAModelT& operator=(const DDAModelT&) = delete;
+    ~DDAModelT() { tdda_model_destroy(h_); }
+
+    // void bicgstab(int MAX_ITERATION, double MAX_ERROR)     DDAModel.cpp:131-260
+    void bicgstab(int MAX_ITERATION, double MAX_ERROR) { solve(MAX_ITERATION, MAX_ERROR, TDDA_FP64); }
+    // the same solve with the FP32 convolution and FP64 refinement
+    void bicgstab_mixed(int MAX_ITERATION, double MAX_ERROR) { solve(MAX_ITERATION, MAX_ERROR, TDDA_FP32_REFINE); }
+
+    void change_E(const VectorXcd& E) { check(tdda_model_change_E(h_, dptr(E), TDDA_MEM_HOST), "change_E"); }
+    void reset_E() { check(tdda_model_reset_E(h_), "reset_E"); }
+    // UpdateAlpha: reads the structure's current densities, as the reference does
+    void UpdateAlpha() {
+        std::vector<double> diel;
+        core_->read_diel_old(diel);
+        check(tdda_model_update_alpha(h_, diel.data()), "UpdateAlpha");
+        fetch(TDDA_FIELD_AL, al_);
+    }
+    void UpdateAlphaSingle(int idx) {
+        std::vector<double> diel;
+        core_->read_diel_old(diel);
+        check(tdda_model_update_alpha_single(h_, idx, diel.at(3 * (size_t)idx)), "UpdateAlphaSingle");
+        fetch(TDDA_FIELD_AL, al_);
+    }
+    void InitializeP(const VectorXcd& P) {
+        check(tdda_model_initialize_P(h_, dptr(P), TDDA_MEM_HOST), "InitializeP");
+        P_ = P;
+    }
+    VectorXcd Aproductwithalb(const VectorXcd& b) {
+        VectorXcd y(b.size());
+        check(tdda_model_aproduct_with_alb(h_, dptr(b), dptr(y), TDDA_MEM_HOST), "Aproductwithalb");
+        return y;
+    }
+    void update_E_in_structure() {
+        check(tdda_model_update_E_in_structure(h_), "update_E_in_structure");
+        fetch(TDDA_FIELD_EINTERNAL, Einternal_);
+    }
+    void solve_E() {}  // on-lattice fields only: EResult == Einternal (DDAModel.cpp:560-562)
+
+    VectorXcd* get_P() { return &P_; }
+    VectorXcd* get_Einternal() { return &Einternal_; }
+    VectorXcd* get_al() { return &al_; }
+    int get_ITERATION() const { return tdda_model_iterations(h_); }
+    double get_E0() const { return E0_; }
+    AProductCore* get_Core() { return core_; }
+    int get_N() const { return core_->get_N(); }
+    const tdda_solve_info& last_info() const { return info_; }
+    tdda_model* handle() const { return h_; }
+
+   private:
+    void fetch(int field, VectorXcd& out) {
+        check(tdda_model_get(h_, field, dptr(out), TDDA_MEM_HOST), "DDAModel get");
+    }
+    void solve(int max_it, double max_err, int precision) {
+        if (verbose_) std::cout << "--------------Calculation start. Iterative method used: BICGSTAB---------------\n\n";
+        const tdda_status st = precision == TDDA_FP64 ? tdda_model_bicgstab(h_, max_it, max_err, &info_)
+                                                      : tdda_model_solve_mixed(h_, max_it, max_err, &info_);
+        if (st != TDDA_OK && st != TDDA_NOT_CONVERGED && st != TDDA_BREAKDOWN) check(st, "bicgstab");
+        fetch(TDDA_FIELD_P, P_);
+        if (st == TDDA_NOT_CONVERGED) {
+            std::cout << "                ERROR:does not converge in " << max_it << " iterations" << std::endl;
+        } else if (verbose_) {
+            if (st == TDDA_BREAKDOWN)
+                std::cout << "----------------------------r0dotrl==(0,0), nan is going to occur so stop now"
+                             "------------------------\n";
+            std::cout << "              Error: " << info_.error << "\n              Iteration: " << get_ITERATION()
+                      << "\n"
+                      << std::endl;
+        }
+    }
+
+    AProductCore* core_;
+    tdda_model* h_ = nullptr;
+    double nK_[3], nE0_[3], E0_;
+    bool verbose_;
+    size_t n3_ = 0;
+    VectorXcd P_, Einternal_, al_;
+    tdda_solve_info info_{};
+};
+
+using DDAModel = DDAModelT<>;
+
+}  // namespace tdda
