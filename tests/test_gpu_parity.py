@@ -213,4 +213,4 @@ def test_update_alpha_matches_oracle():
     om.UpdateAlpha(d3)
     assert rel(m.get_al(), om.al) <= 1e-14
     m.reset_E()
-    assert rel(m.get_E(), om.E) <= 1e-15
+    assert rel(m.get_E(), om.E) <= 1e-14  # device sincos against the host libm

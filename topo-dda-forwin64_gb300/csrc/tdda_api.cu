@@ -157,6 +157,7 @@ struct tdda_core_s {
     std::vector<cd> material;  // normalised
     std::vector<int> R;
     int* cellmap = nullptr;
+    int* Rdev = nullptr;  // 3N lattice indices
     double2* green64 = nullptr;
     float2* green32 = nullptr;
     double2* tw64[3] = {nullptr, nullptr, nullptr};
@@ -189,7 +190,6 @@ struct tdda_model_s {
     float2 *fP = nullptr, *fE = nullptr, *fal = nullptr, *fr = nullptr, *fr0 = nullptr, *fp = nullptr, *fu = nullptr,
            *ft = nullptr, *fAp = nullptr, *fAt = nullptr;
     std::vector<void*> allocs;
-    cd* stage = nullptr;  // pinned host staging, 3N complex
     bool P_zero = true;
     int ITERATION = 0;
     double Error = 0.0;
@@ -197,10 +197,14 @@ struct tdda_model_s {
 
 namespace {
 
-template <typename T> tdda_status dalloc(std::vector<void*>& list, T** p, size_t count) {
+// Device buffers are stream-ordered allocations from the device's memory pool
+// (cudaMallocAsync / cudaFreeAsync on the owner's stream): creating and
+// destroying cores and models never synchronises the device, so several can
+// be set up and torn down while other solves run (the serving loop).
+template <typename T> tdda_status dalloc(std::vector<void*>& list, T** p, size_t count, cudaStream_t stream) {
     void* q = nullptr;
-    cudaError_t e = cudaMalloc(&q, sizeof(T) * std::max<size_t>(count, 1));
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    cudaError_t e = cudaMallocAsync(&q, sizeof(T) * std::max<size_t>(count, 1), stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync");
     list.push_back(q);
     *p = (T*)q;
     return TDDA_OK;
@@ -212,9 +216,31 @@ template <typename T> tdda_status dalloc(std::vector<void*>& list, T** p, size_t
         if (s_ != TDDA_OK) return s_;          \
     } while (0)
 
-void free_all(std::vector<void*>& list) {
-    for (void* q : list) cudaFree(q);
+void free_all(std::vector<void*>& list, cudaStream_t stream) {
+    for (void* q : list) cudaFreeAsync(q, stream);
     list.clear();
+}
+
+// keep freed pool memory cached for reuse instead of returning it to the
+// driver at every synchronisation (once per device)
+std::mutex g_pool_mu;
+bool g_pool_ready[64];
+tdda_status ensure_pool(int device) {
+    if (device < 0 || device >= 64) return TDDA_OK;
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (g_pool_ready[device]) return TDDA_OK;
+    cudaMemPool_t pool;
+    cudaError_t e = cudaDeviceGetDefaultMemPool(&pool, device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetDefaultMemPool");
+    unsigned long long thr = ~0ull;
+    e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemPoolSetAttribute");
+    g_pool_ready[device] = true;
+    return TDDA_OK;
+}
+
+template <typename T> tdda_status dalloc_c(tdda_core* c, T** p, size_t count) {
+    return dalloc(c->allocs, p, count, c->stream);
 }
 
 cudaMemcpyKind kind_in(int mem) { return mem == TDDA_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice; }
@@ -243,16 +269,11 @@ RhsVecs<float> vecs32(tdda_core* c, tdda_model* m, int slot) {
 tdda_status model_upload_fields(tdda_model* m, bool field_E, bool field_al) {
     tdda_core* c = m->core;
     const int N = c->N;
-    cd* buf = m->stage;
-    const size_t bytes = sizeof(cd) * 3 * (size_t)N;
     if (field_E) {
-        using namespace std::complex_literals;
-        for (int i = 0; i < N; i++) {
-            const double ph = c->K * c->d *
-                              (m->nK[0] * c->R[3 * i] + m->nK[1] * c->R[3 * i + 1] + m->nK[2] * c->R[3 * i + 2]);
-            for (int j = 0; j < 3; j++) buf[3 * i + j] = m->E0 * m->nE0[j] * (std::cos(ph) + std::sin(ph) * 1i);
-        }
-        TDDA_CK(cudaMemcpyAsync(m->E, buf, bytes, cudaMemcpyHostToDevice, c->stream));
+        // E_inc = E0 n_E0 exp(i K d n_K . R) on the device (DDAModel.cpp:47-51)
+        TDDA_CK1(tdda::launch_model_incident(N, c->Rdev, make_double3(m->nK[0], m->nK[1], m->nK[2]),
+                                             make_double3(m->nE0[0], m->nE0[1], m->nE0[2]), m->E0, c->K, c->d, m->E,
+                                             c->stream));
         TDDA_CK(cudaStreamSynchronize(c->stream));
     }
     if (field_al) {
@@ -289,7 +310,7 @@ tdda_status model_alloc_f32(tdda_model* m) {
     if (m->fP) return TDDA_OK;
     const size_t n3 = 3 * (size_t)m->core->N;
     float2** v[] = {&m->fP, &m->fE, &m->fal, &m->fr, &m->fr0, &m->fp, &m->fu, &m->ft, &m->fAp, &m->fAt};
-    for (float2** q : v) TDDA_TRY(dalloc(m->allocs, q, n3));
+    for (float2** q : v) TDDA_TRY(dalloc(m->allocs, q, n3, m->core->stream));
     TDDA_CK1(tdda::launch_to_f32((int)n3, m->al, m->fal, m->core->stream));
     return TDDA_OK;
 }
@@ -760,29 +781,32 @@ tdda_status tdda_core_create(const tdda_core_desc* desc, tdda_core** out) {
     const size_t n3 = 3 * (size_t)g.N;
     const long long H6 = 6LL * g.Hx * g.Hy * g.Hz;
     const long long Mfull = (long long)g.px.M * g.py.M * g.pz.M;
-    TDDA_CORE_TRY(dalloc(c->allocs, &c->cellmap, cellmap.size()));
-    TDDA_CORE_TRY(dalloc(c->allocs, &c->green64, (size_t)H6));
-    TDDA_CORE_TRY(dalloc(c->allocs, &c->green32, (size_t)H6));
+    TDDA_CORE_TRY(ensure_pool(c->device));
+    TDDA_CORE_TRY(dalloc_c(c, &c->cellmap, cellmap.size()));
+    TDDA_CORE_TRY(dalloc_c(c, &c->Rdev, 3 * (size_t)g.N));
+    TDDA_CORE_TRY(dalloc_c(c, &c->green64, (size_t)H6));
+    TDDA_CORE_TRY(dalloc_c(c, &c->green32, (size_t)H6));
     for (int a = 0; a < 3; a++) {
-        TDDA_CORE_TRY(dalloc(c->allocs, &c->tw64[a], (size_t)plans[a]->M));
-        TDDA_CORE_TRY(dalloc(c->allocs, &c->tw32[a], (size_t)plans[a]->M));
+        TDDA_CORE_TRY(dalloc_c(c, &c->tw64[a], (size_t)plans[a]->M));
+        TDDA_CORE_TRY(dalloc_c(c, &c->tw32[a], (size_t)plans[a]->M));
     }
-    TDDA_CORE_TRY(dalloc(c->allocs, &c->grid64, (size_t)(g.sb * c->max_rhs)));
-    TDDA_CORE_TRY(dalloc(c->allocs, &c->grid32, (size_t)(g.sb * c->max_rhs)));
-    TDDA_CORE_TRY(dalloc(c->allocs, &c->vin64, n3));
-    TDDA_CORE_TRY(dalloc(c->allocs, &c->vout64, n3));
-    TDDA_CORE_TRY(dalloc(c->allocs, &c->vin32, n3));
-    TDDA_CORE_TRY(dalloc(c->allocs, &c->vout32, n3));
-    TDDA_CORE_TRY(dalloc(c->allocs, &c->rhs64, (size_t)c->max_rhs + 1));
-    TDDA_CORE_TRY(dalloc(c->allocs, &c->rhs32, (size_t)c->max_rhs + 1));
-    TDDA_CORE_TRY(dalloc(c->allocs, &c->st64, (size_t)c->max_rhs));
-    TDDA_CORE_TRY(dalloc(c->allocs, &c->st32, (size_t)c->max_rhs));
-    TDDA_CORE_TRY(dalloc(c->allocs, &c->part, (size_t)c->max_rhs * tdda::kPartSlots * c->maxblk));
-    TDDA_CORE_TRY(dalloc(c->allocs, &c->cnt, (size_t)c->max_rhs * tdda::kCounters));
+    TDDA_CORE_TRY(dalloc_c(c, &c->grid64, (size_t)(g.sb * c->max_rhs)));
+    TDDA_CORE_TRY(dalloc_c(c, &c->grid32, (size_t)(g.sb * c->max_rhs)));
+    TDDA_CORE_TRY(dalloc_c(c, &c->vin64, n3));
+    TDDA_CORE_TRY(dalloc_c(c, &c->vout64, n3));
+    TDDA_CORE_TRY(dalloc_c(c, &c->vin32, n3));
+    TDDA_CORE_TRY(dalloc_c(c, &c->vout32, n3));
+    TDDA_CORE_TRY(dalloc_c(c, &c->rhs64, (size_t)c->max_rhs + 1));
+    TDDA_CORE_TRY(dalloc_c(c, &c->rhs32, (size_t)c->max_rhs + 1));
+    TDDA_CORE_TRY(dalloc_c(c, &c->st64, (size_t)c->max_rhs));
+    TDDA_CORE_TRY(dalloc_c(c, &c->st32, (size_t)c->max_rhs));
+    TDDA_CORE_TRY(dalloc_c(c, &c->part, (size_t)c->max_rhs * tdda::kPartSlots * c->maxblk));
+    TDDA_CORE_TRY(dalloc_c(c, &c->cnt, (size_t)c->max_rhs * tdda::kCounters));
     TDDA_CORE_CK(cudaMallocHost((void**)&c->hst, sizeof(SolveState) * c->max_rhs));
     TDDA_CORE_CK(cudaMemsetAsync(c->cnt, 0, sizeof(unsigned int) * c->max_rhs * tdda::kCounters, c->stream));
     TDDA_CORE_CK(cudaMemcpyAsync(c->cellmap, cellmap.data(), sizeof(int) * cellmap.size(), cudaMemcpyHostToDevice,
                                  c->stream));
+    TDDA_CORE_CK(cudaMemcpyAsync(c->Rdev, c->R.data(), sizeof(int) * c->R.size(), cudaMemcpyHostToDevice, c->stream));
     for (int a = 0; a < 3; a++) {
         std::vector<double2> w64;
         std::vector<float2> w32;
@@ -827,7 +851,8 @@ tdda_status tdda_core_destroy(tdda_core* c) {
         if (e) cudaGraphExecDestroy(e);
     for (auto& e : c->g32.iter)
         if (e) cudaGraphExecDestroy(e);
-    free_all(c->allocs);
+    free_all(c->allocs, c->stream);
+    if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->hst) cudaFreeHost(c->hst);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -907,26 +932,20 @@ tdda_status tdda_model_create(tdda_core* c, const double* nK, double E0, const d
     m->diel_old.assign(diel_old, diel_old + n3);
     double2** v[] = {&m->P, &m->E, &m->al, &m->diel, &m->Ein, &m->r, &m->r0, &m->p, &m->u, &m->t, &m->Ap, &m->At};
     for (double2** q : v) {
-        tdda_status s = dalloc(m->allocs, q, n3);
+        tdda_status s = dalloc(m->allocs, q, n3, c->stream);
         if (s != TDDA_OK) {
             tdda_model_destroy(m);
             return s;
         }
     }
     {
-        tdda_status s = dalloc(m->allocs, &m->dold, n3);
+        tdda_status s = dalloc(m->allocs, &m->dold, n3, c->stream);
         if (s != TDDA_OK) {
             tdda_model_destroy(m);
             return s;
         }
     }
-    cudaError_t e = cudaMallocHost((void**)&m->stage, sizeof(cd) * n3);
-    if (e != cudaSuccess) {
-        m->stage = nullptr;
-        tdda_model_destroy(m);
-        return cuda_fail(e, "cudaMallocHost");
-    }
-    e = cudaMemsetAsync(m->P, 0, sizeof(double2) * n3, c->stream);
+    cudaError_t e = cudaMemsetAsync(m->P, 0, sizeof(double2) * n3, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(m->Ein, 0, sizeof(double2) * n3, c->stream);
     if (e != cudaSuccess) {
         tdda_model_destroy(m);
@@ -945,8 +964,7 @@ tdda_status tdda_model_destroy(tdda_model* m) {
     if (!m) return TDDA_OK;
     cudaSetDevice(m->core->device);
     cudaStreamSynchronize(m->core->stream);
-    free_all(m->allocs);
-    if (m->stage) cudaFreeHost(m->stage);
+    free_all(m->allocs, m->core->stream);
     delete m;
     return TDDA_OK;
 }
@@ -1104,9 +1122,9 @@ tdda_status tdda_fft3d(double* data, int n0, int n1, int n2, int sign) {
         std::vector<double2> w64;
         std::vector<float2> w32;
         twiddles(n[a], w64, w32);
-        tdda_status s = dalloc(tmp, &tw[a], (size_t)n[a]);
+        tdda_status s = dalloc(tmp, &tw[a], (size_t)n[a], (cudaStream_t)0);
         if (s != TDDA_OK) {
-            free_all(tmp);
+            free_all(tmp, 0);
             return s;
         }
         cudaMemcpy(tw[a], w64.data(), sizeof(double2) * n[a], cudaMemcpyHostToDevice);
@@ -1115,7 +1133,8 @@ tdda_status tdda_fft3d(double* data, int n0, int n1, int n2, int sign) {
     count_launches(3);
     if (e == cudaSuccess) e = tdda::launch_fft3d_f64((double2*)data, p[0], p[1], p[2], tw[0], tw[1], tw[2], sign, 0);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
-    free_all(tmp);
+    free_all(tmp, 0);
+    cudaStreamSynchronize(0);
     if (e != cudaSuccess) return cuda_fail(e, "tdda_fft3d");
     return TDDA_OK;
 }

@@ -1,0 +1,84 @@
+// tdda_fft_ct.cuh -- the shared-memory Stockham FFT with a compile-time plan.
+//
+// Same algorithm as smem_fft() in tdda_fft.cuh (radix stages, ping-pong
+// buffers, one barrier per stage), but the length M, the radix sequence, the
+// number of lines L, their strides and the thread count NT are template
+// constants: every index, twiddle step and loop trip count folds at compile
+// time and the per-thread butterfly loops unroll.  The pass kernels use it for
+// the axis lengths of the common lattices and fall back to the runtime plan
+// otherwise.
+#pragma once
+
+#include "tdda_fft.cuh"
+
+namespace tdda {
+
+// radix plan, identical to the host's make_plan(): 8s and 4s (no lone 2 unless
+// the power of two is 2), then 3, 5, 7
+__host__ __device__ constexpr int ct_nrad(int M, int which) {
+    int m = M, a = 0;
+    while (m % 2 == 0) { m /= 2; a++; }
+    int r[16] = {};
+    int n = 0;
+    while (a >= 3 && a != 4) { r[n++] = 8; a -= 3; }
+    while (a >= 2) { r[n++] = 4; a -= 2; }
+    if (a == 1) r[n++] = 2;
+    while (m % 3 == 0) { r[n++] = 3; m /= 3; }
+    while (m % 5 == 0) { r[n++] = 5; m /= 5; }
+    while (m % 7 == 0) { r[n++] = 7; m /= 7; }
+    return which < 0 ? n : r[which];
+}
+__host__ __device__ constexpr int ct_nstages(int M) { return ct_nrad(M, -1); }
+__host__ __device__ constexpr int ct_radix(int M, int st) { return ct_nrad(M, st); }
+
+template <int R, int SIGN, typename T, int M, int NS, int L, int LS, int MS, int NT>
+__device__ __forceinline__ void ct_stage(const cx<T>* __restrict__ x, cx<T>* __restrict__ y, const cx<T>* tw,
+                                         int nvalid, int nout) {
+    constexpr int m = M / R;
+    constexpr int nb = L * m;
+    constexpr int twstep = M / (NS * R);
+#pragma unroll 4
+    for (int w = threadIdx.x; w < nb; w += NT) {
+        const int j = w / L;
+        const int l = w - j * L;
+        const cx<T>* xb = x + l * LS;
+        cx<T> v[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int idx = j + r * m;
+            v[r] = idx < nvalid ? xb[idx * MS] : czero<T>();
+        }
+        const int k = j % NS;
+        if (NS > 1) {
+#pragma unroll
+            for (int r = 1; r < R; r++) {
+                cx<T> t = tw[r * k * twstep];
+                if (SIGN > 0) t.y = -t.y;
+                v[r] = cmul<T>(v[r], t);
+            }
+        }
+        Bfly<R, SIGN, T>::run(v);
+        cx<T>* yb = y + l * LS;
+        const int ob = (j - k) * R + k;
+#pragma unroll
+        for (int q = 0; q < R; q++) {
+            const int idx = ob + q * NS;
+            if (idx < nout) yb[idx * MS] = v[q];
+        }
+    }
+    __syncthreads();
+}
+
+template <int SIGN, typename T, int M, int L, int LS, int MS, int NT, int ST = 0, int NS = 1>
+__device__ __forceinline__ cx<T>* ct_fft(cx<T>* a, cx<T>* b, const cx<T>* tw, int nvalid, int nout) {
+    if constexpr (ST == ct_nstages(M)) {
+        return a;
+    } else {
+        constexpr int R = ct_radix(M, ST);
+        ct_stage<R, SIGN, T, M, NS, L, LS, MS, NT>(a, b, tw, ST == 0 ? nvalid : M,
+                                                   ST == ct_nstages(M) - 1 ? nout : M);
+        return ct_fft<SIGN, T, M, L, LS, MS, NT, ST + 1, NS * R>(b, a, tw, nvalid, nout);
+    }
+}
+
+}  // namespace tdda

@@ -3,8 +3,8 @@
 //
 // HBM layout of one core (one lattice at one wavelength):
 //   cellmap   int32 [Nx][Ny][Nz]          dipole index of each cell, -1 if empty
-//   green64   double2 [Hy][Hz][Hx][6]     folded Green spectrum / (Mx My Mz)
-//   green32   float2  [Hy][Hz][Hx][6]     the same rounded to FP32 (mixed path)
+//   green64   double2 [Hy][Hx][Hz][6]     folded Green spectrum / (Mx My Mz)
+//   green32   float2  [Hy][Hx][Hz][6]     the same rounded to FP32 (mixed path)
 //   tw{x,y,z} double2/float2 [M]          exp(-2 pi i m / M)
 //   grid      cx<T> [nrhs][3][Nx][My][Mz]  FFT work grid (x kept to the lattice)
 // with H = M/2 + 1 per axis (the tensor components are even or odd in each
@@ -78,6 +78,36 @@ enum SnkMode : int {
     SNK_RES = 4,     // r = r0 = p = E - (A P + al P), rho = r0.r   (DDAModel.cpp:164-168)
 };
 
+// -------------------------------------------------------------- pass dispatch
+// The five passes of one A-product.  Each length-specialised translation unit
+// (tdda_pass_z.cu, tdda_pass_xy.cu) holds kernels for a set of FFT lengths;
+// tdda_pass_generic.cu holds the runtime-plan kernels for every length.
+enum PassId : int { PASS_ZFWD = 0, PASS_YFWD = 1, PASS_XPASS = 2, PASS_YINV = 3, PASS_ZINV = 4 };
+template <typename T> struct PassArgs {
+    Geom g;
+    int nrhs;
+    const RhsVecs<T>* rhs;
+    const cx<T>* green;
+    const cx<T>* twx;
+    const cx<T>* twy;
+    const cx<T>* twz;
+    const int* cellmap;
+    cx<T>* grid;
+    cudaStream_t stream;
+};
+// mode: SrcMode for PASS_ZFWD, SnkMode for PASS_ZINV, unused otherwise
+template <typename T> cudaError_t pass_generic(int pass, int mode, const PassArgs<T>& a);
+// return false (nothing launched) when the length has no specialised kernel
+template <typename T> bool pass_ct_z(int pass, int mode, const PassArgs<T>& a, cudaError_t* err);
+template <typename T> bool pass_ct_xy(int pass, int mode, const PassArgs<T>& a, cudaError_t* err);
+cudaError_t configure_pass_generic();
+cudaError_t configure_pass_ct_z();
+cudaError_t configure_pass_ct_xy();
+// the FFT lengths with specialised kernels
+bool ct_has_z(int Mz);
+bool ct_has_xy(int M);
+constexpr size_t kMaxPassSmem = 200 * 1024;
+
 // -------------------------------------------------------------- launchers
 // All launchers enqueue on `stream` and return cudaGetLastError().
 
@@ -125,6 +155,10 @@ struct AlphaParams {
 cudaError_t launch_model_alpha(int n3, const double* diel_old, const AlphaParams& ap, double2* diel, double2* al,
                                float2* fal, cudaStream_t stream);
 
+// E_inc = E0 n_E0 exp(i K d n_K . R)         (DDAModel.cpp:47-51)
+cudaError_t launch_model_incident(int N, const int* R, double3 nK, double3 nE0, double E0, double K, double d,
+                                  double2* E, cudaStream_t stream);
+
 // Einternal = al P / ((2 + eps) / 3)       (DDAModel.cpp:567-575)
 cudaError_t launch_einternal(int n3, const double2* al, const double2* P, const double2* diel, double2* Ein,
                              cudaStream_t stream);
@@ -142,7 +176,6 @@ cudaError_t launch_fft3d_f64(double2* data, const AxisPlan& p0, const AxisPlan& 
 int max_blocks_per_rhs(const Geom& g);
 // largest dynamic shared memory any pass kernel needs for this geometry
 size_t max_pass_smem(const Geom& g);
-constexpr size_t kMaxPassSmem = 200 * 1024;
 
 // raise the dynamic shared-memory limit of every pass kernel (once per device,
 // outside any stream capture)

@@ -22,367 +22,13 @@
 
 #include <algorithm>
 
-#include "tdda_internal.cuh"
+#include "tdda_device.cuh"
 
 namespace tdda {
 
 namespace {
 
-constexpr int kNT = 256;  // threads of every pass and vector kernel
-
-__host__ __device__ inline int iclamp(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
-__host__ __device__ inline int floor_pow2(int v) {
-    int p = 1;
-    while (p * 2 <= v) p *= 2;
-    return p;
-}
-
-__host__ __device__ inline int pad_odd(int m) { return (m % 2 == 0) ? m + 1 : m; }
-
-// Tiles are sized so that the two ping-pong buffers of a block stay within
-// kSmemBudget (two resident blocks per SM at the largest grids).
-constexpr int kSmemBudget = 96 * 1024;
-
-// lines of a z-pass tile: 3 components x LZ (x, y) columns
-template <typename T> __host__ __device__ inline int z_lines(const AxisPlan& pz) {
-    const int per = 2 * 3 * pad_odd(pz.M) * (int)sizeof(cx<T>);
-    return iclamp((kSmemBudget - pz.M * (int)sizeof(cx<T>)) / per, 1, 16);
-}
-// z-tile of a y-pass
-template <typename T> __host__ __device__ inline int y_tile(const AxisPlan& py) {
-    const int per = 2 * py.M * (int)sizeof(cx<T>);
-    return iclamp(floor_pow2((kSmemBudget - py.M * (int)sizeof(cx<T>)) / per), 1, 16);
-}
-// z-tile of the x-pass (3 components per z)
-template <typename T> __host__ __device__ inline int x_tile(const AxisPlan& px) {
-    const int per = 2 * 3 * px.M * (int)sizeof(cx<T>);
-    return iclamp(floor_pow2((kSmemBudget - px.M * (int)sizeof(cx<T>)) / per), 1, 16);
-}
-// lines of a generic row FFT and z-tile of a generic column FFT (FP64)
-__host__ __device__ inline int row_lines(const AxisPlan& p) {
-    return iclamp((kSmemBudget - p.M * 16) / (2 * pad_odd(p.M) * 16), 1, 32);
-}
-__host__ __device__ inline int col_tile(const AxisPlan& p) {
-    return iclamp(floor_pow2((kSmemBudget - p.M * 16) / (2 * p.M * 16)), 1, 16);
-}
-
-template <typename T> __device__ __forceinline__ cx<T> ld(const cx<T>* p) { return *p; }
-
-__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
-    // Smith's algorithm (R. L. Smith, CACM 5(8), 1962)
-    if (fabs(b.x) >= fabs(b.y)) {
-        double r = b.y / b.x, den = b.x + b.y * r;
-        return make_double2((a.x + a.y * r) / den, (a.y - a.x * r) / den);
-    }
-    double r = b.x / b.y, den = b.x * r + b.y;
-    return make_double2((a.x * r + a.y) / den, (a.y * r - a.x) / den);
-}
-__device__ __forceinline__ double2 dmul(double2 a, double2 b) {
-    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-__device__ __forceinline__ bool finite2(double2 a) { return isfinite(a.x) && isfinite(a.y); }
-
-template <typename T> __device__ __forceinline__ cx<T> from_d(double2 a) { return mk<T>(T(a.x), T(a.y)); }
-
-// ------------------------------------------------------------ reductions
-// Block-wide sum of NV doubles in a fixed order; the result is valid in
-// thread 0.  sred must hold NV * blockDim.x doubles.  The partials go through
-// shared memory and one warp adds them: on GB300 every FP64 warp instruction
-// occupies the narrow FP64 pipe for many cycles, so one warp summing the block
-// costs far less than a shuffle tree run by every warp.
-template <int NV> __device__ __forceinline__ void block_sum(double (&v)[NV], double* sred) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nt = blockDim.x;
-#pragma unroll
-    for (int k = 0; k < NV; k++) sred[k * nt + threadIdx.x] = v[k];
-    __syncthreads();
-    if (warp == 0) {
-#pragma unroll
-        for (int k = 0; k < NV; k++) {
-            double a = 0.0;
-            for (int i = lane; i < nt; i += 32) a += sred[k * nt + i];
-            for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-            v[k] = a;
-        }
-    }
-    __syncthreads();
-}
-
-// Publish this block's partials; the last block of the grid (for this
-// right-hand side) sums all partials in block order and returns true in
-// every thread of that block, with the totals in tot (valid in thread 0).
-template <int NV>
-__device__ bool last_block_total(double (&v)[NV], double* part, int nblk, int bid, unsigned int* cnt, double* sred,
-                                 double (&tot)[NV]) {
-    __shared__ int s_last;
-    block_sum<NV>(v, sred);
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int k = 0; k < NV; k++) part[k * nblk + bid] = v[k];
-        __threadfence();
-        unsigned int prev = atomicAdd(cnt, 1u);
-        s_last = (prev == (unsigned int)(nblk - 1));
-    }
-    __syncthreads();
-    if (!s_last) return false;
-    __threadfence();
-#pragma unroll
-    for (int k = 0; k < NV; k++) {
-        double a = 0.0;
-        for (int i = threadIdx.x; i < nblk; i += blockDim.x) a += __ldcg(part + k * nblk + i);
-        tot[k] = a;
-    }
-    block_sum<NV>(tot, sred);
-    if (threadIdx.x == 0) *cnt = 0u;
-    return true;
-}
-
-__device__ __forceinline__ bool rhs_done(const SolveState* st) {
-    return st != nullptr && *((volatile const int*)&st->status) != ST_RUNNING;
-}
-
-template <typename T> __device__ __forceinline__ void stage_tw(cx<T>* stw, const cx<T>* tw, int M) {
-    for (int i = threadIdx.x; i < M; i += blockDim.x) stw[i] = tw[i];
-}
-
-// ================================================================ K1 zfwd
-template <typename T, int SRC>
-__global__ void __launch_bounds__(kNT) k_zfwd(Geom g, const RhsVecs<T>* __restrict__ rhs,
-                                              const cx<T>* __restrict__ twz, const int* __restrict__ cellmap,
-                                              cx<T>* __restrict__ grid) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int b = blockIdx.y;
-    const RhsVecs<T> R = rhs[b];
-    if (rhs_done(R.st)) return;
-    const int Mz = g.pz.M, Nz = g.Nz;
-    const int LZ = z_lines<T>(g.pz), MzP = pad_odd(Mz);
-    cx<T>* stw = reinterpret_cast<cx<T>*>(smem_raw);
-    cx<T>* s = stw + Mz;
-    cx<T>* s2 = s + 3 * LZ * MzP;
-    stage_tw<T>(stw, twz, Mz);
-    const int nlines = g.Nx * g.Ny;
-    const int l0 = blockIdx.x * LZ;
-    const int nl = min(LZ, nlines - l0);
-
-    cx<T> beta, alpha;
-    if (SRC == SRC_PUPD) beta = from_d<T>(R.st->beta);
-    if (SRC == SRC_TUPD) alpha = from_d<T>(R.st->alpha);
-    const cx<T>* src = SRC == SRC_IN ? R.p : R.P;
-    for (int e = threadIdx.x; e < nl * Nz; e += blockDim.x) {
-        const int line = e / Nz, z = e - (e / Nz) * Nz;
-        const int i = cellmap[(long long)(l0 + line) * Nz + z];
-        cx<T> v[3];
-        if (i >= 0) {
-            const long long o = 3LL * i;
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                if (SRC == SRC_PUPD) {
-                    cx<T> pc = R.p[o + c], uc = R.u[o + c], rc = R.r[o + c];
-                    v[c] = cadd<T>(rc, cmul<T>(beta, csub<T>(pc, uc)));
-                    R.p[o + c] = v[c];
-                } else if (SRC == SRC_TUPD) {
-                    cx<T> rc = R.r[o + c], ac = R.Ap[o + c];
-                    v[c] = csub<T>(rc, cmul<T>(alpha, ac));
-                    R.t[o + c] = v[c];
-                } else {
-                    v[c] = src[o + c];
-                }
-            }
-        } else {
-            v[0] = v[1] = v[2] = czero<T>();
-        }
-#pragma unroll
-        for (int c = 0; c < 3; c++) s[(c * LZ + line) * MzP + z] = v[c];
-    }
-    __syncthreads();
-    const cx<T>* res = smem_fft<-1, T>(s, s2, 3 * LZ, MzP, 1, g.pz, stw, Nz, Mz);
-    cx<T>* gb = grid + (long long)b * g.sb;
-    for (int e = threadIdx.x; e < 3 * nl * Mz; e += blockDim.x) {
-        const int cl = e / Mz, z = e - (e / Mz) * Mz;
-        const int c = cl / nl, line = cl - (cl / nl) * nl;
-        const int l = l0 + line, x = l / g.Ny, y = l - (l / g.Ny) * g.Ny;
-        gb[c * g.sc + x * g.sx + y * g.sy + z] = res[(c * LZ + line) * MzP + z];
-    }
-}
-
-// ================================================================ K2/K4 ypass
-template <typename T, int SIGN>
-__global__ void __launch_bounds__(kNT) k_ypass(Geom g, const RhsVecs<T>* __restrict__ rhs,
-                                               const cx<T>* __restrict__ twy, cx<T>* __restrict__ grid) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int b = blockIdx.z;
-    if (rhs_done(rhs[b].st)) return;
-    const int My = g.py.M, Mz = g.pz.M;
-    const int ZT = y_tile<T>(g.py);
-    const int nzt = (Mz + ZT - 1) / ZT;
-    const int x = blockIdx.x / nzt, z0 = (blockIdx.x - x * nzt) * ZT;
-    const int c = blockIdx.y;
-    const int zn = min(ZT, Mz - z0);
-    cx<T>* stw = reinterpret_cast<cx<T>*>(smem_raw);
-    cx<T>* s = stw + My;
-    cx<T>* s2 = s + My * ZT;
-    stage_tw<T>(stw, twy, My);
-    cx<T>* gp = grid + (long long)b * g.sb + c * g.sc + (long long)x * g.sx + z0;
-    const int nin = SIGN < 0 ? g.Ny : My;
-    const int nout = SIGN < 0 ? My : g.Ny;
-    for (int e = threadIdx.x; e < nin * ZT; e += blockDim.x) {
-        const int y = e / ZT, zl = e - (e / ZT) * ZT;
-        if (zl < zn) s[y * ZT + zl] = gp[(long long)y * g.sy + zl];
-    }
-    __syncthreads();
-    const cx<T>* res = smem_fft<SIGN, T>(s, s2, ZT, 1, ZT, g.py, stw, nin, nout);
-    for (int e = threadIdx.x; e < nout * ZT; e += blockDim.x) {
-        const int y = e / ZT, zl = e - (e / ZT) * ZT;
-        if (zl < zn) gp[(long long)y * g.sy + zl] = res[y * ZT + zl];
-    }
-}
-
-// ================================================================ K3 xpass
-// folding of a spectral index and the parity of each tensor component:
-// xx, yy, zz even in all axes; xy odd in x,y; xz odd in x,z; yz odd in y,z
-__device__ __forceinline__ int fold(int k, int M) { return 2 * k > M ? M - k : k; }
-
-template <typename T>
-__global__ void __launch_bounds__(kNT) k_xpass(Geom g, const RhsVecs<T>* __restrict__ rhs,
-                                                const cx<T>* __restrict__ green, const cx<T>* __restrict__ twx,
-                                                cx<T>* __restrict__ grid) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int b = blockIdx.y;
-    if (rhs_done(rhs[b].st)) return;
-    const int Mx = g.px.M, My = g.py.M, Mz = g.pz.M, Nx = g.Nx;
-    const int ZT = x_tile<T>(g.px);
-    const int nzt = (Mz + ZT - 1) / ZT;
-    const int y = blockIdx.x / nzt, z0 = (blockIdx.x - y * nzt) * ZT;
-    const int zn = min(ZT, Mz - z0);
-    const int W = 3 * ZT;  // elements per x in shared memory
-    cx<T>* stw = reinterpret_cast<cx<T>*>(smem_raw);
-    cx<T>* s = stw + Mx;
-    cx<T>* s2 = s + Mx * W;
-    stage_tw<T>(stw, twx, Mx);
-    cx<T>* gp = grid + (long long)b * g.sb + (long long)y * g.sy + z0;
-    for (int e = threadIdx.x; e < Nx * W; e += blockDim.x) {
-        const int x = e / W, r = e - (e / W) * W;
-        const int c = r / ZT, zl = r - (r / ZT) * ZT;
-        if (zl < zn) s[e] = gp[c * g.sc + (long long)x * g.sx + zl];
-        else s[e] = czero<T>();
-    }
-    __syncthreads();
-    cx<T>* res = smem_fft<-1, T>(s, s2, W, 1, W, g.px, stw, Nx, Mx);
-
-    // spectral product: C = A b with the symmetric 3x3 Green tensor
-    const int fy = fold(y, My);
-    const bool uy = 2 * y > My;
-    for (int e = threadIdx.x; e < Mx * ZT; e += blockDim.x) {
-        const int kx = e / ZT, zl = e - (e / ZT) * ZT;
-        const int z = z0 + zl;
-        if (zl >= zn) continue;
-        const int fx = fold(kx, Mx), fz = fold(z, Mz);
-        const bool ux = 2 * kx > Mx, uz = 2 * z > Mz;
-        const cx<T>* gg = green + (((long long)fy * g.Hz + fz) * g.Hx + fx) * 6;
-        cx<T> a0 = gg[0], a1 = gg[1], a2 = gg[2], a3 = gg[3], a4 = gg[4], a5 = gg[5];
-        if (ux != uy) a1 = mk<T>(-a1.x, -a1.y);  // xy: odd in x and y
-        if (ux != uz) a2 = mk<T>(-a2.x, -a2.y);  // xz: odd in x and z
-        if (uy != uz) a4 = mk<T>(-a4.x, -a4.y);  // yz: odd in y and z
-        cx<T>* p = res + kx * W + zl;
-        const cx<T> bx = p[0], by = p[ZT], bz = p[2 * ZT];
-        p[0] = cadd<T>(cadd<T>(cmul<T>(a0, bx), cmul<T>(a1, by)), cmul<T>(a2, bz));
-        p[ZT] = cadd<T>(cadd<T>(cmul<T>(a1, bx), cmul<T>(a3, by)), cmul<T>(a4, bz));
-        p[2 * ZT] = cadd<T>(cadd<T>(cmul<T>(a2, bx), cmul<T>(a4, by)), cmul<T>(a5, bz));
-    }
-    __syncthreads();
-    const cx<T>* out = smem_fft<+1, T>(res, res == s ? s2 : s, W, 1, W, g.px, stw, Mx, Nx);
-    for (int e = threadIdx.x; e < Nx * W; e += blockDim.x) {
-        const int x = e / W, r = e - (e / W) * W;
-        const int c = r / ZT, zl = r - (r / ZT) * ZT;
-        if (zl < zn) gp[c * g.sc + (long long)x * g.sx + zl] = out[e];
-    }
-}
-
-// ================================================================ K5 zinv
-template <typename T, int SRC, int SNK>
-__global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restrict__ rhs,
-                                              const cx<T>* __restrict__ twz, const int* __restrict__ cellmap,
-                                              cx<T>* __restrict__ grid) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ double sred[4 * kNT];
-    const int b = blockIdx.y;
-    const RhsVecs<T> R = rhs[b];
-    if (rhs_done(R.st)) return;
-    const int Mz = g.pz.M, Nz = g.Nz;
-    const int LZ = z_lines<T>(g.pz), MzP = pad_odd(Mz);
-    cx<T>* stw = reinterpret_cast<cx<T>*>(smem_raw);
-    cx<T>* s = stw + Mz;
-    cx<T>* s2 = s + 3 * LZ * MzP;
-    stage_tw<T>(stw, twz, Mz);
-    const int nlines = g.Nx * g.Ny;
-    const int l0 = blockIdx.x * LZ;
-    const int nl = min(LZ, nlines - l0);
-    const cx<T>* gb = grid + (long long)b * g.sb;
-    for (int e = threadIdx.x; e < 3 * nl * Mz; e += blockDim.x) {
-        const int cl = e / Mz, z = e - (e / Mz) * Mz;
-        const int c = cl / nl, line = cl - (cl / nl) * nl;
-        const int l = l0 + line, x = l / g.Ny, y = l - (l / g.Ny) * g.Ny;
-        s[(c * LZ + line) * MzP + z] = gb[c * g.sc + x * g.sx + y * g.sy + z];
-    }
-    __syncthreads();
-    const cx<T>* res = smem_fft<+1, T>(s, s2, 3 * LZ, MzP, 1, g.pz, stw, Mz, Nz);
-
-    // scatter to the dipoles, fused diagonal term and dot products
-    const cx<T>* vsrc = (SRC == SRC_TUPD) ? R.t : (SRC == SRC_P ? R.P : R.p);
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int e = threadIdx.x; e < nl * Nz; e += blockDim.x) {
-        const int line = e / Nz, z = e - (e / Nz) * Nz;
-        const int i = cellmap[(long long)(l0 + line) * Nz + z];
-        if (i < 0) continue;
-        const long long o = 3LL * i;
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            cx<T> val = res[(c * LZ + line) * MzP + z];
-            if (SNK == SNK_OUT) {
-                R.Ap[o + c] = val;
-                continue;
-            }
-            const cx<T> vv = vsrc[o + c];
-            const cx<T> w = cadd<T>(val, cmul<T>(vv, R.al[o + c]));
-            if (SNK == SNK_ALB) {
-                R.Ap[o + c] = w;
-            } else if (SNK == SNK_AP) {
-                R.Ap[o + c] = w;
-                const cx<T> q = R.r0[o + c];  // r0 . Ap
-                acc[0] += (double)q.x * (double)w.x + (double)q.y * (double)w.y;
-                acc[1] += (double)q.x * (double)w.y - (double)q.y * (double)w.x;
-            } else if (SNK == SNK_AT) {
-                R.At[o + c] = w;
-                const cx<T> tt = vv;  // At . t and At . At
-                acc[0] += (double)w.x * (double)tt.x + (double)w.y * (double)tt.y;
-                acc[1] += (double)w.x * (double)tt.y - (double)w.y * (double)tt.x;
-                acc[2] += (double)w.x * (double)w.x + (double)w.y * (double)w.y;
-            } else if (SNK == SNK_RES) {
-                const cx<T> res = csub<T>(R.E[o + c], w);
-                R.r[o + c] = res;
-                R.r0[o + c] = res;
-                R.p[o + c] = res;
-                acc[0] += (double)res.x * (double)res.x + (double)res.y * (double)res.y;
-            }
-        }
-    }
-    if (SNK == SNK_OUT || SNK == SNK_ALB) return;
-    double tot[4];
-    const int nblk = gridDim.x;
-    const int slot = SNK == SNK_AP ? 0 : (SNK == SNK_AT ? 1 : 2);
-    if (!last_block_total<4>(acc, R.part, nblk, blockIdx.x, R.cnt + slot, sred, tot)) return;
-    if (threadIdx.x != 0) return;
-    SolveState* st = R.st;
-    if (SNK == SNK_AP) {
-        double2 r0Ap = make_double2(tot[0], tot[1]);
-        st->alpha = cdiv(st->rho, r0Ap);  // DDAModel.cpp:221
-    } else if (SNK == SNK_AT) {
-        st->zeta = cdiv(make_double2(tot[0], tot[1]), make_double2(tot[2], 0.0));  // DDAModel.cpp:225
-    } else {
-        st->rho = make_double2(tot[0], 0.0);  // r0 . r with r0 = r
-        st->rnorm2 = tot[0];
-    }
-}
-
+using namespace dev;
 // ================================================================ K6 update
 template <typename T>
 __global__ void __launch_bounds__(kNT) k_update(int n3, const RhsVecs<T>* __restrict__ rhs, int is_init) {
@@ -523,8 +169,8 @@ __global__ void k_green_fold(Geom g, const double2* __restrict__ full6, double2*
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < H * 6; e += (long long)gridDim.x * blockDim.x) {
         const int l = (int)(e % 6);
         const long long q = e / 6;
-        const int fx = (int)(q % g.Hx);
-        const int fz = (int)((q / g.Hx) % g.Hz);
+        const int fz = (int)(q % g.Hz);
+        const int fx = (int)((q / g.Hz) % g.Hx);
         const int fy = (int)(q / ((long long)g.Hx * g.Hz));
         const double2 v = full6[l * M + ((long long)fx * My + fy) * Mz + fz];
         const double2 w = make_double2(v.x * inv, v.y * inv);
@@ -620,6 +266,18 @@ __global__ void k_model_alpha(int n3, const double* __restrict__ diel_old, Alpha
     }
 }
 
+__global__ void k_model_incident(int N, const int* __restrict__ R, double3 nK, double3 nE0, double E0, double K,
+                                 double d, double2* __restrict__ E) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        const double ph = K * d * (nK.x * R[3 * i] + nK.y * R[3 * i + 1] + nK.z * R[3 * i + 2]);
+        double sn, cs;
+        sincos(ph, &sn, &cs);
+        const double a[3] = {E0 * nE0.x, E0 * nE0.y, E0 * nE0.z};
+#pragma unroll
+        for (int j = 0; j < 3; j++) E[3 * i + j] = make_double2(a[j] * cs, a[j] * sn);
+    }
+}
+
 // ------------------------------------------------------------ small kernels
 __global__ void k_einternal(int n3, const double2* al, const double2* P, const double2* diel, double2* Ein) {
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x) {
@@ -653,56 +311,28 @@ int grid_reduce(long long n) {
     return (int)(b < 1 ? 1 : b);
 }
 
-template <typename T> size_t zsmem(const Geom& g) {
-    return sizeof(cx<T>) * (size_t)(g.pz.M + 2 * 3 * z_lines<T>(g.pz) * pad_odd(g.pz.M));
-}
-template <typename T> size_t ysmem(const Geom& g) {
-    return sizeof(cx<T>) * (size_t)(g.py.M + 2 * g.py.M * y_tile<T>(g.py));
-}
-template <typename T> size_t xsmem(const Geom& g) {
-    return sizeof(cx<T>) * (size_t)(g.px.M + 2 * g.px.M * 3 * x_tile<T>(g.px));
-}
 size_t rowsmem(const AxisPlan& p) { return sizeof(double2) * (size_t)(p.M + 2 * row_lines(p) * pad_odd(p.M)); }
 size_t colsmem(const AxisPlan& p) { return sizeof(double2) * (size_t)(p.M + 2 * p.M * col_tile(p)); }
 
 
-constexpr int kMaxSmem = 200 * 1024;  // leaves room for the static reduction buffers
-
-template <typename T> cudaError_t configure_t() {
-    cudaError_t e = cudaSuccess;
-    auto set = [&](const void* k) {
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
-    };
-    set((const void*)k_zfwd<T, SRC_IN>);
-    set((const void*)k_zfwd<T, SRC_PUPD>);
-    set((const void*)k_zfwd<T, SRC_TUPD>);
-    set((const void*)k_zfwd<T, SRC_P>);
-    set((const void*)k_ypass<T, -1>);
-    set((const void*)k_ypass<T, +1>);
-    set((const void*)k_xpass<T>);
-    set((const void*)k_zinv<T, SRC_IN, SNK_OUT>);
-    set((const void*)k_zinv<T, SRC_IN, SNK_ALB>);
-    set((const void*)k_zinv<T, SRC_PUPD, SNK_AP>);
-    set((const void*)k_zinv<T, SRC_TUPD, SNK_AT>);
-    set((const void*)k_zinv<T, SRC_P, SNK_RES>);
-    return e;
-}
-
 }  // namespace
 
 cudaError_t configure_kernels() {
-    cudaError_t e = configure_t<double>();
-    if (e == cudaSuccess) e = configure_t<float>();
-    if (e == cudaSuccess) e = cudaFuncSetAttribute((const void*)k_fft_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute((const void*)k_fft_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
+    cudaError_t e = configure_pass_generic();
+    if (e == cudaSuccess) e = configure_pass_ct_z();
+    if (e == cudaSuccess) e = configure_pass_ct_xy();
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute((const void*)k_fft_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxPassSmem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute((const void*)k_fft_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxPassSmem);
     return e;
 }
 
 size_t max_pass_smem(const Geom& g) {
     size_t m = 0;
-    m = std::max(m, zsmem<double>(g));
-    m = std::max(m, ysmem<double>(g));
-    m = std::max(m, xsmem<double>(g));
+    m = std::max(m, zsmem<double>(g.pz.M));
+    m = std::max(m, ysmem<double>(g.py.M));
+    m = std::max(m, xsmem<double>(g.px.M));
     m = std::max(m, rowsmem(g.pz));
     m = std::max(m, colsmem(g.py));
     m = std::max(m, colsmem(g.px));
@@ -710,7 +340,7 @@ size_t max_pass_smem(const Geom& g) {
 }
 
 int max_blocks_per_rhs(const Geom& g) {
-    const int lz = z_lines<float>(g.pz) > z_lines<double>(g.pz) ? z_lines<double>(g.pz) : z_lines<float>(g.pz);
+    const int lz = std::min(z_lines<float>(g.pz.M), z_lines<double>(g.pz.M));
     int nz = (g.Nx * g.Ny + lz - 1) / lz;
     int nv = grid_reduce(3LL * g.N);
     return nz > nv ? nz : nv;
@@ -765,56 +395,18 @@ template <typename T>
 cudaError_t launch_aproduct(const Geom& g, int src, int snk, int nrhs, const RhsVecs<T>* rhs, const cx<T>* green,
                             const cx<T>* twx, const cx<T>* twy, const cx<T>* twz, const int* cellmap, cx<T>* grid,
                             cudaStream_t stream, cudaEvent_t* ev) {
-    cudaError_t err;
-    if (ev) cudaEventRecord(ev[0], stream);
-    const int LZ = z_lines<T>(g.pz);
-    const dim3 gz((g.Nx * g.Ny + LZ - 1) / LZ, nrhs);
-    const size_t smz = zsmem<T>(g);
-    // K1
-    switch (src) {
-        case SRC_IN:
-            k_zfwd<T, SRC_IN><<<gz, kNT, smz, stream>>>(g, rhs, twz, cellmap, grid);
-            break;
-        case SRC_PUPD:
-            k_zfwd<T, SRC_PUPD><<<gz, kNT, smz, stream>>>(g, rhs, twz, cellmap, grid);
-            break;
-        case SRC_TUPD:
-            k_zfwd<T, SRC_TUPD><<<gz, kNT, smz, stream>>>(g, rhs, twz, cellmap, grid);
-            break;
-        default:
-            k_zfwd<T, SRC_P><<<gz, kNT, smz, stream>>>(g, rhs, twz, cellmap, grid);
-            break;
+    const PassArgs<T> a{g, nrhs, rhs, green, twx, twy, twz, cellmap, grid, stream};
+    const int passes[5] = {PASS_ZFWD, PASS_YFWD, PASS_XPASS, PASS_YINV, PASS_ZINV};
+    const int modes[5] = {src, 0, 0, 0, snk};
+    for (int k = 0; k < 5; k++) {
+        if (ev) cudaEventRecord(ev[k], stream);
+        cudaError_t err = cudaSuccess;
+        const bool done = pass_ct_z<T>(passes[k], modes[k], a, &err) || pass_ct_xy<T>(passes[k], modes[k], a, &err);
+        if (!done) err = pass_generic<T>(passes[k], modes[k], a);
+        if (err != cudaSuccess) return err;
     }
-    if ((err = cudaGetLastError())) return err;
-    if (ev) cudaEventRecord(ev[1], stream);
-    // K2
-    const int YT = y_tile<T>(g.py);
-    const dim3 gy(g.Nx * ((g.pz.M + YT - 1) / YT), 3, nrhs);
-    const size_t smy = ysmem<T>(g);
-    k_ypass<T, -1><<<gy, kNT, smy, stream>>>(g, rhs, twy, grid);
-    if ((err = cudaGetLastError())) return err;
-    if (ev) cudaEventRecord(ev[2], stream);
-    // K3
-    const int XT = x_tile<T>(g.px);
-    const dim3 gx(g.py.M * ((g.pz.M + XT - 1) / XT), nrhs);
-    const size_t smx = xsmem<T>(g);
-    k_xpass<T><<<gx, kNT, smx, stream>>>(g, rhs, green, twx, grid);
-    if ((err = cudaGetLastError())) return err;
-    if (ev) cudaEventRecord(ev[3], stream);
-    // K4
-    k_ypass<T, +1><<<gy, kNT, smy, stream>>>(g, rhs, twy, grid);
-    if ((err = cudaGetLastError())) return err;
-    if (ev) cudaEventRecord(ev[4], stream);
-    // K5
-#define TDDA_ZINV(S, K) k_zinv<T, S, K><<<gz, kNT, smz, stream>>>(g, rhs, twz, cellmap, grid)
-    if (snk == SNK_OUT) TDDA_ZINV(SRC_IN, SNK_OUT);
-    else if (snk == SNK_ALB) TDDA_ZINV(SRC_IN, SNK_ALB);
-    else if (snk == SNK_AP) TDDA_ZINV(SRC_PUPD, SNK_AP);
-    else if (snk == SNK_AT) TDDA_ZINV(SRC_TUPD, SNK_AT);
-    else TDDA_ZINV(SRC_P, SNK_RES);
-#undef TDDA_ZINV
     if (ev) cudaEventRecord(ev[5], stream);
-    return cudaGetLastError();
+    return cudaSuccess;
 }
 
 template <typename T>
@@ -846,6 +438,11 @@ cudaError_t launch_einternal(int n3, const double2* al, const double2* P, const 
 cudaError_t launch_model_alpha(int n3, const double* diel_old, const AlphaParams& ap, double2* diel, double2* al,
                                float2* fal, cudaStream_t stream) {
     k_model_alpha<<<grid1d(n3, kNT), kNT, 0, stream>>>(n3, diel_old, ap, diel, al, fal);
+    return cudaGetLastError();
+}
+cudaError_t launch_model_incident(int N, const int* R, double3 nK, double3 nE0, double E0, double K, double d,
+                                  double2* E, cudaStream_t stream) {
+    k_model_incident<<<grid1d(N, kNT), kNT, 0, stream>>>(N, R, nK, nE0, E0, K, d, E);
     return cudaGetLastError();
 }
 cudaError_t launch_to_f32(int n3, const double2* src, float2* dst, cudaStream_t stream) {
