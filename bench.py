@@ -293,6 +293,41 @@ def batched_roofline(w, grid, prof, nrhs, s, peak):
             "algorithmic_bytes": b, "avg_ms": t}
 
 
+def run_serving(tdda, stream, precision, workers, budget, dev):
+    """Replay the request stream in real time through the serving loop."""
+    srv = tdda.Server(hbm_budget_bytes=budget, workers=workers, precision=precision, max_it=MAX_IT, tol=TOL,
+                      max_group=8, device=dev)
+    t0 = srv.clock()
+    ids = []
+    for r in stream:
+        diel = r.diel_old()
+        delay = t0 + r.t_arrival - srv.clock()
+        if delay > 0:
+            time.sleep(delay)
+        ids.append(srv.submit(r.Nx, r.Ny, r.Nz, lattice.bulk(r.Nx, r.Ny, r.Nz), 10.0, r.lam,
+                              np.array([1.0, r.eps_m]), diel, r.incidences))
+    infos = [srv.result(i, with_P=False)[0] for i in ids]
+    peak = srv.stats()["peak_bytes"]
+    srv.close()
+    ok = [i["state"] == tdda.REQ_DONE for i in infos]
+    lat = np.array([(i["t_done"] - i["t_submit"]) * 1e3 for i in infos])
+    span = max(i["t_done"] for i in infos) - min(i["t_submit"] for i in infos)
+    rhs = sum(len(r.incidences) for r in stream)
+    classes = {"N<32k": lambda n: n < 32768, "32k<=N<128k": lambda n: 32768 <= n < 131072,
+               "N>=128k": lambda n: n >= 131072}
+    per = {}
+    for name, f in classes.items():
+        sel = [l for l, r in zip(lat, stream) if f(r.N)]
+        if sel:
+            per[name] = {"requests": len(sel), "p50_ms": float(np.percentile(sel, 50)),
+                         "p99_ms": float(np.percentile(sel, 99))}
+    return {"requests": len(stream), "failed": int(len(ok) - sum(ok)), "rhs_solves": rhs,
+            "value": rhs / span, "unit": UNIT, "requests_per_s": len(stream) / span, "makespan_s": span,
+            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+            "latency_by_size": per, "peak_admitted_bytes": peak,
+            "max_iterations": max(i["iterations"] for i in infos)}
+
+
 def run_ours(args, dist: Dist):
     import torch
 
@@ -394,6 +429,17 @@ def run_ours(args, dist: Dist):
                             "ms_per_batch": b64["ms_per_batch"]},
                    "speedup_fp32_refine": b32["value"] / b64["value"]}
 
+    # serving: the request stream through the continuous-batching loop
+    serving = None
+    if args.serve_requests > 0:
+        stream = lattice.serving_stream(n=args.serve_requests, rate=200.0, seed=5)
+        s32 = run_serving(tdda, stream, tdda.FP32_REFINE, args.serve_workers, 150e9, dev)
+        s64 = run_serving(tdda, stream, tdda.FP64, args.serve_workers, 150e9, dev)
+        serving = {"workload": f"serving stream {args.serve_requests} requests, Poisson 200/s, dims 16-128 "
+                               "log-uniform (z<=32), 1-4 RHS (cfg 5)", "hbm_budget_bytes": 150e9,
+                   "workers": args.serve_workers, "fp32_refine": s32, "fp64": s64,
+                   "speedup_fp32_refine": s32["value"] / s64["value"]}
+
     cpu = None
     if dist.rank == 0:
         base = CpuBaseline(w, args.cpu_threads or (os.cpu_count() or 1))
@@ -421,6 +467,7 @@ def run_ours(args, dist: Dist):
                          "traffic": traffic,
                          "pass_ms_fp32": prof32, "pass_ms_fp64": prof64},
             "batched": batched,
+            "serving": serving,
             "gpu_launches": launches,
             "clocks": clocks,
             "cpu_baseline": cpu,
@@ -453,6 +500,8 @@ def main():
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--batched-steps", type=int, default=3)
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-workers", type=int, default=4)
     ap.add_argument("--aprod-only", type=int, default=0)
     ap.add_argument("--aprod-precision", choices=["fp32", "fp64"], default="fp32")
     ap.add_argument("--reps", type=int, default=3)

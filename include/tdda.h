@@ -143,6 +143,74 @@ int tdda_model_iterations(const tdda_model* model);
 tdda_status tdda_solve_batch(tdda_model* const* models, int n, int precision, int max_it, double max_err,
                              tdda_solve_info* infos);
 
+/* serving loop: continuous batching of solve requests ------------------- */
+/* Requests queue in arrival order.  A worker takes the first request whose
+ * device memory fits the HBM budget that the requests in flight leave free,
+ * together with queued requests that share its operator (lattice, spacing,
+ * wavelength, material, nback) up to max_group right-hand sides, and solves
+ * them in one batched solve on its own CUDA stream while other workers solve
+ * theirs.  No counterpart in the reference, which solves one structure at a
+ * time (main.cpp:577-598); each result equals the same request solved alone. */
+typedef enum tdda_request_state {
+    TDDA_REQ_QUEUED = 0,
+    TDDA_REQ_RUNNING = 1,
+    TDDA_REQ_DONE = 2,
+    TDDA_REQ_FAILED = 3
+} tdda_request_state;
+
+typedef struct tdda_server_desc {
+    int device;
+    double hbm_budget_bytes;  /* device memory the requests in flight may hold */
+    int workers;              /* requests solved concurrently (one stream each) */
+    int precision;            /* TDDA_FP64 or TDDA_FP32_REFINE */
+    int max_it;
+    double tol;
+    int max_group;            /* right-hand sides of one batched solve (<= 64) */
+    int dry_run;              /* scheduler only: no device work, a request takes dry_run_ms */
+    double dry_run_ms;
+} tdda_server_desc;
+
+typedef struct tdda_request_desc {
+    int Nx, Ny, Nz, N;
+    const int* R;             /* 3N lattice indices */
+    double d, lam, nback;
+    const double* material;   /* nmat complex */
+    int nmat;
+    const double* diel_old;   /* 3N densities */
+    int nrhs;                 /* incidences solved on this structure */
+    const double* nK;         /* 3 x nrhs */
+    const double* nE0;        /* 3 x nrhs */
+    const double* E0;         /* nrhs */
+} tdda_request_desc;
+
+typedef struct tdda_request_info {
+    int state;                /* tdda_request_state */
+    int status;               /* worst tdda_status over the right-hand sides */
+    double t_submit, t_start, t_done;  /* seconds on the server clock */
+    int iterations;           /* largest iteration count over the right-hand sides */
+    double error;             /* largest final relative residual */
+    double bytes;             /* device bytes admitted for the request */
+    int group;                /* right-hand sides of the batched solve that carried it */
+} tdda_request_info;
+
+typedef struct tdda_server_s tdda_server;
+
+tdda_status tdda_server_create(const tdda_server_desc* desc, tdda_server** out);
+/* copies the request; *id identifies it */
+tdda_status tdda_server_submit(tdda_server* server, const tdda_request_desc* req, unsigned long long* id);
+/* state and timings of a request; wait != 0 blocks until it has finished.  P,
+ * if not NULL, receives the 3N x nrhs complex polarisations (host memory). */
+tdda_status tdda_server_result(tdda_server* server, unsigned long long id, int wait, tdda_request_info* info,
+                               double* P);
+/* queued and running requests, device bytes in flight now and at most */
+tdda_status tdda_server_stats(tdda_server* server, int* queued, int* running, double* bytes, double* peak_bytes);
+/* seconds since the server was created */
+double tdda_server_clock(const tdda_server* server);
+/* finishes every submitted request, then stops the workers */
+tdda_status tdda_server_destroy(tdda_server* server);
+/* device bytes a request of nrhs right-hand sides holds while it is solved */
+double tdda_request_bytes(int Nx, int Ny, int Nz, int N, int nrhs, int precision);
+
 /* FFT engine ------------------------------------------------------------ */
 /* In-place unnormalised 3-D complex128 FFT of a device array (n0, n1, n2),
  * last index fastest, sign -1 forward / +1 inverse, each n 7-smooth; the

@@ -1,0 +1,100 @@
+"""The continuous-batching solve loop (tdda_server_*).
+
+Scheduler behaviour is tested without a GPU in the server's dry-run mode (the same
+scheduler; each request sleeps instead of solving): admission never exceeds the HBM
+budget, a request that does not fit waits while smaller ones behind it run, requests
+sharing an operator are grouped, a request larger than the whole budget fails.  The GPU
+test checks that each result in a mixed stream equals the same request solved alone.
+"""
+import time
+
+import numpy as np
+import pytest
+
+import tdda
+from tdda import lattice
+
+MAT = np.array([1.0, 4.0 + 0.1j])
+XPOL = ([0.0, 0.0, 1.0], [1.0, 0.0, 0.0], 1.0)
+YPOL = ([0.0, 0.0, 1.0], [0.0, 1.0, 0.0], 1.0)
+
+
+def _req(server, n, lam=500.0, seed=0, incs=(XPOL,)):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    R = lattice.bulk(n, n, n)
+    diel = np.repeat(rng.random(n ** 3), 3)
+    return server.submit(n, n, n, R, 10.0, lam, MAT, diel, list(incs))
+
+
+def test_dry_run_respects_the_budget_and_first_fit():
+    small = tdda.request_bytes(6, 6, 6, 216, 1)
+    big = tdda.request_bytes(12, 12, 12, 1728, 1)
+    budget = big + 0.5 * small  # the big request fits alone, not with a small one beside it
+    s = tdda.Server(hbm_budget_bytes=budget, workers=3, dry_run_ms=40.0)
+    ids = [_req(s, 6, seed=1), _req(s, 12, seed=2), _req(s, 6, seed=3, lam=510.0), _req(s, 6, seed=4, lam=520.0)]
+    peak_seen = 0.0
+    t0 = time.time()
+    while time.time() - t0 < 10:
+        st = s.stats()
+        peak_seen = max(peak_seen, st["bytes"])
+        if st["queued"] == 0 and st["running"] == 0:
+            break
+        time.sleep(0.005)
+    infos = [s.result(i, with_P=False)[0] for i in ids]
+    s.close()
+    assert all(i["state"] == tdda.REQ_DONE for i in infos)
+    assert peak_seen <= budget and s is not None
+    # the big request could not start beside the first small one: the small ones behind it ran first
+    assert infos[1]["t_start"] >= infos[0]["t_done"] - 1e-3
+    assert infos[2]["t_start"] < infos[1]["t_start"]
+
+
+def test_dry_run_groups_requests_sharing_an_operator():
+    s = tdda.Server(hbm_budget_bytes=1e12, workers=1, dry_run_ms=30.0, max_group=4)
+    a = _req(s, 6, seed=1)           # occupies the single worker
+    b = _req(s, 7, seed=2)           # same operator as c: both queued while a runs
+    c = _req(s, 7, seed=2, incs=(XPOL, YPOL))
+    d = _req(s, 7, seed=2, lam=600.0)
+    infos = [s.result(i, with_P=False)[0] for i in (a, b, c, d)]
+    s.close()
+    assert infos[1]["group"] == 3 and infos[2]["group"] == 3 and infos[1]["t_start"] == infos[2]["t_start"]
+    assert infos[3]["group"] == 1
+
+
+def test_request_larger_than_the_budget_fails():
+    s = tdda.Server(hbm_budget_bytes=1e6, workers=1, dry_run_ms=1.0)
+    i = _req(s, 10)
+    info, _ = s.result(i, with_P=False)
+    s.close()
+    assert info["state"] == tdda.REQ_FAILED and info["status"] == tdda.ERR_OUT_OF_MEMORY
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [tdda.FP64, tdda.FP32_REFINE])
+def test_each_result_equals_the_request_alone(precision):
+    if tdda.device_count() < 1:
+        pytest.skip("no CUDA device")
+    rng = np.random.Generator(np.random.PCG64(42))
+    reqs = []
+    for k in range(10):
+        Nx, Ny, Nz = (int(v) for v in rng.integers(4, 12, 3))
+        lam = float(rng.uniform(400, 800))
+        em = [2.25, 4.0 + 0.1j, 6.25 + 0.05j][k % 3]
+        diel = np.repeat(rng.random(Nx * Ny * Nz), 3)
+        incs = [XPOL, YPOL][: 1 + k % 2]
+        reqs.append((Nx, Ny, Nz, lam, np.array([1.0, em]), diel, incs))
+    s = tdda.Server(hbm_budget_bytes=150e9, workers=3, precision=precision)
+    ids = []
+    for r in reqs:
+        Nx, Ny, Nz, lam, mat, diel, incs = r
+        ids.append(s.submit(Nx, Ny, Nz, lattice.bulk(Nx, Ny, Nz), 10.0, lam, mat, diel, incs))
+        time.sleep(float(rng.exponential(0.002)))
+    out = [s.result(i) for i in ids]
+    s.close()
+    for (Nx, Ny, Nz, lam, mat, diel, incs), (info, P) in zip(reqs, out):
+        assert info["state"] == tdda.REQ_DONE, info
+        core = tdda.AProductCore(Nx, Ny, Nz, lattice.bulk(Nx, Ny, Nz), 10.0, lam, mat, max_rhs=len(incs))
+        models = [tdda.DDAModel(core, i[0], i[2], i[1], diel) for i in incs]
+        tdda.solve_batch(models, precision, 10000, 1e-5)
+        for k, m in enumerate(models):
+            assert np.array_equal(P[k], m.get_P())

@@ -22,7 +22,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libtdda.so")
 
-UNITS = ["tdda_kernels.cu", "tdda_api.cu", "tdda_pass_generic.cu", "tdda_pass_z.cu", "tdda_pass_xy.cu"]
+UNITS = ["tdda_kernels.cu", "tdda_api.cu", "tdda_pass_generic.cu", "tdda_pass_z.cu", "tdda_pass_xy.cu",
+         "tdda_server.cu"]
 HEADERS = ["tdda_fft.cuh", "tdda_fft_ct.cuh", "tdda_internal.cuh", "tdda_device.cuh", "tdda_passes.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -63,7 +64,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
             if res.returncode:
                 raise RuntimeError("nvcc failed: " + " ".join(cmd))
     if force or jobs or _newer(LIB, objs):
-        cmd = [nv] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        cmd = [nv] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lpthread"]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode:
             sys.stderr.write(res.stdout + res.stderr)

@@ -221,6 +221,18 @@ void free_all(std::vector<void*>& list, cudaStream_t stream) {
     list.clear();
 }
 
+// raise the kernels' shared-memory limits once per device
+std::mutex g_cfg_mu;
+bool g_cfg_ready[64];
+tdda_status configure_once(int device) {
+    std::lock_guard<std::mutex> lk(g_cfg_mu);
+    if (device >= 0 && device < 64 && g_cfg_ready[device]) return TDDA_OK;
+    cudaError_t e = tdda::configure_kernels();
+    if (e != cudaSuccess) return cuda_fail(e, "configure_kernels");
+    if (device >= 0 && device < 64) g_cfg_ready[device] = true;
+    return TDDA_OK;
+}
+
 // keep freed pool memory cached for reuse instead of returning it to the
 // driver at every synchronisation (once per device)
 std::mutex g_pool_mu;
@@ -826,7 +838,7 @@ tdda_status tdda_core_create(const tdda_core_desc* desc, tdda_core** out) {
     p32.Ap = c->vout32;
     TDDA_CORE_CK(cudaMemcpyAsync(c->rhs64 + c->max_rhs, &p64, sizeof(p64), cudaMemcpyHostToDevice, c->stream));
     TDDA_CORE_CK(cudaMemcpyAsync(c->rhs32 + c->max_rhs, &p32, sizeof(p32), cudaMemcpyHostToDevice, c->stream));
-    TDDA_CORE_CK(tdda::configure_kernels());
+    TDDA_CORE_TRY(configure_once(c->device));
     // Green spectrum (AProductCore.cpp:53-229), on a temporary full grid
     double2* full6 = nullptr;
     TDDA_CORE_CK(cudaMallocAsync((void**)&full6, sizeof(double2) * 6 * (size_t)Mfull, c->stream));
@@ -1217,6 +1229,23 @@ tdda_status tdda_aproduct_noalloc(tdda_core* c, const double* b, double* y) {
                                           c->tw64[1], c->tw64[2], c->cellmap, slot.grid, c->stream));
     TDDA_CK(cudaStreamSynchronize(c->stream));
     return TDDA_OK;
+}
+
+double tdda_request_bytes(int Nx, int Ny, int Nz, int N, int nrhs, int precision) {
+    if (Nx < 1 || Ny < 1 || Nz < 1 || N < 1 || nrhs < 1) return 0.0;
+    const double Mx = smooth_size(2 * Nx - 1), My = smooth_size(2 * Ny - 1), Mz = smooth_size(2 * Nz - 1);
+    const double H = (Mx / 2 + 1) * (My / 2 + 1) * (Mz / 2 + 1);
+    const double n3 = 3.0 * N;
+    const double grid = 3.0 * Nx * My * Mz * nrhs;  // FFT work grid entries
+    double core = (double)Nx * Ny * Nz * 4 + n3 * 4    // cellmap, R
+                  + 6 * H * (16 + 8)                    // Green spectra
+                  + grid * (16 + 8)                     // FP64 and FP32 grids
+                  + n3 * 2 * (16 + 8)                   // product staging
+                  + 6 * Mx * My * Mz * 16               // full Green grid while the core is built
+                  + 1e6;                                // reduction partials, states, twiddles
+    double model = n3 * (12 * 16 + 8);                  // FP64 vectors and densities
+    if (precision == TDDA_FP32_REFINE) model += n3 * 10 * 8;
+    return core + nrhs * model;
 }
 
 }  // extern "C"

@@ -43,8 +43,10 @@ EXPORTS = [
     "tdda_model_initialize_P", "tdda_model_aproduct_with_alb", "tdda_model_bicgstab", "tdda_model_solve_mixed",
     "tdda_model_update_E_in_structure", "tdda_model_get", "tdda_model_iterations", "tdda_solve_batch",
     "tdda_fft3d", "tdda_core_stream", "tdda_kernel_launches", "tdda_profile_aproduct",
-    "tdda_aproduct_noalloc",
+    "tdda_aproduct_noalloc", "tdda_server_create", "tdda_server_submit", "tdda_server_result",
+    "tdda_server_stats", "tdda_server_clock", "tdda_server_destroy", "tdda_request_bytes",
 ]
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 
 
 class TddaError(RuntimeError):
@@ -65,6 +67,30 @@ class SolveInfo(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int), ("iterations", ctypes.c_int), ("error", ctypes.c_double),
                 ("true_residual", ctypes.c_double), ("outer_iterations", ctypes.c_int),
                 ("inner_iterations", ctypes.c_int)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ServerDesc(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_double), ("workers", ctypes.c_int),
+                ("precision", ctypes.c_int), ("max_it", ctypes.c_int), ("tol", ctypes.c_double),
+                ("max_group", ctypes.c_int), ("dry_run", ctypes.c_int), ("dry_run_ms", ctypes.c_double)]
+
+
+class RequestDesc(ctypes.Structure):
+    _fields_ = [("Nx", ctypes.c_int), ("Ny", ctypes.c_int), ("Nz", ctypes.c_int), ("N", ctypes.c_int),
+                ("R", ctypes.POINTER(ctypes.c_int)), ("d", ctypes.c_double), ("lam", ctypes.c_double),
+                ("nback", ctypes.c_double), ("material", ctypes.POINTER(ctypes.c_double)), ("nmat", ctypes.c_int),
+                ("diel_old", ctypes.POINTER(ctypes.c_double)), ("nrhs", ctypes.c_int),
+                ("nK", ctypes.POINTER(ctypes.c_double)), ("nE0", ctypes.POINTER(ctypes.c_double)),
+                ("E0", ctypes.POINTER(ctypes.c_double))]
+
+
+class RequestInfo(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_int), ("status", ctypes.c_int), ("t_submit", ctypes.c_double),
+                ("t_start", ctypes.c_double), ("t_done", ctypes.c_double), ("iterations", ctypes.c_int),
+                ("error", ctypes.c_double), ("bytes", ctypes.c_double), ("group", ctypes.c_int)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -111,6 +137,13 @@ def load() -> ctypes.CDLL:
         "tdda_kernel_launches": (ctypes.c_ulonglong, []),
         "tdda_profile_aproduct": (i, [vp, i, i, i, dp]),
         "tdda_aproduct_noalloc": (i, [vp, vp, vp]),
+        "tdda_server_create": (i, [ctypes.POINTER(ServerDesc), ctypes.POINTER(vp)]),
+        "tdda_server_submit": (i, [vp, ctypes.POINTER(RequestDesc), ctypes.POINTER(ctypes.c_ulonglong)]),
+        "tdda_server_result": (i, [vp, ctypes.c_ulonglong, i, ctypes.POINTER(RequestInfo), vp]),
+        "tdda_server_stats": (i, [vp, ip, ip, dp, dp]),
+        "tdda_server_clock": (d, [vp]),
+        "tdda_server_destroy": (i, [vp]),
+        "tdda_request_bytes": (d, [i, i, i, i, i, i]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -361,3 +394,66 @@ def solve_workload(w, precision: int = FP64, inc=None, tol=None, max_it=None) ->
     model.close()
     core.close()
     return out
+
+
+class Server:
+    """Continuous-batching solve loop (tdda_server_*): submit structures, collect results."""
+
+    def __init__(self, hbm_budget_bytes=150e9, workers=4, precision=FP32_REFINE, max_it=10000, tol=1e-5,
+                 max_group=8, device=0, dry_run_ms=None):
+        d = ServerDesc(int(device), float(hbm_budget_bytes), int(workers), int(precision), int(max_it), float(tol),
+                       int(max_group), int(dry_run_ms is not None), float(dry_run_ms or 0.0))
+        h = ctypes.c_void_p()
+        _check(load().tdda_server_create(ctypes.byref(d), ctypes.byref(h)), "tdda_server_create")
+        self.h = h
+        self._keep = {}
+        self._n = {}
+
+    def submit(self, Nx, Ny, Nz, R, d, lam, material, diel_old, incidences, nback=1.0) -> int:
+        """incidences: list of (nK, nE0, E0)."""
+        R = np.ascontiguousarray(np.asarray(R, dtype=np.int32).reshape(-1))
+        mat = _c128(material)
+        diel = np.ascontiguousarray(diel_old, np.float64)
+        nK = np.ascontiguousarray(np.array([np.asarray(i[0], np.float64) for i in incidences]).reshape(-1))
+        nE = np.ascontiguousarray(np.array([np.asarray(i[1], np.float64) for i in incidences]).reshape(-1))
+        E0 = np.ascontiguousarray(np.array([float(i[2]) for i in incidences]))
+        req = RequestDesc(int(Nx), int(Ny), int(Nz), R.size // 3, R.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                          float(d), float(lam), float(nback), _dptr(mat.view(np.float64)), mat.size, _dptr(diel),
+                          len(incidences), _dptr(nK), _dptr(nE), _dptr(E0))
+        rid = ctypes.c_ulonglong()
+        _check(load().tdda_server_submit(self.h, ctypes.byref(req), ctypes.byref(rid)), "tdda_server_submit")
+        self._n[rid.value] = (R.size // 3, len(incidences))
+        return rid.value
+
+    def result(self, rid: int, wait: bool = True, with_P: bool = True):
+        info = RequestInfo()
+        N, nrhs = self._n[rid]
+        P = np.zeros(3 * N * nrhs, np.complex128) if with_P else None
+        _check(load().tdda_server_result(self.h, ctypes.c_ulonglong(rid), int(wait), ctypes.byref(info),
+                                         _ptr(P) if with_P else None), "tdda_server_result")
+        return info.as_dict(), (P.reshape(nrhs, 3 * N) if with_P else None)
+
+    def stats(self) -> dict:
+        q, r = ctypes.c_int(), ctypes.c_int()
+        b, pk = ctypes.c_double(), ctypes.c_double()
+        _check(load().tdda_server_stats(self.h, ctypes.byref(q), ctypes.byref(r), ctypes.byref(b), ctypes.byref(pk)),
+               "tdda_server_stats")
+        return {"queued": q.value, "running": r.value, "bytes": b.value, "peak_bytes": pk.value}
+
+    def clock(self) -> float:
+        return load().tdda_server_clock(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().tdda_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def request_bytes(Nx, Ny, Nz, N, nrhs, precision=FP32_REFINE) -> float:
+    return float(load().tdda_request_bytes(Nx, Ny, Nz, N, nrhs, precision))

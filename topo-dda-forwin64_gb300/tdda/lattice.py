@@ -172,3 +172,46 @@ def config(idx: int, seed: int = 1234) -> Workload:
     return Workload(name=f"cfg{idx}", Nx=Nx, Ny=Ny, Nz=Nz, d=d, lam=lam,
                     material=np.array([1.0 + 0j, em]), rho=np.clip(rho, 0.0, 1.0),
                     R=bulk(Nx, Ny, Nz), incidences=inc)
+
+
+@dataclass
+class ServeRequest:
+    t_arrival: float
+    Nx: int
+    Ny: int
+    Nz: int
+    lam: float
+    eps_m: complex
+    seed: int
+    incidences: list
+
+    @property
+    def N(self) -> int:
+        return self.Nx * self.Ny * self.Nz
+
+    def diel_old(self) -> np.ndarray:
+        rng = np.random.Generator(np.random.PCG64(self.seed))
+        return np.repeat(rng.random(self.N), 3)
+
+
+def serving_stream(n: int = 512, rate: float = 200.0, seed: int = 5, lo: int = 16, hi: int = 128,
+                   zhi: int = 32) -> list:
+    """The serving workload: n solve requests with Poisson arrivals (mean `rate` per s),
+    lattice dims log-uniform per axis in [lo, hi] (z capped at zhi), d = 10 nm,
+    wavelength U[400, 800] nm, eps_m in {2.25, 4.0+0.1i, 6.25+0.05i}, rho ~ U[0, 1],
+    1-4 right-hand sides drawn from x/y polarisation x polar angles 0/15/30/45 deg."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    pool = config(3).incidences  # the 8 incidences of the batched workload
+    t = 0.0
+    out = []
+    for k in range(n):
+        t += float(rng.exponential(1.0 / rate))
+        dims = [int(round(math.exp(rng.uniform(math.log(lo), math.log(hi))))) for _ in range(3)]
+        dims[2] = min(dims[2], zhi)
+        lam = float(rng.uniform(400.0, 800.0))
+        em = [2.25 + 0j, 4.0 + 0.1j, 6.25 + 0.05j][int(rng.integers(0, 3))]
+        nrhs = int(rng.integers(1, 5))
+        pick = rng.choice(len(pool), size=nrhs, replace=False)
+        incs = [(pool[i].nK, pool[i].nE0, pool[i].E0) for i in pick]
+        out.append(ServeRequest(t, dims[0], dims[1], dims[2], lam, em, int(rng.integers(0, 2**31)), incs))
+    return out
