@@ -1,0 +1,208 @@
+"""Topology-optimisation loop around the batched solver (the caller of the hot path).
+
+The reference's EvoDDAModel::EvoOptimization (EvoDDAModel.cpp:393-765) runs, per
+iteration, a forward solve, a finite-difference objective derivative, an adjoint
+solve with the same matrix (A is complex symmetric), gradient assembly, an
+optimiser step and a density update.  This loop keeps that structure for a point
+objective f = |E(r_obs)|^2 (ObjPointEDDAModel, ObjDDAModel.cpp:20-96, evaluates
+E(r_obs) = E_inc(r_obs) - sum_j A(r_obs - r_j) P_j) and makes two changes:
+
+* the adjoint source is exact instead of finite differences.  With
+  E_obs = E_inc(r_obs) + sum_k b_k . P and b_k[j] = -A(r_obs - r_j) e_k,
+  df/dP = sum_k conj(E_obs,k) b_k, so the adjoint solution is
+  lambda = sum_k conj(E_obs,k) lambda_k with A lambda_k = b_k.  The three
+  lambda_k and the forward P are solved together, four right-hand sides in one
+  batched solve per iteration (tdda_solve_batch);
+* dal/drho is analytic: 1/alpha_LDR(eps) = 1/a1 + T/d^3 (tools.cpp:617-630),
+  so dal/deps = -3/(c (eps-1)^2) + (b2 + b3 S)(K d)^2/d^3.
+
+Design parameters theta live on one xy quadrant; rho = filter(mirror4(theta)),
+extruded along z (the reference's 2-D extruded design with 4-fold symmetry,
+SpacePara.cpp:8-48, and its linear cone filter).  df/dtheta follows by the
+transposed chain.  The step is gradient ascent: the gradient is scaled so that
+its mean magnitude is at least 0.1 (EvoDDAModel.cpp:734-738) and multiplied by
+epsilon = 0.1, so the mean step is 0.01; theta is clipped to [0, 1].
+
+The solves run on the GPU through libtdda; the O(N) glue (objective, lambda
+combination, gradient) is host numpy.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import FP32_REFINE, AProductCore, DDAModel, lattice, solve_batch
+
+B1, B2, B3 = -1.891531, 0.1648469, -1.7700004  # LDR coefficients (tools.cpp:618-620)
+
+
+def ldr_tensor(K: float, x, y, z) -> np.ndarray:
+    """LDR interaction tensor (AProductCore.cpp:588-623) at offsets (x, y, z) in nm.
+    Returns (6, n) complex: xx, xy, xz, yy, yz, zz; zero at r = 0."""
+    x, y, z = (np.asarray(v, np.float64) for v in (x, y, z))
+    xs, ys, zs = x * x, y * y, z * z
+    rn = np.sqrt(xs + ys + zs)
+    out = np.zeros((6,) + rn.shape, np.complex128)
+    ok = rn != 0
+    r = rn[ok]
+    rsq, rcu = r * r, r * r * r
+    c1 = np.exp(1j * K * r) / rcu
+    c2 = (1.0 - 1j * K * r) / rsq
+    c3 = K * K - 3.0 * c2
+    out[0, ok] = c1 * (c2 * (rsq - 3 * xs[ok]) - K * K * (ys[ok] + zs[ok]))
+    out[1, ok] = c1 * (x[ok] * y[ok] * c3)
+    out[2, ok] = c1 * (z[ok] * x[ok] * c3)
+    out[3, ok] = c1 * (c2 * (rsq - 3 * ys[ok]) - K * K * (zs[ok] + xs[ok]))
+    out[4, ok] = c1 * (y[ok] * z[ok] * c3)
+    out[5, ok] = c1 * (c2 * (rsq - 3 * zs[ok]) - K * K * (xs[ok] + ys[ok]))
+    return out
+
+
+def point_sources(R: np.ndarray, d: float, K: float, r_obs) -> np.ndarray:
+    """b_k[j] = -A(r_obs - d R_j) e_k for k = x, y, z: (3, 3N) complex."""
+    R = np.asarray(R).reshape(-1, 3)
+    t = ldr_tensor(K, r_obs[0] - d * R[:, 0], r_obs[1] - d * R[:, 1], r_obs[2] - d * R[:, 2])
+    # symmetric tensor: column k = row k
+    rows = [(0, 1, 2), (1, 3, 4), (2, 4, 5)]
+    b = np.zeros((3, R.shape[0], 3), np.complex128)
+    for k, (a0, a1, a2) in enumerate(rows):
+        b[k, :, 0], b[k, :, 1], b[k, :, 2] = -t[a0], -t[a1], -t[a2]
+    return b.reshape(3, -1)
+
+
+def dal_deps(eps: np.ndarray, K: float, d: float, S: float) -> np.ndarray:
+    c = 3 * d ** 3 / (4 * math.pi)
+    return -3.0 / (c * (eps - 1.0) ** 2) + (B2 + B3 * S) * (K * d) ** 2 / d ** 3
+
+
+class DesignMap:
+    """theta (quadrant, hx x hy) -> rho (Nx x Ny, extruded along z) and its transpose."""
+
+    def __init__(self, Nx: int, Ny: int, r: float = 2.0):
+        self.Nx, self.Ny, self.r = Nx, Ny, r
+        self.hx, self.hy = (Nx + 1) // 2, (Ny + 1) // 2
+        self.ix = np.minimum(np.arange(Nx), Nx - 1 - np.arange(Nx))
+        self.iy = np.minimum(np.arange(Ny), Ny - 1 - np.arange(Ny))
+        ri = int(math.ceil(r))
+        self.taps = [(dx, dy, r - math.sqrt(dx * dx + dy * dy)) for dx in range(-ri, ri + 1)
+                     for dy in range(-ri, ri + 1) if dx * dx + dy * dy <= r * r - 0.01]
+        wsum = np.zeros((Nx, Ny))
+        for dx, dy, w in self.taps:
+            wsum[self._dst(dx, Nx), self._dst(dy, Ny)] += w
+        self.wsum = wsum
+
+    @staticmethod
+    def _src(dd, n):
+        return slice(max(0, dd), n + min(0, dd))
+
+    @staticmethod
+    def _dst(dd, n):
+        return slice(max(0, -dd), n + min(0, -dd))
+
+    def mirror(self, theta):
+        return theta[self.ix][:, self.iy]
+
+    def mirror_t(self, g):
+        out = np.zeros((self.hx, self.hy))
+        np.add.at(out, (self.ix[:, None], self.iy[None, :]), g)
+        return out
+
+    def filter(self, a):
+        acc = np.zeros_like(a)
+        for dx, dy, w in self.taps:
+            acc[self._dst(dx, self.Nx), self._dst(dy, self.Ny)] += w * a[self._src(dx, self.Nx), self._src(dy, self.Ny)]
+        return acc / self.wsum
+
+    def filter_t(self, g):
+        gw = g / self.wsum
+        out = np.zeros_like(g)
+        for dx, dy, w in self.taps:
+            out[self._src(dx, self.Nx), self._src(dy, self.Ny)] += w * gw[self._dst(dx, self.Nx), self._dst(dy, self.Ny)]
+        return out
+
+    def rho(self, theta):
+        return self.filter(self.mirror(theta))
+
+    def grad_theta(self, g_xy):
+        return self.mirror_t(self.filter_t(g_xy))
+
+
+@dataclass
+class StepResult:
+    objective: float
+    iterations: list
+    grad_theta: np.ndarray
+
+
+class TopoLoop:
+    """Point-|E|^2 topology optimisation with forward + 3 adjoint solves batched per step."""
+
+    def __init__(self, Nx, Ny, Nz, d, lam, material, theta0, r_obs, precision=FP32_REFINE, tol=1e-5,
+                 max_it=10000, nK=(0.0, 0.0, 1.0), nE0=(1.0, 0.0, 0.0), E0=1.0, filter_r=2.0, epsilon=0.1):
+        self.Nx, self.Ny, self.Nz, self.d = Nx, Ny, Nz, d
+        self.R = lattice.bulk(Nx, Ny, Nz)
+        self.map = DesignMap(Nx, Ny, filter_r)
+        self.theta = np.array(theta0, np.float64).reshape(self.map.hx, self.map.hy)
+        self.precision, self.tol, self.max_it, self.epsilon = precision, tol, max_it, epsilon
+        self.nK, self.nE0, self.E0 = np.array(nK, float), np.array(nE0, float), float(E0)
+        self.r_obs = np.array(r_obs, float)
+        self.core = AProductCore(Nx, Ny, Nz, self.R, d, lam, material, max_rhs=4)
+        self.K = self.core.K
+        self.mat = self.core.get_material()  # normalised (vacuum -> 1.01)
+        self.S = float(np.sum((self.nE0 * self.nK) ** 2))
+        diel = self._diel()
+        self.fwd = DDAModel(self.core, self.nK, self.E0, self.nE0, diel)
+        self.b = point_sources(self.R, d, self.K, self.r_obs)
+        self.adj = []
+        for k in range(3):
+            m = DDAModel(self.core, self.nK, self.E0, self.nE0, diel)
+            m.change_E(self.b[k])
+            self.adj.append(m)
+        self.Einc_obs = self.E0 * self.nE0 * np.exp(1j * self.K * float(self.nK @ self.r_obs))
+        self.zero = np.zeros(self.R.size, np.complex128)  # 3N
+
+    def _rho(self):
+        return np.clip(self.map.rho(self.theta), 0.0, 1.0)
+
+    def _diel(self):
+        rho_xy = self._rho()
+        rho = np.repeat(rho_xy[:, :, None], self.Nz, axis=2).ravel()
+        return np.repeat(rho, 3)
+
+    def objective_parts(self, P):
+        E_obs = self.Einc_obs + self.b @ P
+        return E_obs, float(np.sum(np.abs(E_obs) ** 2))
+
+    def evaluate(self):
+        """Solve forward + adjoints at the current theta; return f and df/dtheta."""
+        diel = self._diel()
+        models = [self.fwd] + self.adj
+        for m in models:
+            m.UpdateAlpha(diel)
+            m.InitializeP(self.zero)
+        infos = solve_batch(models, self.precision, self.max_it, self.tol)
+        P = self.fwd.get_P()
+        E_obs, f = self.objective_parts(P)
+        lam = sum(np.conj(E_obs[k]) * self.adj[k].get_P() for k in range(3))
+        eps = self.mat[0] + diel * (self.mat[1] - self.mat[0])
+        dal = dal_deps(eps, self.K, self.d, self.S) * (self.mat[1] - self.mat[0])
+        g_dip = -2.0 * np.real((lam * dal * P).reshape(-1, 3).sum(axis=1))
+        g_xy = g_dip.reshape(self.Nx, self.Ny, self.Nz).sum(axis=2)
+        # rho is clipped to [0, 1]; the filter keeps it inside, so the clip is inactive
+        return StepResult(f, [i["iterations"] for i in infos], self.map.grad_theta(g_xy))
+
+    def step(self) -> StepResult:
+        r = self.evaluate()
+        g = r.grad_theta.copy()
+        mean = float(np.mean(np.abs(g)))
+        if 0 < mean < 0.1:  # EvoDDAModel.cpp:734-736
+            g /= mean / 0.1
+        self.theta = np.clip(self.theta + self.epsilon * g, 0.0, 1.0)
+        return r
+
+    def close(self):
+        for m in [self.fwd] + self.adj:
+            m.close()
+        self.core.close()
