@@ -85,8 +85,9 @@ def test_aproduct_equals_direct_sum_on_odd_boxes():
 
 
 def test_aproduct_config_shapes_against_oracle():
+    """Every compiled FFT length (x/y 40, 128, 160, 192; z 20, 32, 40, 48) against the oracle."""
     rng = np.random.Generator(np.random.PCG64(3))
-    for idx in (1, 2):
+    for idx in (1, 2, 3, 4):
         w = tdda.lattice.config(idx)
         c = tdda.AProductCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material)
         oc = O.OracleCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material, grid=c.grid, pruned=True)

@@ -191,6 +191,77 @@ template <int SIGN, typename T> struct Bfly<3, SIGN, T> : BflyOdd<3, SIGN, T> {}
 template <int SIGN, typename T> struct Bfly<5, SIGN, T> : BflyOdd<5, SIGN, T> {};
 template <int SIGN, typename T> struct Bfly<7, SIGN, T> : BflyOdd<7, SIGN, T> {};
 
+// ------------------------------------------------------ composite butterflies
+// DFT of length R = R1 R2 in registers: with n = R2 n1 + n2 and k = k1 + R1 k2,
+//   X[k] = sum_n2 W_R^(n2 k1) W_R2^(n2 k2) sum_n1 x[R2 n1 + n2] W_R1^(n1 k1):
+// R2 DFTs of length R1, twiddles W_R^(n2 k1), R1 DFTs of length R2.  The
+// constants cos / sin(2 pi m / R) are tabulated below.
+template <int R> struct RootTab;
+template <> struct RootTab<10> {
+    static __device__ __forceinline__ double c(int m) {
+        constexpr double t[10] = {1, 0.80901699437494745, 0.30901699437494745, -0.30901699437494734, -0.80901699437494734, -1, -0.80901699437494756, -0.30901699437494756, 0.30901699437494723, 0.80901699437494734};
+        return t[m % 10];
+    }
+    static __device__ __forceinline__ double s(int m) {
+        constexpr double t[10] = {0, 0.58778525229247314, 0.95105651629515353, 0.95105651629515364, 0.58778525229247325, 1.2246467991473532e-16, -0.58778525229247303, -0.95105651629515353, -0.95105651629515364, -0.58778525229247336};
+        return t[m % 10];
+    }
+};
+template <> struct RootTab<12> {
+    static __device__ __forceinline__ double c(int m) {
+        constexpr double t[12] = {1, 0.86602540378443871, 0.50000000000000011, 6.123233995736766e-17, -0.49999999999999978, -0.86602540378443871, -1, -0.86602540378443882, -0.50000000000000044, -1.8369701987210297e-16, 0.50000000000000011, 0.86602540378443837};
+        return t[m % 12];
+    }
+    static __device__ __forceinline__ double s(int m) {
+        constexpr double t[12] = {0, 0.49999999999999994, 0.8660254037844386, 1, 0.86602540378443871, 0.49999999999999994, 1.2246467991473532e-16, -0.49999999999999972, -0.86602540378443837, -1, -0.8660254037844386, -0.50000000000000044};
+        return t[m % 12];
+    }
+};
+template <> struct RootTab<16> {
+    static __device__ __forceinline__ double c(int m) {
+        constexpr double t[16] = {1, 0.92387953251128674, 0.70710678118654757, 0.38268343236508984, 6.123233995736766e-17, -0.38268343236508973, -0.70710678118654746, -0.92387953251128674, -1, -0.92387953251128685, -0.70710678118654768, -0.38268343236509034, -1.8369701987210297e-16, 0.38268343236509, 0.70710678118654735, 0.92387953251128652};
+        return t[m % 16];
+    }
+    static __device__ __forceinline__ double s(int m) {
+        constexpr double t[16] = {0, 0.38268343236508978, 0.70710678118654746, 0.92387953251128674, 1, 0.92387953251128674, 0.70710678118654757, 0.38268343236508989, 1.2246467991473532e-16, -0.38268343236508967, -0.70710678118654746, -0.92387953251128652, -1, -0.92387953251128663, -0.70710678118654768, -0.38268343236509039};
+        return t[m % 16];
+    }
+};
+
+template <int R1, int R2, int SIGN, typename T> struct BflyComp {
+    static __device__ __forceinline__ void run(cx<T>* v) {
+        constexpr int R = R1 * R2;
+        cx<T> y[R2][R1];
+#pragma unroll
+        for (int n2 = 0; n2 < R2; n2++) {
+            cx<T> a[R1];
+#pragma unroll
+            for (int n1 = 0; n1 < R1; n1++) a[n1] = v[R2 * n1 + n2];
+            Bfly<R1, SIGN, T>::run(a);
+#pragma unroll
+            for (int k1 = 0; k1 < R1; k1++) {
+                if (n2 > 0 && k1 > 0) {
+                    const T c = T(RootTab<R>::c(n2 * k1)), s = T(SIGN) * T(RootTab<R>::s(n2 * k1));
+                    a[k1] = mk<T>(a[k1].x * c - a[k1].y * s, a[k1].x * s + a[k1].y * c);
+                }
+                y[n2][k1] = a[k1];
+            }
+        }
+#pragma unroll
+        for (int k1 = 0; k1 < R1; k1++) {
+            cx<T> b[R2];
+#pragma unroll
+            for (int n2 = 0; n2 < R2; n2++) b[n2] = y[n2][k1];
+            Bfly<R2, SIGN, T>::run(b);
+#pragma unroll
+            for (int k2 = 0; k2 < R2; k2++) v[k1 + R1 * k2] = b[k2];
+        }
+    }
+};
+template <int SIGN, typename T> struct Bfly<16, SIGN, T> : BflyComp<4, 4, SIGN, T> {};
+template <int SIGN, typename T> struct Bfly<12, SIGN, T> : BflyComp<4, 3, SIGN, T> {};
+template <int SIGN, typename T> struct Bfly<10, SIGN, T> : BflyComp<2, 5, SIGN, T> {};
+
 // ----------------------------------------------------------------- one stage
 // Out-of-place (ping-pong) stage: reads x, writes y, then a barrier.  Each
 // thread loops over butterflies, holding one radix-R butterfly in registers.

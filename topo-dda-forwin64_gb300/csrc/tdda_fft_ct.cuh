@@ -13,9 +13,16 @@
 
 namespace tdda {
 
-// radix plan, identical to the host's make_plan(): 8s and 4s (no lone 2 unless
-// the power of two is 2), then 3, 5, 7
-__host__ __device__ constexpr int ct_nrad(int M, int which) {
+// radix plan: the host's make_plan() (8s and 4s, no lone 2 unless the power
+// of two is 2, then 3, 5, 7).  With big set (the FP32 passes, latency-bound)
+// some lengths take a two-stage plan of larger in-register radices, which
+// needs fewer shared-memory passes; the FP64 passes, bound by the FP64 pipe,
+// keep the plan with the fewest multiplications.
+__host__ __device__ constexpr int ct_nrad(int M, int which, bool big = false) {
+    if (big && M == 128) return which < 0 ? 2 : (which == 0 ? 16 : 8);
+    if (big && M == 192) return which < 0 ? 2 : (which == 0 ? 16 : 12);
+    if (big && M == 160) return which < 0 ? 2 : (which == 0 ? 16 : 10);
+    if (big && M == 48) return which < 0 ? 2 : (which == 0 ? 16 : 3);
     int m = M, a = 0;
     while (m % 2 == 0) { m /= 2; a++; }
     int r[16] = {};
@@ -28,8 +35,8 @@ __host__ __device__ constexpr int ct_nrad(int M, int which) {
     while (m % 7 == 0) { r[n++] = 7; m /= 7; }
     return which < 0 ? n : r[which];
 }
-__host__ __device__ constexpr int ct_nstages(int M) { return ct_nrad(M, -1); }
-__host__ __device__ constexpr int ct_radix(int M, int st) { return ct_nrad(M, st); }
+__host__ __device__ constexpr int ct_nstages(int M, bool big) { return ct_nrad(M, -1, big); }
+__host__ __device__ constexpr int ct_radix(int M, int st, bool big) { return ct_nrad(M, st, big); }
 
 template <int R, int SIGN, typename T, int M, int NS, int L, int LS, int MS, int NT>
 __device__ __forceinline__ void ct_stage(const cx<T>* __restrict__ x, cx<T>* __restrict__ y, const cx<T>* tw,
@@ -71,12 +78,13 @@ __device__ __forceinline__ void ct_stage(const cx<T>* __restrict__ x, cx<T>* __r
 
 template <int SIGN, typename T, int M, int L, int LS, int MS, int NT, int ST = 0, int NS = 1>
 __device__ __forceinline__ cx<T>* ct_fft(cx<T>* a, cx<T>* b, const cx<T>* tw, int nvalid, int nout) {
-    if constexpr (ST == ct_nstages(M)) {
+    constexpr bool big = sizeof(T) == 4;
+    if constexpr (ST == ct_nstages(M, big)) {
         return a;
     } else {
-        constexpr int R = ct_radix(M, ST);
+        constexpr int R = ct_radix(M, ST, big);
         ct_stage<R, SIGN, T, M, NS, L, LS, MS, NT>(a, b, tw, ST == 0 ? nvalid : M,
-                                                   ST == ct_nstages(M) - 1 ? nout : M);
+                                                   ST == ct_nstages(M, big) - 1 ? nout : M);
         return ct_fft<SIGN, T, M, L, LS, MS, NT, ST + 1, NS * R>(b, a, tw, nvalid, nout);
     }
 }
