@@ -144,7 +144,7 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def pass_bytes(grid, Nx, Ny, Nz, N, s):
+def pass_bytes(grid, Nx, Ny, Nz, N, s, fused=False):
     """Algorithmic bytes of the five A-product passes for one right-hand side.
 
     Pass model of the survey's canonical count, on the grid (Mx, My, Mz) actually used:
@@ -152,15 +152,24 @@ def pass_bytes(grid, Nx, Ny, Nz, N, s):
     y-forward pass reads those and writes 3 Nx My Mz, the x pass reads and writes
     3 Nx My Mz and reads the six Green components on the full grid (6 Mx My Mz,
     the canonical count; the folded layout actually stores 6 Hx Hy Hz), the inverse
-    passes mirror the forward ones.  s = bytes per complex entry."""
+    passes mirror the forward ones.  s = bytes per complex entry.  With fused z+y
+    passes (3 kernels per product) entries 0 and 3 are the fused kernels."""
     Mx, My, Mz = grid
     zf = 3 * N + 3 * Nx * Ny * Mz
     yf = 3 * Nx * Ny * Mz + 3 * Nx * My * Mz
     xp = 2 * 3 * Nx * My * Mz + 6 * Mx * My * Mz
+    if fused:  # k_zyfwd / k_yzinv: the 3N vector in, the 3 Nx My Mz plane out (and back)
+        zy = 3 * N + 3 * Nx * My * Mz
+        return [zy * s, 0, xp * s, zy * s, 0]
     return [zf * s, yf * s, xp * s, yf * s, zf * s]
 
 
 PASS_NAMES = ["k_zfwd", "k_ypass(fwd)", "k_xpass", "k_ypass(inv)", "k_zinv"]
+FUSED_NAMES = ["k_zyfwd", "-", "k_xpass", "k_yzinv", "-"]
+
+
+def pass_names(fused):
+    return FUSED_NAMES if fused else PASS_NAMES
 
 
 # ------------------------------------------------------------------ CPU baseline
@@ -273,7 +282,7 @@ def time_batch(tdda, torch, w, incs, precision, steps, dev, flush_l2):
     prof = core.profile_aproduct(precision, len(incs), 5)
     out = {"rhs": len(incs), "value": len(incs) * steps / (sum(ms) / 1000.0), "unit": UNIT, "steps": steps,
            "ms_per_batch": sum(ms) / steps, "iterations": [i["iterations"] for i in infos],
-           "pass_ms": prof, "grid": list(core.grid)}
+           "pass_ms": prof, "kernels": pass_names(core.pass_count(precision) == 3), "grid": list(core.grid)}
     for m in models:
         m.close()
     core.close()
@@ -430,7 +439,9 @@ def run_ours(args, dist: Dist):
     shares = [(n32 * t, "fp32", k) for k, t in enumerate(prof32)] + [(n64 * t, "fp64", k) for k, t in enumerate(prof64)]
     _, prec, k = max(shares)
     s = 8 if prec == "fp32" else 16
-    bytes_k = pass_bytes(core.grid, w.Nx, w.Ny, w.Nz, w.N, s)[k]
+    fused = core.pass_count(tdda.FP32_REFINE if prec == "fp32" else tdda.FP64) == 3
+    names = pass_names(fused)
+    bytes_k = pass_bytes(core.grid, w.Nx, w.Ny, w.Nz, w.N, s, fused)[k]
     t_k = (prof32 if prec == "fp32" else prof64)[k]
     peaks = measured_peaks()
     achieved = bytes_k / (t_k * 1e-3) / 1e9
@@ -438,7 +449,7 @@ def run_ours(args, dist: Dist):
     tf = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     if os.path.exists(tf):
         with open(tf) as f:
-            traffic = json.load(f).get(f"{PASS_NAMES[k]}:{prec}")
+            traffic = json.load(f).get(f"{names[k]}:{prec}")
 
     # batched right-hand sides: the 96x96x24 lattice with its 8 incidences in one solve
     batched = None
@@ -493,11 +504,13 @@ def run_ours(args, dist: Dist):
                      "latency_ms": {"p50": float(np.percentile(ms64, 50)), "p99": float(np.percentile(ms64, 99))},
                      "iterations": r64[-1][1]["iterations"], "speedup_fp32_refine": value / fp64_value},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "roofline": {"kernel": f"{PASS_NAMES[k]} ({prec})", "bound": "hbm", "achieved": achieved,
+            "roofline": {"kernel": f"{names[k]} ({prec})", "bound": "hbm", "achieved": achieved,
                          "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
                          "peak_source": peaks["source"], "algorithmic_bytes": bytes_k, "avg_ms": t_k,
                          "traffic": traffic,
-                         "pass_ms_fp32": prof32, "pass_ms_fp64": prof64},
+                         "pass_ms_fp32": prof32, "pass_ms_fp64": prof64,
+                         "kernels_fp32": pass_names(core.pass_count(tdda.FP32_REFINE) == 3),
+                         "kernels_fp64": pass_names(core.pass_count(tdda.FP64) == 3)},
             "batched": batched,
             "serving": serving,
             "topo": topo_line,

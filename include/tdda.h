@@ -241,6 +241,12 @@ unsigned long long tdda_kernel_launches(void);
  * over `reps` plain products of nrhs right-hand sides, timed with CUDA events
  * on the core's stream. */
 tdda_status tdda_profile_aproduct(tdda_core* core, int precision, int nrhs, int reps, double* ms5);
+/* Kernels of one A-product at this precision: 5 (the passes above) or 3, when
+ * the z and y passes are fused (FP32 on the compiled plane sizes).  With 3,
+ * tdda_profile_aproduct reports the fused forward kernel in ms5[0], the fused
+ * inverse in ms5[3], and ms5[1], ms5[4] hold only the gap between two events.
+ * -1 for an invalid argument. */
+int tdda_core_pass_count(const tdda_core* core, int precision);
 
 #ifdef __cplusplus
 }

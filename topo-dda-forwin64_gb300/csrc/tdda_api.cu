@@ -345,16 +345,32 @@ template <> struct Prec<float> {
     static cudaGraphExec_t& graph(tdda_core* c, int n) { return c->g32.iter[n]; }
 };
 
+// kernels of one A-product at precision T: 3 with the fused z+y passes, else 5
+template <typename T> int product_kernels(const tdda_core* c) { return tdda::zy_fused(c->g, sizeof(T) == 4) ? 3 : 5; }
+
 template <typename T>
 cudaError_t aprod(tdda_core* c, int src, int snk, int n, const RhsVecs<T>* rhs, cudaEvent_t* ev = nullptr) {
-    count_launches(5);
+    count_launches(product_kernels<T>(c));
     return tdda::launch_aproduct<T>(c->g, src, snk, n, rhs, Prec<T>::green(c), Prec<T>::tw(c, 0), Prec<T>::tw(c, 1),
                                     Prec<T>::tw(c, 2), c->cellmap, Prec<T>::grid(c), c->stream, ev);
 }
 
+// One BiCGSTAB step.  FP64 (the drop-in): the reference's recurrence with its
+// three reductions, the update of P and r in k_update.  FP32 (the inner solve
+// of the mixed form): the update is deferred into the next step's gather and
+// r0.r, |r|^2 follow from sums taken with At (SNK_AT_DEF), so a step is two
+// products and no separate update kernel.
+template <typename T> constexpr bool kDeferred = sizeof(T) == 4;
+
+template <typename T> int step_kernels(const tdda_core* c) { return 2 * product_kernels<T>(c) + (kDeferred<T> ? 0 : 1); }
+
 template <typename T> cudaError_t enqueue_iteration(tdda_core* c, int n) {
     const RhsVecs<T>* rhs = Prec<T>::rhs(c);
     cudaError_t e;
+    if (kDeferred<T>) {
+        if ((e = aprod<T>(c, tdda::SRC_PUPD_DEF, tdda::SNK_AP, n, rhs))) return e;  // update, p, Ap, alpha
+        return aprod<T>(c, tdda::SRC_TUPD, tdda::SNK_AT_DEF, n, rhs);              // t, At, zeta, rho, beta
+    }
     if ((e = aprod<T>(c, tdda::SRC_PUPD, tdda::SNK_AP, n, rhs))) return e;  // p, Ap, alpha
     if ((e = aprod<T>(c, tdda::SRC_TUPD, tdda::SNK_AT, n, rhs))) return e;  // t, At, zeta
     count_launches(1);
@@ -391,8 +407,12 @@ template <typename T> tdda_status krylov(tdda_core* c, int n, bool p_zero, int m
         TDDA_CK(aprod<T>(c, tdda::SRC_P, tdda::SNK_RES, n, rhs));  // r = r0 = p = E - A P
     }
     TDDA_CK(aprod<T>(c, tdda::SRC_IN, tdda::SNK_AP, n, rhs));    // Ap0, alpha
-    TDDA_CK(aprod<T>(c, tdda::SRC_TUPD, tdda::SNK_AT, n, rhs));  // t, At0, zeta
-    TDDA_CK1(tdda::launch_update<T>(c->g, n, rhs, 1, c->stream));
+    if (kDeferred<T>) {
+        TDDA_CK(aprod<T>(c, tdda::SRC_TUPD, tdda::SNK_AT_DEF, n, rhs));  // t, At0, zeta, rho, beta
+    } else {
+        TDDA_CK(aprod<T>(c, tdda::SRC_TUPD, tdda::SNK_AT, n, rhs));  // t, At0, zeta
+        TDDA_CK1(tdda::launch_update<T>(c->g, n, rhs, 1, c->stream));
+    }
     cudaGraphExec_t ex;
     TDDA_TRY(get_iteration_graph<T>(c, n, &ex));
     int done_it = 0;
@@ -403,11 +423,12 @@ template <typename T> tdda_status krylov(tdda_core* c, int n, bool p_zero, int m
         for (int i = 0; i < n; i++) running |= c->hst[i].status == tdda::ST_RUNNING;
         if (!running || done_it > max_it) break;
         for (int k = 0; k < kChunk; k++) {
-            count_launches(11);
+            count_launches(step_kernels<T>(c));
             TDDA_CK(cudaGraphLaunch(ex, c->stream));
         }
         done_it += kChunk;
     }
+    if (kDeferred<T>) TDDA_CK1(tdda::launch_finish<T>(c->g, n, rhs, c->stream));  // the last step's update
     return TDDA_OK;
 }
 
@@ -428,6 +449,7 @@ SolveState fresh_state(double tol, int max_it, int iterations) {
     s.max_it = max_it;
     s.iterations = iterations;
     s.status = tdda::ST_RUNNING;
+    s.init = 1;
     return s;
 }
 
@@ -1161,6 +1183,11 @@ tdda_status tdda_core_stream(const tdda_core* c, void** stream) {
 }
 
 unsigned long long tdda_kernel_launches(void) { return g_launches.load(); }
+
+int tdda_core_pass_count(const tdda_core* c, int precision) {
+    if (!c || (precision != TDDA_FP64 && precision != TDDA_FP32_REFINE)) return -1;
+    return tdda::zy_fused(c->g, precision == TDDA_FP32_REFINE) ? 3 : 5;
+}
 
 tdda_status tdda_profile_aproduct(tdda_core* c, int precision, int nrhs, int reps, double* ms5) {
     if (!c || !ms5 || reps < 1 || nrhs < 1 || nrhs > c->max_rhs ||

@@ -7,6 +7,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "tdda_internal.cuh"
 
 namespace tdda {
@@ -97,14 +99,57 @@ template <int NV> __device__ __forceinline__ void block_sum(double (&v)[NV], dou
     __syncthreads();
 }
 
-// Publish this block's partials; the last block of the grid (for this
-// right-hand side) sums all partials in block order and returns true in
-// every thread of that block, with the totals in tot (valid in thread 0).
+// Accumulator of the per-thread partial sums.  The FP64 kernels add in FP64.
+// The FP32 kernels (the inner solve of the mixed form) keep GB300's narrow
+// FP64 pipe out of their reductions: each thread adds its few products (at
+// most 8 in the vector kernels, at most 24 in the passes) in FP32, and the
+// warp, block and grid sums are double-float (hi, lo) pairs of FP32 values
+// added with Knuth's TwoSum, about 44 bits.  Every order is fixed, so the
+// sums are deterministic.
+template <typename T> using acc_t = typename std::conditional<sizeof(T) == 4, float, double>::type;
+
+// (a.x + a.y) + (b.x + b.y) as a double-float pair (TwoSum of the high parts,
+// D. E. Knuth, TAOCP vol. 2, 4.2.2; the low parts added; renormalised)
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+    const float s = a.x + b.x;
+    const float bp = s - a.x;
+    const float e = (a.x - (s - bp)) + (b.x - bp);
+    const float lo = e + a.y + b.y;
+    const float hi = s + lo;
+    return make_float2(hi, lo - (hi - s));
+}
+
+// Block sum of double-float values; the result is valid in thread 0.
+// sred must hold 32 * NV float2.
+template <int NV> __device__ __forceinline__ void block_sum(float2 (&v)[NV], float2* sred) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        float2 a = v[k];
+        for (int o = 16; o > 0; o >>= 1)
+            a = df_add(a, make_float2(__shfl_down_sync(0xffffffffu, a.x, o), __shfl_down_sync(0xffffffffu, a.y, o)));
+        if (lane == 0) sred[k * 32 + warp] = a;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            float2 a = sred[k * 32];
+            for (int w = 1; w < nw; w++) a = df_add(a, sred[k * 32 + w]);
+            v[k] = a;
+        }
+    }
+    __syncthreads();
+}
+
+// Publish this block's sums (valid in thread 0); the last block of the grid
+// (for this right-hand side) sums all partials in block order and returns
+// true in every thread of that block, with the totals in tot (valid in
+// thread 0).
 template <int NV>
-__device__ bool last_block_total(double (&v)[NV], double* part, int nblk, int bid, unsigned int* cnt, double* sred,
-                                 double (&tot)[NV]) {
+__device__ bool publish_total(const double (&v)[NV], double* part, int nblk, int bid, unsigned int* cnt, double* sred,
+                              double (&tot)[NV]) {
     __shared__ int s_last;
-    block_sum<NV>(v, sred);
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int k = 0; k < NV; k++) part[k * nblk + bid] = v[k];
@@ -124,6 +169,202 @@ __device__ bool last_block_total(double (&v)[NV], double* part, int nblk, int bi
     block_sum<NV>(tot, sred);
     if (threadIdx.x == 0) *cnt = 0u;
     return true;
+}
+
+template <int NV>
+__device__ bool last_block_total(double (&v)[NV], double* part, int nblk, int bid, unsigned int* cnt, double* sred,
+                                 double (&tot)[NV]) {
+    block_sum<NV>(v, sred);
+    return publish_total<NV>(v, part, nblk, bid, cnt, sred, tot);
+}
+// FP32 partials: double-float block and grid sums; the partial slots hold one
+// float2 (hi, lo) each.  tot = hi + lo in FP64 (valid in thread 0).  sred
+// must hold 32 * NV float2, i.e. 32 * NV doubles (a float2 is 8 bytes).
+template <int NV>
+__device__ bool last_block_total(float (&v)[NV], double* part, int nblk, int bid, unsigned int* cnt, double* sred,
+                                 double (&tot)[NV]) {
+    __shared__ int s_last;
+    float2* sr2 = reinterpret_cast<float2*>(sred);
+    float2* part2 = reinterpret_cast<float2*>(part);
+    float2 a[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++) a[k] = make_float2(v[k], 0.f);
+    block_sum<NV>(a, sr2);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) part2[k * nblk + bid] = a[k];
+        __threadfence();
+        unsigned int prev = atomicAdd(cnt, 1u);
+        s_last = (prev == (unsigned int)(nblk - 1));
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        float2 q = make_float2(0.f, 0.f);
+        for (int i = threadIdx.x; i < nblk; i += blockDim.x) q = df_add(q, __ldcg(part2 + k * nblk + i));
+        a[k] = q;
+    }
+    block_sum<NV>(a, sr2);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) tot[k] = (double)a[k].x + (double)a[k].y;
+        *cnt = 0u;
+    }
+    return true;
+}
+
+// Shared scratch of a reduction kernel, in doubles: NV * nt for the FP64
+// block sum, 32 * NV float2 (8 bytes each, one per warp slot) for the
+// double-float one.
+template <typename T, int NV> __host__ __device__ constexpr int sred_size() {
+    static_assert(sizeof(float2) == sizeof(double), "a float2 slot is one double");
+    return sizeof(T) == 4 ? 32 * NV : NV * kNT;
+}
+
+// The end of one BiCGSTAB step, given r0.r and |r|^2 of the new residual
+// (DDAModel.cpp:218-255): convergence (not after the initial products,
+// DDAModel.cpp:177-182), the iteration limit, breakdown on r0.rl = 0
+// (DDAModel.cpp:193-215) and beta for the next step.  Run by one thread.
+__device__ __forceinline__ void finish_step(SolveState* st, double2 rho, double rn2, bool is_init) {
+    st->rho_prev = st->rho;
+    st->rho = rho;
+    st->rnorm2 = rn2;
+    const double err = sqrt(rn2) / st->Enorm;
+    if (!is_init) {
+        st->it += 1;
+        if (err <= st->tol) {  // DDAModel.cpp:232-235
+            st->status = ST_CONVERGED;
+            st->iterations = st->it;
+            st->error = err;
+            return;
+        }
+    }
+    if (st->it >= st->max_it) {  // the loop of DDAModel.cpp:186 ends
+        st->status = ST_MAXITER;
+        st->error = err;
+        return;
+    }
+    if (st->rho_prev.x == 0.0 && st->rho_prev.y == 0.0) {  // DDAModel.cpp:193-215
+        st->status = ST_BREAKDOWN;
+        st->iterations = st->it + 1;
+        st->error = err;
+        return;
+    }
+    // beta = (alpha / zeta) * (r0 . r) / (r0 . rl)      DDAModel.cpp:218
+    st->beta = cdiv(dmul(cdiv(st->alpha, st->zeta), st->rho), st->rho_prev);
+    // the reference would iterate on NaN up to the limit; stop and report it
+    if (!finite2(st->rho) || !isfinite(err) || !finite2(st->beta)) {
+        st->status = ST_NAN;
+        st->error = err;
+    }
+}
+
+// The step end of the deferred-update form (SNK_AT_DEF) from the five sums
+// At.t, At.At, r0.t, r0.At, t.t: zeta = At.t / At.At, and for
+// r = t - zeta At: r0.r = r0.t - zeta r0.At and
+// |r|^2 = t.t - 2 Re(conj(zeta) At.t) + |zeta|^2 At.At.
+__device__ __forceinline__ void finish_step_deferred(SolveState* st, const double (&tot)[8]) {
+    const double2 Att = make_double2(tot[0], tot[1]);
+    const double AtAt = tot[2];
+    const double2 r0t = make_double2(tot[3], tot[4]), r0At = make_double2(tot[5], tot[6]);
+    const double tt = tot[7];
+    const double2 zeta = cdiv(Att, make_double2(AtAt, 0.0));  // DDAModel.cpp:225
+    st->zeta = zeta;
+    const double2 zr = dmul(zeta, r0At);
+    const double2 rho = make_double2(r0t.x - zr.x, r0t.y - zr.y);
+    double rn2 = tt - 2.0 * (zeta.x * Att.x + zeta.y * Att.y) + (zeta.x * zeta.x + zeta.y * zeta.y) * AtAt;
+    if (!(rn2 > 0.0)) rn2 = isnan(rn2) ? rn2 : 0.0;
+    const bool init = st->init != 0;
+    st->init = 0;
+    st->pending = 1;
+    finish_step(st, rho, rn2, init);
+}
+
+// The FP32 inner solve forms its step scalars with FP32 division and square
+// root (its kernels use them in FP32); only the cancelling differences
+// r0.t - zeta r0.At and t.t - ... stay FP64 multiply-adds.  The state keeps
+// doubles.
+__device__ __forceinline__ float2 to_f2(double2 a) { return make_float2((float)a.x, (float)a.y); }
+__device__ __forceinline__ double2 to_d2(float2 a) { return make_double2(a.x, a.y); }
+__device__ __forceinline__ float2 fmul2(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ float2 fdiv2(float2 a, float2 b) {
+    // Smith's algorithm (R. L. Smith, CACM 5(8), 1962)
+    if (fabsf(b.x) >= fabsf(b.y)) {
+        const float r = b.y / b.x, den = b.x + b.y * r;
+        return make_float2((a.x + a.y * r) / den, (a.y - a.x * r) / den);
+    }
+    const float r = b.x / b.y, den = b.x * r + b.y;
+    return make_float2((a.x * r + a.y) / den, (a.y * r - a.x) / den);
+}
+
+__device__ __forceinline__ void finish_step_f32(SolveState* st, double2 rho, double rn2, bool is_init) {
+    st->rho_prev = st->rho;
+    st->rho = rho;
+    st->rnorm2 = rn2;
+    const float err = sqrtf((float)rn2) / (float)st->Enorm;
+    if (!is_init) {
+        st->it += 1;
+        if (err <= (float)st->tol) {  // DDAModel.cpp:232-235
+            st->status = ST_CONVERGED;
+            st->iterations = st->it;
+            st->error = err;
+            return;
+        }
+    }
+    if (st->it >= st->max_it) {
+        st->status = ST_MAXITER;
+        st->error = err;
+        return;
+    }
+    if (st->rho_prev.x == 0.0 && st->rho_prev.y == 0.0) {  // DDAModel.cpp:193-215
+        st->status = ST_BREAKDOWN;
+        st->iterations = st->it + 1;
+        st->error = err;
+        return;
+    }
+    const float2 beta = fdiv2(fmul2(fdiv2(to_f2(st->alpha), to_f2(st->zeta)), to_f2(rho)), to_f2(st->rho_prev));
+    st->beta = to_d2(beta);
+    if (!isfinite(rho.x) || !isfinite(rho.y) || !isfinite(err) || !isfinite(beta.x) || !isfinite(beta.y)) {
+        st->status = ST_NAN;
+        st->error = err;
+    }
+}
+
+__device__ __forceinline__ void finish_step_deferred_f32(SolveState* st, const double (&tot)[8]) {
+    const double2 Att = make_double2(tot[0], tot[1]);
+    const double AtAt = tot[2];
+    const double2 r0t = make_double2(tot[3], tot[4]), r0At = make_double2(tot[5], tot[6]);
+    const double tt = tot[7];
+    const double2 zeta = to_d2(fdiv2(to_f2(Att), make_float2((float)AtAt, 0.f)));
+    st->zeta = zeta;
+    const double2 zr = dmul(zeta, r0At);
+    const double2 rho = make_double2(r0t.x - zr.x, r0t.y - zr.y);
+    double rn2 = tt - 2.0 * (zeta.x * Att.x + zeta.y * Att.y) + (zeta.x * zeta.x + zeta.y * zeta.y) * AtAt;
+    if (!(rn2 > 0.0)) rn2 = isnan(rn2) ? rn2 : 0.0;
+    const bool init = st->init != 0;
+    st->init = 0;
+    st->pending = 1;
+    finish_step_f32(st, rho, rn2, init);
+}
+
+// The scalars a sink pass forms from its grid totals (thread 0 of the last block).
+template <typename T, int SNK, int NV> __device__ __forceinline__ void finalize_sink(SolveState* st, const double (&tot)[NV]) {
+    if constexpr (SNK == SNK_RES) {
+        st->rho = make_double2(tot[0], 0.0);  // r0 . r with r0 = r
+        st->rnorm2 = tot[0];
+    } else if constexpr (sizeof(T) == 4) {
+        if constexpr (SNK == SNK_AT_DEF) finish_step_deferred_f32(st, tot);
+        else if constexpr (SNK == SNK_AP) st->alpha = to_d2(fdiv2(to_f2(st->rho), make_float2((float)tot[0], (float)tot[1])));
+        else if constexpr (SNK == SNK_AT)
+            st->zeta = to_d2(fdiv2(make_float2((float)tot[0], (float)tot[1]), make_float2((float)tot[2], 0.f)));
+    } else {
+        if constexpr (SNK == SNK_AT_DEF) finish_step_deferred(st, tot);
+        else if constexpr (SNK == SNK_AP) st->alpha = cdiv(st->rho, make_double2(tot[0], tot[1]));  // DDAModel.cpp:221
+        else if constexpr (SNK == SNK_AT)
+            st->zeta = cdiv(make_double2(tot[0], tot[1]), make_double2(tot[2], 0.0));  // DDAModel.cpp:225
+    }
 }
 
 __device__ __forceinline__ bool rhs_done(const SolveState* st) {

@@ -41,6 +41,8 @@ struct SolveState {
     int it;            // completed loop iterations
     int max_it;
     int iterations;    // ITERATION as the reference reports it
+    int init;          // the next step finalisation is the initial one (no convergence check)
+    int pending;       // deferred update of P and r not yet applied (FP32 inner solve)
 };
 
 // per right-hand side: the vectors of one solve (AoS [x,y,z] per dipole)
@@ -59,7 +61,7 @@ template <typename T> struct RhsVecs {
     double* part;        // reduction partials, kPartSlots x maxblk doubles
     unsigned int* cnt;   // last-block counters, kCounters
 };
-constexpr int kPartSlots = 4;
+constexpr int kPartSlots = 8;
 constexpr int kCounters = 8;
 
 // what the first z-pass transforms (the fused vector update of the solver)
@@ -68,6 +70,9 @@ enum SrcMode : int {
     SRC_PUPD = 1,    // p = r + beta (p - u)         (DDAModel.cpp:219)
     SRC_TUPD = 2,    // t = r - alpha Ap             (DDAModel.cpp:222)
     SRC_P = 3,       // v = P                        (DDAModel.cpp:164)
+    SRC_PUPD_DEF = 4,  // apply the deferred update of the previous step
+                       // (u = zeta Ap, P += alpha p + zeta r - alpha u,
+                       // r = t - zeta At), then p = r + beta (p - u)
 };
 // what the last z-pass does with A v
 enum SnkMode : int {
@@ -76,6 +81,9 @@ enum SnkMode : int {
     SNK_AP = 2,      // Ap = A p + al p, alpha = (r0.r) / (r0.Ap)
     SNK_AT = 3,      // At = A t + al t, zeta = (At.t) / (At.At)
     SNK_RES = 4,     // r = r0 = p = E - (A P + al P), rho = r0.r   (DDAModel.cpp:164-168)
+    SNK_AT_DEF = 5,  // At = A t + al t; zeta, and r0.r and |r|^2 of r = t - zeta At from
+                     // r0.t, r0.At, t.t, At.t, At.At; the step logic of launch_update;
+                     // the update of P and r is left pending (SRC_PUPD_DEF, launch_finish)
 };
 
 // -------------------------------------------------------------- pass dispatch
@@ -100,6 +108,12 @@ template <typename T> cudaError_t pass_generic(int pass, int mode, const PassArg
 // return false (nothing launched) when the length has no specialised kernel
 template <typename T> bool pass_ct_z(int pass, int mode, const PassArgs<T>& a, cudaError_t* err);
 template <typename T> bool pass_ct_xy(int pass, int mode, const PassArgs<T>& a, cudaError_t* err);
+// fused z+y passes: pass PASS_ZFWD launches k_zyfwd (z and y forward), pass
+// PASS_ZINV launches k_yzinv (y and z inverse); only for the planes zy_fused()
+// accepts (FP32, compiled (My, Mz) pairs); false means nothing was launched
+template <typename T> bool pass_zy(int pass, int mode, const PassArgs<T>& a, cudaError_t* err);
+bool zy_fused(const Geom& g, bool fp32);
+cudaError_t configure_pass_zy();
 cudaError_t configure_pass_generic();
 cudaError_t configure_pass_ct_z();
 cudaError_t configure_pass_ct_xy();
@@ -117,7 +131,8 @@ cudaError_t launch_green(const Geom& g, double K, double d, const double2* tw64x
                          float2* green32, cudaStream_t stream);
 
 // One A-product over nrhs right-hand sides.  rhs[] lives in device memory.
-// ev, when given, holds 6 events recorded before K1..K5 and after K5.
+// ev, when given, holds 6 events recorded before K1..K5 and after K5; with
+// the fused z+y passes ev[1] = ev[2] and ev[4] = ev[5] (K2 and K4 take no time).
 // For SRC_IN with SNK_OUT / SNK_ALB the vectors used are rhs[b].p (input)
 // and rhs[b].Ap (output); SNK_RES reads P and E and writes r, r0, p.
 template <typename T>
@@ -131,6 +146,11 @@ cudaError_t launch_aproduct(const Geom& g, int src, int snk, int nrhs, const Rhs
 // initial products (DDAModel.cpp:177-182), which checks no convergence.
 template <typename T>
 cudaError_t launch_update(const Geom& g, int nrhs, const RhsVecs<T>* rhs, int is_init, cudaStream_t stream);
+
+// Applies the pending deferred update of P and r (SNK_AT_DEF) of every
+// right-hand side that has one; the end of the FP32 inner solve.
+template <typename T>
+cudaError_t launch_finish(const Geom& g, int nrhs, const RhsVecs<T>* rhs, cudaStream_t stream);
 
 // |E| of every right-hand side into st->Enorm, and reset of the state.
 template <typename T>

@@ -32,12 +32,12 @@ using namespace dev;
 // ================================================================ K6 update
 template <typename T>
 __global__ void __launch_bounds__(kNT) k_update(int n3, const RhsVecs<T>* __restrict__ rhs, int is_init) {
-    __shared__ double sred[4 * kNT];
+    __shared__ double sred[sred_size<T, 4>()];
     const int b = blockIdx.y;
     const RhsVecs<T> R = rhs[b];
     if (rhs_done(R.st)) return;
     const cx<T> alpha = from_d<T>(R.st->alpha), zeta = from_d<T>(R.st->zeta);
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    acc_t<T> acc[4] = {0, 0, 0, 0};
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x) {
         const cx<T> Ap = R.Ap[e], r = R.r[e], p = R.p[e], t = R.t[e], At = R.At[e], r0 = R.r0[e];
         cx<T> P = R.P[e];
@@ -48,58 +48,43 @@ __global__ void __launch_bounds__(kNT) k_update(int n3, const RhsVecs<T>* __rest
         R.u[e] = u;
         R.P[e] = P;
         R.r[e] = rn;
-        acc[0] += (double)r0.x * (double)rn.x + (double)r0.y * (double)rn.y;
-        acc[1] += (double)r0.x * (double)rn.y - (double)r0.y * (double)rn.x;
-        acc[2] += (double)rn.x * (double)rn.x + (double)rn.y * (double)rn.y;
+        acc[0] += r0.x * rn.x + r0.y * rn.y;
+        acc[1] += r0.x * rn.y - r0.y * rn.x;
+        acc[2] += rn.x * rn.x + rn.y * rn.y;
     }
     double tot[4];
     if (!last_block_total<4>(acc, R.part, gridDim.x, blockIdx.x, R.cnt + 3, sred, tot)) return;
     if (threadIdx.x != 0) return;
-    SolveState* st = R.st;
-    st->rho_prev = st->rho;
-    st->rho = make_double2(tot[0], tot[1]);
-    st->rnorm2 = tot[2];
-    const double err = sqrt(tot[2]) / st->Enorm;
-    if (!is_init) {
-        st->it += 1;
-        if (err <= st->tol) {  // DDAModel.cpp:232-235
-            st->status = ST_CONVERGED;
-            st->iterations = st->it;
-            st->error = err;
-            return;
-        }
-    }
-    if (st->it >= st->max_it) {  // the loop of DDAModel.cpp:186 ends
-        st->status = ST_MAXITER;
-        st->error = err;
-        return;
-    }
-    if (st->rho_prev.x == 0.0 && st->rho_prev.y == 0.0) {  // DDAModel.cpp:193-215
-        st->status = ST_BREAKDOWN;
-        st->iterations = st->it + 1;
-        st->error = err;
-        return;
-    }
-    // beta = (alpha / zeta) * (r0 . r) / (r0 . rl)      DDAModel.cpp:218
-    st->beta = cdiv(dmul(cdiv(st->alpha, st->zeta), st->rho), st->rho_prev);
-    // the reference would iterate on NaN up to the limit; stop and report it
-    if (!finite2(st->rho) || !isfinite(err) || !finite2(st->beta)) {
-        st->status = ST_NAN;
-        st->error = err;
+    finish_step(R.st, make_double2(tot[0], tot[1]), tot[2], is_init != 0);
+}
+
+// The deferred update of the last step (SNK_AT_DEF) for every right-hand side
+// that has one pending: u = zeta Ap; P += alpha p + zeta r - alpha u;
+// r = t - zeta At.
+template <typename T> __global__ void __launch_bounds__(kNT) k_finish(int n3, const RhsVecs<T>* __restrict__ rhs) {
+    const RhsVecs<T> R = rhs[blockIdx.y];
+    if (R.st == nullptr || !R.st->pending) return;
+    const cx<T> alpha = from_d<T>(R.st->alpha), zeta = from_d<T>(R.st->zeta);
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x) {
+        const cx<T> u = cmul<T>(zeta, R.Ap[e]);
+        const cx<T> r = R.r[e];
+        const cx<T> z = csub<T>(cmul<T>(zeta, r), cmul<T>(alpha, u));
+        R.P[e] = cadd<T>(cadd<T>(R.P[e], cmul<T>(alpha, R.p[e])), z);
+        R.r[e] = csub<T>(R.t[e], cmul<T>(zeta, R.At[e]));
     }
 }
 
 // |E| of each right-hand side
 template <typename T>
 __global__ void __launch_bounds__(kNT) k_solve_begin(int n3, const RhsVecs<T>* __restrict__ rhs, int resid_is_rhs) {
-    __shared__ double sred[4 * kNT];
+    __shared__ double sred[sred_size<T, 4>()];
     const int b = blockIdx.y;
     const RhsVecs<T> R = rhs[b];
     if (rhs_done(R.st)) return;
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    acc_t<T> acc[4] = {0, 0, 0, 0};
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x) {
         const cx<T> v = R.E[e];
-        acc[0] += (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+        acc[0] += v.x * v.x + v.y * v.y;
         if (resid_is_rhs) {
             R.r[e] = v;
             R.r0[e] = v;
@@ -305,9 +290,18 @@ int grid1d(long long n, int nt) {
 }
 // reductions over a vector: four entries per thread keeps the FP64 block
 // sums few while leaving enough threads to cover memory latency
-int grid_reduce(long long n) {
-    long long b = (n + 4LL * kNT - 1) / (4LL * kNT);
-    if (b > 152 * 8) b = 152 * 8;
+// blocks of a grid-stride reduction over n entries.  FP64 kernels: 4 entries
+// per thread, at most 8 blocks per SM (each block's FP64 block sum occupies
+// the narrow FP64 pipe).  FP32 kernels: 2 entries per thread for latency
+// hiding, and at most 8 per thread (their per-thread partials are FP32).
+int grid_reduce(long long n, bool fp32) {
+    long long b;
+    if (fp32) {
+        b = std::min((n + 2LL * kNT - 1) / (2LL * kNT), std::max(152LL * 16, (n + 8LL * kNT - 1) / (8LL * kNT)));
+    } else {
+        b = (n + 4LL * kNT - 1) / (4LL * kNT);
+        if (b > 152 * 8) b = 152 * 8;
+    }
     return (int)(b < 1 ? 1 : b);
 }
 
@@ -321,6 +315,7 @@ cudaError_t configure_kernels() {
     cudaError_t e = configure_pass_generic();
     if (e == cudaSuccess) e = configure_pass_ct_z();
     if (e == cudaSuccess) e = configure_pass_ct_xy();
+    if (e == cudaSuccess) e = configure_pass_zy();
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute((const void*)k_fft_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxPassSmem);
     if (e == cudaSuccess)
@@ -342,8 +337,9 @@ size_t max_pass_smem(const Geom& g) {
 int max_blocks_per_rhs(const Geom& g) {
     const int lz = std::min(z_lines<float>(g.pz.M), z_lines<double>(g.pz.M));
     int nz = (g.Nx * g.Ny + lz - 1) / lz;
-    int nv = grid_reduce(3LL * g.N);
-    return nz > nv ? nz : nv;
+    int nv = std::max(grid_reduce(3LL * g.N, false), grid_reduce(3LL * g.N, true));
+    int nzy = 3 * g.Nx;  // fused z+y passes: one block per (x plane, component)
+    return std::max(nz, std::max(nv, nzy));
 }
 
 // ------------------------------------------------------------------ launchers
@@ -396,6 +392,20 @@ cudaError_t launch_aproduct(const Geom& g, int src, int snk, int nrhs, const Rhs
                             const cx<T>* twx, const cx<T>* twy, const cx<T>* twz, const int* cellmap, cx<T>* grid,
                             cudaStream_t stream, cudaEvent_t* ev) {
     const PassArgs<T> a{g, nrhs, rhs, green, twx, twy, twz, cellmap, grid, stream};
+    if (zy_fused(g, sizeof(T) == 4)) {
+        cudaError_t err = cudaSuccess;
+        if (ev) cudaEventRecord(ev[0], stream);
+        if (!pass_zy<T>(PASS_ZFWD, src, a, &err)) return cudaErrorInvalidValue;
+        if (err != cudaSuccess) return err;
+        if (ev) cudaEventRecord(ev[1], stream), cudaEventRecord(ev[2], stream);
+        if (!pass_ct_xy<T>(PASS_XPASS, 0, a, &err)) err = pass_generic<T>(PASS_XPASS, 0, a);
+        if (err != cudaSuccess) return err;
+        if (ev) cudaEventRecord(ev[3], stream);
+        if (!pass_zy<T>(PASS_ZINV, snk, a, &err)) return cudaErrorInvalidValue;
+        if (err != cudaSuccess) return err;
+        if (ev) cudaEventRecord(ev[4], stream), cudaEventRecord(ev[5], stream);
+        return cudaSuccess;
+    }
     const int passes[5] = {PASS_ZFWD, PASS_YFWD, PASS_XPASS, PASS_YINV, PASS_ZINV};
     const int modes[5] = {src, 0, 0, 0, snk};
     for (int k = 0; k < 5; k++) {
@@ -411,21 +421,28 @@ cudaError_t launch_aproduct(const Geom& g, int src, int snk, int nrhs, const Rhs
 
 template <typename T>
 cudaError_t launch_update(const Geom& g, int nrhs, const RhsVecs<T>* rhs, int is_init, cudaStream_t stream) {
-    const dim3 gr(grid_reduce(3LL * g.N), nrhs);
+    const dim3 gr(grid_reduce(3LL * g.N, sizeof(T) == 4), nrhs);
     k_update<T><<<gr, kNT, 0, stream>>>(3 * g.N, rhs, is_init);
     return cudaGetLastError();
 }
 
 template <typename T>
+cudaError_t launch_finish(const Geom& g, int nrhs, const RhsVecs<T>* rhs, cudaStream_t stream) {
+    const dim3 gr(grid1d(3LL * g.N, kNT), nrhs);
+    k_finish<T><<<gr, kNT, 0, stream>>>(3 * g.N, rhs);
+    return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t launch_solve_begin(const Geom& g, int nrhs, const RhsVecs<T>* rhs, cudaStream_t stream) {
-    const dim3 gr(grid_reduce(3LL * g.N), nrhs);
+    const dim3 gr(grid_reduce(3LL * g.N, sizeof(T) == 4), nrhs);
     k_solve_begin<T><<<gr, kNT, 0, stream>>>(3 * g.N, rhs, 0);
     return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_residual_is_rhs(const Geom& g, int nrhs, const RhsVecs<T>* rhs, cudaStream_t stream) {
-    const dim3 gr(grid_reduce(3LL * g.N), nrhs);
+    const dim3 gr(grid_reduce(3LL * g.N, sizeof(T) == 4), nrhs);
     k_solve_begin<T><<<gr, kNT, 0, stream>>>(3 * g.N, rhs, 1);
     return cudaGetLastError();
 }
@@ -463,6 +480,7 @@ template <typename T> cudaError_t launch_zero(long long n, cx<T>* v, cudaStream_
                                             const cx<T>*, const cx<T>*, const cx<T>*, const int*, cx<T>*,         \
                                             cudaStream_t, cudaEvent_t*);                                           \
     template cudaError_t launch_update<T>(const Geom&, int, const RhsVecs<T>*, int, cudaStream_t);                 \
+    template cudaError_t launch_finish<T>(const Geom&, int, const RhsVecs<T>*, cudaStream_t);                      \
     template cudaError_t launch_solve_begin<T>(const Geom&, int, const RhsVecs<T>*, cudaStream_t);                 \
     template cudaError_t launch_residual_is_rhs<T>(const Geom&, int, const RhsVecs<T>*, cudaStream_t);             \
     template cudaError_t launch_zero<T>(long long, cx<T>*, cudaStream_t);

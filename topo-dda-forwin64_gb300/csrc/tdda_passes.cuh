@@ -16,6 +16,23 @@
 namespace tdda {
 namespace dev {
 
+// One entry of the deferred-update step (SRC_PUPD_DEF): the update of the
+// previous step (DDAModel.cpp:226-230: u = zeta Ap, z = zeta r - alpha u,
+// P += alpha p + z, r = t - zeta At), then the new direction
+// p = r + beta (p - u) (DDAModel.cpp:219), which is returned.
+template <typename T>
+__device__ __forceinline__ cx<T> deferred_step(const RhsVecs<T>& R, long long o, cx<T> alpha, cx<T> zeta, cx<T> beta) {
+    const cx<T> Ap = R.Ap[o], r = R.r[o], p = R.p[o], t = R.t[o], At = R.At[o];
+    const cx<T> u = cmul<T>(zeta, Ap);
+    const cx<T> z = csub<T>(cmul<T>(zeta, r), cmul<T>(alpha, u));
+    R.P[o] = cadd<T>(cadd<T>(R.P[o], cmul<T>(alpha, p)), z);
+    const cx<T> rn = csub<T>(t, cmul<T>(zeta, At));
+    R.r[o] = rn;
+    const cx<T> pn = cadd<T>(rn, cmul<T>(beta, csub<T>(p, u)));
+    R.p[o] = pn;
+    return pn;
+}
+
 // ------------------------------------------------------------ K1 zfwd
 template <typename T, int SRC, int CM>
 __global__ void __launch_bounds__(kNT) k_zfwd(Geom g, const RhsVecs<T>* __restrict__ rhs,
@@ -37,9 +54,10 @@ __global__ void __launch_bounds__(kNT) k_zfwd(Geom g, const RhsVecs<T>* __restri
     const int l0 = blockIdx.x * LZ;
     const int nl = min(LZ, nlines - l0);
 
-    cx<T> beta, alpha;
-    if (SRC == SRC_PUPD) beta = from_d<T>(R.st->beta);
-    if (SRC == SRC_TUPD) alpha = from_d<T>(R.st->alpha);
+    cx<T> beta, alpha, zeta;
+    if (SRC == SRC_PUPD || SRC == SRC_PUPD_DEF) beta = from_d<T>(R.st->beta);
+    if (SRC == SRC_TUPD || SRC == SRC_PUPD_DEF) alpha = from_d<T>(R.st->alpha);
+    if (SRC == SRC_PUPD_DEF) zeta = from_d<T>(R.st->zeta);
     const cx<T>* src = SRC == SRC_IN ? R.p : R.P;
     for (int e = threadIdx.x; e < nl * Nz; e += blockDim.x) {
         const int line = e / Nz, z = e - (e / Nz) * Nz;
@@ -53,6 +71,8 @@ __global__ void __launch_bounds__(kNT) k_zfwd(Geom g, const RhsVecs<T>* __restri
                     cx<T> pc = R.p[o + c], uc = R.u[o + c], rc = R.r[o + c];
                     v[c] = cadd<T>(rc, cmul<T>(beta, csub<T>(pc, uc)));
                     R.p[o + c] = v[c];
+                } else if (SRC == SRC_PUPD_DEF) {
+                    v[c] = deferred_step<T>(R, o + c, alpha, zeta, beta);
                 } else if (SRC == SRC_TUPD) {
                     cx<T> rc = R.r[o + c], ac = R.Ap[o + c];
                     v[c] = csub<T>(rc, cmul<T>(alpha, ac));
@@ -208,7 +228,8 @@ __global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restri
                                               const cx<T>* __restrict__ twz, const int* __restrict__ cellmap,
                                               cx<T>* __restrict__ grid) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ double sred[4 * kNT];
+    constexpr int NV = SNK == SNK_AT_DEF ? 8 : 4;
+    __shared__ double sred[sred_size<T, NV>()];
     const int b = blockIdx.y;
     const RhsVecs<T> R = rhs[b];
     if (rhs_done(R.st)) return;
@@ -237,7 +258,7 @@ __global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restri
 
     // scatter to the dipoles, fused diagonal term and dot products
     const cx<T>* vsrc = (SRC == SRC_TUPD) ? R.t : (SRC == SRC_P ? R.P : R.p);
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    acc_t<T> acc[NV] = {};
     for (int e = threadIdx.x; e < nl * Nz; e += blockDim.x) {
         const int line = e / Nz, z = e - (e / Nz) * Nz;
         const int i = cellmap[(long long)(l0 + line) * Nz + z];
@@ -257,40 +278,235 @@ __global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restri
             } else if (SNK == SNK_AP) {
                 R.Ap[o + c] = w;
                 const cx<T> q = R.r0[o + c];  // r0 . Ap
-                acc[0] += (double)q.x * (double)w.x + (double)q.y * (double)w.y;
-                acc[1] += (double)q.x * (double)w.y - (double)q.y * (double)w.x;
-            } else if (SNK == SNK_AT) {
+                acc[0] += q.x * w.x + q.y * w.y;
+                acc[1] += q.x * w.y - q.y * w.x;
+            } else if (SNK == SNK_AT || SNK == SNK_AT_DEF) {
                 R.At[o + c] = w;
                 const cx<T> tt = vv;  // At . t and At . At
-                acc[0] += (double)w.x * (double)tt.x + (double)w.y * (double)tt.y;
-                acc[1] += (double)w.x * (double)tt.y - (double)w.y * (double)tt.x;
-                acc[2] += (double)w.x * (double)w.x + (double)w.y * (double)w.y;
+                acc[0] += w.x * tt.x + w.y * tt.y;
+                acc[1] += w.x * tt.y - w.y * tt.x;
+                acc[2] += w.x * w.x + w.y * w.y;
+                if constexpr (SNK == SNK_AT_DEF) {  // r0 . t, r0 . At, t . t
+                    const cx<T> q = R.r0[o + c];
+                    acc[3] += q.x * tt.x + q.y * tt.y;
+                    acc[4] += q.x * tt.y - q.y * tt.x;
+                    acc[5] += q.x * w.x + q.y * w.y;
+                    acc[6] += q.x * w.y - q.y * w.x;
+                    acc[7] += tt.x * tt.x + tt.y * tt.y;
+                }
             } else if (SNK == SNK_RES) {
                 const cx<T> res = csub<T>(R.E[o + c], w);
                 R.r[o + c] = res;
                 R.r0[o + c] = res;
                 R.p[o + c] = res;
-                acc[0] += (double)res.x * (double)res.x + (double)res.y * (double)res.y;
+                acc[0] += res.x * res.x + res.y * res.y;
             }
         }
     }
     if (SNK == SNK_OUT || SNK == SNK_ALB) return;
-    double tot[4];
+    double tot[NV];
     const int nblk = gridDim.x;
-    const int slot = SNK == SNK_AP ? 0 : (SNK == SNK_AT ? 1 : 2);
-    if (!last_block_total<4>(acc, R.part, nblk, blockIdx.x, R.cnt + slot, sred, tot)) return;
+    const int slot = SNK == SNK_AP ? 0 : (SNK == SNK_AT || SNK == SNK_AT_DEF ? 1 : 2);
+    if (!last_block_total<NV>(acc, R.part, nblk, blockIdx.x, R.cnt + slot, sred, tot)) return;
     if (threadIdx.x != 0) return;
-    SolveState* st = R.st;
-    if (SNK == SNK_AP) {
-        double2 r0Ap = make_double2(tot[0], tot[1]);
-        st->alpha = cdiv(st->rho, r0Ap);  // DDAModel.cpp:221
-    } else if (SNK == SNK_AT) {
-        st->zeta = cdiv(make_double2(tot[0], tot[1]), make_double2(tot[2], 0.0));  // DDAModel.cpp:225
-    } else {
-        st->rho = make_double2(tot[0], 0.0);  // r0 . r with r0 = r
-        st->rnorm2 = tot[0];
+    finalize_sink<T, SNK, NV>(R.st, tot);
+}
+
+// ------------------------------------------------------------ fused z+y passes
+// For the FP32 passes of the compiled (My, Mz) pairs one block holds the whole
+// My x Mz plane of one component of one x-plane in shared memory, so K1+K2
+// become one kernel (k_zyfwd) and K4+K5 another (k_yzinv): the plane makes no
+// round trip through L2 between the z and y transforms and an A-product is
+// three launches instead of five.  Grid: (3 Nx, nrhs), block (x, c) =
+// (blockIdx.x / 3, blockIdx.x % 3).  Plane layout in shared memory: [y][z],
+// row stride ZP.  Lattice data occupies rows y < Ny <= LY and columns
+// z < Nz <= LZ (M >= 2N - 1 on every axis).
+template <typename T, int MY, int MZ> struct ZyPlane {
+    static constexpr int ZP = pad_odd(MZ);
+    static constexpr int LY = (MY + 1) / 2;
+    static constexpr int LZ = (MZ + 1) / 2;
+    static constexpr size_t smem = sizeof(cx<T>) * (size_t)(MY + MZ + 2 * MY * ZP);
+};
+
+template <typename T, int SRC, int MY, int MZ>
+__global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restrict__ rhs,
+                                               const cx<T>* __restrict__ twy, const cx<T>* __restrict__ twz,
+                                               const int* __restrict__ cellmap, cx<T>* __restrict__ grid) {
+    using PL = ZyPlane<T, MY, MZ>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int b = blockIdx.y;
+    const RhsVecs<T> R = rhs[b];
+    if (rhs_done(R.st)) return;
+    const int x = blockIdx.x / 3, c = blockIdx.x - 3 * (blockIdx.x / 3);
+    const int Ny = g.Ny, Nz = g.Nz;
+    cx<T>* stwy = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* stwz = stwy + MY;
+    cx<T>* s = stwz + MZ;
+    cx<T>* s2 = s + MY * PL::ZP;
+    stage_tw<T>(stwy, twy, MY);
+    stage_tw<T>(stwz, twz, MZ);
+
+    cx<T> beta, alpha, zeta;
+    if (SRC == SRC_PUPD || SRC == SRC_PUPD_DEF) beta = from_d<T>(R.st->beta);
+    if (SRC == SRC_TUPD || SRC == SRC_PUPD_DEF) alpha = from_d<T>(R.st->alpha);
+    if (SRC == SRC_PUPD_DEF) zeta = from_d<T>(R.st->zeta);
+    const cx<T>* src = SRC == SRC_IN ? R.p : R.P;
+    const int* cm = cellmap + (long long)x * Ny * Nz;
+    for (int e = threadIdx.x; e < PL::LY * PL::LZ; e += kNT) {
+        const int y = e / PL::LZ, z = e - (e / PL::LZ) * PL::LZ;
+        cx<T> v = czero<T>();
+        const int i = (y < Ny && z < Nz) ? cm[y * Nz + z] : -1;
+        if (i >= 0) {
+            const long long o = 3LL * i + c;
+            if (SRC == SRC_PUPD) {
+                const cx<T> pc = R.p[o], uc = R.u[o], rc = R.r[o];
+                v = cadd<T>(rc, cmul<T>(beta, csub<T>(pc, uc)));
+                R.p[o] = v;
+            } else if (SRC == SRC_PUPD_DEF) {
+                v = deferred_step<T>(R, o, alpha, zeta, beta);
+            } else if (SRC == SRC_TUPD) {
+                const cx<T> rc = R.r[o], ac = R.Ap[o];
+                v = csub<T>(rc, cmul<T>(alpha, ac));
+                R.t[o] = v;
+            } else {
+                v = src[o];
+            }
+        }
+        s[y * PL::ZP + z] = v;
+    }
+    __syncthreads();
+    // z transform of the LY rows (inputs z < Nz), then y transform of the Mz columns (inputs y < Ny)
+    cx<T>* r1 = ct_fft<-1, T, MZ, PL::LY, PL::ZP, 1, kNT>(s, s2, stwz, Nz, MZ);
+    const cx<T>* r2 = ct_fft<-1, T, MY, MZ, 1, PL::ZP, kNT>(r1, r1 == s ? s2 : s, stwy, Ny, MY);
+    cx<T>* gp = grid + (long long)b * g.sb + c * g.sc + (long long)x * g.sx;
+    for (int e = threadIdx.x; e < MY * MZ; e += kNT) {
+        const int y = e / MZ, z = e - (e / MZ) * MZ;
+        gp[(long long)y * g.sy + z] = r2[y * PL::ZP + z];
     }
 }
+
+template <typename T, int SRC, int SNK, int MY, int MZ>
+__global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restrict__ rhs,
+                                               const cx<T>* __restrict__ twy, const cx<T>* __restrict__ twz,
+                                               const int* __restrict__ cellmap, cx<T>* __restrict__ grid) {
+    using PL = ZyPlane<T, MY, MZ>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int NV = SNK == SNK_AT_DEF ? 8 : 4;
+    __shared__ double sred[sred_size<T, NV>()];
+    const int b = blockIdx.y;
+    const RhsVecs<T> R = rhs[b];
+    if (rhs_done(R.st)) return;
+    const int x = blockIdx.x / 3, c = blockIdx.x - 3 * (blockIdx.x / 3);
+    const int Ny = g.Ny, Nz = g.Nz;
+    cx<T>* stwy = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* stwz = stwy + MY;
+    cx<T>* s = stwz + MZ;
+    cx<T>* s2 = s + MY * PL::ZP;
+    stage_tw<T>(stwy, twy, MY);
+    stage_tw<T>(stwz, twz, MZ);
+    const cx<T>* gp = grid + (long long)b * g.sb + c * g.sc + (long long)x * g.sx;
+    for (int e = threadIdx.x; e < MY * MZ; e += kNT) {
+        const int y = e / MZ, z = e - (e / MZ) * MZ;
+        s[y * PL::ZP + z] = gp[(long long)y * g.sy + z];
+    }
+    __syncthreads();
+    // y transform of the Mz columns (outputs y < Ny), then z transform of the
+    // LY rows (outputs z < Nz); rows Ny..LY-1 are transformed and dropped
+    cx<T>* r1 = ct_fft<+1, T, MY, MZ, 1, PL::ZP, kNT>(s, s2, stwy, MY, Ny);
+    const cx<T>* res = ct_fft<+1, T, MZ, PL::LY, PL::ZP, 1, kNT>(r1, r1 == s ? s2 : s, stwz, MZ, Nz);
+
+    // scatter component c to the dipoles, fused diagonal term and dot products
+    const cx<T>* vsrc = (SRC == SRC_TUPD) ? R.t : (SRC == SRC_P ? R.P : R.p);
+    const int* cm = cellmap + (long long)x * Ny * Nz;
+    acc_t<T> acc[NV] = {};
+    for (int e = threadIdx.x; e < PL::LY * PL::LZ; e += kNT) {
+        const int y = e / PL::LZ, z = e - (e / PL::LZ) * PL::LZ;
+        const int i = (y < Ny && z < Nz) ? cm[y * Nz + z] : -1;
+        if (i < 0) continue;
+        const long long o = 3LL * i + c;
+        const cx<T> val = res[y * PL::ZP + z];
+        if (SNK == SNK_OUT) {
+            R.Ap[o] = val;
+            continue;
+        }
+        const cx<T> vv = vsrc[o];
+        const cx<T> w = cadd<T>(val, cmul<T>(vv, R.al[o]));
+        if (SNK == SNK_ALB) {
+            R.Ap[o] = w;
+        } else if (SNK == SNK_AP) {
+            R.Ap[o] = w;
+            const cx<T> q = R.r0[o];  // r0 . Ap
+            acc[0] += q.x * w.x + q.y * w.y;
+            acc[1] += q.x * w.y - q.y * w.x;
+        } else if (SNK == SNK_AT || SNK == SNK_AT_DEF) {
+            R.At[o] = w;
+            acc[0] += w.x * vv.x + w.y * vv.y;  // At . t
+            acc[1] += w.x * vv.y - w.y * vv.x;
+            acc[2] += w.x * w.x + w.y * w.y;    // At . At
+            if constexpr (SNK == SNK_AT_DEF) {  // r0 . t, r0 . At, t . t
+                const cx<T> q = R.r0[o];
+                acc[3] += q.x * vv.x + q.y * vv.y;
+                acc[4] += q.x * vv.y - q.y * vv.x;
+                acc[5] += q.x * w.x + q.y * w.y;
+                acc[6] += q.x * w.y - q.y * w.x;
+                acc[7] += vv.x * vv.x + vv.y * vv.y;
+            }
+        } else if (SNK == SNK_RES) {
+            const cx<T> rr = csub<T>(R.E[o], w);
+            R.r[o] = rr;
+            R.r0[o] = rr;
+            R.p[o] = rr;
+            acc[0] += rr.x * rr.x + rr.y * rr.y;
+        }
+    }
+    if (SNK == SNK_OUT || SNK == SNK_ALB) return;
+    double tot[NV];
+    const int slot = SNK == SNK_AP ? 0 : (SNK == SNK_AT || SNK == SNK_AT_DEF ? 1 : 2);
+    if (!last_block_total<NV>(acc, R.part, gridDim.x, blockIdx.x, R.cnt + slot, sred, tot)) return;
+    if (threadIdx.x != 0) return;
+    finalize_sink<T, SNK, NV>(R.st, tot);
+}
+
+template <typename T, int MY, int MZ> struct ZyLaunch {
+    // pass: PASS_ZFWD (k_zyfwd, mode = SrcMode) or PASS_ZINV (k_yzinv, mode = SnkMode)
+    static cudaError_t run(int pass, int mode, const PassArgs<T>& a) {
+        const dim3 grid(3 * a.g.Nx, a.nrhs);
+        const size_t sm = ZyPlane<T, MY, MZ>::smem;
+        const Geom& g = a.g;
+        if (pass == PASS_ZFWD) {
+            switch (mode) {
+                case SRC_IN: k_zyfwd<T, SRC_IN, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
+                case SRC_PUPD: k_zyfwd<T, SRC_PUPD, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
+                case SRC_TUPD: k_zyfwd<T, SRC_TUPD, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
+                case SRC_PUPD_DEF: k_zyfwd<T, SRC_PUPD_DEF, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
+                default: k_zyfwd<T, SRC_P, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
+            }
+        } else {
+            switch (mode) {
+                case SNK_OUT: k_yzinv<T, SRC_IN, SNK_OUT, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
+                case SNK_ALB: k_yzinv<T, SRC_IN, SNK_ALB, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
+                case SNK_AP: k_yzinv<T, SRC_PUPD, SNK_AP, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
+                case SNK_AT: k_yzinv<T, SRC_TUPD, SNK_AT, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
+                case SNK_AT_DEF: k_yzinv<T, SRC_TUPD, SNK_AT_DEF, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
+                default: k_yzinv<T, SRC_P, SNK_RES, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
+            }
+        }
+        return cudaGetLastError();
+    }
+    static cudaError_t configure() {
+        const void* ks[] = {(const void*)k_zyfwd<T, SRC_IN, MY, MZ>, (const void*)k_zyfwd<T, SRC_PUPD, MY, MZ>,
+                            (const void*)k_zyfwd<T, SRC_TUPD, MY, MZ>, (const void*)k_zyfwd<T, SRC_P, MY, MZ>,
+                            (const void*)k_zyfwd<T, SRC_PUPD_DEF, MY, MZ>, (const void*)k_yzinv<T, SRC_TUPD, SNK_AT_DEF, MY, MZ>,
+                            (const void*)k_yzinv<T, SRC_IN, SNK_OUT, MY, MZ>, (const void*)k_yzinv<T, SRC_IN, SNK_ALB, MY, MZ>,
+                            (const void*)k_yzinv<T, SRC_PUPD, SNK_AP, MY, MZ>, (const void*)k_yzinv<T, SRC_TUPD, SNK_AT, MY, MZ>,
+                            (const void*)k_yzinv<T, SRC_P, SNK_RES, MY, MZ>};
+        for (const void* k : ks) {
+            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxPassSmem);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
+};
 
 // ------------------------------------------------------------ launchers
 // Launches pass `pass` (PASS_*) of an A-product for the length CM (0: runtime).
@@ -312,6 +528,7 @@ template <typename T, int CM> struct PassLaunch {
                     case SRC_IN: k_zfwd<T, SRC_IN, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid); break;
                     case SRC_PUPD: k_zfwd<T, SRC_PUPD, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid); break;
                     case SRC_TUPD: k_zfwd<T, SRC_TUPD, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid); break;
+                    case SRC_PUPD_DEF: k_zfwd<T, SRC_PUPD_DEF, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid); break;
                     default: k_zfwd<T, SRC_P, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid); break;
                 }
             } else {
@@ -320,6 +537,7 @@ template <typename T, int CM> struct PassLaunch {
                     case SNK_ALB: k_zinv<T, SRC_IN, SNK_ALB, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid); break;
                     case SNK_AP: k_zinv<T, SRC_PUPD, SNK_AP, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid); break;
                     case SNK_AT: k_zinv<T, SRC_TUPD, SNK_AT, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid); break;
+                    case SNK_AT_DEF: k_zinv<T, SRC_TUPD, SNK_AT_DEF, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid); break;
                     default: k_zinv<T, SRC_P, SNK_RES, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid); break;
                 }
             }
@@ -356,6 +574,7 @@ template <typename T, int CM> struct PassLaunch {
     static cudaError_t configure_z() {
         const void* ks[] = {(const void*)k_zfwd<T, SRC_IN, CM>, (const void*)k_zfwd<T, SRC_PUPD, CM>,
                             (const void*)k_zfwd<T, SRC_TUPD, CM>, (const void*)k_zfwd<T, SRC_P, CM>,
+                            (const void*)k_zfwd<T, SRC_PUPD_DEF, CM>, (const void*)k_zinv<T, SRC_TUPD, SNK_AT_DEF, CM>,
                             (const void*)k_zinv<T, SRC_IN, SNK_OUT, CM>, (const void*)k_zinv<T, SRC_IN, SNK_ALB, CM>,
                             (const void*)k_zinv<T, SRC_PUPD, SNK_AP, CM>, (const void*)k_zinv<T, SRC_TUPD, SNK_AT, CM>,
                             (const void*)k_zinv<T, SRC_P, SNK_RES, CM>};

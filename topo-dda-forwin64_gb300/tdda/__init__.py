@@ -42,7 +42,7 @@ EXPORTS = [
     "tdda_model_update_alpha", "tdda_model_update_alpha_single", "tdda_model_change_E", "tdda_model_reset_E",
     "tdda_model_initialize_P", "tdda_model_aproduct_with_alb", "tdda_model_bicgstab", "tdda_model_solve_mixed",
     "tdda_model_update_E_in_structure", "tdda_model_get", "tdda_model_iterations", "tdda_solve_batch",
-    "tdda_fft3d", "tdda_core_stream", "tdda_kernel_launches", "tdda_profile_aproduct",
+    "tdda_fft3d", "tdda_core_stream", "tdda_kernel_launches", "tdda_profile_aproduct", "tdda_core_pass_count",
     "tdda_aproduct_noalloc", "tdda_server_create", "tdda_server_submit", "tdda_server_result",
     "tdda_server_stats", "tdda_server_clock", "tdda_server_destroy", "tdda_request_bytes",
 ]
@@ -136,6 +136,7 @@ def load() -> ctypes.CDLL:
         "tdda_core_stream": (i, [vp, ctypes.POINTER(vp)]),
         "tdda_kernel_launches": (ctypes.c_ulonglong, []),
         "tdda_profile_aproduct": (i, [vp, i, i, i, dp]),
+        "tdda_core_pass_count": (i, [vp, i]),
         "tdda_aproduct_noalloc": (i, [vp, vp, vp]),
         "tdda_server_create": (i, [ctypes.POINTER(ServerDesc), ctypes.POINTER(vp)]),
         "tdda_server_submit": (i, [vp, ctypes.POINTER(RequestDesc), ctypes.POINTER(ctypes.c_ulonglong)]),
@@ -236,6 +237,13 @@ class AProductCore:
         p = ctypes.c_void_p()
         _check(load().tdda_core_stream(self.h, ctypes.byref(p)), "tdda_core_stream")
         return p.value or 0
+
+    def pass_count(self, precision: int = FP32_REFINE) -> int:
+        """Kernels of one A-product: 5, or 3 when the z and y passes are fused."""
+        n = load().tdda_core_pass_count(self.h, int(precision))
+        if n < 0:
+            raise ValueError(f"pass_count: invalid precision {precision}")
+        return n
 
     def profile_aproduct(self, precision: int = FP32_REFINE, nrhs: int = 1, reps: int = 10) -> list:
         """Average ms of the five passes of one A-product (CUDA events on the core stream)."""
