@@ -450,6 +450,7 @@ SolveState fresh_state(double tol, int max_it, int iterations) {
     s.iterations = iterations;
     s.status = tdda::ST_RUNNING;
     s.init = 1;
+    s.tol32 = (float)tol;
     return s;
 }
 
@@ -768,6 +769,8 @@ tdda_status tdda_core_create(const tdda_core_desc* desc, tdda_core** out) {
         }
         cell = i;
     }
+    g.dense = 1;
+    for (size_t k = 0; k < cellmap.size() && g.dense; k++) g.dense = cellmap[k] == (int)k;
     // FFT length per axis: smallest 7-smooth >= 2N-1 (the reference's
     // 2N-1, AProductCore.cpp:41-43, gives the same linear convolution)
     int Ms[3] = {smooth_size(2 * g.Nx - 1), smooth_size(2 * g.Ny - 1), smooth_size(2 * g.Nz - 1)};

@@ -111,35 +111,42 @@ template <typename T> using acc_t = typename std::conditional<sizeof(T) == 4, fl
 // (a.x + a.y) + (b.x + b.y) as a double-float pair (TwoSum of the high parts,
 // D. E. Knuth, TAOCP vol. 2, 4.2.2; the low parts added; renormalised)
 __device__ __forceinline__ float2 df_add(float2 a, float2 b) {
-    const float s = a.x + b.x;
-    const float bp = s - a.x;
-    const float e = (a.x - (s - bp)) + (b.x - bp);
-    const float lo = e + a.y + b.y;
-    const float hi = s + lo;
-    return make_float2(hi, lo - (hi - s));
+    // explicit round-to-nearest operations: no contraction or reassociation
+    const float s = __fadd_rn(a.x, b.x);
+    const float bp = __fsub_rn(s, a.x);
+    const float e = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bp)), __fsub_rn(b.x, bp));
+    const float lo = __fadd_rn(__fadd_rn(e, a.y), b.y);
+    const float hi = __fadd_rn(s, lo);
+    return make_float2(hi, __fsub_rn(lo, __fsub_rn(hi, s)));
 }
 
-// Block sum of double-float values; the result is valid in thread 0.
-// sred must hold 32 * NV float2.
+// Block sum of double-float values, result in v[] of every thread.  Each
+// warp sums its lanes with a shuffle tree, then warp k adds the per-warp sums
+// of value k with a second tree (NV <= warps per block), so no thread runs a
+// serial loop.  sred must hold 32 * NV float2; the caller puts a barrier
+// between two calls on the same sred.
 template <int NV> __device__ __forceinline__ void block_sum(float2 (&v)[NV], float2* sred) {
+    static_assert(NV <= kNT / 32, "one warp per summed value");
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
     for (int k = 0; k < NV; k++) {
         float2 a = v[k];
+#pragma unroll
         for (int o = 16; o > 0; o >>= 1)
             a = df_add(a, make_float2(__shfl_down_sync(0xffffffffu, a.x, o), __shfl_down_sync(0xffffffffu, a.y, o)));
         if (lane == 0) sred[k * 32 + warp] = a;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (warp < NV) {
+        float2 a = lane < nw ? sred[warp * 32 + lane] : make_float2(0.f, 0.f);
 #pragma unroll
-        for (int k = 0; k < NV; k++) {
-            float2 a = sred[k * 32];
-            for (int w = 1; w < nw; w++) a = df_add(a, sred[k * 32 + w]);
-            v[k] = a;
-        }
+        for (int o = 16; o > 0; o >>= 1)
+            a = df_add(a, make_float2(__shfl_down_sync(0xffffffffu, a.x, o), __shfl_down_sync(0xffffffffu, a.y, o)));
+        if (lane == 0) sred[warp * 32] = a;
     }
     __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; k++) v[k] = sred[k * 32];
 }
 
 // Publish this block's sums (valid in thread 0); the last block of the grid
@@ -178,21 +185,20 @@ __device__ bool last_block_total(double (&v)[NV], double* part, int nblk, int bi
     return publish_total<NV>(v, part, nblk, bid, cnt, sred, tot);
 }
 // FP32 partials: double-float block and grid sums; the partial slots hold one
-// float2 (hi, lo) each.  tot = hi + lo in FP64 (valid in thread 0).  sred
-// must hold 32 * NV float2, i.e. 32 * NV doubles (a float2 is 8 bytes).
+// float2 (hi, lo) each.  tot: the double-float totals (valid in thread 0).
+// sred must hold 32 * NV float2, i.e. 32 * NV doubles (a float2 is 8 bytes).
 template <int NV>
 __device__ bool last_block_total(float (&v)[NV], double* part, int nblk, int bid, unsigned int* cnt, double* sred,
-                                 double (&tot)[NV]) {
+                                 float2 (&tot)[NV]) {
     __shared__ int s_last;
     float2* sr2 = reinterpret_cast<float2*>(sred);
     float2* part2 = reinterpret_cast<float2*>(part);
-    float2 a[NV];
 #pragma unroll
-    for (int k = 0; k < NV; k++) a[k] = make_float2(v[k], 0.f);
-    block_sum<NV>(a, sr2);
+    for (int k = 0; k < NV; k++) tot[k] = make_float2(v[k], 0.f);
+    block_sum<NV>(tot, sr2);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int k = 0; k < NV; k++) part2[k * nblk + bid] = a[k];
+        for (int k = 0; k < NV; k++) part2[k * nblk + bid] = tot[k];
         __threadfence();
         unsigned int prev = atomicAdd(cnt, 1u);
         s_last = (prev == (unsigned int)(nblk - 1));
@@ -204,16 +210,15 @@ __device__ bool last_block_total(float (&v)[NV], double* part, int nblk, int bid
     for (int k = 0; k < NV; k++) {
         float2 q = make_float2(0.f, 0.f);
         for (int i = threadIdx.x; i < nblk; i += blockDim.x) q = df_add(q, __ldcg(part2 + k * nblk + i));
-        a[k] = q;
+        tot[k] = q;
     }
-    block_sum<NV>(a, sr2);
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int k = 0; k < NV; k++) tot[k] = (double)a[k].x + (double)a[k].y;
-        *cnt = 0u;
-    }
+    block_sum<NV>(tot, sr2);
+    if (threadIdx.x == 0) *cnt = 0u;
     return true;
 }
+
+// grid totals of a reduction kernel: FP64, or double-float pairs for FP32
+template <typename T> using tot_t = typename std::conditional<sizeof(T) == 4, float2, double>::type;
 
 // Shared scratch of a reduction kernel, in doubles: NV * nt for the FP64
 // block sum, 32 * NV float2 (8 bytes each, one per warp slot) for the
@@ -282,12 +287,10 @@ __device__ __forceinline__ void finish_step_deferred(SolveState* st, const doubl
     finish_step(st, rho, rn2, init);
 }
 
-// The FP32 inner solve forms its step scalars with FP32 division and square
-// root (its kernels use them in FP32); only the cancelling differences
-// r0.t - zeta r0.At and t.t - ... stay FP64 multiply-adds.  The state keeps
-// doubles.
-__device__ __forceinline__ float2 to_f2(double2 a) { return make_float2((float)a.x, (float)a.y); }
-__device__ __forceinline__ double2 to_d2(float2 a) { return make_double2(a.x, a.y); }
+// The FP32 inner solve forms its step scalars in FP32 from the hi parts of
+// the double-float totals (its kernels use them in FP32), and keeps them in
+// the FP32 fields of the state; nothing on its critical path touches the
+// FP64 pipe.
 __device__ __forceinline__ float2 fmul2(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 __device__ __forceinline__ float2 fdiv2(float2 a, float2 b) {
     // Smith's algorithm (R. L. Smith, CACM 5(8), 1962)
@@ -299,14 +302,14 @@ __device__ __forceinline__ float2 fdiv2(float2 a, float2 b) {
     return make_float2((a.x * r + a.y) / den, (a.y * r - a.x) / den);
 }
 
-__device__ __forceinline__ void finish_step_f32(SolveState* st, double2 rho, double rn2, bool is_init) {
-    st->rho_prev = st->rho;
-    st->rho = rho;
-    st->rnorm2 = rn2;
-    const float err = sqrtf((float)rn2) / (float)st->Enorm;
+// finish_step for the FP32 state
+__device__ __forceinline__ void finish_step_f32(SolveState* st, float2 rho, float rn2, bool is_init) {
+    st->rho_prev32 = st->rho32;
+    st->rho32 = rho;
+    const float err = sqrtf(rn2) / st->Enorm32;
     if (!is_init) {
         st->it += 1;
-        if (err <= (float)st->tol) {  // DDAModel.cpp:232-235
+        if (err <= st->tol32) {  // DDAModel.cpp:232-235
             st->status = ST_CONVERGED;
             st->iterations = st->it;
             st->error = err;
@@ -318,31 +321,35 @@ __device__ __forceinline__ void finish_step_f32(SolveState* st, double2 rho, dou
         st->error = err;
         return;
     }
-    if (st->rho_prev.x == 0.0 && st->rho_prev.y == 0.0) {  // DDAModel.cpp:193-215
+    if (st->rho_prev32.x == 0.f && st->rho_prev32.y == 0.f) {  // DDAModel.cpp:193-215
         st->status = ST_BREAKDOWN;
         st->iterations = st->it + 1;
         st->error = err;
         return;
     }
-    const float2 beta = fdiv2(fmul2(fdiv2(to_f2(st->alpha), to_f2(st->zeta)), to_f2(rho)), to_f2(st->rho_prev));
-    st->beta = to_d2(beta);
+    const float2 beta = fdiv2(fmul2(fdiv2(st->alpha32, st->zeta32), rho), st->rho_prev32);  // DDAModel.cpp:218
+    st->beta32 = beta;
     if (!isfinite(rho.x) || !isfinite(rho.y) || !isfinite(err) || !isfinite(beta.x) || !isfinite(beta.y)) {
         st->status = ST_NAN;
         st->error = err;
     }
 }
 
-__device__ __forceinline__ void finish_step_deferred_f32(SolveState* st, const double (&tot)[8]) {
-    const double2 Att = make_double2(tot[0], tot[1]);
-    const double AtAt = tot[2];
-    const double2 r0t = make_double2(tot[3], tot[4]), r0At = make_double2(tot[5], tot[6]);
-    const double tt = tot[7];
-    const double2 zeta = to_d2(fdiv2(to_f2(Att), make_float2((float)AtAt, 0.f)));
-    st->zeta = zeta;
-    const double2 zr = dmul(zeta, r0At);
-    const double2 rho = make_double2(r0t.x - zr.x, r0t.y - zr.y);
-    double rn2 = tt - 2.0 * (zeta.x * Att.x + zeta.y * Att.y) + (zeta.x * zeta.x + zeta.y * zeta.y) * AtAt;
-    if (!(rn2 > 0.0)) rn2 = isnan(rn2) ? rn2 : 0.0;
+// The deferred step end (SNK_AT_DEF) on FP32 state: zeta = At.t / At.At,
+// r0.r = r0.t - zeta r0.At, |r|^2 = t.t - 2 Re(conj(zeta) At.t) + |zeta|^2 At.At.
+// The cancelling differences lose at most ~1e-7 t.t, the size of the FP32
+// rounding of t itself; the outer FP64 residual check bounds the result.
+__device__ __forceinline__ void finish_step_deferred_f32(SolveState* st, const float2 (&tot)[8]) {
+    const float2 Att = make_float2(tot[0].x, tot[1].x);
+    const float AtAt = tot[2].x;
+    const float2 r0t = make_float2(tot[3].x, tot[4].x), r0At = make_float2(tot[5].x, tot[6].x);
+    const float tt = tot[7].x;
+    const float2 zeta = fdiv2(Att, make_float2(AtAt, 0.f));  // DDAModel.cpp:225
+    st->zeta32 = zeta;
+    const float2 zr = fmul2(zeta, r0At);
+    const float2 rho = make_float2(r0t.x - zr.x, r0t.y - zr.y);
+    float rn2 = tt - 2.f * (zeta.x * Att.x + zeta.y * Att.y) + (zeta.x * zeta.x + zeta.y * zeta.y) * AtAt;
+    if (!(rn2 > 0.f)) rn2 = isnan(rn2) ? rn2 : 0.f;
     const bool init = st->init != 0;
     st->init = 0;
     st->pending = 1;
@@ -350,21 +357,35 @@ __device__ __forceinline__ void finish_step_deferred_f32(SolveState* st, const d
 }
 
 // The scalars a sink pass forms from its grid totals (thread 0 of the last block).
-template <typename T, int SNK, int NV> __device__ __forceinline__ void finalize_sink(SolveState* st, const double (&tot)[NV]) {
-    if constexpr (SNK == SNK_RES) {
-        st->rho = make_double2(tot[0], 0.0);  // r0 . r with r0 = r
-        st->rnorm2 = tot[0];
-    } else if constexpr (sizeof(T) == 4) {
-        if constexpr (SNK == SNK_AT_DEF) finish_step_deferred_f32(st, tot);
-        else if constexpr (SNK == SNK_AP) st->alpha = to_d2(fdiv2(to_f2(st->rho), make_float2((float)tot[0], (float)tot[1])));
-        else if constexpr (SNK == SNK_AT)
-            st->zeta = to_d2(fdiv2(make_float2((float)tot[0], (float)tot[1]), make_float2((float)tot[2], 0.f)));
+template <typename T, int SNK, int NV> __device__ __forceinline__ void finalize_sink(SolveState* st, const tot_t<T> (&tot)[NV]) {
+    if constexpr (sizeof(T) == 4) {
+        if constexpr (SNK == SNK_RES) st->rho32 = make_float2(tot[0].x, 0.f);
+        else if constexpr (SNK == SNK_AT_DEF) finish_step_deferred_f32(st, tot);
+        else if constexpr (SNK == SNK_AP) st->alpha32 = fdiv2(st->rho32, make_float2(tot[0].x, tot[1].x));
+        else if constexpr (SNK == SNK_AT) st->zeta32 = fdiv2(make_float2(tot[0].x, tot[1].x), make_float2(tot[2].x, 0.f));
     } else {
-        if constexpr (SNK == SNK_AT_DEF) finish_step_deferred(st, tot);
-        else if constexpr (SNK == SNK_AP) st->alpha = cdiv(st->rho, make_double2(tot[0], tot[1]));  // DDAModel.cpp:221
-        else if constexpr (SNK == SNK_AT)
+        if constexpr (SNK == SNK_RES) {
+            st->rho = make_double2(tot[0], 0.0);  // r0 . r with r0 = r
+            st->rnorm2 = tot[0];
+        } else if constexpr (SNK == SNK_AT_DEF) {
+            finish_step_deferred(st, tot);
+        } else if constexpr (SNK == SNK_AP) {
+            st->alpha = cdiv(st->rho, make_double2(tot[0], tot[1]));  // DDAModel.cpp:221
+        } else if constexpr (SNK == SNK_AT) {
             st->zeta = cdiv(make_double2(tot[0], tot[1]), make_double2(tot[2], 0.0));  // DDAModel.cpp:225
+        }
     }
+}
+
+// step scalars as the kernels of precision T use them
+template <typename T> __device__ __forceinline__ cx<T> st_alpha(const SolveState* s) {
+    if constexpr (sizeof(T) == 4) return s->alpha32; else return s->alpha;
+}
+template <typename T> __device__ __forceinline__ cx<T> st_beta(const SolveState* s) {
+    if constexpr (sizeof(T) == 4) return s->beta32; else return s->beta;
+}
+template <typename T> __device__ __forceinline__ cx<T> st_zeta(const SolveState* s) {
+    if constexpr (sizeof(T) == 4) return s->zeta32; else return s->zeta;
 }
 
 __device__ __forceinline__ bool rhs_done(const SolveState* st) {

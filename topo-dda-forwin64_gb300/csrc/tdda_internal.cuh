@@ -23,6 +23,8 @@ struct Geom {
     AxisPlan px, py, pz;
     int Hx, Hy, Hz;    // folded Green extents
     long long sy, sx, sc, sb;  // grid strides (y, x, component, rhs) in elements
+    int dense;         // 1: the full box in build_a_bulk order, dipole (x Ny + y) Nz + z
+                       // in every cell (tools.cpp:497-510), so no cellmap lookup
 };
 
 // solver status values (mirrored in include/tdda.h)
@@ -43,6 +45,10 @@ struct SolveState {
     int iterations;    // ITERATION as the reference reports it
     int init;          // the next step finalisation is the initial one (no convergence check)
     int pending;       // deferred update of P and r not yet applied (FP32 inner solve)
+    // The FP32 inner solve keeps its step scalars in FP32 (its kernels use
+    // them so): no FP64 conversion or arithmetic on its critical path.
+    float2 alpha32, beta32, zeta32, rho32, rho_prev32;
+    float Enorm32, tol32;
 };
 
 // per right-hand side: the vectors of one solve (AoS [x,y,z] per dipole)

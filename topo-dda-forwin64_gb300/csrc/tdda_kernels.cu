@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(kNT) k_update(int n3, const RhsVecs<T>* __rest
     const int b = blockIdx.y;
     const RhsVecs<T> R = rhs[b];
     if (rhs_done(R.st)) return;
-    const cx<T> alpha = from_d<T>(R.st->alpha), zeta = from_d<T>(R.st->zeta);
+    const cx<T> alpha = st_alpha<T>(R.st), zeta = st_zeta<T>(R.st);
     acc_t<T> acc[4] = {0, 0, 0, 0};
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x) {
         const cx<T> Ap = R.Ap[e], r = R.r[e], p = R.p[e], t = R.t[e], At = R.At[e], r0 = R.r0[e];
@@ -52,10 +52,11 @@ __global__ void __launch_bounds__(kNT) k_update(int n3, const RhsVecs<T>* __rest
         acc[1] += r0.x * rn.y - r0.y * rn.x;
         acc[2] += rn.x * rn.x + rn.y * rn.y;
     }
-    double tot[4];
+    tot_t<T> tot[4];
     if (!last_block_total<4>(acc, R.part, gridDim.x, blockIdx.x, R.cnt + 3, sred, tot)) return;
     if (threadIdx.x != 0) return;
-    finish_step(R.st, make_double2(tot[0], tot[1]), tot[2], is_init != 0);
+    if constexpr (sizeof(T) == 4) finish_step_f32(R.st, make_float2(tot[0].x, tot[1].x), tot[2].x, is_init != 0);
+    else finish_step(R.st, make_double2(tot[0], tot[1]), tot[2], is_init != 0);
 }
 
 // The deferred update of the last step (SNK_AT_DEF) for every right-hand side
@@ -64,7 +65,7 @@ __global__ void __launch_bounds__(kNT) k_update(int n3, const RhsVecs<T>* __rest
 template <typename T> __global__ void __launch_bounds__(kNT) k_finish(int n3, const RhsVecs<T>* __restrict__ rhs) {
     const RhsVecs<T> R = rhs[blockIdx.y];
     if (R.st == nullptr || !R.st->pending) return;
-    const cx<T> alpha = from_d<T>(R.st->alpha), zeta = from_d<T>(R.st->zeta);
+    const cx<T> alpha = st_alpha<T>(R.st), zeta = st_zeta<T>(R.st);
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x) {
         const cx<T> u = cmul<T>(zeta, R.Ap[e]);
         const cx<T> r = R.r[e];
@@ -91,13 +92,18 @@ __global__ void __launch_bounds__(kNT) k_solve_begin(int n3, const RhsVecs<T>* _
             R.p[e] = v;
         }
     }
-    double tot[4];
+    tot_t<T> tot[4];
     if (!last_block_total<4>(acc, R.part, gridDim.x, blockIdx.x, R.cnt + 4, sred, tot)) return;
     if (threadIdx.x != 0) return;
-    R.st->Enorm = sqrt(tot[0]);
-    if (resid_is_rhs) {
-        R.st->rho = make_double2(tot[0], 0.0);
-        R.st->rnorm2 = tot[0];
+    if constexpr (sizeof(T) == 4) {
+        R.st->Enorm32 = sqrtf(tot[0].x);
+        if (resid_is_rhs) R.st->rho32 = make_float2(tot[0].x, 0.f);
+    } else {
+        R.st->Enorm = sqrt(tot[0]);
+        if (resid_is_rhs) {
+            R.st->rho = make_double2(tot[0], 0.0);
+            R.st->rnorm2 = tot[0];
+        }
     }
 }
 

@@ -6,10 +6,27 @@ namespace tdda {
 
 bool ct_has_xy(int M) { return M == 40 || M == 128 || M == 160 || M == 192; }
 
+// z-columns per block of the register-form x pass (k_xpass2), per length
+template <int M> constexpr int xpass2_tile() { return M == 128 ? 16 : 8; }
+
 template <typename T> bool pass_ct_xy(int pass, int mode, const PassArgs<T>& a, cudaError_t* err) {
     (void)mode;
     const bool y = pass == PASS_YFWD || pass == PASS_YINV;
     if (!y && pass != PASS_XPASS) return false;
+    if constexpr (sizeof(T) == 4) {  // FP32: the register form on the two-stage plans
+        if (!y) {
+            switch (a.g.px.M) {
+#define TDDA_X2(M)                                                                       \
+    case M: *err = dev::XLaunch2<T, M, xpass2_tile<M>()>::run(a); return true;
+                TDDA_X2(40)
+                TDDA_X2(128)
+                TDDA_X2(160)
+                TDDA_X2(192)
+#undef TDDA_X2
+                default: break;
+            }
+        }
+    }
     switch (y ? a.g.py.M : a.g.px.M) {
 #define TDDA_XY(M)                                                                                      \
     case M:                                                                                             \
@@ -36,6 +53,10 @@ cudaError_t configure_pass_ct_xy() {
     if (!e) e = dev::PassLaunch<double, 128>::configure_xy();
     if (!e) e = dev::PassLaunch<double, 160>::configure_xy();
     if (!e) e = dev::PassLaunch<double, 192>::configure_xy();
+    if (!e) e = dev::XLaunch2<float, 40, xpass2_tile<40>()>::configure();
+    if (!e) e = dev::XLaunch2<float, 128, xpass2_tile<128>()>::configure();
+    if (!e) e = dev::XLaunch2<float, 160, xpass2_tile<160>()>::configure();
+    if (!e) e = dev::XLaunch2<float, 192, xpass2_tile<192>()>::configure();
     return e;
 }
 

@@ -55,9 +55,9 @@ __global__ void __launch_bounds__(kNT) k_zfwd(Geom g, const RhsVecs<T>* __restri
     const int nl = min(LZ, nlines - l0);
 
     cx<T> beta, alpha, zeta;
-    if (SRC == SRC_PUPD || SRC == SRC_PUPD_DEF) beta = from_d<T>(R.st->beta);
-    if (SRC == SRC_TUPD || SRC == SRC_PUPD_DEF) alpha = from_d<T>(R.st->alpha);
-    if (SRC == SRC_PUPD_DEF) zeta = from_d<T>(R.st->zeta);
+    if (SRC == SRC_PUPD || SRC == SRC_PUPD_DEF) beta = st_beta<T>(R.st);
+    if (SRC == SRC_TUPD || SRC == SRC_PUPD_DEF) alpha = st_alpha<T>(R.st);
+    if (SRC == SRC_PUPD_DEF) zeta = st_zeta<T>(R.st);
     const cx<T>* src = SRC == SRC_IN ? R.p : R.P;
     for (int e = threadIdx.x; e < nl * Nz; e += blockDim.x) {
         const int line = e / Nz, z = e - (e / Nz) * Nz;
@@ -222,6 +222,137 @@ __global__ void __launch_bounds__(kNT) k_xpass(Geom g, const RhsVecs<T>* __restr
     }
 }
 
+// ------------------------------------------------------------ K3, register form
+// x pass for an FFT length with a two-stage plan M = R1 R2 (the FP32 plans of
+// tdda_fft_ct.cuh).  Stockham order: the forward's first stage (radix R1,
+// butterfly j < R2) reads x = j + R2 r and writes j R1 + q; its second stage
+// (radix R2, butterfly j < R1, twiddles w^(r j)) leaves the spectrum at
+// kx = j + R1 q in the registers of one thread; the inverse's first stage
+// (radix R2, no twiddles) needs exactly those values, so the second forward
+// stage, the spectral product and the first inverse stage run in registers,
+// for the three components of one (y, z) column.  The first and last stages
+// read and write the grid directly.  Two shared-memory round trips instead of
+// six, three barriers.  One block: ZT z-columns of one y row, NT = ZT R1
+// threads (one register-stage task each).
+template <typename T, int M, int ZT>
+__global__ void __launch_bounds__(ZT * ct_radix(M, 0, true)) k_xpass2(Geom g, const RhsVecs<T>* __restrict__ rhs,
+                                                                   const cx<T>* __restrict__ green,
+                                                                   const cx<T>* __restrict__ twx,
+                                                                   cx<T>* __restrict__ grid) {
+    constexpr int R1 = ct_radix(M, 0, true), R2 = ct_radix(M, 1, true);
+    static_assert(ct_nstages(M, true) == 2 && R1 * R2 == M, "two-stage plan");
+    constexpr int NT = ZT * R1, W = 3 * ZT, WP = W + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<T>* stw = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* s = stw + M;  // [M][WP]
+    const int b = blockIdx.y;
+    if (rhs_done(rhs[b].st)) return;
+    const int My = g.py.M, Mz = g.pz.M, Nx = g.Nx;
+    const int nzt = (Mz + ZT - 1) / ZT;
+    const int y = blockIdx.x / nzt, z0 = (blockIdx.x - y * nzt) * ZT;
+    const int zn = min(ZT, Mz - z0);
+    stage_tw<T>(stw, twx, M);
+    cx<T>* gp = grid + (long long)b * g.sb + (long long)y * g.sy + z0;
+
+    // forward stage 1: radix R1 over x = j + R2 r < Nx, grid -> s[j R1 + q][line]
+    for (int w = threadIdx.x; w < W * R2; w += NT) {
+        const int l = w % W, j = w / W;
+        const int c = l / ZT, zl = l - c * ZT;
+        const cx<T>* src = gp + c * g.sc + zl;
+        cx<T> v[R1];
+#pragma unroll
+        for (int r = 0; r < R1; r++) {
+            const int xx = j + R2 * r;
+            v[r] = (zl < zn && xx < Nx) ? src[(long long)xx * g.sx] : czero<T>();
+        }
+        Bfly<R1, -1, T>::run(v);
+#pragma unroll
+        for (int q = 0; q < R1; q++) s[(j * R1 + q) * WP + l] = v[q];
+    }
+    __syncthreads();
+
+    // forward stage 2, spectral product, inverse stage 1: task (zl, j), j < R1
+    const int zl = threadIdx.x % ZT, j = threadIdx.x / ZT;
+    cx<T> X[3][R2];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+#pragma unroll
+        for (int r = 0; r < R2; r++) {
+            cx<T> t = s[(j + R1 * r) * WP + c * ZT + zl];
+            if (r > 0) t = cmul<T>(t, stw[r * j]);
+            X[c][r] = t;
+        }
+        Bfly<R2, -1, T>::run(X[c]);  // X[c][q]: spectrum at kx = j + R1 q
+    }
+    if (zl < zn) {  // columns past Mz (a partial tile) hold zeros and are never stored
+        const int z = z0 + zl;
+        const int fy = fold(y, My), fz = fold(z, Mz);
+        const bool uy = 2 * y > My, uz = 2 * z > Mz;
+#pragma unroll
+        for (int q = 0; q < R2; q++) {
+            const int kx = j + R1 * q;
+            const int fx = fold(kx, M);
+            const bool ux = 2 * kx > M;
+            cx<T> a0, a1, a2, a3, a4, a5;
+            load_green6<T>(green + (((long long)fy * g.Hx + fx) * g.Hz + fz) * 6, a0, a1, a2, a3, a4, a5);
+            if (ux != uy) a1 = mk<T>(-a1.x, -a1.y);  // xy: odd in x and y
+            if (ux != uz) a2 = mk<T>(-a2.x, -a2.y);  // xz: odd in x and z
+            if (uy != uz) a4 = mk<T>(-a4.x, -a4.y);  // yz: odd in y and z
+            const cx<T> bx = X[0][q], by = X[1][q], bz = X[2][q];
+            X[0][q] = cadd<T>(cadd<T>(cmul<T>(a0, bx), cmul<T>(a1, by)), cmul<T>(a2, bz));
+            X[1][q] = cadd<T>(cadd<T>(cmul<T>(a1, bx), cmul<T>(a3, by)), cmul<T>(a4, bz));
+            X[2][q] = cadd<T>(cadd<T>(cmul<T>(a2, bx), cmul<T>(a4, by)), cmul<T>(a5, bz));
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) Bfly<R2, +1, T>::run(X[c]);  // inverse stage 1: outputs j R2 + q
+    __syncthreads();  // every stage-2 read of s is done
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+#pragma unroll
+        for (int q = 0; q < R2; q++) s[(j * R2 + q) * WP + c * ZT + zl] = X[c][q];
+    __syncthreads();
+
+    // inverse stage 2: radix R1, butterfly j < R2, twiddles conj(w^(r j)), outputs x = j + R2 q < Nx
+    for (int w = threadIdx.x; w < W * R2; w += NT) {
+        const int l = w % W, jj = w / W;
+        const int c = l / ZT, zz = l - c * ZT;
+        cx<T> v[R1];
+#pragma unroll
+        for (int r = 0; r < R1; r++) {
+            cx<T> t = s[(jj + R2 * r) * WP + l];
+            if (r > 0) {
+                cx<T> tw = stw[r * jj];
+                tw.y = -tw.y;
+                t = cmul<T>(t, tw);
+            }
+            v[r] = t;
+        }
+        Bfly<R1, +1, T>::run(v);
+        cx<T>* dst = gp + c * g.sc + zz;
+#pragma unroll
+        for (int q = 0; q < R1; q++) {
+            const int xx = jj + R2 * q;
+            if (zz < zn && xx < Nx) dst[(long long)xx * g.sx] = v[q];
+        }
+    }
+}
+
+template <typename T, int M, int ZT> struct XLaunch2 {
+    static constexpr int NT = ZT * ct_radix(M, 0, true);
+    static constexpr size_t smem = sizeof(cx<T>) * (size_t)(M + M * (3 * ZT + 1));
+    static cudaError_t run(const PassArgs<T>& a) {
+        const Geom& g = a.g;
+        const dim3 grid(g.py.M * ((g.pz.M + ZT - 1) / ZT), a.nrhs);
+        k_xpass2<T, M, ZT><<<grid, NT, smem, a.stream>>>(g, a.rhs, a.green, a.twx, a.grid);
+        return cudaGetLastError();
+    }
+    static cudaError_t configure() {
+        return cudaFuncSetAttribute((const void*)k_xpass2<T, M, ZT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kMaxPassSmem);
+    }
+};
+
 // ------------------------------------------------------------ K5 zinv
 template <typename T, int SRC, int SNK, int CM>
 __global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restrict__ rhs,
@@ -304,7 +435,7 @@ __global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restri
         }
     }
     if (SNK == SNK_OUT || SNK == SNK_ALB) return;
-    double tot[NV];
+    tot_t<T> tot[NV];
     const int nblk = gridDim.x;
     const int slot = SNK == SNK_AP ? 0 : (SNK == SNK_AT || SNK == SNK_AT_DEF ? 1 : 2);
     if (!last_block_total<NV>(acc, R.part, nblk, blockIdx.x, R.cnt + slot, sred, tot)) return;
@@ -321,6 +452,119 @@ __global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restri
 // (blockIdx.x / 3, blockIdx.x % 3).  Plane layout in shared memory: [y][z],
 // row stride ZP.  Lattice data occupies rows y < Ny <= LY and columns
 // z < Nz <= LZ (M >= 2N - 1 on every axis).
+// Gather of CH grid cells of one component: o[q] = 3 i + c of the dipole in
+// cell q, or -1 for an empty cell (v[q] = 0).  All loads come before the
+// first store.
+template <typename T, int SRC, int CH>
+__device__ __forceinline__ void gather_chunk(const RhsVecs<T>& R, const long long (&o)[CH], cx<T> (&v)[CH],
+                                             const cx<T>* src, cx<T> alpha, cx<T> beta, cx<T> zeta) {
+    if constexpr (SRC == SRC_PUPD_DEF) {
+        cx<T> Ap[CH], r[CH], p[CH], t[CH], At[CH], P[CH];
+#pragma unroll
+        for (int q = 0; q < CH; q++)
+            if (o[q] >= 0) {
+                Ap[q] = R.Ap[o[q]]; r[q] = R.r[o[q]]; p[q] = R.p[o[q]];
+                t[q] = R.t[o[q]]; At[q] = R.At[o[q]]; P[q] = R.P[o[q]];
+            }
+#pragma unroll
+        for (int q = 0; q < CH; q++) {
+            v[q] = czero<T>();
+            if (o[q] < 0) continue;
+            // the previous step's update (DDAModel.cpp:226-230), then p (DDAModel.cpp:219)
+            const cx<T> u = cmul<T>(zeta, Ap[q]);
+            const cx<T> z = csub<T>(cmul<T>(zeta, r[q]), cmul<T>(alpha, u));
+            R.P[o[q]] = cadd<T>(cadd<T>(P[q], cmul<T>(alpha, p[q])), z);
+            const cx<T> rn = csub<T>(t[q], cmul<T>(zeta, At[q]));
+            R.r[o[q]] = rn;
+            v[q] = cadd<T>(rn, cmul<T>(beta, csub<T>(p[q], u)));
+            R.p[o[q]] = v[q];
+        }
+    } else if constexpr (SRC == SRC_PUPD) {
+        cx<T> p[CH], u[CH], r[CH];
+#pragma unroll
+        for (int q = 0; q < CH; q++)
+            if (o[q] >= 0) { p[q] = R.p[o[q]]; u[q] = R.u[o[q]]; r[q] = R.r[o[q]]; }
+#pragma unroll
+        for (int q = 0; q < CH; q++) {
+            v[q] = czero<T>();
+            if (o[q] < 0) continue;
+            v[q] = cadd<T>(r[q], cmul<T>(beta, csub<T>(p[q], u[q])));
+            R.p[o[q]] = v[q];
+        }
+    } else if constexpr (SRC == SRC_TUPD) {
+        cx<T> r[CH], ap[CH];
+#pragma unroll
+        for (int q = 0; q < CH; q++)
+            if (o[q] >= 0) { r[q] = R.r[o[q]]; ap[q] = R.Ap[o[q]]; }
+#pragma unroll
+        for (int q = 0; q < CH; q++) {
+            v[q] = czero<T>();
+            if (o[q] < 0) continue;
+            v[q] = csub<T>(r[q], cmul<T>(alpha, ap[q]));
+            R.t[o[q]] = v[q];
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < CH; q++) v[q] = o[q] >= 0 ? src[o[q]] : czero<T>();
+    }
+}
+
+// Scatter of CH grid cells of one component (A v in res[slot[q]]) with the
+// sink's diagonal term, stores and dot-product terms.  All loads come before
+// the first store.
+template <typename T, int SRC, int SNK, int CH, int NV>
+__device__ __forceinline__ void scatter_chunk(const RhsVecs<T>& R, const long long (&o)[CH], const int (&slot)[CH],
+                                              const cx<T>* res, acc_t<T> (&acc)[NV]) {
+    const cx<T>* vsrc = (SRC == SRC_TUPD) ? R.t : (SRC == SRC_P ? R.P : R.p);
+    cx<T> val[CH], vv[CH], al[CH], q2[CH];
+#pragma unroll
+    for (int q = 0; q < CH; q++) {
+        if (o[q] < 0) continue;
+        val[q] = res[slot[q]];
+        if constexpr (SNK != SNK_OUT) { vv[q] = vsrc[o[q]]; al[q] = R.al[o[q]]; }
+        if constexpr (SNK == SNK_AP || SNK == SNK_AT_DEF) q2[q] = R.r0[o[q]];
+        if constexpr (SNK == SNK_RES) q2[q] = R.E[o[q]];
+    }
+#pragma unroll
+    for (int q = 0; q < CH; q++) {
+        if (o[q] < 0) continue;
+        if constexpr (SNK == SNK_OUT) {
+            R.Ap[o[q]] = val[q];
+            continue;
+        } else {
+            const cx<T> w = cadd<T>(val[q], cmul<T>(vv[q], al[q]));
+            if constexpr (SNK == SNK_ALB) {
+                R.Ap[o[q]] = w;
+            } else if constexpr (SNK == SNK_AP) {
+                R.Ap[o[q]] = w;
+                const cx<T> r0 = q2[q];  // r0 . Ap
+                acc[0] += r0.x * w.x + r0.y * w.y;
+                acc[1] += r0.x * w.y - r0.y * w.x;
+            } else if constexpr (SNK == SNK_AT || SNK == SNK_AT_DEF) {
+                R.At[o[q]] = w;
+                const cx<T> t = vv[q];
+                acc[0] += w.x * t.x + w.y * t.y;  // At . t
+                acc[1] += w.x * t.y - w.y * t.x;
+                acc[2] += w.x * w.x + w.y * w.y;  // At . At
+                if constexpr (SNK == SNK_AT_DEF) {  // r0 . t, r0 . At, t . t
+                    const cx<T> r0 = q2[q];
+                    acc[3] += r0.x * t.x + r0.y * t.y;
+                    acc[4] += r0.x * t.y - r0.y * t.x;
+                    acc[5] += r0.x * w.x + r0.y * w.y;
+                    acc[6] += r0.x * w.y - r0.y * w.x;
+                    acc[7] += t.x * t.x + t.y * t.y;
+                }
+            } else {  // SNK_RES
+                const cx<T> rr = csub<T>(q2[q], w);
+                R.r[o[q]] = rr;
+                R.r0[o[q]] = rr;
+                R.p[o[q]] = rr;
+                acc[0] += rr.x * rr.x + rr.y * rr.y;
+            }
+        }
+    }
+}
+
 template <typename T, int MY, int MZ> struct ZyPlane {
     static constexpr int ZP = pad_odd(MZ);
     static constexpr int LY = (MY + 1) / 2;
@@ -347,32 +591,34 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
     stage_tw<T>(stwz, twz, MZ);
 
     cx<T> beta, alpha, zeta;
-    if (SRC == SRC_PUPD || SRC == SRC_PUPD_DEF) beta = from_d<T>(R.st->beta);
-    if (SRC == SRC_TUPD || SRC == SRC_PUPD_DEF) alpha = from_d<T>(R.st->alpha);
-    if (SRC == SRC_PUPD_DEF) zeta = from_d<T>(R.st->zeta);
+    if (SRC == SRC_PUPD || SRC == SRC_PUPD_DEF) beta = st_beta<T>(R.st);
+    if (SRC == SRC_TUPD || SRC == SRC_PUPD_DEF) alpha = st_alpha<T>(R.st);
+    if (SRC == SRC_PUPD_DEF) zeta = st_zeta<T>(R.st);
     const cx<T>* src = SRC == SRC_IN ? R.p : R.P;
     const int* cm = cellmap + (long long)x * Ny * Nz;
-    for (int e = threadIdx.x; e < PL::LY * PL::LZ; e += kNT) {
-        const int y = e / PL::LZ, z = e - (e / PL::LZ) * PL::LZ;
-        cx<T> v = czero<T>();
-        const int i = (y < Ny && z < Nz) ? cm[y * Nz + z] : -1;
-        if (i >= 0) {
-            const long long o = 3LL * i + c;
-            if (SRC == SRC_PUPD) {
-                const cx<T> pc = R.p[o], uc = R.u[o], rc = R.r[o];
-                v = cadd<T>(rc, cmul<T>(beta, csub<T>(pc, uc)));
-                R.p[o] = v;
-            } else if (SRC == SRC_PUPD_DEF) {
-                v = deferred_step<T>(R, o, alpha, zeta, beta);
-            } else if (SRC == SRC_TUPD) {
-                const cx<T> rc = R.r[o], ac = R.Ap[o];
-                v = csub<T>(rc, cmul<T>(alpha, ac));
-                R.t[o] = v;
-            } else {
-                v = src[o];
-            }
+    const int ibase = x * Ny * Nz;
+    // cells in chunks of CH per thread: every load of a chunk is issued before
+    // its first store, so the chunk costs one memory latency, not CH
+    constexpr int NCELL = PL::LY * PL::LZ, NE = (NCELL + kNT - 1) / kNT, CH = NE < 4 ? NE : 4;
+#pragma unroll
+    for (int c0 = 0; c0 < NE; c0 += CH) {
+        int slot[CH];
+        long long o[CH];
+#pragma unroll
+        for (int q = 0; q < CH; q++) {
+            const int e = threadIdx.x + (c0 + q) * kNT;
+            const int y = e / PL::LZ, z = e - (e / PL::LZ) * PL::LZ;
+            const bool cell = c0 + q < NE && e < NCELL;
+            slot[q] = cell ? y * PL::ZP + z : -1;
+            int i = -1;
+            if (cell && y < Ny && z < Nz) i = g.dense ? ibase + y * Nz + z : cm[y * Nz + z];
+            o[q] = i >= 0 ? 3LL * i + c : -1LL;
         }
-        s[y * PL::ZP + z] = v;
+        cx<T> v[CH];
+        gather_chunk<T, SRC, CH>(R, o, v, src, alpha, beta, zeta);
+#pragma unroll
+        for (int q = 0; q < CH; q++)
+            if (slot[q] >= 0) s[slot[q]] = v[q];
     }
     __syncthreads();
     // z transform of the LY rows (inputs z < Nz), then y transform of the Mz columns (inputs y < Ny)
@@ -416,51 +662,28 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
     const cx<T>* res = ct_fft<+1, T, MZ, PL::LY, PL::ZP, 1, kNT>(r1, r1 == s ? s2 : s, stwz, MZ, Nz);
 
     // scatter component c to the dipoles, fused diagonal term and dot products
-    const cx<T>* vsrc = (SRC == SRC_TUPD) ? R.t : (SRC == SRC_P ? R.P : R.p);
     const int* cm = cellmap + (long long)x * Ny * Nz;
+    const int ibase = x * Ny * Nz;
     acc_t<T> acc[NV] = {};
-    for (int e = threadIdx.x; e < PL::LY * PL::LZ; e += kNT) {
-        const int y = e / PL::LZ, z = e - (e / PL::LZ) * PL::LZ;
-        const int i = (y < Ny && z < Nz) ? cm[y * Nz + z] : -1;
-        if (i < 0) continue;
-        const long long o = 3LL * i + c;
-        const cx<T> val = res[y * PL::ZP + z];
-        if (SNK == SNK_OUT) {
-            R.Ap[o] = val;
-            continue;
+    constexpr int NCELL = PL::LY * PL::LZ, NE = (NCELL + kNT - 1) / kNT, CH = NE < 4 ? NE : 4;
+#pragma unroll
+    for (int c0 = 0; c0 < NE; c0 += CH) {
+        int slot[CH];
+        long long o[CH];
+#pragma unroll
+        for (int q = 0; q < CH; q++) {
+            const int e = threadIdx.x + (c0 + q) * kNT;
+            const int y = e / PL::LZ, z = e - (e / PL::LZ) * PL::LZ;
+            const bool cell = c0 + q < NE && e < NCELL;
+            slot[q] = cell ? y * PL::ZP + z : -1;
+            int i = -1;
+            if (cell && y < Ny && z < Nz) i = g.dense ? ibase + y * Nz + z : cm[y * Nz + z];
+            o[q] = i >= 0 ? 3LL * i + c : -1LL;
         }
-        const cx<T> vv = vsrc[o];
-        const cx<T> w = cadd<T>(val, cmul<T>(vv, R.al[o]));
-        if (SNK == SNK_ALB) {
-            R.Ap[o] = w;
-        } else if (SNK == SNK_AP) {
-            R.Ap[o] = w;
-            const cx<T> q = R.r0[o];  // r0 . Ap
-            acc[0] += q.x * w.x + q.y * w.y;
-            acc[1] += q.x * w.y - q.y * w.x;
-        } else if (SNK == SNK_AT || SNK == SNK_AT_DEF) {
-            R.At[o] = w;
-            acc[0] += w.x * vv.x + w.y * vv.y;  // At . t
-            acc[1] += w.x * vv.y - w.y * vv.x;
-            acc[2] += w.x * w.x + w.y * w.y;    // At . At
-            if constexpr (SNK == SNK_AT_DEF) {  // r0 . t, r0 . At, t . t
-                const cx<T> q = R.r0[o];
-                acc[3] += q.x * vv.x + q.y * vv.y;
-                acc[4] += q.x * vv.y - q.y * vv.x;
-                acc[5] += q.x * w.x + q.y * w.y;
-                acc[6] += q.x * w.y - q.y * w.x;
-                acc[7] += vv.x * vv.x + vv.y * vv.y;
-            }
-        } else if (SNK == SNK_RES) {
-            const cx<T> rr = csub<T>(R.E[o], w);
-            R.r[o] = rr;
-            R.r0[o] = rr;
-            R.p[o] = rr;
-            acc[0] += rr.x * rr.x + rr.y * rr.y;
-        }
+        scatter_chunk<T, SRC, SNK, CH, NV>(R, o, slot, res, acc);
     }
     if (SNK == SNK_OUT || SNK == SNK_ALB) return;
-    double tot[NV];
+    tot_t<T> tot[NV];
     const int slot = SNK == SNK_AP ? 0 : (SNK == SNK_AT || SNK == SNK_AT_DEF ? 1 : 2);
     if (!last_block_total<NV>(acc, R.part, gridDim.x, blockIdx.x, R.cnt + slot, sred, tot)) return;
     if (threadIdx.x != 0) return;
