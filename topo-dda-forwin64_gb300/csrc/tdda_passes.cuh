@@ -452,8 +452,8 @@ __global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restri
 // (blockIdx.x / 3, blockIdx.x % 3).  Plane layout in shared memory: [y][z],
 // row stride ZP.  Lattice data occupies rows y < Ny <= LY and columns
 // z < Nz <= LZ (M >= 2N - 1 on every axis).
-// Gather of CH grid cells of one component: o[q] = 3 i + c of the dipole in
-// cell q, or -1 for an empty cell (v[q] = 0).  All loads come before the
+// Gather of CH entries of one component: o[q] = 3 i + c of the dipole in
+// cell q, or -1 for an empty or padding cell (v[q] = 0).  All loads come before the
 // first store.
 template <typename T, int SRC, int CH>
 __device__ __forceinline__ void gather_chunk(const RhsVecs<T>& R, const long long (&o)[CH], cx<T> (&v)[CH],
@@ -509,18 +509,17 @@ __device__ __forceinline__ void gather_chunk(const RhsVecs<T>& R, const long lon
     }
 }
 
-// Scatter of CH grid cells of one component (A v in res[slot[q]]) with the
-// sink's diagonal term, stores and dot-product terms.  All loads come before
+// Scatter of CH entries of one component (A v in val[q], dipole entry o[q] or
+// -1) with the sink's diagonal term, stores and dot-product terms.  All loads come before
 // the first store.
 template <typename T, int SRC, int SNK, int CH, int NV>
-__device__ __forceinline__ void scatter_chunk(const RhsVecs<T>& R, const long long (&o)[CH], const int (&slot)[CH],
-                                              const cx<T>* res, acc_t<T> (&acc)[NV]) {
+__device__ __forceinline__ void scatter_chunk(const RhsVecs<T>& R, const long long (&o)[CH], const cx<T> (&val)[CH],
+                                              acc_t<T> (&acc)[NV]) {
     const cx<T>* vsrc = (SRC == SRC_TUPD) ? R.t : (SRC == SRC_P ? R.P : R.p);
-    cx<T> val[CH], vv[CH], al[CH], q2[CH];
+    cx<T> vv[CH], al[CH], q2[CH];
 #pragma unroll
     for (int q = 0; q < CH; q++) {
         if (o[q] < 0) continue;
-        val[q] = res[slot[q]];
         if constexpr (SNK != SNK_OUT) { vv[q] = vsrc[o[q]]; al[q] = R.al[o[q]]; }
         if constexpr (SNK == SNK_AP || SNK == SNK_AT_DEF) q2[q] = R.r0[o[q]];
         if constexpr (SNK == SNK_RES) q2[q] = R.E[o[q]];
@@ -572,11 +571,22 @@ template <typename T, int MY, int MZ> struct ZyPlane {
     static constexpr size_t smem = sizeof(cx<T>) * (size_t)(MY + MZ + 2 * MY * ZP);
 };
 
+// Both axes use their two-stage plans (z: Mz = A1 A2, y: My = B1 B2): the
+// first z stage gathers its inputs straight from the dipole vectors and the
+// last y stage writes the grid (k_zyfwd); the first y stage reads the grid
+// and the last z stage scatters straight to the dipoles (k_yzinv).  Three
+// barriers per kernel.  Row-wise stages map consecutive threads to
+// consecutive rows y (odd row stride ZP: no bank conflicts), column-wise
+// stages to consecutive z.
 template <typename T, int SRC, int MY, int MZ>
 __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restrict__ rhs,
                                                const cx<T>* __restrict__ twy, const cx<T>* __restrict__ twz,
                                                const int* __restrict__ cellmap, cx<T>* __restrict__ grid) {
     using PL = ZyPlane<T, MY, MZ>;
+    constexpr int A1 = ct_radix(MZ, 0, true), A2 = ct_radix(MZ, 1, true);
+    constexpr int B1 = ct_radix(MY, 0, true), B2 = ct_radix(MY, 1, true);
+    static_assert(ct_nstages(MZ, true) == 2 && ct_nstages(MY, true) == 2, "two-stage plans");
+    constexpr int ZP = PL::ZP, LY = PL::LY;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int b = blockIdx.y;
     const RhsVecs<T> R = rhs[b];
@@ -586,7 +596,7 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
     cx<T>* stwy = reinterpret_cast<cx<T>*>(smem_raw);
     cx<T>* stwz = stwy + MY;
     cx<T>* s = stwz + MZ;
-    cx<T>* s2 = s + MY * PL::ZP;
+    cx<T>* s2 = s + MY * ZP;
     stage_tw<T>(stwy, twy, MY);
     stage_tw<T>(stwz, twz, MZ);
 
@@ -597,9 +607,10 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
     const cx<T>* src = SRC == SRC_IN ? R.p : R.P;
     const int* cm = cellmap + (long long)x * Ny * Nz;
     const int ibase = x * Ny * Nz;
-    // cells in chunks of CH per thread: every load of a chunk is issued before
-    // its first store, so the chunk costs one memory latency, not CH
-    constexpr int NCELL = PL::LY * PL::LZ, NE = (NCELL + kNT - 1) / kNT, CH = NE < 4 ? NE : 4;
+
+    // gather: consecutive threads take consecutive cells (y, z), z fastest, in
+    // chunks of CH cells whose loads are issued before their stores
+    constexpr int LZ = PL::LZ, NCELL = LY * LZ, NE = (NCELL + kNT - 1) / kNT, CH = NE < 4 ? NE : 4;
 #pragma unroll
     for (int c0 = 0; c0 < NE; c0 += CH) {
         int slot[CH];
@@ -607,9 +618,9 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
 #pragma unroll
         for (int q = 0; q < CH; q++) {
             const int e = threadIdx.x + (c0 + q) * kNT;
-            const int y = e / PL::LZ, z = e - (e / PL::LZ) * PL::LZ;
+            const int y = e / LZ, z = e - (e / LZ) * LZ;
             const bool cell = c0 + q < NE && e < NCELL;
-            slot[q] = cell ? y * PL::ZP + z : -1;
+            slot[q] = cell ? y * ZP + z : -1;
             int i = -1;
             if (cell && y < Ny && z < Nz) i = g.dense ? ibase + y * Nz + z : cm[y * Nz + z];
             o[q] = i >= 0 ? 3LL * i + c : -1LL;
@@ -620,14 +631,63 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
         for (int q = 0; q < CH; q++)
             if (slot[q] >= 0) s[slot[q]] = v[q];
     }
+    __syncthreads();  // also publishes the twiddles
+    // z stage 1: task (y < LY, j < A2) reads z = j + A2 r < LZ (columns past LZ
+    // are not gathered: zero), writes j A1 + q
+    constexpr int RV = (LZ + A2 - 1) / A2;
+    for (int w = threadIdx.x; w < LY * A2; w += kNT) {
+        const int y = w % LY, j = w / LY;
+        cx<T> v[A1];
+#pragma unroll
+        for (int r = 0; r < A1; r++) v[r] = (r < RV && j + A2 * r < LZ) ? s[y * ZP + j + A2 * r] : czero<T>();
+        Bfly<A1, -1, T>::run(v);
+#pragma unroll
+        for (int q = 0; q < A1; q++) s2[y * ZP + j * A1 + q] = v[q];
+    }
     __syncthreads();
-    // z transform of the LY rows (inputs z < Nz), then y transform of the Mz columns (inputs y < Ny)
-    cx<T>* r1 = ct_fft<-1, T, MZ, PL::LY, PL::ZP, 1, kNT>(s, s2, stwz, Nz, MZ);
-    const cx<T>* r2 = ct_fft<-1, T, MY, MZ, 1, PL::ZP, kNT>(r1, r1 == s ? s2 : s, stwy, Ny, MY);
+    // z stage 2: task (y, j < A1) reads j + A1 r with twiddles w^(r j), writes j + A1 q
+    for (int w = threadIdx.x; w < LY * A1; w += kNT) {
+        const int y = w % LY, j = w / LY;
+        cx<T> v[A2];
+#pragma unroll
+        for (int r = 0; r < A2; r++) {
+            cx<T> t = s2[y * ZP + j + A1 * r];
+            if (r > 0) t = cmul<T>(t, stwz[r * j]);
+            v[r] = t;
+        }
+        Bfly<A2, -1, T>::run(v);
+#pragma unroll
+        for (int q = 0; q < A2; q++) s[y * ZP + j + A1 * q] = v[q];
+    }
+    __syncthreads();
+    // y stage 1: task (kz < Mz, j < B2) reads rows y = j + B2 r < Ny
+    for (int w = threadIdx.x; w < MZ * B2; w += kNT) {
+        const int kz = w % MZ, j = w / MZ;
+        cx<T> v[B1];
+#pragma unroll
+        for (int r = 0; r < B1; r++) {
+            const int y = j + B2 * r;
+            v[r] = y < Ny ? s[y * ZP + kz] : czero<T>();
+        }
+        Bfly<B1, -1, T>::run(v);
+#pragma unroll
+        for (int q = 0; q < B1; q++) s2[(j * B1 + q) * ZP + kz] = v[q];
+    }
+    __syncthreads();
+    // y stage 2 to the grid plane [y][z]: task (kz, j < B1), rows j + B1 q
     cx<T>* gp = grid + (long long)b * g.sb + c * g.sc + (long long)x * g.sx;
-    for (int e = threadIdx.x; e < MY * MZ; e += kNT) {
-        const int y = e / MZ, z = e - (e / MZ) * MZ;
-        gp[(long long)y * g.sy + z] = r2[y * PL::ZP + z];
+    for (int w = threadIdx.x; w < MZ * B1; w += kNT) {
+        const int kz = w % MZ, j = w / MZ;
+        cx<T> v[B2];
+#pragma unroll
+        for (int r = 0; r < B2; r++) {
+            cx<T> t = s2[(j + B1 * r) * ZP + kz];
+            if (r > 0) t = cmul<T>(t, stwy[r * j]);
+            v[r] = t;
+        }
+        Bfly<B2, -1, T>::run(v);
+#pragma unroll
+        for (int q = 0; q < B2; q++) gp[(long long)(j + B1 * q) * g.sy + kz] = v[q];
     }
 }
 
@@ -636,8 +696,12 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
                                                const cx<T>* __restrict__ twy, const cx<T>* __restrict__ twz,
                                                const int* __restrict__ cellmap, cx<T>* __restrict__ grid) {
     using PL = ZyPlane<T, MY, MZ>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int A1 = ct_radix(MZ, 0, true), A2 = ct_radix(MZ, 1, true);
+    constexpr int B1 = ct_radix(MY, 0, true), B2 = ct_radix(MY, 1, true);
+    static_assert(ct_nstages(MZ, true) == 2 && ct_nstages(MY, true) == 2, "two-stage plans");
+    constexpr int ZP = PL::ZP, LY = PL::LY;
     constexpr int NV = SNK == SNK_AT_DEF ? 8 : 4;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double sred[sred_size<T, NV>()];
     const int b = blockIdx.y;
     const RhsVecs<T> R = rhs[b];
@@ -647,40 +711,99 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
     cx<T>* stwy = reinterpret_cast<cx<T>*>(smem_raw);
     cx<T>* stwz = stwy + MY;
     cx<T>* s = stwz + MZ;
-    cx<T>* s2 = s + MY * PL::ZP;
+    cx<T>* s2 = s + MY * ZP;
     stage_tw<T>(stwy, twy, MY);
     stage_tw<T>(stwz, twz, MZ);
     const cx<T>* gp = grid + (long long)b * g.sb + c * g.sc + (long long)x * g.sx;
-    for (int e = threadIdx.x; e < MY * MZ; e += kNT) {
-        const int y = e / MZ, z = e - (e / MZ) * MZ;
-        s[y * PL::ZP + z] = gp[(long long)y * g.sy + z];
+
+    // y stage 1 on the grid plane: task (kz < Mz, j < B2) reads rows j + B2 r
+    for (int w = threadIdx.x; w < MZ * B2; w += kNT) {
+        const int kz = w % MZ, j = w / MZ;
+        cx<T> v[B1];
+#pragma unroll
+        for (int r = 0; r < B1; r++) v[r] = gp[(long long)(j + B2 * r) * g.sy + kz];
+        Bfly<B1, +1, T>::run(v);
+#pragma unroll
+        for (int q = 0; q < B1; q++) s[(j * B1 + q) * ZP + kz] = v[q];
+    }
+    __syncthreads();  // also publishes the twiddles
+    // y stage 2: task (kz, j < B1), twiddles conj(w^(r j)), rows j + B1 q < Ny kept
+    for (int w = threadIdx.x; w < MZ * B1; w += kNT) {
+        const int kz = w % MZ, j = w / MZ;
+        cx<T> v[B2];
+#pragma unroll
+        for (int r = 0; r < B2; r++) {
+            cx<T> t = s[(j + B1 * r) * ZP + kz];
+            if (r > 0) {
+                cx<T> tw = stwy[r * j];
+                tw.y = -tw.y;
+                t = cmul<T>(t, tw);
+            }
+            v[r] = t;
+        }
+        Bfly<B2, +1, T>::run(v);
+#pragma unroll
+        for (int q = 0; q < B2; q++) {
+            const int y = j + B1 * q;
+            if (y < Ny) s2[y * ZP + kz] = v[q];
+        }
     }
     __syncthreads();
-    // y transform of the Mz columns (outputs y < Ny), then z transform of the
-    // LY rows (outputs z < Nz); rows Ny..LY-1 are transformed and dropped
-    cx<T>* r1 = ct_fft<+1, T, MY, MZ, 1, PL::ZP, kNT>(s, s2, stwy, MY, Ny);
-    const cx<T>* res = ct_fft<+1, T, MZ, PL::LY, PL::ZP, 1, kNT>(r1, r1 == s ? s2 : s, stwz, MZ, Nz);
-
-    // scatter component c to the dipoles, fused diagonal term and dot products
+    // z stage 1 on the rows y < Ny: task (y, j < A2) reads z = j + A2 r
+    for (int w = threadIdx.x; w < LY * A2; w += kNT) {
+        const int y = w % LY, j = w / LY;
+        if (y >= Ny) continue;
+        cx<T> v[A1];
+#pragma unroll
+        for (int r = 0; r < A1; r++) v[r] = s2[y * ZP + j + A2 * r];
+        Bfly<A1, +1, T>::run(v);
+#pragma unroll
+        for (int q = 0; q < A1; q++) s[y * ZP + j * A1 + q] = v[q];
+    }
+    __syncthreads();
+    // z stage 2: task (y, j < A1), twiddles conj(w^(r j)), outputs z = j + A1 q < LZ
+    constexpr int LZ = PL::LZ, QV = (LZ + A1 - 1) / A1;
+    for (int w = threadIdx.x; w < LY * A1; w += kNT) {
+        const int y = w % LY, j = w / LY;
+        if (y >= Ny) continue;
+        cx<T> v[A2];
+#pragma unroll
+        for (int r = 0; r < A2; r++) {
+            cx<T> t = s[y * ZP + j + A1 * r];
+            if (r > 0) {
+                cx<T> tw = stwz[r * j];
+                tw.y = -tw.y;
+                t = cmul<T>(t, tw);
+            }
+            v[r] = t;
+        }
+        Bfly<A2, +1, T>::run(v);
+#pragma unroll
+        for (int q = 0; q < QV; q++)
+            if (j + A1 * q < LZ) s2[y * ZP + j + A1 * q] = v[q];
+    }
+    __syncthreads();
+    // scatter component c: consecutive threads take consecutive cells (y, z),
+    // in chunks of CH whose loads are issued before their stores
     const int* cm = cellmap + (long long)x * Ny * Nz;
     const int ibase = x * Ny * Nz;
     acc_t<T> acc[NV] = {};
-    constexpr int NCELL = PL::LY * PL::LZ, NE = (NCELL + kNT - 1) / kNT, CH = NE < 4 ? NE : 4;
+    constexpr int NCELL = LY * LZ, NE = (NCELL + kNT - 1) / kNT, CH = NE < 4 ? NE : 4;
 #pragma unroll
     for (int c0 = 0; c0 < NE; c0 += CH) {
-        int slot[CH];
         long long o[CH];
+        cx<T> vo[CH];
 #pragma unroll
         for (int q = 0; q < CH; q++) {
             const int e = threadIdx.x + (c0 + q) * kNT;
-            const int y = e / PL::LZ, z = e - (e / PL::LZ) * PL::LZ;
-            const bool cell = c0 + q < NE && e < NCELL;
-            slot[q] = cell ? y * PL::ZP + z : -1;
+            const int y = e / LZ, z = e - (e / LZ) * LZ;
+            const bool cell = c0 + q < NE && e < NCELL && y < Ny && z < Nz;
             int i = -1;
-            if (cell && y < Ny && z < Nz) i = g.dense ? ibase + y * Nz + z : cm[y * Nz + z];
+            if (cell) i = g.dense ? ibase + y * Nz + z : cm[y * Nz + z];
             o[q] = i >= 0 ? 3LL * i + c : -1LL;
+            vo[q] = i >= 0 ? s2[y * ZP + z] : czero<T>();
         }
-        scatter_chunk<T, SRC, SNK, CH, NV>(R, o, slot, res, acc);
+        scatter_chunk<T, SRC, SNK, CH, NV>(R, o, vo, acc);
     }
     if (SNK == SNK_OUT || SNK == SNK_ALB) return;
     tot_t<T> tot[NV];
