@@ -335,25 +335,25 @@ __device__ __forceinline__ void finish_step_f32(SolveState* st, float2 rho, floa
     }
 }
 
-// The deferred step end (SNK_AT_DEF) on FP32 state: zeta = At.t / At.At,
-// r0.r = r0.t - zeta r0.At, |r|^2 = t.t - 2 Re(conj(zeta) At.t) + |zeta|^2 At.At.
-// The cancelling differences lose at most ~1e-7 t.t, the size of the FP32
-// rounding of t itself; the outer FP64 residual check bounds the result.
+// The deferred step end (SNK_AT_DEF) on FP32 state: zeta = At.t / At.At in
+// FP32 (the value the update applies), then for r = t - zeta At
+// r0.r = r0.t - zeta r0.At and |r|^2 = t.t - 2 Re(conj(zeta) At.t) + |zeta|^2 At.At
+// as FP64 multiply-adds on the double-float totals: these differences cancel
+// as r becomes small next to t, and no FP64 division or root is needed.
+__device__ __forceinline__ double df_d(float2 a) { return (double)a.x + (double)a.y; }
 __device__ __forceinline__ void finish_step_deferred_f32(SolveState* st, const float2 (&tot)[8]) {
-    const float2 Att = make_float2(tot[0].x, tot[1].x);
-    const float AtAt = tot[2].x;
-    const float2 r0t = make_float2(tot[3].x, tot[4].x), r0At = make_float2(tot[5].x, tot[6].x);
-    const float tt = tot[7].x;
-    const float2 zeta = fdiv2(Att, make_float2(AtAt, 0.f));  // DDAModel.cpp:225
+    const float2 zeta = fdiv2(make_float2(tot[0].x, tot[1].x), make_float2(tot[2].x, 0.f));  // DDAModel.cpp:225
     st->zeta32 = zeta;
-    const float2 zr = fmul2(zeta, r0At);
-    const float2 rho = make_float2(r0t.x - zr.x, r0t.y - zr.y);
-    float rn2 = tt - 2.f * (zeta.x * Att.x + zeta.y * Att.y) + (zeta.x * zeta.x + zeta.y * zeta.y) * AtAt;
-    if (!(rn2 > 0.f)) rn2 = isnan(rn2) ? rn2 : 0.f;
+    const double zx = zeta.x, zy = zeta.y;
+    const double ax = df_d(tot[0]), ay = df_d(tot[1]), bb = df_d(tot[2]);
+    const double tx = df_d(tot[3]), ty = df_d(tot[4]), ux = df_d(tot[5]), uy = df_d(tot[6]), cc = df_d(tot[7]);
+    const float2 rho = make_float2((float)(tx - (zx * ux - zy * uy)), (float)(ty - (zx * uy + zy * ux)));
+    double rn2 = cc - 2.0 * (zx * ax + zy * ay) + (zx * zx + zy * zy) * bb;
+    if (!(rn2 > 0.0)) rn2 = isnan(rn2) ? rn2 : 0.0;
     const bool init = st->init != 0;
     st->init = 0;
     st->pending = 1;
-    finish_step_f32(st, rho, rn2, init);
+    finish_step_f32(st, rho, (float)rn2, init);
 }
 
 // The scalars a sink pass forms from its grid totals (thread 0 of the last block).
