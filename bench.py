@@ -164,12 +164,22 @@ def pass_bytes(grid, Nx, Ny, Nz, N, s, fused=False):
     return [zf * s, yf * s, xp * s, yf * s, zf * s]
 
 
-PASS_NAMES = ["k_zfwd", "k_ypass(fwd)", "k_xpass", "k_ypass(inv)", "k_zinv"]
-FUSED_NAMES = ["k_zyfwd", "-", "k_xpass", "k_yzinv", "-"]
+def ncu_traffic(key):
+    """DRAM bytes per launch of a kernel from the committed ncu summary table, or None."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            parts = line.split("#")[0].split()
+            if len(parts) == 2 and parts[0] == key:
+                return int(parts[1])
+    return None
 
 
-def pass_names(fused):
-    return FUSED_NAMES if fused else PASS_NAMES
+def pass_names(core, precision):
+    """Kernel of each profile slot, from the library ("-" where a fused kernel covers it)."""
+    return [n or "-" for n in core.pass_names(precision)]
 
 
 # ------------------------------------------------------------------ CPU baseline
@@ -282,14 +292,14 @@ def time_batch(tdda, torch, w, incs, precision, steps, dev, flush_l2):
     prof = core.profile_aproduct(precision, len(incs), 5)
     out = {"rhs": len(incs), "value": len(incs) * steps / (sum(ms) / 1000.0), "unit": UNIT, "steps": steps,
            "ms_per_batch": sum(ms) / steps, "iterations": [i["iterations"] for i in infos],
-           "pass_ms": prof, "kernels": pass_names(core.pass_count(precision) == 3), "grid": list(core.grid)}
+           "pass_ms": prof, "kernels": pass_names(core, precision), "grid": list(core.grid)}
     for m in models:
         m.close()
     core.close()
     return out, prof, n32
 
 
-def batched_roofline(w, grid, prof, nrhs, s, peak):
+def batched_roofline(w, grid, prof, nrhs, s, peak, kernel):
     """Roofline of the x pass (the largest) for nrhs right-hand sides: the Green tensor is
     read once per launch, the grid once per right-hand side."""
     Mx, My, Mz = grid
@@ -298,8 +308,8 @@ def batched_roofline(w, grid, prof, nrhs, s, peak):
     b = grid_bytes + green_bytes
     t = prof[2]
     ach = b / (t * 1e-3) / 1e9
-    return {"kernel": "k_xpass", "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-            "algorithmic_bytes": b, "avg_ms": t}
+    return {"kernel": kernel, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+            "algorithmic_bytes": b, "avg_ms": t, "traffic": ncu_traffic(f"{kernel}:fp32:cfg3x{nrhs}")}
 
 
 def run_serving(tdda, stream, precision, workers, budget, dev):
@@ -452,24 +462,22 @@ def run_ours(args, dist: Dist):
     shares = [(n32 * t, "fp32", k) for k, t in enumerate(prof32)] + [(n64 * t, "fp64", k) for k, t in enumerate(prof64)]
     _, prec, k = max(shares)
     s = 8 if prec == "fp32" else 16
-    fused = core.pass_count(tdda.FP32_REFINE if prec == "fp32" else tdda.FP64) == 3
-    names = pass_names(fused)
+    pprec = tdda.FP32_REFINE if prec == "fp32" else tdda.FP64
+    fused = core.pass_count(pprec) == 3
+    names = pass_names(core, pprec)
     bytes_k = pass_bytes(core.grid, w.Nx, w.Ny, w.Nz, w.N, s, fused)[k]
     t_k = (prof32 if prec == "fp32" else prof64)[k]
     peaks = measured_peaks()
     achieved = bytes_k / (t_k * 1e-3) / 1e9
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "ncu_traffic.json")
-    if os.path.exists(tf):
-        with open(tf) as f:
-            traffic = json.load(f).get(f"{names[k]}:{prec}")
+    traffic = ncu_traffic(f"{names[k]}:{prec}:cfg2")
 
     # batched right-hand sides: the 96x96x24 lattice with its 8 incidences in one solve
     batched = None
     if not args.no_batched:
         w3 = lattice.config(3)
         b32, prof_b, _ = time_batch(tdda, torch, w3, w3.incidences, tdda.FP32_REFINE, args.batched_steps, dev, flush_l2)
-        b32["roofline"] = batched_roofline(w3, tuple(b32["grid"]), prof_b, len(w3.incidences), 8, peaks["hbm_gbs"])
+        b32["roofline"] = batched_roofline(w3, tuple(b32["grid"]), prof_b, len(w3.incidences), 8, peaks["hbm_gbs"],
+                                           b32["kernels"][2])
         b64, _, _ = time_batch(tdda, torch, w3, w3.incidences, tdda.FP64, 1, dev, flush_l2)
         batched = {"workload": "batched 8 RHS 96x96x24 (cfg 3)", "dipoles": w3.N, "fp32_refine": b32,
                    "fp64": {"value": b64["value"], "unit": UNIT, "iterations": b64["iterations"],
@@ -519,8 +527,8 @@ def run_ours(args, dist: Dist):
                          "peak_source": peaks["source"], "algorithmic_bytes": bytes_k, "avg_ms": t_k,
                          "traffic": traffic,
                          "pass_ms_fp32": prof32, "pass_ms_fp64": prof64,
-                         "kernels_fp32": pass_names(core.pass_count(tdda.FP32_REFINE) == 3),
-                         "kernels_fp64": pass_names(core.pass_count(tdda.FP64) == 3)},
+                         "kernels_fp32": pass_names(core, tdda.FP32_REFINE),
+                         "kernels_fp64": pass_names(core, tdda.FP64)},
             "batched": batched,
             "serving": serving,
             "topo": topo_line,

@@ -247,6 +247,11 @@ tdda_status tdda_profile_aproduct(tdda_core* core, int precision, int nrhs, int 
  * inverse in ms5[3], and ms5[1], ms5[4] hold only the gap between two events.
  * -1 for an invalid argument. */
 int tdda_core_pass_count(const tdda_core* core, int precision);
+/* Kernel that runs pass `pass` (0..4, the slots of tdda_profile_aproduct) at
+ * this precision: "k_zfwd", "k_ypass", "k_xpass", "k_zinv", or with the
+ * fused and register forms "k_zyfwd", "k_xpass2", "k_yzinv"; "" for a slot
+ * that a fused kernel covers; NULL for an invalid argument.  Static string. */
+const char* tdda_core_pass_name(const tdda_core* core, int precision, int pass);
 
 #ifdef __cplusplus
 }

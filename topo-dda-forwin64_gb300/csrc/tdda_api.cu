@@ -1187,6 +1187,19 @@ tdda_status tdda_core_stream(const tdda_core* c, void** stream) {
 
 unsigned long long tdda_kernel_launches(void) { return g_launches.load(); }
 
+const char* tdda_core_pass_name(const tdda_core* c, int precision, int pass) {
+    if (!c || pass < 0 || pass > 4 || (precision != TDDA_FP64 && precision != TDDA_FP32_REFINE)) return nullptr;
+    const bool fp32 = precision == TDDA_FP32_REFINE;
+    const bool fused = tdda::zy_fused(c->g, fp32);
+    switch (pass) {
+        case 0: return fused ? "k_zyfwd" : "k_zfwd";
+        case 1: return fused ? "" : "k_ypass";
+        case 2: return fp32 && tdda::xpass2_length(c->g.px.M) ? "k_xpass2" : "k_xpass";
+        case 3: return fused ? "k_yzinv" : "k_ypass";
+        default: return fused ? "" : "k_zinv";
+    }
+}
+
 int tdda_core_pass_count(const tdda_core* c, int precision) {
     if (!c || (precision != TDDA_FP64 && precision != TDDA_FP32_REFINE)) return -1;
     return tdda::zy_fused(c->g, precision == TDDA_FP32_REFINE) ? 3 : 5;

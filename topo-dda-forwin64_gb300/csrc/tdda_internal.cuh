@@ -126,6 +126,8 @@ cudaError_t configure_pass_ct_xy();
 // the FFT lengths with specialised kernels
 bool ct_has_z(int Mz);
 bool ct_has_xy(int M);
+// FFT x lengths whose FP32 x pass is the register form (k_xpass2)
+bool xpass2_length(int M);
 constexpr size_t kMaxPassSmem = 200 * 1024;
 
 // -------------------------------------------------------------- launchers

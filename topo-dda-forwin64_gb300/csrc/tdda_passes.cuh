@@ -234,8 +234,8 @@ __global__ void __launch_bounds__(kNT) k_xpass(Geom g, const RhsVecs<T>* __restr
 // read and write the grid directly.  Two shared-memory round trips instead of
 // six, three barriers.  One block: ZT z-columns of one y row, NT = ZT R1
 // threads (one register-stage task each).
-template <typename T, int M, int ZT>
-__global__ void __launch_bounds__(ZT * ct_radix(M, 0, true)) k_xpass2(Geom g, const RhsVecs<T>* __restrict__ rhs,
+template <typename T, int M, int ZT, int MINB>
+__global__ void __launch_bounds__(ZT * ct_radix(M, 0, true), MINB) k_xpass2(Geom g, const RhsVecs<T>* __restrict__ rhs,
                                                                    const cx<T>* __restrict__ green,
                                                                    const cx<T>* __restrict__ twx,
                                                                    cx<T>* __restrict__ grid) {
@@ -338,17 +338,17 @@ __global__ void __launch_bounds__(ZT * ct_radix(M, 0, true)) k_xpass2(Geom g, co
     }
 }
 
-template <typename T, int M, int ZT> struct XLaunch2 {
+template <typename T, int M, int ZT, int MINB = 1> struct XLaunch2 {
     static constexpr int NT = ZT * ct_radix(M, 0, true);
     static constexpr size_t smem = sizeof(cx<T>) * (size_t)(M + M * (3 * ZT + 1));
     static cudaError_t run(const PassArgs<T>& a) {
         const Geom& g = a.g;
         const dim3 grid(g.py.M * ((g.pz.M + ZT - 1) / ZT), a.nrhs);
-        k_xpass2<T, M, ZT><<<grid, NT, smem, a.stream>>>(g, a.rhs, a.green, a.twx, a.grid);
+        k_xpass2<T, M, ZT, MINB><<<grid, NT, smem, a.stream>>>(g, a.rhs, a.green, a.twx, a.grid);
         return cudaGetLastError();
     }
     static cudaError_t configure() {
-        return cudaFuncSetAttribute((const void*)k_xpass2<T, M, ZT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        return cudaFuncSetAttribute((const void*)k_xpass2<T, M, ZT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)kMaxPassSmem);
     }
 };
@@ -568,7 +568,9 @@ template <typename T, int MY, int MZ> struct ZyPlane {
     static constexpr int ZP = pad_odd(MZ);
     static constexpr int LY = (MY + 1) / 2;
     static constexpr int LZ = (MZ + 1) / 2;
-    static constexpr size_t smem = sizeof(cx<T>) * (size_t)(MY + MZ + 2 * MY * ZP);
+    // twiddles, buffer A of My rows and buffer B of LY rows (the z stages and
+    // the lattice side never need more than LY rows)
+    static constexpr size_t smem = sizeof(cx<T>) * (size_t)(MY + MZ + (MY + LY) * ZP);
 };
 
 // Both axes use their two-stage plans (z: Mz = A1 A2, y: My = B1 B2): the
@@ -595,8 +597,8 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
     const int Ny = g.Ny, Nz = g.Nz;
     cx<T>* stwy = reinterpret_cast<cx<T>*>(smem_raw);
     cx<T>* stwz = stwy + MY;
-    cx<T>* s = stwz + MZ;
-    cx<T>* s2 = s + MY * ZP;
+    cx<T>* sA = stwz + MZ;     // My rows
+    cx<T>* sB = sA + MY * ZP;  // LY rows
     stage_tw<T>(stwy, twy, MY);
     stage_tw<T>(stwz, twz, MZ);
 
@@ -629,7 +631,7 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
         gather_chunk<T, SRC, CH>(R, o, v, src, alpha, beta, zeta);
 #pragma unroll
         for (int q = 0; q < CH; q++)
-            if (slot[q] >= 0) s[slot[q]] = v[q];
+            if (slot[q] >= 0) sB[slot[q]] = v[q];
     }
     __syncthreads();  // also publishes the twiddles
     // z stage 1: task (y < LY, j < A2) reads z = j + A2 r < LZ (columns past LZ
@@ -639,10 +641,10 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
         const int y = w % LY, j = w / LY;
         cx<T> v[A1];
 #pragma unroll
-        for (int r = 0; r < A1; r++) v[r] = (r < RV && j + A2 * r < LZ) ? s[y * ZP + j + A2 * r] : czero<T>();
+        for (int r = 0; r < A1; r++) v[r] = (r < RV && j + A2 * r < LZ) ? sB[y * ZP + j + A2 * r] : czero<T>();
         Bfly<A1, -1, T>::run(v);
 #pragma unroll
-        for (int q = 0; q < A1; q++) s2[y * ZP + j * A1 + q] = v[q];
+        for (int q = 0; q < A1; q++) sA[y * ZP + j * A1 + q] = v[q];
     }
     __syncthreads();
     // z stage 2: task (y, j < A1) reads j + A1 r with twiddles w^(r j), writes j + A1 q
@@ -651,13 +653,13 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
         cx<T> v[A2];
 #pragma unroll
         for (int r = 0; r < A2; r++) {
-            cx<T> t = s2[y * ZP + j + A1 * r];
+            cx<T> t = sA[y * ZP + j + A1 * r];
             if (r > 0) t = cmul<T>(t, stwz[r * j]);
             v[r] = t;
         }
         Bfly<A2, -1, T>::run(v);
 #pragma unroll
-        for (int q = 0; q < A2; q++) s[y * ZP + j + A1 * q] = v[q];
+        for (int q = 0; q < A2; q++) sB[y * ZP + j + A1 * q] = v[q];
     }
     __syncthreads();
     // y stage 1: task (kz < Mz, j < B2) reads rows y = j + B2 r < Ny
@@ -667,11 +669,11 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
 #pragma unroll
         for (int r = 0; r < B1; r++) {
             const int y = j + B2 * r;
-            v[r] = y < Ny ? s[y * ZP + kz] : czero<T>();
+            v[r] = y < Ny ? sB[y * ZP + kz] : czero<T>();
         }
         Bfly<B1, -1, T>::run(v);
 #pragma unroll
-        for (int q = 0; q < B1; q++) s2[(j * B1 + q) * ZP + kz] = v[q];
+        for (int q = 0; q < B1; q++) sA[(j * B1 + q) * ZP + kz] = v[q];
     }
     __syncthreads();
     // y stage 2 to the grid plane [y][z]: task (kz, j < B1), rows j + B1 q
@@ -681,7 +683,7 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
         cx<T> v[B2];
 #pragma unroll
         for (int r = 0; r < B2; r++) {
-            cx<T> t = s2[(j + B1 * r) * ZP + kz];
+            cx<T> t = sA[(j + B1 * r) * ZP + kz];
             if (r > 0) t = cmul<T>(t, stwy[r * j]);
             v[r] = t;
         }
@@ -710,8 +712,8 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
     const int Ny = g.Ny, Nz = g.Nz;
     cx<T>* stwy = reinterpret_cast<cx<T>*>(smem_raw);
     cx<T>* stwz = stwy + MY;
-    cx<T>* s = stwz + MZ;
-    cx<T>* s2 = s + MY * ZP;
+    cx<T>* sA = stwz + MZ;     // My rows
+    cx<T>* sB = sA + MY * ZP;  // LY rows
     stage_tw<T>(stwy, twy, MY);
     stage_tw<T>(stwz, twz, MZ);
     const cx<T>* gp = grid + (long long)b * g.sb + c * g.sc + (long long)x * g.sx;
@@ -724,7 +726,7 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
         for (int r = 0; r < B1; r++) v[r] = gp[(long long)(j + B2 * r) * g.sy + kz];
         Bfly<B1, +1, T>::run(v);
 #pragma unroll
-        for (int q = 0; q < B1; q++) s[(j * B1 + q) * ZP + kz] = v[q];
+        for (int q = 0; q < B1; q++) sA[(j * B1 + q) * ZP + kz] = v[q];
     }
     __syncthreads();  // also publishes the twiddles
     // y stage 2: task (kz, j < B1), twiddles conj(w^(r j)), rows j + B1 q < Ny kept
@@ -733,7 +735,7 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
         cx<T> v[B2];
 #pragma unroll
         for (int r = 0; r < B2; r++) {
-            cx<T> t = s[(j + B1 * r) * ZP + kz];
+            cx<T> t = sA[(j + B1 * r) * ZP + kz];
             if (r > 0) {
                 cx<T> tw = stwy[r * j];
                 tw.y = -tw.y;
@@ -745,7 +747,7 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
 #pragma unroll
         for (int q = 0; q < B2; q++) {
             const int y = j + B1 * q;
-            if (y < Ny) s2[y * ZP + kz] = v[q];
+            if (y < Ny) sB[y * ZP + kz] = v[q];
         }
     }
     __syncthreads();
@@ -755,10 +757,10 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
         if (y >= Ny) continue;
         cx<T> v[A1];
 #pragma unroll
-        for (int r = 0; r < A1; r++) v[r] = s2[y * ZP + j + A2 * r];
+        for (int r = 0; r < A1; r++) v[r] = sB[y * ZP + j + A2 * r];
         Bfly<A1, +1, T>::run(v);
 #pragma unroll
-        for (int q = 0; q < A1; q++) s[y * ZP + j * A1 + q] = v[q];
+        for (int q = 0; q < A1; q++) sA[y * ZP + j * A1 + q] = v[q];
     }
     __syncthreads();
     // z stage 2: task (y, j < A1), twiddles conj(w^(r j)), outputs z = j + A1 q < LZ
@@ -769,7 +771,7 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
         cx<T> v[A2];
 #pragma unroll
         for (int r = 0; r < A2; r++) {
-            cx<T> t = s[y * ZP + j + A1 * r];
+            cx<T> t = sA[y * ZP + j + A1 * r];
             if (r > 0) {
                 cx<T> tw = stwz[r * j];
                 tw.y = -tw.y;
@@ -780,7 +782,7 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
         Bfly<A2, +1, T>::run(v);
 #pragma unroll
         for (int q = 0; q < QV; q++)
-            if (j + A1 * q < LZ) s2[y * ZP + j + A1 * q] = v[q];
+            if (j + A1 * q < LZ) sB[y * ZP + j + A1 * q] = v[q];
     }
     __syncthreads();
     // scatter component c: consecutive threads take consecutive cells (y, z),
@@ -801,7 +803,7 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
             int i = -1;
             if (cell) i = g.dense ? ibase + y * Nz + z : cm[y * Nz + z];
             o[q] = i >= 0 ? 3LL * i + c : -1LL;
-            vo[q] = i >= 0 ? s2[y * ZP + z] : czero<T>();
+            vo[q] = i >= 0 ? sB[y * ZP + z] : czero<T>();
         }
         scatter_chunk<T, SRC, SNK, CH, NV>(R, o, vo, acc);
     }

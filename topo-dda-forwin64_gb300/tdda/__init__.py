@@ -43,6 +43,7 @@ EXPORTS = [
     "tdda_model_initialize_P", "tdda_model_aproduct_with_alb", "tdda_model_bicgstab", "tdda_model_solve_mixed",
     "tdda_model_update_E_in_structure", "tdda_model_get", "tdda_model_iterations", "tdda_solve_batch",
     "tdda_fft3d", "tdda_core_stream", "tdda_kernel_launches", "tdda_profile_aproduct", "tdda_core_pass_count",
+    "tdda_core_pass_name",
     "tdda_aproduct_noalloc", "tdda_server_create", "tdda_server_submit", "tdda_server_result",
     "tdda_server_stats", "tdda_server_clock", "tdda_server_destroy", "tdda_request_bytes",
 ]
@@ -137,6 +138,7 @@ def load() -> ctypes.CDLL:
         "tdda_kernel_launches": (ctypes.c_ulonglong, []),
         "tdda_profile_aproduct": (i, [vp, i, i, i, dp]),
         "tdda_core_pass_count": (i, [vp, i]),
+        "tdda_core_pass_name": (ctypes.c_char_p, [vp, i, i]),
         "tdda_aproduct_noalloc": (i, [vp, vp, vp]),
         "tdda_server_create": (i, [ctypes.POINTER(ServerDesc), ctypes.POINTER(vp)]),
         "tdda_server_submit": (i, [vp, ctypes.POINTER(RequestDesc), ctypes.POINTER(ctypes.c_ulonglong)]),
@@ -244,6 +246,16 @@ class AProductCore:
         if n < 0:
             raise ValueError(f"pass_count: invalid precision {precision}")
         return n
+
+    def pass_names(self, precision: int = FP32_REFINE) -> list:
+        """Kernel of each of the five profile slots ("" where a fused kernel covers the slot)."""
+        out = []
+        for k in range(5):
+            n = load().tdda_core_pass_name(self.h, int(precision), k)
+            if n is None:
+                raise ValueError(f"pass_names: invalid precision {precision}")
+            out.append(n.decode())
+        return out
 
     def profile_aproduct(self, precision: int = FP32_REFINE, nrhs: int = 1, reps: int = 10) -> list:
         """Average ms of the five passes of one A-product (CUDA events on the core stream)."""
