@@ -136,6 +136,14 @@ tdda_status tdda_model_get(const tdda_model* model, int field, double* out, int 
 /* DDAModel::get_ITERATION (DDAModel.h:59). */
 int tdda_model_iterations(const tdda_model* model);
 
+/* The field at off-lattice points from the model's current P:
+ * E(r) = E0 nE0 exp(i K nK.r) - sum_i A(r - d R_i) P_i, with A the LDR tensor
+ * (ObjPointEDDAModel, ObjDDAModel.cpp:20-96; DDAModel::solve_E,
+ * DDAModel.cpp:530-565, which takes lattice indices: pass d * RResult).
+ * points: 3*npts doubles in nm; E: 3*npts complex (interleaved doubles);
+ * both in host or device memory per mem.  FP64; a point on a dipole site
+ * takes the zero tensor for that dipole. */
+tdda_status tdda_model_field_at(tdda_model* model, int npts, const double* points, double* E, int mem);
 /* batched solve: n models on one core, one launch per pass -------------- */
 /* The forward and adjoint solves of EvoDDAModel::EvoOptimization
  * (EvoDDAModel.cpp:435-436, 596-600), or several incidences on one lattice,

@@ -59,6 +59,7 @@ def lib() -> ctypes.CDLL:
         L.or_model_bicgstab.argtypes = [vp, ctypes.c_int, ctypes.c_double, ip, dp]
         L.or_model_update_E_in_structure.argtypes = [vp]
         L.or_model_get.argtypes = [vp, ctypes.c_int, dp]
+        L.or_model_field_at.argtypes = [vp, ctypes.c_int, dp, dp]
         _LIB = L
     return _LIB
 
@@ -190,6 +191,13 @@ class OracleModel:
     def InitializeP(self, P):
         P = _c128(P)
         lib().or_model_initialize_P(self.h, _dp(P.view(np.float64)))
+
+    def field_at(self, points) -> np.ndarray:
+        """E at off-lattice points (npts x 3, nm) -> npts x 3 complex (ObjDDAModel.cpp:83-96)."""
+        pts = np.ascontiguousarray(points, np.float64).reshape(-1, 3)
+        out = np.zeros((pts.shape[0], 3), np.complex128)
+        lib().or_model_field_at(self.h, pts.shape[0], _dp(pts), _dp(out.view(np.float64)))
+        return out
 
     def Aproductwithalb(self, b) -> np.ndarray:
         b = _c128(b)

@@ -8,10 +8,12 @@
  * Aproductwithalb / bicgstab / update_E_in_structure.
  *
  * I/O is raw little-endian binary (see tests/golden/make_golden.py):
- *   in : int32 mode (0 aprod, 1 solve, 2 ldr); int32 Nx Ny Nz N;
+ *   in : int32 mode (0 aprod, 1 solve, 2 ldr, 3 solve then the point-field
+ *        objective ObjPointEDDAModel::GetVal at points); int32 Nx Ny Nz N;
  *        f64 d lam nback; int32 nmat; f64 material[2 nmat]; f64 nK[3] E0 nE0[3];
  *        int32 max_it; f64 max_err; int32 R[3N]; f64 diel_old[3N];
  *        int32 nvec; f64 vec[nvec][6N]   (mode 2: vec = nvec points of 3 f64)
+ *        mode 3 appends int32 npts; f64 pts[npts][3]
  *   out: see the per-mode writers below.
  */
 #include <cstdio>
@@ -23,6 +25,7 @@
 #include "AProductCore.h"
 #include "CoreStructure.h"
 #include "DDAModel.h"
+#include "ObjDDAModel.h"
 #include "Space.h"
 #include "SpacePara.h"
 #include "Structure.h"
@@ -86,6 +89,12 @@ int main(int argc, char** argv) {
     size_t veclen = mode == 2 ? 3 : 6 * (size_t)N;
     std::vector<double> vecs(nvec * veclen);
     rd.get(vecs.data(), vecs.size());
+    std::vector<double> pts;
+    if (mode == 3) {
+        int npts = rd.get<int32_t>();
+        pts.resize(3 * (size_t)npts);
+        rd.get(pts.data(), pts.size());
+    }
     std::fclose(fi);
 
     // main.cpp:176-220 ("DDA input"): bulk space, one structure, SpacePara, CoreStructure
@@ -153,6 +162,14 @@ int main(int argc, char** argv) {
         std::fwrite(&it, 4, 1, fo);
         put_cvec(fo, *Model.get_P());
         put_cvec(fo, *Model.get_Einternal());
+        if (mode == 3) {
+            // ObjDDAModel.cpp:20-96: |E| at each point from the solved P
+            for (size_t p = 0; p + 2 < pts.size(); p += 3) {
+                ObjPointEDDAModel obj(std::vector<double>{pts[p], pts[p + 1], pts[p + 2]}, &Model);
+                double v = obj.GetVal();
+                std::fwrite(&v, 8, 1, fo);
+            }
+        }
     }
     std::fclose(fo);
     return 0;

@@ -465,6 +465,34 @@ void or_model_update_E_in_structure(or_model* m) {
     }
 }
 
+/* The field at off-lattice points: E(r) = E_ext(r) - sum_i A(r - d R_i) P_i
+ * with E_ext = E0 nE0 exp(i K nK.r), accumulated as ObjPointEDDAModel does
+ * (ObjDDAModel.cpp:42-44 for E_ext, :57-66 for the terms, :83-96 for the
+ * order: start at E_ext, subtract dipole by dipole).  DDAModel::solve_E
+ * (DDAModel.cpp:530-565) sums the same terms.  pts: npts x 3 in nm;
+ * E_out: npts x 3 complex, interleaved. */
+void or_model_field_at(const or_model* m, int npts, const double* pts, double* E_out) {
+    const or_core* c = m->core;
+    double A[12];
+    for (int p = 0; p < npts; p++) {
+        const double x = pts[3 * p], y = pts[3 * p + 1], z = pts[3 * p + 2];
+        const double ph = c->K * (m->nK[0] * x + m->nK[1] * y + m->nK[2] * z);
+        const cd e = cos(ph) + sin(ph) * I;
+        cd s[3];
+        for (int j = 0; j < 3; j++) s[j] = (m->E0 * m->nE0[j]) * e;
+        for (int i = 0; i < c->N; i++) {
+            or_ldr_inter(c->K, x - c->d * c->R[3 * i], y - c->d * c->R[3 * i + 1], z - c->d * c->R[3 * i + 2], A);
+            const cd a00 = A[0] + A[1] * I, a01 = A[2] + A[3] * I, a02 = A[4] + A[5] * I;
+            const cd a11 = A[6] + A[7] * I, a12 = A[8] + A[9] * I, a22 = A[10] + A[11] * I;
+            const cd px = m->P[3 * i], py = m->P[3 * i + 1], pz = m->P[3 * i + 2];
+            s[0] -= a00 * px + a01 * py + a02 * pz;
+            s[1] -= a01 * px + a11 * py + a12 * pz;
+            s[2] -= a02 * px + a12 * py + a22 * pz;
+        }
+        for (int j = 0; j < 3; j++) st(E_out, 3L * p + j, s[j]);
+    }
+}
+
 void or_model_get(const or_model* m, int what, double* out) {
     const cd* src = what == 0 ? m->P : what == 1 ? m->E : what == 2 ? m->al : what == 3 ? m->diel : m->Ein;
     for (long i = 0; i < m->n3; i++) st(out, i, src[i]);

@@ -67,6 +67,9 @@ void or_model_initialize_P(or_model* m, const double* P);
 int or_model_aproduct_with_alb(or_model* m, const double* b, double* y);
 int or_model_bicgstab(or_model* m, int max_it, double max_err, int* iterations, double* error);
 void or_model_update_E_in_structure(or_model* m);
+/* E(r) = E_ext(r) - sum_i A(r - d R_i) P_i at npts points (nm) into
+ * E_out (npts x 3 complex) */
+void or_model_field_at(const or_model* m, int npts, const double* pts, double* E_out);
 /* what: 0 P, 1 E, 2 al, 3 diel, 4 Einternal (each 3N complex) */
 void or_model_get(const or_model* m, int what, double* out);
 

@@ -1,6 +1,8 @@
 // Solves one lattice through the C++ drop-in (tdda.hpp) with the reference's
-// call sequence (main.cpp:245-251) and writes ITERATION, P and Einternal to a
-// file for tests/test_cpp_mirror.py to check against the oracle.
+// call sequence (main.cpp:245-251), then evaluates the field at the lattice
+// points RResult (solve_E, DDAModel.cpp:530-565), and writes ITERATION, P,
+// Einternal and EResult to a file for tests/test_cpp_mirror.py to check
+// against the oracle.
 //
 //   mirror_solve Nx Ny Nz d lam eps_re eps_im tol precision(0|1) out.bin
 // densities: rho_i = 0.5 + 0.5 sin(0.37 i), the same in the Python test.
@@ -65,18 +67,23 @@ int main(int argc, char** argv) {
     std::vector<std::complex<double>> material = {1.0, em};
     const double nK[3] = {0, 0, 1}, nE0[3] = {1, 0, 0};
     tdda::AProductCore Core(&S, lam, material, 1.0, "LDR");
-    tdda::DDAModel TestModel(&Core, nK, 1.0, nE0, false);
+    // RResult: lattice points (units of d) above, beside, past a corner of and far from the box
+    const std::vector<int> RResult = {S.Nx / 2, S.Ny / 2, S.Nz + 10, -5, S.Ny / 2, S.Nz / 2,
+                                      S.Nx + 3, -2, -4, 2 * S.Nx, 2 * S.Ny, 2 * S.Nz};
+    tdda::DDAModel TestModel(&Core, nK, 1.0, nE0, &RResult, false);
     if (precision == 0)
         TestModel.bicgstab(100000, tol);
     else
         TestModel.bicgstab_mixed(100000, tol);
     TestModel.update_E_in_structure();
+    TestModel.solve_E();
     FILE* f = std::fopen(argv[10], "wb");
     if (!f) return 2;
     const int it = TestModel.get_ITERATION();
     std::fwrite(&it, 4, 1, f);
     std::fwrite(TestModel.get_P()->data(), 16, TestModel.get_P()->size(), f);
     std::fwrite(TestModel.get_Einternal()->data(), 16, TestModel.get_Einternal()->size(), f);
+    std::fwrite(TestModel.get_EResult()->data(), 16, TestModel.get_EResult()->size(), f);
     std::fclose(f);
     std::printf("ITERATION %d P[0] %.17g %.17g\n", it, (*TestModel.get_P())[0].real(), (*TestModel.get_P())[0].imag());
     return 0;

@@ -10,6 +10,9 @@ on seeded inputs.  Each fixture stores its inputs and the reference's outputs:
                    DDAModel.cpp:577-586) of seeded vectors
   solve_*.npz      bicgstab + update_E_in_structure (DDAModel.cpp:131-260,
                    567-575): ITERATION, the printed Error, P, Einternal
+  field_*.npz      a solve, then the point-field objective
+                   ObjPointEDDAModel::GetVal (ObjDDAModel.cpp:20-96) at
+                   off-lattice points: |E_ext(r) - sum_i A(r - d R_i) P_i|
 
 Run from the repository root:  python tests/golden/make_golden.py
 It needs /root/reference, so it runs in the development container only; the
@@ -60,10 +63,15 @@ def write_input(path, mode, Nx, Ny, Nz, R, d, lam, nback, material, nK, E0, nE0,
             f.write(np.asarray(v).astype("<c16" if mode != 2 else "<f8").tobytes())
 
 
-def run(mode, **kw):
+def run(mode, points=None, **kw):
     with tempfile.TemporaryDirectory() as td:
         fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
         write_input(fin, mode, **kw)
+        if points is not None:
+            pts = np.ascontiguousarray(points, "<f8").reshape(-1, 3)
+            with open(fin, "ab") as f:
+                f.write(struct.pack("<i", pts.shape[0]))
+                f.write(pts.tobytes())
         pr = subprocess.run([DRIVER, fin, fout], capture_output=True, text=True, check=True)
         with open(fout, "rb") as f:
             raw = f.read()
@@ -163,6 +171,21 @@ def gen_solve(name, w: lattice.Workload, inc=None, P0=None, Ein=None, max_it=100
     print(f"solve_{name}: N={N} iterations={it} error={err:.6g} P[0]={P[0]}")
 
 
+def gen_field(name, w: lattice.Workload, points, inc=None):
+    N = w.N
+    pts = np.asarray(points, np.float64).reshape(-1, 3)
+    raw, _ = run(3, points=pts, **case_kw(w, inc), vecs=[])
+    off = 12 * N + 48 * N
+    it = struct.unpack_from("<i", raw, off)[0]
+    off += 4
+    P = np.frombuffer(raw, "<c16", count=3 * N, offset=off)
+    off += 96 * N
+    absE = np.frombuffer(raw, "<f8", count=pts.shape[0], offset=off)
+    np.savez_compressed(os.path.join(HERE, f"field_{name}.npz"), **inputs_dict(w, inc), iterations=it, P=P,
+                        points=pts, absE=absE)
+    print(f"field_{name}: N={N} iterations={it} |E|={absE}")
+
+
 def main():
     build_driver()
     gen_ldr()
@@ -182,6 +205,13 @@ def main():
     # warm start + a replaced right-hand side (the adjoint's change_E / InitializeP)
     wa = small_workload("adj8x8x4", 8, 8, 4, 15)
     gen_solve("adj8x8x4", wa, P0=0.01 * rand_vec(3 * wa.N, 400), Ein=rand_vec(3 * wa.N, 500))
+    # the point field of the solved cfg 1 structure: above the centre (the topology objective's
+    # point), beside, below, far off, and inside the box between lattice sites
+    gen_field("cfg1", lattice.config(1), [[95.0, 95.0, 190.0], [-50.0, 95.0, 45.0], [95.0, 95.0, -80.0],
+                                          [300.0, -100.0, 400.0], [95.0, 95.0, 45.0], [12.5, 3.0, 51.0]])
+    # the same on the sparse lattice under oblique incidence (every n_K component in E_ext)
+    gen_field("sparse10x9x6", ws, [[45.0, 40.0, 150.0], [-30.0, 0.0, 25.0], [140.0, 100.0, -40.0],
+                                   [47.5, 42.5, 27.5]], inc)
 
 
 if __name__ == "__main__":

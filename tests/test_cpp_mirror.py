@@ -1,8 +1,8 @@
 """The C++ drop-in (topo-dda-forwin64_gb300/cpp/tdda.hpp) used with the reference's call sequence.
 
 tests/cpp/mirror_solve.cpp builds a structure with the reference CoreStructure's getters,
-constructs AProductCore / DDAModel, runs bicgstab + update_E_in_structure and dumps the
-results; here they are compared with the oracle.  Compiling is a CPU test; running is a
+constructs AProductCore / DDAModel (with RResult points), runs bicgstab +
+update_E_in_structure + solve_E and dumps the results; here they are compared with the oracle.  Compiling is a CPU test; running is a
 GPU test.
 """
 import math
@@ -58,5 +58,9 @@ def test_mirror_solve_matches_oracle(tmp_path, precision, tol, bound):
     assert om.bicgstab(100000, 1e-12) == O.CONVERGED
     om.update_E_in_structure()
     assert it > 0, r.stdout
+    EResult = np.frombuffer(raw, "<c16", count=12, offset=4 + 96 * N)
+    RResult = np.array([[Nx // 2, Ny // 2, Nz + 10], [-5, Ny // 2, Nz // 2], [Nx + 3, -2, -4],
+                        [2 * Nx, 2 * Ny, 2 * Nz]], np.float64)
     assert rel(P, om.P) <= bound
     assert rel(Ein, om.Einternal) <= bound
+    assert rel(EResult, om.field_at(d * RResult).ravel()) <= bound

@@ -215,3 +215,25 @@ def test_update_alpha_matches_oracle():
     assert rel(m.get_al(), om.al) <= 1e-14
     m.reset_E()
     assert rel(m.get_E(), om.E) <= 1e-14  # device sincos against the host libm
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["cfg1", "sparse10x9x6"])
+def test_point_field_matches_reference(name):
+    """E at off-lattice points (tdda_model_field_at) from the reference's solved P:
+    |E| against ObjPointEDDAModel::GetVal run by the reference, the components against the
+    oracle's sum (ObjDDAModel.cpp:20-96)."""
+    g = golden(f"field_{name}.npz")
+    Nx, Ny, Nz = (int(v) for v in g["box"])
+    core = tdda.AProductCore(Nx, Ny, Nz, g["R"], float(g["d"]), float(g["lam"]), g["material"], float(g["nback"]))
+    m = tdda.DDAModel(core, g["nK"], float(g["E0"]), g["nE0"], g["diel_old"])
+    m.InitializeP(g["P"])
+    E = m.field_at(g["points"])
+    absE = np.sqrt(np.sum(np.abs(E) ** 2, axis=1))
+    assert np.max(np.abs(absE - g["absE"]) / g["absE"]) <= 1e-12
+    oc = O.OracleCore(Nx, Ny, Nz, g["R"], float(g["d"]), float(g["lam"]), g["material"], float(g["nback"]))
+    om = O.OracleModel(oc, g["nK"], float(g["E0"]), g["nE0"], g["diel_old"])
+    om.InitializeP(g["P"])
+    assert rel(E.ravel(), om.field_at(g["points"]).ravel()) <= 1e-12
+    m.close()
+    core.close()

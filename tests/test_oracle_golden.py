@@ -102,3 +102,17 @@ def test_solve_rounding_sensitivity():
     assert st == O.CONVERGED
     assert rel(mt.P, gt["P"]) <= 1e-9
     assert rel(mt.Einternal, gt["Einternal"]) <= 1e-9
+
+
+@pytest.mark.parametrize("name", ["cfg1", "sparse10x9x6"])
+def test_point_field_matches_reference(name):
+    """E at off-lattice points from the solved P (ObjPointEDDAModel::GetVal,
+    ObjDDAModel.cpp:20-96): the restated sum reproduces the reference's |E|."""
+    g = golden(f"field_{name}.npz")
+    Nx, Ny, Nz = (int(v) for v in g["box"])
+    core = O.OracleCore(Nx, Ny, Nz, g["R"], float(g["d"]), float(g["lam"]), g["material"], float(g["nback"]))
+    m = O.OracleModel(core, g["nK"], float(g["E0"]), g["nE0"], g["diel_old"])
+    m.InitializeP(g["P"])
+    E = m.field_at(g["points"])
+    absE = np.sqrt(np.sum(np.abs(E) ** 2, axis=1))
+    assert np.max(np.abs(absE - g["absE"]) / g["absE"]) <= 1e-13

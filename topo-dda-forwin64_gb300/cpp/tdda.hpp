@@ -163,6 +163,17 @@ template <class VectorXcd = std::vector<cplx>> class DDAModelT {
         al_ = VectorXcd(n3_);
         fetch(TDDA_FIELD_AL, al_);
     }
+    // DDAModel(AProductCore*, Vector3d n_K, double E0, Vector3d n_E0, VectorXi* RResult,
+    // bool verbose = true) (DDAModel.cpp:71-108): solve_E evaluates the field at the lattice
+    // points RResult (3 integers per point, in units of d)
+    template <class V3, class VI>
+    DDAModelT(AProductCore* Core, const V3& n_K, double E0, const V3& n_E0, const VI* RResult, bool verbose = true)
+        : DDAModelT(Core, n_K, E0, n_E0, verbose) {
+        if (RResult->size() % 3 != 0) throw std::invalid_argument("RResult does not have a size with 3*integer");
+        rresult_.resize(RResult->size());
+        for (size_t i = 0; i < rresult_.size(); i++) rresult_[i] = Core->get_d() * (double)(*RResult)[i];
+        EResult_ = VectorXcd(rresult_.size());
+    }
     DDAModelT(const DDAModelT&) = delete;
     DDAModelT& operator=(const DDAModelT&) = delete;
     ~DDAModelT() { tdda_model_destroy(h_); }
@@ -200,7 +211,18 @@ template <class VectorXcd = std::vector<cplx>> class DDAModelT {
         check(tdda_model_update_E_in_structure(h_), "update_E_in_structure");
         fetch(TDDA_FIELD_EINTERNAL, Einternal_);
     }
-    void solve_E() {}  // on-lattice fields only: EResult == Einternal (DDAModel.cpp:560-562)
+    // DDAModel.cpp:530-565: with RResult, E = E_ext - sum_i A(r - d R_i) P_i at d * RResult
+    // (the incident field as ObjDDAModel.cpp:42-44 writes it; the reference's solve_E mixes
+    // up the coordinates in two of its three phase terms, :544-545); without, Einternal.
+    void solve_E() {
+        if (rresult_.empty()) {
+            EResult_ = Einternal_;
+            return;
+        }
+        check(tdda_model_field_at(h_, (int)(rresult_.size() / 3), rresult_.data(), dptr(EResult_), TDDA_MEM_HOST),
+              "solve_E");
+    }
+    VectorXcd* get_EResult() { return &EResult_; }
 
     VectorXcd* get_P() { return &P_; }
     VectorXcd* get_Einternal() { return &Einternal_; }
@@ -213,6 +235,8 @@ template <class VectorXcd = std::vector<cplx>> class DDAModelT {
     tdda_model* handle() const { return h_; }
 
    private:
+    std::vector<double> rresult_;  // d * RResult, nm
+    VectorXcd EResult_;
     void fetch(int field, VectorXcd& out) {
         check(tdda_model_get(h_, field, dptr(out), TDDA_MEM_HOST), "DDAModel get");
     }

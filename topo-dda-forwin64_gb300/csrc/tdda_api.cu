@@ -1141,6 +1141,43 @@ tdda_status tdda_model_get(const tdda_model* m, int field, double* out, int mem)
 
 int tdda_model_iterations(const tdda_model* m) { return m ? m->ITERATION : -1; }
 
+tdda_status tdda_model_field_at(tdda_model* m, int npts, const double* points, double* E, int mem) {
+    if (!m || npts < 0 || (npts > 0 && (!points || !E))) {
+        set_err("invalid argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    if (npts == 0) return TDDA_OK;
+    tdda_core* c = m->core;
+    TDDA_TRY(set_device(c->device));
+    const int nb = tdda::field_blocks(c->N, npts);
+    std::vector<void*> tmp;
+    double* dpts = nullptr;
+    double2 *part = nullptr, *dE = nullptr;
+    tdda_status st = dalloc(tmp, &part, 3 * (size_t)nb * npts, c->stream);
+    if (st == TDDA_OK && mem != TDDA_MEM_DEVICE) st = dalloc(tmp, &dpts, 3 * (size_t)npts, c->stream);
+    if (st == TDDA_OK && mem != TDDA_MEM_DEVICE) st = dalloc(tmp, &dE, 3 * (size_t)npts, c->stream);
+    cudaError_t e = cudaSuccess;
+    if (st == TDDA_OK) {
+        if (mem != TDDA_MEM_DEVICE) {
+            e = cudaMemcpyAsync(dpts, points, sizeof(double) * 3 * (size_t)npts, cudaMemcpyHostToDevice, c->stream);
+        } else {
+            dpts = const_cast<double*>(points);
+            dE = reinterpret_cast<double2*>(E);
+        }
+        count_launches(2 * ((npts + 32767) / 32768));
+        if (e == cudaSuccess)
+            e = tdda::launch_field_at(c->N, c->Rdev, c->d, c->K, m->P, npts, dpts, make_double3(m->nK[0], m->nK[1], m->nK[2]),
+                                      make_double3(m->nE0[0], m->nE0[1], m->nE0[2]), m->E0, part, dE, c->stream);
+        if (e == cudaSuccess && mem != TDDA_MEM_DEVICE)
+            e = cudaMemcpyAsync(E, dE, sizeof(double2) * 3 * (size_t)npts, cudaMemcpyDeviceToHost, c->stream);
+    }
+    free_all(tmp, c->stream);
+    if (st != TDDA_OK) return st;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "field at points");
+    return TDDA_OK;
+}
+
 tdda_status tdda_fft3d(double* data, int n0, int n1, int n2, int sign) {
     AxisPlan p[3];
     int n[3] = {n0, n1, n2};

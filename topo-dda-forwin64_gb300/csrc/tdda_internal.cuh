@@ -187,6 +187,12 @@ cudaError_t launch_model_alpha(int n3, const double* diel_old, const AlphaParams
 cudaError_t launch_model_incident(int N, const int* R, double3 nK, double3 nE0, double E0, double K, double d,
                                   double2* E, cudaStream_t stream);
 
+// E at npts points (nm): E_ext - sum_i A(r - d R_i) P_i, FP64 (ObjDDAModel.cpp:42-96).
+// part holds 3 * field_blocks(N, npts) * npts double2.
+int field_blocks(int N, int npts);
+cudaError_t launch_field_at(int N, const int* R, double d, double K, const double2* P, int npts, const double* pts,
+                            double3 nK, double3 nE0, double E0, double2* part, double2* E, cudaStream_t stream);
+
 // Einternal = al P / ((2 + eps) / 3)       (DDAModel.cpp:567-575)
 cudaError_t launch_einternal(int n3, const double2* al, const double2* P, const double2* diel, double2* Ein,
                              cudaStream_t stream);

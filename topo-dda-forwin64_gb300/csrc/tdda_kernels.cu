@@ -108,6 +108,33 @@ __global__ void __launch_bounds__(kNT) k_solve_begin(int n3, const RhsVecs<T>* _
 }
 
 // ================================================================ K0 green
+// LDR_inter (AProductCore.cpp:588-623) at the offset (x, y, z) nm: the six
+// components xx, xy, xz, yy, yz, zz; r = 0 gives the zero tensor
+__device__ __forceinline__ void ldr_tensor(double K, double x, double y, double z, double2 (&t)[6]) {
+    const double xs = x * x, ys = y * y, zs = z * z;
+    const double rn = sqrt(xs + ys + zs);
+    if (rn == 0.0) {
+#pragma unroll
+        for (int l = 0; l < 6; l++) t[l] = make_double2(0.0, 0.0);
+        return;
+    }
+    const double rsq = rn * rn, rcu = rn * rn * rn;
+    double sn, cs;
+    sincos(K * rn, &sn, &cs);
+    const double2 c1 = make_double2(cs / rcu, sn / rcu);        // e^{iKr} / r^3
+    const double2 c2 = make_double2(1.0 / rsq, -(K * rn) / rsq);  // (1 - iKr) / r^2
+    const double2 c3 = make_double2(K * K - 3.0 * c2.x, -3.0 * c2.y);
+    double2 v[6];
+    v[0] = make_double2(c2.x * (rsq - 3 * xs) - K * K * (ys + zs), c2.y * (rsq - 3 * xs));
+    v[1] = make_double2(x * y * c3.x, x * y * c3.y);
+    v[2] = make_double2(z * x * c3.x, z * x * c3.y);
+    v[3] = make_double2(c2.x * (rsq - 3 * ys) - K * K * (zs + xs), c2.y * (rsq - 3 * ys));
+    v[4] = make_double2(y * z * c3.x, y * z * c3.y);
+    v[5] = make_double2(c2.x * (rsq - 3 * zs) - K * K * (xs + ys), c2.y * (rsq - 3 * zs));
+#pragma unroll
+    for (int l = 0; l < 6; l++) t[l] = dmul(c1, v[l]);
+}
+
 __global__ void k_green_real(Geom g, double K, double d, double2* __restrict__ full6) {
     const int Mx = g.px.M, My = g.py.M, Mz = g.pz.M;
     const long long M = (long long)Mx * My * Mz;
@@ -120,33 +147,68 @@ __global__ void k_green_real(Geom g, double K, double d, double2* __restrict__ f
         int oy = j < g.Ny ? j : (j > My - g.Ny ? j - My : INT32_MIN);
         int oz = k < g.Nz ? k : (k > Mz - g.Nz ? k - Mz : INT32_MIN);
         double2 t[6];
-#pragma unroll
-        for (int l = 0; l < 6; l++) t[l] = make_double2(0.0, 0.0);
         if (ox != INT32_MIN && oy != INT32_MIN && oz != INT32_MIN) {
-            // LDR_inter (AProductCore.cpp:588-623); r = 0 gives the zero tensor
-            const double x = d * ox, y = d * oy, z = d * oz;
-            const double xs = x * x, ys = y * y, zs = z * z;
-            const double rn = sqrt(xs + ys + zs);
-            if (rn != 0.0) {
-                const double rsq = rn * rn, rcu = rn * rn * rn;
-                double sn, cs;
-                sincos(K * rn, &sn, &cs);
-                const double2 c1 = make_double2(cs / rcu, sn / rcu);        // e^{iKr} / r^3
-                const double2 c2 = make_double2(1.0 / rsq, -(K * rn) / rsq);  // (1 - iKr) / r^2
-                const double2 c3 = make_double2(K * K - 3.0 * c2.x, -3.0 * c2.y);
-                double2 v[6];
-                v[0] = make_double2(c2.x * (rsq - 3 * xs) - K * K * (ys + zs), c2.y * (rsq - 3 * xs));
-                v[1] = make_double2(x * y * c3.x, x * y * c3.y);
-                v[2] = make_double2(z * x * c3.x, z * x * c3.y);
-                v[3] = make_double2(c2.x * (rsq - 3 * ys) - K * K * (zs + xs), c2.y * (rsq - 3 * ys));
-                v[4] = make_double2(y * z * c3.x, y * z * c3.y);
-                v[5] = make_double2(c2.x * (rsq - 3 * zs) - K * K * (xs + ys), c2.y * (rsq - 3 * zs));
+            ldr_tensor(K, d * ox, d * oy, d * oz, t);
+        } else {
 #pragma unroll
-                for (int l = 0; l < 6; l++) t[l] = dmul(c1, v[l]);
-            }
+            for (int l = 0; l < 6; l++) t[l] = make_double2(0.0, 0.0);
         }
 #pragma unroll
         for (int l = 0; l < 6; l++) full6[l * M + e] = t[l];
+    }
+}
+
+// ================================================================ field at points
+// E(r_p) = E_ext(r_p) - sum_i A(r_p - d R_i) P_i (ObjDDAModel.cpp:42-96,
+// DDAModel.cpp:530-565), FP64.  Pass 1: block (b, p) sums the dipoles
+// i = b*nt + t, b*nt + t + gridDim.x*nt, ... for point p in a fixed order and
+// writes its three complex partials; pass 2 adds the nb partials of each point
+// in block order and subtracts them from the incident field.
+__global__ void __launch_bounds__(kNT) k_field_partial(int N, const int* __restrict__ R, double d, double K,
+                                                       const double2* __restrict__ P, const double* __restrict__ pts,
+                                                       double2* __restrict__ part) {
+    __shared__ double sred[6 * kNT];
+    const int p = blockIdx.y;
+    const double x = pts[3 * p], y = pts[3 * p + 1], z = pts[3 * p + 2];
+    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        double2 t[6];
+        ldr_tensor(K, x - d * R[3 * i], y - d * R[3 * i + 1], z - d * R[3 * i + 2], t);
+        const double2 px = P[3 * i], py = P[3 * i + 1], pz = P[3 * i + 2];
+        const double2 s0 = dmul(t[0], px), s1 = dmul(t[1], py), s2 = dmul(t[2], pz);
+        const double2 u0 = dmul(t[1], px), u1 = dmul(t[3], py), u2 = dmul(t[4], pz);
+        const double2 w0 = dmul(t[2], px), w1 = dmul(t[4], py), w2 = dmul(t[5], pz);
+        acc[0] += s0.x + s1.x + s2.x;
+        acc[1] += s0.y + s1.y + s2.y;
+        acc[2] += u0.x + u1.x + u2.x;
+        acc[3] += u0.y + u1.y + u2.y;
+        acc[4] += w0.x + w1.x + w2.x;
+        acc[5] += w0.y + w1.y + w2.y;
+    }
+    block_sum<6>(acc, sred);
+    if (threadIdx.x == 0) {
+        double2* o = part + ((long long)p * gridDim.x + blockIdx.x) * 3;
+        o[0] = make_double2(acc[0], acc[1]);
+        o[1] = make_double2(acc[2], acc[3]);
+        o[2] = make_double2(acc[4], acc[5]);
+    }
+}
+
+__global__ void k_field_sum(int npts, int nb, const double2* __restrict__ part, const double* __restrict__ pts,
+                            double3 nK, double3 nE0, double E0, double K, double2* __restrict__ E) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npts) return;
+    double sn, cs;
+    sincos(K * (nK.x * pts[3 * p] + nK.y * pts[3 * p + 1] + nK.z * pts[3 * p + 2]), &sn, &cs);
+    const double amp[3] = {E0 * nE0.x, E0 * nE0.y, E0 * nE0.z};
+    for (int j = 0; j < 3; j++) {
+        double2 s = make_double2(0.0, 0.0);
+        for (int b = 0; b < nb; b++) {
+            const double2 v = part[((long long)p * nb + b) * 3 + j];
+            s.x += v.x;
+            s.y += v.y;
+        }
+        E[3 * p + j] = make_double2(amp[j] * cs - s.x, amp[j] * sn - s.y);
     }
 }
 
@@ -451,6 +513,29 @@ cudaError_t launch_residual_is_rhs(const Geom& g, int nrhs, const RhsVecs<T>* rh
     const dim3 gr(grid_reduce(3LL * g.N, sizeof(T) == 4), nrhs);
     k_solve_begin<T><<<gr, kNT, 0, stream>>>(3 * g.N, rhs, 1);
     return cudaGetLastError();
+}
+
+int field_blocks(int N, int npts) {
+    const int per_point = std::max(1, (N + kNT - 1) / kNT);
+    const int fill = std::max(1, (152 * 8) / std::max(1, npts));
+    return std::min(per_point, fill);
+}
+
+cudaError_t launch_field_at(int N, const int* R, double d, double K, const double2* P, int npts, const double* pts,
+                            double3 nK, double3 nE0, double E0, double2* part, double2* E, cudaStream_t stream) {
+    const int nb = field_blocks(N, npts);
+    constexpr int kChunk = 32768;  // points per launch (gridDim.y <= 65535)
+    for (int p0 = 0; p0 < npts; p0 += kChunk) {
+        const int np = std::min(kChunk, npts - p0);
+        double2* pp = part + 3LL * nb * p0;
+        k_field_partial<<<dim3(nb, np), kNT, 0, stream>>>(N, R, d, K, P, pts + 3LL * p0, pp);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        k_field_sum<<<grid1d(np, 128), 128, 0, stream>>>(np, nb, pp, pts + 3LL * p0, nK, nE0, E0, K, E + 3LL * p0);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_einternal(int n3, const double2* al, const double2* P, const double2* diel, double2* Ein,

@@ -41,7 +41,8 @@ EXPORTS = [
     "tdda_core_info", "tdda_aproduct", "tdda_core_ldr_inter", "tdda_model_create", "tdda_model_destroy",
     "tdda_model_update_alpha", "tdda_model_update_alpha_single", "tdda_model_change_E", "tdda_model_reset_E",
     "tdda_model_initialize_P", "tdda_model_aproduct_with_alb", "tdda_model_bicgstab", "tdda_model_solve_mixed",
-    "tdda_model_update_E_in_structure", "tdda_model_get", "tdda_model_iterations", "tdda_solve_batch",
+    "tdda_model_update_E_in_structure", "tdda_model_get", "tdda_model_iterations", "tdda_model_field_at",
+    "tdda_solve_batch",
     "tdda_fft3d", "tdda_core_stream", "tdda_kernel_launches", "tdda_profile_aproduct", "tdda_core_pass_count",
     "tdda_core_pass_name",
     "tdda_aproduct_noalloc", "tdda_server_create", "tdda_server_submit", "tdda_server_result",
@@ -132,6 +133,7 @@ def load() -> ctypes.CDLL:
         "tdda_model_update_E_in_structure": (i, [vp]),
         "tdda_model_get": (i, [vp, i, vp, i]),
         "tdda_model_iterations": (i, [vp]),
+        "tdda_model_field_at": (i, [vp, i, vp, vp, i]),
         "tdda_solve_batch": (i, [ctypes.POINTER(vp), i, i, i, d, ctypes.POINTER(SolveInfo)]),
         "tdda_fft3d": (i, [vp, i, i, i, i]),
         "tdda_core_stream": (i, [vp, ctypes.POINTER(vp)]),
@@ -319,6 +321,15 @@ class DDAModel:
     def get_diel(self): return self._get(FIELD_DIEL)
     def get_Einternal(self): return self._get(FIELD_EINTERNAL)
     def get_ITERATION(self) -> int: return load().tdda_model_iterations(self.h)
+
+    def field_at(self, points) -> np.ndarray:
+        """E at off-lattice points (npts x 3, nm) from the current P: npts x 3 complex
+        (ObjDDAModel.cpp:20-96; DDAModel::solve_E with points d * RResult)."""
+        pts = np.ascontiguousarray(points, np.float64).reshape(-1, 3)
+        out = np.zeros((pts.shape[0], 3), np.complex128)
+        _check(load().tdda_model_field_at(self.h, pts.shape[0], _ptr(pts), _ptr(out), MEM_HOST),
+               "tdda_model_field_at")
+        return out
 
     def UpdateAlpha(self, diel_old):
         diel = np.ascontiguousarray(diel_old, np.float64)
