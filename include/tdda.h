@@ -117,7 +117,8 @@ tdda_status tdda_model_update_alpha(tdda_model* model, const double* diel_old);
 /* DDAModel::UpdateAlphaSingle (DDAModel.cpp:489-528) after the density of
  * dipole idx became `value` (CoreStructure::UpdateStrSingle). */
 tdda_status tdda_model_update_alpha_single(tdda_model* model, int idx, double value);
-/* DDAModel::change_E / reset_E / InitializeP (DDAModel.cpp:453-468, 731-733). */
+/* DDAModel::change_E / reset_E / InitializeP (DDAModel.cpp:453-468, 731-733).
+ * InitializeP with P = NULL sets P = 0 on the device without a transfer. */
 tdda_status tdda_model_change_E(tdda_model* model, const double* E, int mem);
 tdda_status tdda_model_reset_E(tdda_model* model);
 tdda_status tdda_model_initialize_P(tdda_model* model, const double* P, int mem);
@@ -144,6 +145,22 @@ int tdda_model_iterations(const tdda_model* model);
  * both in host or device memory per mem.  FP64; a point on a dipole site
  * takes the zero tensor for that dipole. */
 tdda_status tdda_model_field_at(tdda_model* model, int npts, const double* points, double* E, int mem);
+
+/* Adjoint sensitivity of the design densities, the product of the adjoint
+ * field with the derivative of the system matrix (EvoDDAModel.cpp:610-638):
+ *   s[i] = sum over the dipoles j of parameter i of
+ *          Re( sum_c lambda[3j+c] * dal_j/drho_j * P[3j+c] )
+ * with P the forward model's polarisation, lambda = sum_k coef[k] P(adj[k])
+ * (the adjoint solutions, 1 <= nadj <= 8, coef as nadj interleaved complex),
+ * and dal/drho the derivative of the forward model's inverse LDR
+ * polarisability (tools.cpp:617-630) through its density interpolation
+ * (DDAModel.cpp:54-63; 0 above density 1, where the table is piecewise
+ * constant).  Parameter i owns dipoles[offsets[i] .. offsets[i+1]-1] (the
+ * reference's Paratogeometry lists).  FP64, each sum in list order.  The
+ * reference's gradient is devx - s (EvoDDAModel.cpp:640); for a point-|E|^2
+ * objective with coef = conj(E_obs) over the basis adjoints it is -2 s. */
+tdda_status tdda_model_density_gradient(const tdda_model* fwd, int nadj, tdda_model* const* adj, const double* coef,
+                                        int nparam, const int* offsets, const int* dipoles, double* s);
 /* batched solve: n models on one core, one launch per pass -------------- */
 /* The forward and adjoint solves of EvoDDAModel::EvoOptimization
  * (EvoDDAModel.cpp:435-436, 596-600), or several incidences on one lattice,

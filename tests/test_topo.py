@@ -1,11 +1,14 @@
 """The topology-optimisation loop (tdda/topo.py): the caller of the solve path.
 
 CPU: the LDR tensor restated with numpy equals the oracle's; the design map's transpose
-is its adjoint; dal/deps equals a finite difference of 1/alpha_LDR.  GPU: the adjoint
-gradient (forward + 3 basis adjoints batched) equals central finite differences of the
-objective, and gradient ascent raises the objective.
+is its adjoint; dal/deps equals a finite difference of 1/alpha_LDR; the optimiser moments
+follow EvoDDAModel.cpp:673-731.  GPU: the device objective and sensitivity equal their host
+restatement from the downloaded fields; the adjoint gradient (forward + 3 basis adjoints
+batched) equals central finite differences of the objective; gradient ascent raises the
+objective.
 """
 import math
+from types import SimpleNamespace
 
 import numpy as np
 import pytest
@@ -13,6 +16,7 @@ import pytest
 import oracle as O
 import tdda
 from tdda import topo
+from conftest import rel
 
 
 def test_ldr_tensor_matches_oracle():
@@ -82,3 +86,51 @@ def test_gradient_ascent_raises_the_objective():
     f = [loop.step().objective for _ in range(6)]
     loop.close()
     assert f[-1] > f[0]
+
+
+def test_adam_moments_follow_the_reference():
+    """EvoDDAModel.cpp:673-690: bias correction inside the moving averages, beta2 = 1 - (1-beta1)^2."""
+    st = SimpleNamespace(iteration=0, method="Adam", epsilon=0.05, V=None, S_ad=None, gsq=None)
+    g0 = np.array([[0.3, -2.0]])
+    out0, eps0 = topo.TopoLoop._moments(st, g0.copy())
+    assert np.allclose(out0, g0 / (np.abs(g0) + 1e-8)) and eps0 == 0.1
+    st.iteration = 4
+    g1 = np.array([[-0.1, 1.0]])
+    b1, b2 = 0.9, 1 - 0.1 ** 2
+    V = b1 * g0 + (1 - b1) * g1 / (1 - b1 ** 5)
+    S = b2 * g0 ** 2 + (1 - b2) * g1 ** 2 / (1 - b2 ** 5)
+    out1, eps1 = topo.TopoLoop._moments(st, g1.copy())
+    assert np.allclose(out1, V / (np.sqrt(S) + 1e-8)) and eps1 == 0.05
+    ag = SimpleNamespace(iteration=0, method="Adagrad", epsilon=0.1, gsq=np.zeros((1, 2)))
+    out, _ = topo.TopoLoop._moments(ag, g0.copy())
+    assert np.allclose(out, g0 / np.sqrt(g0 ** 2 / 100000 + 1))
+
+
+@pytest.mark.gpu
+def test_device_glue_equals_host_restatement():
+    """tdda_model_field_at and tdda_model_density_gradient against the same quantities
+    formed on the host from the downloaded forward and adjoint fields."""
+    if tdda.device_count() < 1:
+        pytest.skip("no CUDA device")
+    Nx, Ny, Nz, d = 8, 6, 4, 10.0
+    rng = np.random.Generator(np.random.PCG64(10))
+    dm = topo.DesignMap(Nx, Ny, 2.0)
+    th0 = 0.3 + 0.4 * rng.random((dm.hx, dm.hy))
+    r_obs = (d * (Nx - 1) / 2 + 3.0, d * (Ny - 1) / 2, d * (Nz - 1) + 80.0)
+    mat = np.array([1.0, 6.25 + 0.05j])
+    loop = topo.TopoLoop(Nx, Ny, Nz, d, 550.0, mat, th0, r_obs, precision=tdda.FP64, tol=1e-11,
+                         nK=(math.sin(0.3), 0.0, math.cos(0.3)), nE0=(math.cos(0.3), 0.0, -math.sin(0.3)))
+    r = loop.evaluate()
+    P = loop.fwd.get_P()
+    lams = [a.get_P() for a in loop.adj]
+    E_obs = loop.Einc_obs + loop.b @ P
+    assert r.objective == pytest.approx(float(np.sum(np.abs(E_obs) ** 2)), rel=1e-12)
+    lam = sum(np.conj(E_obs[k]) * lams[k] for k in range(3))
+    diel = loop._diel()
+    m = loop.mat
+    eps = m[0] + diel * (m[1] - m[0])
+    dal = topo.dal_deps(eps, loop.K, d, loop.S) * (m[1] - m[0])
+    g_dip = -2.0 * np.real((lam * dal * P).reshape(-1, 3).sum(axis=1))
+    g_host = dm.grad_theta(g_dip.reshape(Nx, Ny, Nz).sum(axis=2))
+    assert rel(r.grad_theta, g_host) <= 1e-10
+    loop.close()

@@ -278,6 +278,23 @@ RhsVecs<float> vecs32(tdda_core* c, tdda_model* m, int slot) {
 }
 
 // incident field and polarisability of a model (DDAModel.cpp:47-63)
+
+// LDR polarisability constants of one model (tools.cpp:617-630) and the
+// normalised material table (AProductCore.cpp:19-24)
+tdda::AlphaParams alpha_params(const tdda_model* m) {
+    const tdda_core* c = m->core;
+    tdda::AlphaParams ap;
+    std::memset(&ap, 0, sizeof(ap));
+    ap.a1c = 3 * std::pow(c->d, 3) / (4 * kPi);
+    ap.d3 = std::pow(c->d, 3);
+    ap.Kd2 = std::pow(c->K * c->d, 2);
+    ap.rad = (2.0 / 3.0) * std::pow(c->K * c->d, 3);
+    ap.S = std::pow(m->nE0[0] * m->nK[0], 2) + std::pow(m->nE0[1] * m->nK[1], 2) + std::pow(m->nE0[2] * m->nK[2], 2);
+    ap.nmat = c->nmat;
+    for (int k = 0; k < c->nmat; k++) ap.mat[k] = make_double2(c->material[k].real(), c->material[k].imag());
+    return ap;
+}
+
 tdda_status model_upload_fields(tdda_model* m, bool field_E, bool field_al) {
     tdda_core* c = m->core;
     const int N = c->N;
@@ -301,15 +318,7 @@ tdda_status model_upload_fields(tdda_model* m, bool field_E, bool field_al) {
                 return TDDA_ERR_INVALID_ARGUMENT;
             }
         }
-        tdda::AlphaParams ap;
-        std::memset(&ap, 0, sizeof(ap));
-        ap.a1c = 3 * std::pow(c->d, 3) / (4 * kPi);
-        ap.d3 = std::pow(c->d, 3);
-        ap.Kd2 = std::pow(c->K * c->d, 2);
-        ap.rad = (2.0 / 3.0) * std::pow(c->K * c->d, 3);
-        ap.S = std::pow(m->nE0[0] * m->nK[0], 2) + std::pow(m->nE0[1] * m->nK[1], 2) + std::pow(m->nE0[2] * m->nK[2], 2);
-        ap.nmat = c->nmat;
-        for (int k = 0; k < c->nmat; k++) ap.mat[k] = make_double2(c->material[k].real(), c->material[k].imag());
+        const tdda::AlphaParams ap = alpha_params(m);
         TDDA_CK(cudaMemcpyAsync(m->dold, m->diel_old.data(), sizeof(double) * 3 * (size_t)N, cudaMemcpyHostToDevice,
                                 c->stream));
         TDDA_CK1(tdda::launch_model_alpha(3 * N, m->dold, ap, m->diel, m->al, m->fal, c->stream));
@@ -1050,12 +1059,18 @@ tdda_status tdda_model_reset_E(tdda_model* m) {
 }
 
 tdda_status tdda_model_initialize_P(tdda_model* m, const double* P, int mem) {
-    if (!m || !P) {
-        set_err("null argument");
+    if (!m) {
+        set_err("null model");
         return TDDA_ERR_INVALID_ARGUMENT;
     }
     TDDA_TRY(set_device(m->core->device));
     const size_t n = 6 * (size_t)m->core->N;
+    if (!P) {  // P = 0 without a transfer
+        TDDA_CK(cudaMemsetAsync(m->P, 0, sizeof(double) * n, m->core->stream));
+        TDDA_CK(cudaStreamSynchronize(m->core->stream));
+        m->P_zero = true;
+        return TDDA_OK;
+    }
     TDDA_CK(cudaMemcpyAsync(m->P, P, sizeof(double) * n, kind_in(mem), m->core->stream));
     bool zero = mem == TDDA_MEM_HOST;
     for (size_t i = 0; zero && i < n; i++) zero = P[i] == 0.0;
@@ -1140,6 +1155,66 @@ tdda_status tdda_model_get(const tdda_model* m, int field, double* out, int mem)
 }
 
 int tdda_model_iterations(const tdda_model* m) { return m ? m->ITERATION : -1; }
+
+tdda_status tdda_model_density_gradient(const tdda_model* fwd, int nadj, tdda_model* const* adj, const double* coef,
+                                        int nparam, const int* offsets, const int* dipoles, double* s_out) {
+    if (!fwd || nadj < 1 || nadj > 8 || !adj || !coef || nparam < 0 || !offsets || !dipoles || !s_out) {
+        set_err("invalid argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    tdda_core* c = fwd->core;
+    for (int k = 0; k < nadj; k++)
+        if (!adj[k] || adj[k]->core != c) {
+            set_err("adjoint model %d is missing or on another core", k);
+            return TDDA_ERR_INVALID_ARGUMENT;
+        }
+    const int nd = nparam > 0 ? offsets[nparam] : 0;
+    if (offsets[0] != 0) {
+        set_err("offsets[0] must be 0");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    for (int i = 0; i < nparam; i++)
+        if (offsets[i + 1] < offsets[i]) {
+            set_err("offsets must not decrease (parameter %d)", i);
+            return TDDA_ERR_INVALID_ARGUMENT;
+        }
+    for (int q = 0; q < nd; q++)
+        if (dipoles[q] < 0 || dipoles[q] >= c->N) {
+            set_err("dipole %d of the parameter map is outside 0..%d", dipoles[q], c->N - 1);
+            return TDDA_ERR_INVALID_ARGUMENT;
+        }
+    if (nparam == 0) return TDDA_OK;
+    TDDA_TRY(set_device(c->device));
+    tdda::GradArgs ga{};
+    ga.nadj = nadj;
+    for (int k = 0; k < nadj; k++) {
+        ga.lam[k] = adj[k]->P;
+        ga.coef[k] = make_double2(coef[2 * k], coef[2 * k + 1]);
+    }
+    std::vector<void*> tmp;
+    int *doff = nullptr, *ddip = nullptr;
+    double* dout = nullptr;
+    tdda_status st = dalloc(tmp, &doff, (size_t)nparam + 1, c->stream);
+    if (st == TDDA_OK) st = dalloc(tmp, &ddip, (size_t)std::max(nd, 1), c->stream);
+    if (st == TDDA_OK) st = dalloc(tmp, &dout, (size_t)nparam, c->stream);
+    cudaError_t e = cudaSuccess;
+    if (st == TDDA_OK) {
+        e = cudaMemcpyAsync(doff, offsets, sizeof(int) * ((size_t)nparam + 1), cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess && nd > 0)
+            e = cudaMemcpyAsync(ddip, dipoles, sizeof(int) * (size_t)nd, cudaMemcpyHostToDevice, c->stream);
+        count_launches(1);
+        if (e == cudaSuccess)
+            e = tdda::launch_density_gradient(nparam, doff, ddip, fwd->P, fwd->diel, fwd->dold, alpha_params(fwd), ga,
+                                              dout, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(s_out, dout, sizeof(double) * (size_t)nparam, cudaMemcpyDeviceToHost, c->stream);
+    }
+    free_all(tmp, c->stream);
+    if (st != TDDA_OK) return st;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "density gradient");
+    return TDDA_OK;
+}
 
 tdda_status tdda_model_field_at(tdda_model* m, int npts, const double* points, double* E, int mem) {
     if (!m || npts < 0 || (npts > 0 && (!points || !E))) {

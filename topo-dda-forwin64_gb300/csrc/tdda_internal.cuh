@@ -193,6 +193,18 @@ int field_blocks(int N, int npts);
 cudaError_t launch_field_at(int N, const int* R, double d, double K, const double2* P, int npts, const double* pts,
                             double3 nK, double3 nE0, double E0, double2* part, double2* E, cudaStream_t stream);
 
+// Adjoint sensitivity per design parameter (EvoDDAModel.cpp:610-638):
+//   s_i = sum_{q in [off_i, off_i+1)} Re( sum_c lam_{3j+c} dal_j/drho_j P_{3j+c} ), j = dip_q,
+//   lam = sum_k coef_k lam_k.  FP64, one thread per parameter in list order.
+struct GradArgs {
+    int nadj;
+    const double2* lam[8];
+    double2 coef[8];
+};
+cudaError_t launch_density_gradient(int nparam, const int* off, const int* dip, const double2* P, const double2* eps,
+                                    const double* diel_old, const AlphaParams& ap, const GradArgs& ga, double* s,
+                                    cudaStream_t stream);
+
 // Einternal = al P / ((2 + eps) / 3)       (DDAModel.cpp:567-575)
 cudaError_t launch_einternal(int n3, const double2* al, const double2* P, const double2* diel, double2* Ein,
                              cudaStream_t stream);

@@ -319,6 +319,41 @@ __global__ void k_model_alpha(int n3, const double* __restrict__ diel_old, Alpha
     }
 }
 
+// d(al)/d(rho) for entry e: al = 1 / alpha_LDR(eps) = 1/a_CM + (b1 + b2 eps + b3 S eps)(Kd)^2/d^3
+// - i(2/3)(Kd)^3/d^3 (tools.cpp:617-630), so dal/deps = -3 / (c (eps - 1)^2) + (b2 + b3 S)(Kd)^2/d^3
+// with c = 3 d^3 / (4 pi); eps interpolates the material table linearly in rho below 1
+// (DDAModel.cpp:54-63), so deps/drho = mat[1] - mat[0] there (the left derivative at rho = 1);
+// above 1 the table is piecewise constant and the derivative is 0.
+__device__ __forceinline__ double2 dal_drho(double2 eps, double v, const AlphaParams& ap) {
+    const double b2 = 0.1648469, b3 = -1.7700004;  // LDR coefficients (tools.cpp:618-620)
+    if (v > 1.0 || ap.nmat < 2) return make_double2(0.0, 0.0);
+    const double2 em1 = make_double2(eps.x - 1.0, eps.y);
+    const double2 sq = dmul(em1, em1);
+    const double2 t = cdiv(make_double2(-3.0 / ap.a1c, 0.0), sq);
+    const double2 dal = make_double2(t.x + (b2 + b3 * ap.S) * ap.Kd2 / ap.d3, t.y);
+    return dmul(dal, make_double2(ap.mat[1].x - ap.mat[0].x, ap.mat[1].y - ap.mat[0].y));
+}
+
+__global__ void k_density_gradient(int nparam, const int* __restrict__ off, const int* __restrict__ dip,
+                                   const double2* __restrict__ P, const double2* __restrict__ eps,
+                                   const double* __restrict__ diel_old, AlphaParams ap, GradArgs ga,
+                                   double* __restrict__ s) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nparam) return;
+    double acc = 0.0;
+    for (int q = off[i]; q < off[i + 1]; q++) {
+        const int j = dip[q];
+        for (int c = 0; c < 3; c++) {
+            const int e = 3 * j + c;
+            double2 lam = make_double2(0.0, 0.0);
+            for (int k = 0; k < ga.nadj; k++) lam = dadd(lam, dmul(ga.coef[k], ga.lam[k][e]));
+            const double2 t = dmul(dmul(lam, dal_drho(eps[e], diel_old[e], ap)), P[e]);
+            acc += t.x;
+        }
+    }
+    s[i] = acc;
+}
+
 __global__ void k_model_incident(int N, const int* __restrict__ R, double3 nK, double3 nE0, double E0, double K,
                                  double d, double2* __restrict__ E) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
@@ -546,6 +581,12 @@ cudaError_t launch_einternal(int n3, const double2* al, const double2* P, const 
 cudaError_t launch_model_alpha(int n3, const double* diel_old, const AlphaParams& ap, double2* diel, double2* al,
                                float2* fal, cudaStream_t stream) {
     k_model_alpha<<<grid1d(n3, kNT), kNT, 0, stream>>>(n3, diel_old, ap, diel, al, fal);
+    return cudaGetLastError();
+}
+cudaError_t launch_density_gradient(int nparam, const int* off, const int* dip, const double2* P, const double2* eps,
+                                    const double* diel_old, const AlphaParams& ap, const GradArgs& ga, double* s,
+                                    cudaStream_t stream) {
+    k_density_gradient<<<grid1d(nparam, 128), 128, 0, stream>>>(nparam, off, dip, P, eps, diel_old, ap, ga, s);
     return cudaGetLastError();
 }
 cudaError_t launch_model_incident(int N, const int* R, double3 nK, double3 nE0, double E0, double K, double d,

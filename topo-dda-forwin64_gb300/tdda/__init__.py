@@ -42,6 +42,7 @@ EXPORTS = [
     "tdda_model_update_alpha", "tdda_model_update_alpha_single", "tdda_model_change_E", "tdda_model_reset_E",
     "tdda_model_initialize_P", "tdda_model_aproduct_with_alb", "tdda_model_bicgstab", "tdda_model_solve_mixed",
     "tdda_model_update_E_in_structure", "tdda_model_get", "tdda_model_iterations", "tdda_model_field_at",
+    "tdda_model_density_gradient",
     "tdda_solve_batch",
     "tdda_fft3d", "tdda_core_stream", "tdda_kernel_launches", "tdda_profile_aproduct", "tdda_core_pass_count",
     "tdda_core_pass_name",
@@ -134,6 +135,7 @@ def load() -> ctypes.CDLL:
         "tdda_model_get": (i, [vp, i, vp, i]),
         "tdda_model_iterations": (i, [vp]),
         "tdda_model_field_at": (i, [vp, i, vp, vp, i]),
+        "tdda_model_density_gradient": (i, [vp, i, vp, vp, i, vp, vp, vp]),
         "tdda_solve_batch": (i, [ctypes.POINTER(vp), i, i, i, d, ctypes.POINTER(SolveInfo)]),
         "tdda_fft3d": (i, [vp, i, i, i, i]),
         "tdda_core_stream": (i, [vp, ctypes.POINTER(vp)]),
@@ -322,6 +324,18 @@ class DDAModel:
     def get_Einternal(self): return self._get(FIELD_EINTERNAL)
     def get_ITERATION(self) -> int: return load().tdda_model_iterations(self.h)
 
+    def density_gradient(self, adjoints, coef, offsets, dipoles) -> np.ndarray:
+        """Per design parameter, Re(sum lambda * dal/drho * P) over its dipoles, with
+        lambda = sum_k coef[k] * P(adjoints[k]) (EvoDDAModel.cpp:610-638)."""
+        adj = (ctypes.c_void_p * len(adjoints))(*[a.h for a in adjoints])
+        cf = np.ascontiguousarray(coef, np.complex128)
+        off = np.ascontiguousarray(offsets, np.int32)
+        dip = np.ascontiguousarray(dipoles, np.int32)
+        out = np.zeros(off.size - 1, np.float64)
+        _check(load().tdda_model_density_gradient(self.h, len(adjoints), adj, _ptr(cf), off.size - 1, _ptr(off),
+                                                  _ptr(dip), _ptr(out)), "tdda_model_density_gradient")
+        return out
+
     def field_at(self, points) -> np.ndarray:
         """E at off-lattice points (npts x 3, nm) from the current P: npts x 3 complex
         (ObjDDAModel.cpp:20-96; DDAModel::solve_E with points d * RResult)."""
@@ -345,7 +359,11 @@ class DDAModel:
     def reset_E(self):
         _check(load().tdda_model_reset_E(self.h), "tdda_model_reset_E")
 
-    def InitializeP(self, P):
+    def InitializeP(self, P=None):
+        """P = the given host vector, or zero on the device (no transfer) when P is None."""
+        if P is None:
+            _check(load().tdda_model_initialize_P(self.h, None, MEM_HOST), "tdda_model_initialize_P")
+            return
         P = _c128(P, self.n3)
         _check(load().tdda_model_initialize_P(self.h, _ptr(P), MEM_HOST), "tdda_model_initialize_P")
 

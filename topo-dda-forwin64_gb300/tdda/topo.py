@@ -23,8 +23,14 @@ transposed chain.  The step is gradient ascent: the gradient is scaled so that
 its mean magnitude is at least 0.1 (EvoDDAModel.cpp:734-738) and multiplied by
 epsilon = 0.1, so the mean step is 0.01; theta is clipped to [0, 1].
 
-The solves run on the GPU through libtdda; the O(N) glue (objective, lambda
-combination, gradient) is host numpy.
+The step follows EvoDDAModel.cpp:640-735: optional Adam / Adamdecay / Adagrad
+moments on the parameter gradient, the mean-magnitude normalisation and the
+step epsilon * g.
+
+Everything O(N) runs on the GPU through libtdda: the batched solves, the
+objective (tdda_model_field_at at r_obs) and the per-column adjoint sensitivity
+(tdda_model_density_gradient); P never leaves the device.  The host keeps the
+O(Nx Ny) design map (mirror, filter and their transposes) and the optimiser.
 """
 from __future__ import annotations
 
@@ -140,7 +146,8 @@ class TopoLoop:
     """Point-|E|^2 topology optimisation with forward + 3 adjoint solves batched per step."""
 
     def __init__(self, Nx, Ny, Nz, d, lam, material, theta0, r_obs, precision=FP32_REFINE, tol=1e-5,
-                 max_it=10000, nK=(0.0, 0.0, 1.0), nE0=(1.0, 0.0, 0.0), E0=1.0, filter_r=2.0, epsilon=0.1):
+                 max_it=10000, nK=(0.0, 0.0, 1.0), nE0=(1.0, 0.0, 0.0), E0=1.0, filter_r=2.0, epsilon=0.1,
+                 method="grad"):
         self.Nx, self.Ny, self.Nz, self.d = Nx, Ny, Nz, d
         self.R = lattice.bulk(Nx, Ny, Nz)
         self.map = DesignMap(Nx, Ny, filter_r)
@@ -161,7 +168,17 @@ class TopoLoop:
             m.change_E(self.b[k])
             self.adj.append(m)
         self.Einc_obs = self.E0 * self.nE0 * np.exp(1j * self.K * float(self.nK @ self.r_obs))
-        self.zero = np.zeros(self.R.size, np.complex128)  # 3N
+        # design parameter of the sensitivity sum: the (x, y) column; in build_a_bulk order the
+        # dipoles of column x Ny + y are (x Ny + y) Nz + z, z < Nz
+        N = Nx * Ny * Nz
+        self.col_off = np.arange(0, N + 1, Nz, dtype=np.int32)
+        self.col_dip = np.arange(N, dtype=np.int32)
+        if method not in ("grad", "Adam", "Adamdecay", "Adagrad"):
+            raise ValueError(f"unknown optimiser {method!r}")
+        self.method = method
+        self.iteration = 0
+        self.V = self.S_ad = None
+        self.gsq = np.zeros_like(self.theta)  # Adagrad accumulator (EvoDDAModel.cpp:36)
 
     def _rho(self):
         return np.clip(self.map.rho(self.theta), 0.0, 1.0)
@@ -171,35 +188,53 @@ class TopoLoop:
         rho = np.repeat(rho_xy[:, :, None], self.Nz, axis=2).ravel()
         return np.repeat(rho, 3)
 
-    def objective_parts(self, P):
-        E_obs = self.Einc_obs + self.b @ P
-        return E_obs, float(np.sum(np.abs(E_obs) ** 2))
-
     def evaluate(self):
         """Solve forward + adjoints at the current theta; return f and df/dtheta."""
         diel = self._diel()
         models = [self.fwd] + self.adj
         for m in models:
             m.UpdateAlpha(diel)
-            m.InitializeP(self.zero)
+            m.InitializeP()
         infos = solve_batch(models, self.precision, self.max_it, self.tol)
-        P = self.fwd.get_P()
-        E_obs, f = self.objective_parts(P)
-        lam = sum(np.conj(E_obs[k]) * self.adj[k].get_P() for k in range(3))
-        eps = self.mat[0] + diel * (self.mat[1] - self.mat[0])
-        dal = dal_deps(eps, self.K, self.d, self.S) * (self.mat[1] - self.mat[0])
-        g_dip = -2.0 * np.real((lam * dal * P).reshape(-1, 3).sum(axis=1))
-        g_xy = g_dip.reshape(self.Nx, self.Ny, self.Nz).sum(axis=2)
+        E_obs = self.fwd.field_at(self.r_obs[None, :])[0]  # E_inc(r_obs) - sum_j A(r_obs - r_j) P_j
+        f = float(np.sum(np.abs(E_obs) ** 2))
+        # df/drho_j = 2 Re(conj(E_obs) . dE_obs/drho_j) = -2 Re(lambda_j dal_j P_j), lambda = sum_k conj(E_k) lambda_k
+        s = self.fwd.density_gradient(self.adj, np.conj(E_obs), self.col_off, self.col_dip)
+        g_xy = (-2.0 * s).reshape(self.Nx, self.Ny)
         # rho is clipped to [0, 1]; the filter keeps it inside, so the clip is inactive
         return StepResult(f, [i["iterations"] for i in infos], self.map.grad_theta(g_xy))
 
+    def _moments(self, g):
+        """Adam / Adamdecay / Adagrad of EvoDDAModel.cpp:673-731 (beta1 = 0.9,
+        beta2 = 1 - (1 - beta1)^2, bias correction inside the moving averages as there)."""
+        it, b1 = self.iteration, 0.9
+        b2 = 1 - (1 - b1) ** 2
+        eps = self.epsilon
+        if self.method in ("Adam", "Adamdecay"):
+            if it == 0:
+                self.V = (1 - b1) * g / (1 - b1 ** (it + 1))
+                self.S_ad = (1 - b2) * g ** 2 / (1 - b2 ** (it + 1))
+            else:
+                self.V = b1 * self.V + (1 - b1) * g / (1 - b1 ** (it + 1))
+                self.S_ad = b2 * self.S_ad + (1 - b2) * g ** 2 / (1 - b2 ** (it + 1))
+            g = self.V / (np.sqrt(self.S_ad) + 1e-8)
+            if it <= 3:
+                eps = 0.1
+            elif self.method == "Adamdecay" and it >= 150:
+                eps = self.epsilon * math.exp(-(it - 150) / 10.0)
+        elif self.method == "Adagrad":
+            self.gsq += g ** 2 / 100000
+            g = g / np.sqrt(self.gsq + 1)
+        return g, eps
+
     def step(self) -> StepResult:
         r = self.evaluate()
-        g = r.grad_theta.copy()
+        g, eps = self._moments(r.grad_theta.copy())
         mean = float(np.mean(np.abs(g)))
         if 0 < mean < 0.1:  # EvoDDAModel.cpp:734-736
             g /= mean / 0.1
-        self.theta = np.clip(self.theta + self.epsilon * g, 0.0, 1.0)
+        self.theta = np.clip(self.theta + eps * g, 0.0, 1.0)
+        self.iteration += 1
         return r
 
     def close(self):
