@@ -91,6 +91,14 @@ int tdda_device_count(void);
  * (AProductCore.h:51, AProductCore.cpp:12-249): material normalisation,
  * Green tensor on the padded grid, its spectrum -- all on the device. */
 tdda_status tdda_core_create(const tdda_core_desc* desc, tdda_core** out);
+/* AProductCore's periodic constructor (AProductCore.cpp:251-536): the lattice
+ * repeats with period Lm along x and Ln along y (nm).  The interaction tensor
+ * at each offset is the sum of its images m in [-MAXm, MAXm], n in [-MAXn,
+ * MAXn], each damped by exp(-(0.01 K r)^4) (AProductCore.cpp:573-586).  The
+ * material bump of this constructor applies below |eps| = 1.01 (:263-268).
+ * Everything after construction is as tdda_core_create. */
+tdda_status tdda_core_create_periodic(const tdda_core_desc* desc, int MAXm, int MAXn, double Lm, double Ln,
+                                      tdda_core** out);
 /* Replaces AProductCore::~AProductCore (AProductCore.cpp:538-558). */
 tdda_status tdda_core_destroy(tdda_core* core);
 /* AProductCore::get_K / get_material (AProductCore.h:72,75) and the FFT grid

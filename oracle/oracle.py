@@ -40,6 +40,10 @@ def lib() -> ctypes.CDLL:
         L.or_core_create.restype = vp
         L.or_core_create.argtypes = [ctypes.c_int] * 4 + [ip] + [ctypes.c_double] * 3 + [
             ctypes.c_int, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.or_core_create_periodic.restype = vp
+        L.or_core_create_periodic.argtypes = [ctypes.c_int] * 4 + [ip] + [ctypes.c_double] * 3 + [
+            ctypes.c_int, dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+            ctypes.c_int, ctypes.c_int]
         L.or_core_destroy.argtypes = [vp]
         L.or_core_set_pruned.argtypes = [vp, ctypes.c_int]
         L.or_core_K.restype = ctypes.c_double
@@ -101,13 +105,20 @@ def aproduct_direct(R: np.ndarray, d: float, K: float, b) -> np.ndarray:
 class OracleCore:
     """AProductCore restated (AProductCore.cpp:12-249, 697-758)."""
 
-    def __init__(self, Nx, Ny, Nz, R, d, lam, material, nback=1.0, grid=None, pruned=False):
+    def __init__(self, Nx, Ny, Nz, R, d, lam, material, nback=1.0, grid=None, pruned=False, periodic=None):
+        """periodic = (MAXm, MAXn, Lm, Ln) selects the periodic constructor (AProductCore.cpp:251-536)."""
         self.R = np.ascontiguousarray(R, np.int32).reshape(-1)
         self.N = self.R.size // 3
         mat = _c128(material)
         M = grid or (0, 0, 0)
-        h = lib().or_core_create(Nx, Ny, Nz, self.N, _ip(self.R), d, lam, nback, mat.size,
-                                 _dp(mat.view(np.float64)), int(M[0]), int(M[1]), int(M[2]))
+        if periodic is None:
+            h = lib().or_core_create(Nx, Ny, Nz, self.N, _ip(self.R), d, lam, nback, mat.size,
+                                     _dp(mat.view(np.float64)), int(M[0]), int(M[1]), int(M[2]))
+        else:
+            mm, mn, Lm, Ln = periodic
+            h = lib().or_core_create_periodic(Nx, Ny, Nz, self.N, _ip(self.R), d, lam, nback, mat.size,
+                                              _dp(mat.view(np.float64)), int(mm), int(mn), float(Lm), float(Ln),
+                                              int(M[0]), int(M[1]), int(M[2]))
         if not h:
             raise ValueError("oracle core rejected its arguments")
         self.h = h

@@ -9,11 +9,14 @@
  *
  * I/O is raw little-endian binary (see tests/golden/make_golden.py):
  *   in : int32 mode (0 aprod, 1 solve, 2 ldr, 3 solve then the point-field
- *        objective ObjPointEDDAModel::GetVal at points); int32 Nx Ny Nz N;
+ *        objective ObjPointEDDAModel::GetVal at points, 4 aprod on the
+ *        periodic core); int32 Nx Ny Nz N;
  *        f64 d lam nback; int32 nmat; f64 material[2 nmat]; f64 nK[3] E0 nE0[3];
  *        int32 max_it; f64 max_err; int32 R[3N]; f64 diel_old[3N];
  *        int32 nvec; f64 vec[nvec][6N]   (mode 2: vec = nvec points of 3 f64)
  *        mode 3 appends int32 npts; f64 pts[npts][3]
+ *        mode 4 (A-products on the periodic core, AProductCore.cpp:251-536)
+ *        appends int32 MAXm MAXn; f64 Lm Ln
  *   out: see the per-mode writers below.
  */
 #include <cstdio>
@@ -86,9 +89,17 @@ int main(int argc, char** argv) {
     std::vector<double> dielraw(3 * N);
     rd.get(dielraw.data(), dielraw.size());
     int nvec = rd.get<int32_t>();
-    size_t veclen = mode == 2 ? 3 : 6 * (size_t)N;
+    size_t veclen = mode == 2 ? 3 : 6 * (size_t)N;  // modes 0, 1, 3, 4: 3N complex
     std::vector<double> vecs(nvec * veclen);
     rd.get(vecs.data(), vecs.size());
+    int MAXm = 0, MAXn = 0;
+    double Lm = 0, Ln = 0;
+    if (mode == 4) {
+        MAXm = rd.get<int32_t>();
+        MAXn = rd.get<int32_t>();
+        Lm = rd.get<double>();
+        Ln = rd.get<double>();
+    }
     std::vector<double> pts;
     if (mode == 3) {
         int npts = rd.get<int32_t>();
@@ -115,7 +126,8 @@ int main(int argc, char** argv) {
 
     VectorXcd material(nmat);
     for (int i = 0; i < nmat; i++) material(i) = std::complex<double>(mat[2 * i], mat[2 * i + 1]);
-    AProductCore Core(&CStr, lam, material, nback, "LDR");
+    AProductCore Core = mode == 4 ? AProductCore(&CStr, lam, material, nback, MAXm, MAXn, Lm, Ln, "LDR")
+                                  : AProductCore(&CStr, lam, material, nback, "LDR");
 
     FILE* fo = std::fopen(argv[2], "wb");
     if (!fo) return 2;
@@ -142,7 +154,7 @@ int main(int argc, char** argv) {
         std::fwrite(&r, 4, 1, fo);
     }
     put_cvec(fo, *Model.get_al());
-    if (mode == 0) {
+    if (mode == 0 || mode == 4) {
         for (int v = 0; v < nvec; v++) {
             VectorXcd b = to_cvec(vecs, v * veclen, 3 * N);
             VectorXcd y = Core.Aproduct(b);

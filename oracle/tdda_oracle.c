@@ -134,8 +134,37 @@ static void fft3(or_core* c, oc_cplx* g, int sign, int prune_in, int prune_out) 
     }
 }
 
+/* AProductCore::A_dic_generator(x, y, z, m, n) (AProductCore.cpp:573-586):
+ * the LDR tensor of the image (m, n) of a lattice periodic in x and y with
+ * periods Lm, Ln, damped by exp(-(gamma K r)^4), gamma = 0.01 */
+static void ldr_image(double K, double x, double y, double z, int m, int n, double Lm, double Ln, double* t) {
+    const double gamma = 0.01;
+    x = x + m * Lm;
+    y = y + n * Ln;
+    or_ldr_inter(K, x, y, z, t);
+    const double ph = exp(-pow(gamma * K * sqrt(x * x + y * y + z * z), 4));
+    for (int l = 0; l < 12; l++) t[l] *= ph;
+}
+
+static or_core* core_create(int Nx, int Ny, int Nz, int N, const int* R, double d, double lam, double nback,
+                            int nmat, const double* material, int Mx, int My, int Mz, int periodic, int MAXm,
+                            int MAXn, double Lm, double Ln);
+
 or_core* or_core_create(int Nx, int Ny, int Nz, int N, const int* R, double d, double lam,
                         double nback, int nmat, const double* material, int Mx, int My, int Mz) {
+    return core_create(Nx, Ny, Nz, N, R, d, lam, nback, nmat, material, Mx, My, Mz, 0, 0, 0, 0.0, 0.0);
+}
+
+or_core* or_core_create_periodic(int Nx, int Ny, int Nz, int N, const int* R, double d, double lam, double nback,
+                                 int nmat, const double* material, int MAXm, int MAXn, double Lm, double Ln,
+                                 int Mx, int My, int Mz) {
+    if (MAXm < 0 || MAXn < 0) return NULL;
+    return core_create(Nx, Ny, Nz, N, R, d, lam, nback, nmat, material, Mx, My, Mz, 1, MAXm, MAXn, Lm, Ln);
+}
+
+static or_core* core_create(int Nx, int Ny, int Nz, int N, const int* R, double d, double lam, double nback,
+                            int nmat, const double* material, int Mx, int My, int Mz, int periodic, int MAXm,
+                            int MAXn, double Lm, double Ln) {
     if (Nx < 1 || Ny < 1 || Nz < 1 || N < 0 || nmat < 1) return NULL;
     or_core* c = (or_core*)calloc(1, sizeof(or_core));
     if (!c) return NULL;
@@ -181,7 +210,18 @@ or_core* or_core_create(int Nx, int Ny, int Nz, int N, const int* R, double d, d
             for (int k = 0; k < c->Mz; k++) {
                 int oz;
                 if (!grid_offset(k, Nz, c->Mz, &oz)) continue;
-                or_ldr_inter(c->K, d * ox, d * oy, d * oz, t);
+                if (periodic) {
+                    /* AProductCore.cpp:300-328: the sum over the images, m outer, n inner */
+                    double ti[12];
+                    memset(t, 0, sizeof(t));
+                    for (int m = -MAXm; m <= MAXm; m++)
+                        for (int n = -MAXn; n <= MAXn; n++) {
+                            ldr_image(c->K, d * ox, d * oy, d * oz, m, n, Lm, Ln, ti);
+                            for (int l = 0; l < 12; l++) t[l] = t[l] + ti[l];
+                        }
+                } else {
+                    or_ldr_inter(c->K, d * ox, d * oy, d * oz, t);
+                }
                 long g = gidx(c, i, j, k);
                 for (int l = 0; l < 6; l++) {
                     c->A[l][g].re = t[2 * l];

@@ -46,6 +46,12 @@ typedef struct or_core or_core;
  * >= 2N-1 gives the same linear convolution. */
 or_core* or_core_create(int Nx, int Ny, int Nz, int N, const int* R, double d, double lam,
                         double nback, int nmat, const double* material, int Mx, int My, int Mz);
+/* the periodic constructor (AProductCore.cpp:251-536): the tensor at each
+ * offset is the sum of its images over m in [-MAXm, MAXm], n in [-MAXn, MAXn]
+ * with periods Lm (x) and Ln (y), each damped by exp(-(0.01 K r)^4) */
+or_core* or_core_create_periodic(int Nx, int Ny, int Nz, int N, const int* R, double d, double lam, double nback,
+                                 int nmat, const double* material, int MAXm, int MAXn, double Lm, double Ln,
+                                 int Mx, int My, int Mz);
 void or_core_destroy(or_core* c);
 void or_core_set_pruned(or_core* c, int pruned);
 double or_core_K(const or_core* c);

@@ -84,6 +84,13 @@ int main(int argc, char** argv) {
     std::fwrite(TestModel.get_P()->data(), 16, TestModel.get_P()->size(), f);
     std::fwrite(TestModel.get_Einternal()->data(), 16, TestModel.get_Einternal()->size(), f);
     std::fwrite(TestModel.get_EResult()->data(), 16, TestModel.get_EResult()->size(), f);
+    // the periodic constructor on the same structure (AProductCore.cpp:251-536): the product of
+    // the solved P and one image tensor
+    tdda::AProductCore PCore(&S, lam, material, 1.0, 2, 1, S.Nx * S.d, S.Ny * S.d, "LDR");
+    const std::vector<std::complex<double>> y = PCore.Aproduct(*TestModel.get_P());
+    std::fwrite(y.data(), 16, y.size(), f);
+    const auto A = PCore.A_dic_generator(10.0, 20.0, 5.0, 1, -1);
+    for (int i = 0; i < 3; i++) std::fwrite(A[i].data(), 16, 3, f);
     std::fclose(f);
     std::printf("ITERATION %d P[0] %.17g %.17g\n", it, (*TestModel.get_P())[0].real(), (*TestModel.get_P())[0].imag());
     return 0;

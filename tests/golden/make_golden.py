@@ -8,6 +8,7 @@ on seeded inputs.  Each fixture stores its inputs and the reference's outputs:
   ldr.npz          LDR_inter (AProductCore.cpp:588-623) at a set of offsets
   aprod_*.npz      Aproduct / Aproductwithalb (AProductCore.cpp:697-758,
                    DDAModel.cpp:577-586) of seeded vectors
+  aprodper_*.npz   the same on the periodic core (AProductCore.cpp:251-536)
   solve_*.npz      bicgstab + update_E_in_structure (DDAModel.cpp:131-260,
                    567-575): ITERATION, the printed Error, P, Einternal
   field_*.npz      a solve, then the point-field objective
@@ -63,10 +64,14 @@ def write_input(path, mode, Nx, Ny, Nz, R, d, lam, nback, material, nK, E0, nE0,
             f.write(np.asarray(v).astype("<c16" if mode != 2 else "<f8").tobytes())
 
 
-def run(mode, points=None, **kw):
+def run(mode, points=None, periodic=None, **kw):
     with tempfile.TemporaryDirectory() as td:
         fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
         write_input(fin, mode, **kw)
+        if periodic is not None:
+            with open(fin, "ab") as f:
+                f.write(struct.pack("<2i2d", int(periodic[0]), int(periodic[1]), float(periodic[2]),
+                                    float(periodic[3])))
         if points is not None:
             pts = np.ascontiguousarray(points, "<f8").reshape(-1, 3)
             with open(fin, "ab") as f:
@@ -143,6 +148,24 @@ def gen_aprod(name, w: lattice.Workload, nvec, seed):
     print(f"aprod_{name}: N={N} |y|={np.linalg.norm(ys[0]):.6g}")
 
 
+def gen_aprod_periodic(name, w: lattice.Workload, periodic, nvec, seed):
+    N = w.N
+    vecs = [rand_vec(3 * N, seed + v) for v in range(nvec)]
+    raw, _ = run(4, periodic=periodic, **case_kw(w), vecs=vecs)
+    off = 12 * N
+    al = np.frombuffer(raw, "<c16", count=3 * N, offset=off)
+    off += 48 * N
+    ys, yws = [], []
+    for _ in range(nvec):
+        ys.append(np.frombuffer(raw, "<c16", count=3 * N, offset=off))
+        off += 48 * N
+        yws.append(np.frombuffer(raw, "<c16", count=3 * N, offset=off))
+        off += 48 * N
+    np.savez_compressed(os.path.join(HERE, f"aprodper_{name}.npz"), **inputs_dict(w), al=al, b=np.array(vecs),
+                        y=np.array(ys), y_alb=np.array(yws), periodic=np.array(periodic, np.float64))
+    print(f"aprodper_{name}: N={N} periodic={periodic} |y|={np.linalg.norm(ys[0]):.6g}")
+
+
 def gen_solve(name, w: lattice.Workload, inc=None, P0=None, Ein=None, max_it=10000, max_err=1e-5):
     N = w.N
     vecs = []
@@ -205,6 +228,11 @@ def main():
     # warm start + a replaced right-hand side (the adjoint's change_E / InitializeP)
     wa = small_workload("adj8x8x4", 8, 8, 4, 15)
     gen_solve("adj8x8x4", wa, P0=0.01 * rand_vec(3 * wa.N, 400), Ein=rand_vec(3 * wa.N, 500))
+    # periodic cores: a unit cell repeated with its own period, and a sparse cell in a wider
+    # non-square array
+    gen_aprod_periodic("cell6x5x3", small_workload("cell6x5x3", 6, 5, 3, 16), (3, 3, 60.0, 50.0), 2, 600)
+    gen_aprod_periodic("sparse5x4x3", small_workload("sparse5x4x3", 5, 4, 3, 17, keep=0.7, shuffle=True),
+                       (5, 2, 75.0, 52.0), 1, 700)
     # the point field of the solved cfg 1 structure: above the centre (the topology objective's
     # point), beside, below, far off, and inside the box between lattice sites
     gen_field("cfg1", lattice.config(1), [[95.0, 95.0, 190.0], [-50.0, 95.0, 45.0], [95.0, 95.0, -80.0],

@@ -51,3 +51,14 @@ def test_fcd_method_is_reported_unsupported():
     with pytest.raises(tdda.TddaError) as e:
         tdda.AProductCore(2, 2, 2, R, 10.0, 500.0, mat, method="FCD")
     assert e.value.status == tdda.ERR_UNSUPPORTED
+
+
+def test_periodic_core_rejects_bad_images_before_touching_a_device():
+    L = tdda.load()
+    h = ctypes.c_void_p()
+    desc = tdda.CoreDesc()
+    assert L.tdda_core_create_periodic(ctypes.byref(desc), -1, 2, 10.0, 10.0, ctypes.byref(h)) == \
+        tdda.ERR_INVALID_ARGUMENT
+    assert L.tdda_core_create_periodic(ctypes.byref(desc), 2, 2, float("nan"), 10.0, ctypes.byref(h)) == \
+        tdda.ERR_INVALID_ARGUMENT
+    assert b"periodic" in L.tdda_last_error()

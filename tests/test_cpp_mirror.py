@@ -64,3 +64,14 @@ def test_mirror_solve_matches_oracle(tmp_path, precision, tol, bound):
     assert rel(P, om.P) <= bound
     assert rel(Ein, om.Einternal) <= bound
     assert rel(EResult, om.field_at(d * RResult).ravel()) <= bound
+    # periodic core (MAXm 2, MAXn 1, periods of the box): the product of the solved P, and the
+    # image tensor A_dic_generator(10, 20, 5, m=1, n=-1)
+    off = 4 + 96 * N + 12 * 16
+    y = np.frombuffer(raw, "<c16", count=3 * N, offset=off)
+    A = np.frombuffer(raw, "<c16", count=9, offset=off + 48 * N).reshape(3, 3)
+    opc = O.OracleCore(Nx, Ny, Nz, R, d, lam, np.array([1.0, em]), periodic=(2, 1, Nx * d, Ny * d))
+    assert rel(y, opc.Aproduct(P)) <= 1e-12
+    x_, y_, z_ = 10.0 + Nx * d, 20.0 - Ny * d, 5.0
+    t = O.ldr_inter(opc.K, x_, y_, z_) * math.exp(-(0.01 * opc.K * math.sqrt(x_ ** 2 + y_ ** 2 + z_ ** 2)) ** 4)
+    full = np.array([[t[0], t[1], t[2]], [t[1], t[3], t[4]], [t[2], t[4], t[5]]])
+    assert np.max(np.abs(A - full)) <= 1e-15 * np.max(np.abs(full))

@@ -237,3 +237,44 @@ def test_point_field_matches_reference(name):
     assert rel(E.ravel(), om.field_at(g["points"]).ravel()) <= 1e-12
     m.close()
     core.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["cell6x5x3", "sparse5x4x3"])
+def test_periodic_aproduct_matches_reference(name):
+    """tdda_core_create_periodic: the image sums on the device (AProductCore.cpp:251-536)
+    against the reference's periodic A-products."""
+    g = golden(f"aprodper_{name}.npz")
+    Nx, Ny, Nz = (int(v) for v in g["box"])
+    mm, mn, Lm, Ln = g["periodic"]
+    core = tdda.AProductCore(Nx, Ny, Nz, g["R"], float(g["d"]), float(g["lam"]), g["material"], float(g["nback"]),
+                             periodic=(int(mm), int(mn), float(Lm), float(Ln)))
+    m = tdda.DDAModel(core, g["nK"], float(g["E0"]), g["nE0"], g["diel_old"])
+    for b, y, yw in zip(g["b"], g["y"], g["y_alb"]):
+        assert rel(core.Aproduct(b), y) <= 1e-12
+        assert rel(core.Aproduct(b, tdda.FP32_REFINE), y) <= 1e-5
+        assert rel(m.Aproductwithalb(b), yw) <= 1e-12
+    m.close()
+    core.close()
+
+
+@pytest.mark.gpu
+def test_periodic_solve_matches_oracle():
+    """A BiCGSTAB solve on a periodic core, FP64 to 1e-10 and FP32+refine to 1e-5, against
+    the oracle's periodic solve."""
+    Nx, Ny, Nz, d, lam = 7, 6, 3, 10.0, 540.0
+    R = tdda.lattice.bulk(Nx, Ny, Nz)
+    rho = np.repeat(0.5 + 0.5 * np.cos(0.21 * np.arange(Nx * Ny * Nz)), 3)
+    per = (4, 4, 70.0, 60.0)
+    mat = np.array([1.0, 2.25 + 0.02j])
+    oc = O.OracleCore(Nx, Ny, Nz, R, d, lam, mat, periodic=per)
+    om = O.OracleModel(oc, [0, 0, 1], 1.0, [1, 0, 0], rho)
+    assert om.bicgstab(10000, 1e-12) == O.CONVERGED
+    core = tdda.AProductCore(Nx, Ny, Nz, R, d, lam, mat, periodic=per)
+    for prec, tol, bound in ((tdda.FP64, 1e-10, 1e-9), (tdda.FP32_REFINE, 1e-5, 2e-4)):
+        m = tdda.DDAModel(core, [0, 0, 1], 1.0, [1, 0, 0], rho)
+        info = m.bicgstab(10000, tol) if prec == tdda.FP64 else m.solve_mixed(10000, tol)
+        assert info["status"] == 0
+        assert rel(m.get_P(), om.P) <= bound
+        m.close()
+    core.close()

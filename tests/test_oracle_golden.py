@@ -116,3 +116,18 @@ def test_point_field_matches_reference(name):
     E = m.field_at(g["points"])
     absE = np.sqrt(np.sum(np.abs(E) ** 2, axis=1))
     assert np.max(np.abs(absE - g["absE"]) / g["absE"]) <= 1e-13
+
+
+@pytest.mark.parametrize("name", ["cell6x5x3", "sparse5x4x3"])
+def test_periodic_aproduct_matches_reference(name):
+    """The periodic constructor's image sums (AProductCore.cpp:251-536, 573-586)."""
+    g = golden(f"aprodper_{name}.npz")
+    Nx, Ny, Nz = (int(v) for v in g["box"])
+    mm, mn, Lm, Ln = g["periodic"]
+    core = O.OracleCore(Nx, Ny, Nz, g["R"], float(g["d"]), float(g["lam"]), g["material"], float(g["nback"]),
+                        periodic=(int(mm), int(mn), float(Lm), float(Ln)))
+    model = O.OracleModel(core, g["nK"], float(g["E0"]), g["nE0"], g["diel_old"])
+    assert rel(model.al, g["al"]) <= 1e-15
+    for b, y, yw in zip(g["b"], g["y"], g["y_alb"]):
+        assert rel(core.Aproduct(b), y) <= 1e-14
+        assert rel(model.Aproductwithalb(b), yw) <= 1e-14

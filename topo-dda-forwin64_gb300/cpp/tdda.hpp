@@ -29,6 +29,7 @@
 #pragma once
 
 #include <array>
+#include <cmath>
 #include <complex>
 #include <cstdio>
 #include <functional>
@@ -57,6 +58,25 @@ class AProductCore {
     AProductCore(CStrT* CStr, double lam, const MatVec& material, double nback, const std::string& method,
                  int max_rhs = 1, int device = 0)
         : lam_(lam), nback_(nback) {
+        init(CStr, material, method, max_rhs, device, false);
+    }
+    // AProductCore(CoreStructure*, double lam, VectorXcd material, double nback, int MAXm, int MAXn,
+    //              double Lm, double Ln, string method)     AProductCore.cpp:251-536
+    template <class CStrT, class MatVec>
+    AProductCore(CStrT* CStr, double lam, const MatVec& material, double nback, int MAXm, int MAXn, double Lm,
+                 double Ln, const std::string& method, int max_rhs = 1, int device = 0)
+        : lam_(lam), nback_(nback), MAXm_(MAXm), MAXn_(MAXn), Lm_(Lm), Ln_(Ln) {
+        init(CStr, material, method, max_rhs, device, true);
+    }
+    AProductCore(const AProductCore&) = delete;
+    AProductCore& operator=(const AProductCore&) = delete;
+    ~AProductCore() { tdda_core_destroy(h_); }
+
+   private:
+    template <class CStrT, class MatVec>
+    void init(CStrT* CStr, const MatVec& material, const std::string& method, int max_rhs, int device,
+              bool periodic) {
+        const double lam = lam_, nback = nback_;
         if (method != "LDR" && method != "FCD")
             throw std::invalid_argument("\"" + method + "\" is not a valid polarizabiliy calculation method.");
         N_ = CStr->get_N();
@@ -91,13 +111,15 @@ class AProductCore {
         desc.method = method == "LDR" ? TDDA_METHOD_LDR : TDDA_METHOD_FCD;
         desc.max_rhs = max_rhs;
         desc.device = device;
-        check(tdda_core_create(&desc, &h_), "AProductCore");
+        if (periodic)
+            check(tdda_core_create_periodic(&desc, MAXm_, MAXn_, Lm_, Ln_, &h_), "AProductCore");
+        else
+            check(tdda_core_create(&desc, &h_), "AProductCore");
         material_.resize(material.size());
         check(tdda_core_info(h_, &K_, grid_.data(), reinterpret_cast<double*>(material_.data())), "AProductCore");
     }
-    AProductCore(const AProductCore&) = delete;
-    AProductCore& operator=(const AProductCore&) = delete;
-    ~AProductCore() { tdda_core_destroy(h_); }
+
+   public:
 
     // VectorXcd Aproduct(VectorXcd& b)     AProductCore.cpp:697-758
     template <class V> V Aproduct(const V& b) {
@@ -115,6 +137,16 @@ class AProductCore {
     }
     std::array<std::array<cplx, 3>, 3> A_dic_generator(double x, double y, double z) const {
         return LDR_inter(x, y, z);
+    }
+    // Matrix3cd A_dic_generator(double x, double y, double z, int m, int n)     AProductCore.cpp:573-586
+    std::array<std::array<cplx, 3>, 3> A_dic_generator(double x, double y, double z, int m, int n) const {
+        x = x + m * Lm_;
+        y = y + n * Ln_;
+        auto r = A_dic_generator(x, y, z);
+        const double ph = std::exp(-std::pow(0.01 * K_ * std::sqrt(x * x + y * y + z * z), 4));
+        for (auto& row : r)
+            for (auto& v : row) v *= ph;
+        return r;
     }
 
     int get_N() const { return N_; }
@@ -140,6 +172,8 @@ class AProductCore {
     std::vector<cplx> material_;
     std::array<int, 3> grid_{{0, 0, 0}};
     std::function<void(std::vector<double>&)> diel_old_;
+    int MAXm_ = 0, MAXn_ = 0;  // periodic images (AProductCore.h members of the periodic ctor)
+    double Lm_ = 0, Ln_ = 0;
 };
 
 // DDAModel over a complex vector type VectorXcd (Eigen::VectorXcd or

@@ -176,6 +176,8 @@ struct tdda_core_s {
     Graphs<double> g64;
     Graphs<float> g32;
     std::vector<void*> allocs;
+    bool is_periodic = false;
+    tdda::PeriodicImages periodic{};
 };
 
 struct tdda_model_s {
@@ -708,7 +710,26 @@ int tdda_device_count(void) {
     return n;
 }
 
-tdda_status tdda_core_create(const tdda_core_desc* desc, tdda_core** out) {
+namespace {
+tdda_status core_create(const tdda_core_desc* desc, const tdda::PeriodicImages* pi, tdda_core** out);
+}
+
+tdda_status tdda_core_create(const tdda_core_desc* desc, tdda_core** out) { return core_create(desc, nullptr, out); }
+
+tdda_status tdda_core_create_periodic(const tdda_core_desc* desc, int MAXm, int MAXn, double Lm, double Ln,
+                                      tdda_core** out) {
+    g_err.clear();
+    if (MAXm < 0 || MAXn < 0 || MAXm > 4096 || MAXn > 4096 || !std::isfinite(Lm) || !std::isfinite(Ln)) {
+        set_err("invalid periodic images (MAXm %d, MAXn %d, Lm %g, Ln %g)", MAXm, MAXn, Lm, Ln);
+        if (out) *out = nullptr;
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    const tdda::PeriodicImages pi{MAXm, MAXn, Lm, Ln};
+    return core_create(desc, &pi, out);
+}
+
+namespace {
+tdda_status core_create(const tdda_core_desc* desc, const tdda::PeriodicImages* pi, tdda_core** out) {
     g_err.clear();
     if (!desc || !out) {
         set_err("null argument");
@@ -750,10 +771,11 @@ tdda_status tdda_core_create(const tdda_core_desc* desc, tdda_core** out) {
     c->nback = desc->nback;
     c->K = 2 * kPi / (c->lam / c->nback);  // AProductCore.cpp:17
     c->material.resize(c->nmat);
-    for (int i = 0; i < c->nmat; i++) {  // AProductCore.cpp:19-24
+    for (int i = 0; i < c->nmat; i++) {  // AProductCore.cpp:19-24 (the periodic ctor, :263-268, bumps below 1.01)
         cd m(desc->material[2 * i], desc->material[2 * i + 1]);
         m = m / (c->nback * c->nback);
-        if (std::sqrt(std::norm(m)) <= 1.01) m = m + 0.01;
+        const double a = std::sqrt(std::norm(m));
+        if (pi ? a < 1.01 : a <= 1.01) m = m + 0.01;
         c->material[i] = m;
     }
     c->R.assign(desc->R, desc->R + 3 * (size_t)desc->N);
@@ -873,21 +895,26 @@ tdda_status tdda_core_create(const tdda_core_desc* desc, tdda_core** out) {
     TDDA_CORE_CK(cudaMemcpyAsync(c->rhs64 + c->max_rhs, &p64, sizeof(p64), cudaMemcpyHostToDevice, c->stream));
     TDDA_CORE_CK(cudaMemcpyAsync(c->rhs32 + c->max_rhs, &p32, sizeof(p32), cudaMemcpyHostToDevice, c->stream));
     TDDA_CORE_TRY(configure_once(c->device));
-    // Green spectrum (AProductCore.cpp:53-229), on a temporary full grid
+    // Green spectrum (AProductCore.cpp:53-229; periodic: :300-520), on a temporary full grid
     double2* full6 = nullptr;
+    double2* oct = nullptr;
     TDDA_CORE_CK(cudaMallocAsync((void**)&full6, sizeof(double2) * 6 * (size_t)Mfull, c->stream));
-    count_launches(5);
+    if (pi) TDDA_CORE_CK(cudaMallocAsync((void**)&oct, sizeof(double2) * 6 * (size_t)g.Nx * g.Ny * g.Nz, c->stream));
+    count_launches(pi ? 6 : 5);
     cudaError_t ge = tdda::launch_green(g, c->K, c->d, c->tw64[0], c->tw64[1], c->tw64[2], full6, c->green64,
-                                        c->green32, c->stream);
+                                        c->green32, c->stream, pi, oct);
     cudaError_t fe = cudaFreeAsync(full6, c->stream);
+    if (oct && fe == cudaSuccess) fe = cudaFreeAsync(oct, c->stream);
     TDDA_CORE_CK(ge);
     TDDA_CORE_CK(fe);
     TDDA_CORE_CK(cudaStreamSynchronize(c->stream));
+    if (pi) c->periodic = *pi, c->is_periodic = true;
 #undef TDDA_CORE_TRY
 #undef TDDA_CORE_CK
     *out = c;
     return TDDA_OK;
 }
+}  // namespace
 
 tdda_status tdda_core_destroy(tdda_core* c) {
     if (!c) return TDDA_OK;

@@ -133,10 +133,19 @@ constexpr size_t kMaxPassSmem = 200 * 1024;
 // -------------------------------------------------------------- launchers
 // All launchers enqueue on `stream` and return cudaGetLastError().
 
-// Green spectrum: LDR tensor on the full grid, 3-D forward FFT, fold, scale.
+// images of a lattice periodic in x and y (AProductCore.cpp:251-536)
+struct PeriodicImages {
+    int MAXm, MAXn;  // images m in [-MAXm, MAXm] (x), n in [-MAXn, MAXn] (y)
+    double Lm, Ln;   // periods, nm
+};
+
+// Green spectrum: LDR tensor on the full grid (the sum over the images when pi
+// is given, through the octant table oct of 6 Nx Ny Nz entries), 3-D forward
+// FFT, fold, scale.
 cudaError_t launch_green(const Geom& g, double K, double d, const double2* tw64x, const double2* tw64y,
                          const double2* tw64z, double2* full6 /* 6*Mx*My*Mz scratch */, double2* green64,
-                         float2* green32, cudaStream_t stream);
+                         float2* green32, cudaStream_t stream, const PeriodicImages* pi = nullptr,
+                         double2* oct = nullptr);
 
 // One A-product over nrhs right-hand sides.  rhs[] lives in device memory.
 // ev, when given, holds 6 events recorded before K1..K5 and after K5; with

@@ -212,6 +212,70 @@ __global__ void k_field_sum(int npts, int nb, const double2* __restrict__ part, 
     }
 }
 
+// Periodic lattice (AProductCore.cpp:251-536): the tensor at offset o is the
+// sum over the images (m, n) of LDR(o d + (m Lm, n Ln, 0)), each damped by
+// exp(-(gamma K r)^4), gamma = 0.01 (AProductCore.cpp:573-586).  The image sum
+// is symmetric in m and n, so every component keeps the parity of the
+// free-space tensor and the octant o >= 0 determines the rest.  One block
+// per octant offset sums the (2 MAXm + 1)(2 MAXn + 1) images in a fixed order.
+__global__ void __launch_bounds__(kNT) k_green_periodic_octant(Geom g, double K, double d, PeriodicImages pi,
+                                                               double2* __restrict__ oct) {
+    __shared__ double sred[12 * kNT];
+    const int o = blockIdx.x;  // (ox Ny + oy) Nz + oz
+    const int oz = o % g.Nz, oy = (o / g.Nz) % g.Ny, ox = o / (g.Nz * g.Ny);
+    const int nm = 2 * pi.MAXm + 1, nimg = nm * (2 * pi.MAXn + 1);
+    double acc[12];
+#pragma unroll
+    for (int l = 0; l < 12; l++) acc[l] = 0.0;
+    for (int q = threadIdx.x; q < nimg; q += blockDim.x) {
+        const int m = q % nm - pi.MAXm, n = q / nm - pi.MAXn;
+        const double x = d * ox + m * pi.Lm, y = d * oy + n * pi.Ln, z = d * oz;
+        double2 t[6];
+        ldr_tensor(K, x, y, z, t);
+        const double gk = 0.01 * K * sqrt(x * x + y * y + z * z);
+        const double g2 = gk * gk;
+        const double ph = exp(-(g2 * g2));
+#pragma unroll
+        for (int l = 0; l < 6; l++) {
+            acc[2 * l] += t[l].x * ph;
+            acc[2 * l + 1] += t[l].y * ph;
+        }
+    }
+    block_sum<12>(acc, sred);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int l = 0; l < 6; l++) oct[(long long)o * 6 + l] = make_double2(acc[2 * l], acc[2 * l + 1]);
+    }
+}
+
+// the full padded grid from the octant: xx, yy, zz even in every axis; xy odd
+// in x and y, xz in x and z, yz in y and z
+__global__ void k_green_expand(Geom g, const double2* __restrict__ oct, double2* __restrict__ full6) {
+    const int Mx = g.px.M, My = g.py.M, Mz = g.pz.M;
+    const long long M = (long long)Mx * My * Mz;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < M; e += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(e % Mz);
+        const int j = (int)((e / Mz) % My);
+        const int i = (int)(e / ((long long)Mz * My));
+        int ox = i < g.Nx ? i : (i > Mx - g.Nx ? i - Mx : INT32_MIN);
+        int oy = j < g.Ny ? j : (j > My - g.Ny ? j - My : INT32_MIN);
+        int oz = k < g.Nz ? k : (k > Mz - g.Nz ? k - Mz : INT32_MIN);
+        double2 t[6];
+        if (ox != INT32_MIN && oy != INT32_MIN && oz != INT32_MIN) {
+            const double sx = ox < 0 ? -1.0 : 1.0, sy = oy < 0 ? -1.0 : 1.0, sz = oz < 0 ? -1.0 : 1.0;
+            const double2* src = oct + (((long long)abs(ox) * g.Ny + abs(oy)) * g.Nz + abs(oz)) * 6;
+            const double sg[6] = {1.0, sx * sy, sx * sz, 1.0, sy * sz, 1.0};
+#pragma unroll
+            for (int l = 0; l < 6; l++) t[l] = make_double2(sg[l] * src[l].x, sg[l] * src[l].y);
+        } else {
+#pragma unroll
+            for (int l = 0; l < 6; l++) t[l] = make_double2(0.0, 0.0);
+        }
+#pragma unroll
+        for (int l = 0; l < 6; l++) full6[l * M + e] = t[l];
+    }
+}
+
 // fold the spectrum to the octant, scale by 1/M, write FP64 and FP32 copies
 __global__ void k_green_fold(Geom g, const double2* __restrict__ full6, double2* __restrict__ green64,
                              float2* __restrict__ green32) {
@@ -464,11 +528,22 @@ cudaError_t fft_cols(double2* data, int nouter, int o1, long long s1, long long 
 }  // namespace
 
 cudaError_t launch_green(const Geom& g, double K, double d, const double2* twx, const double2* twy, const double2* twz,
-                         double2* full6, double2* green64, float2* green32, cudaStream_t stream) {
+                         double2* full6, double2* green64, float2* green32, cudaStream_t stream,
+                         const PeriodicImages* pi, double2* oct) {
     const int Mx = g.px.M, My = g.py.M, Mz = g.pz.M;
     const long long M = (long long)Mx * My * Mz;
-    k_green_real<<<grid1d(M, kNT), kNT, 0, stream>>>(g, K, d, full6);
-    cudaError_t err = cudaGetLastError();
+    cudaError_t err;
+    if (pi) {
+        k_green_periodic_octant<<<g.Nx * g.Ny * g.Nz, kNT, 0, stream>>>(g, K, d, *pi, oct);
+        err = cudaGetLastError();
+        if (!err) {
+            k_green_expand<<<grid1d(M, kNT), kNT, 0, stream>>>(g, oct, full6);
+            err = cudaGetLastError();
+        }
+    } else {
+        k_green_real<<<grid1d(M, kNT), kNT, 0, stream>>>(g, K, d, full6);
+        err = cudaGetLastError();
+    }
     // the six components form a (6 Mx, My, Mz) array for the z and y axes;
     // the x axis runs over the outer pairs (component, y)
     if (!err) err = fft_rows(full6, 6LL * Mx * My, g.pz, twz, -1, stream);

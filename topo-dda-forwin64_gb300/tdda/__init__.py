@@ -37,7 +37,8 @@ METHODS = {"LDR": 0, "FCD": 1}
 
 # every entry point declared in include/tdda.h
 EXPORTS = [
-    "tdda_abi_version", "tdda_last_error", "tdda_device_count", "tdda_core_create", "tdda_core_destroy",
+    "tdda_abi_version", "tdda_last_error", "tdda_device_count", "tdda_core_create", "tdda_core_create_periodic",
+    "tdda_core_destroy",
     "tdda_core_info", "tdda_aproduct", "tdda_core_ldr_inter", "tdda_model_create", "tdda_model_destroy",
     "tdda_model_update_alpha", "tdda_model_update_alpha_single", "tdda_model_change_E", "tdda_model_reset_E",
     "tdda_model_initialize_P", "tdda_model_aproduct_with_alb", "tdda_model_bicgstab", "tdda_model_solve_mixed",
@@ -135,6 +136,7 @@ def load() -> ctypes.CDLL:
         "tdda_model_get": (i, [vp, i, vp, i]),
         "tdda_model_iterations": (i, [vp]),
         "tdda_model_field_at": (i, [vp, i, vp, vp, i]),
+        "tdda_core_create_periodic": (i, [ctypes.POINTER(CoreDesc), i, i, d, d, ctypes.POINTER(vp)]),
         "tdda_model_density_gradient": (i, [vp, i, vp, vp, i, vp, vp, vp]),
         "tdda_solve_batch": (i, [ctypes.POINTER(vp), i, i, i, d, ctypes.POINTER(SolveInfo)]),
         "tdda_fft3d": (i, [vp, i, i, i, i]),
@@ -193,7 +195,9 @@ def _dptr(a: np.ndarray):
 class AProductCore:
     """The interaction operator of one lattice at one wavelength (AProductCore.h:12-81)."""
 
-    def __init__(self, Nx, Ny, Nz, R, d, lam, material, nback=1.0, method="LDR", max_rhs=1, device=0):
+    def __init__(self, Nx, Ny, Nz, R, d, lam, material, nback=1.0, method="LDR", max_rhs=1, device=0,
+                 periodic=None):
+        """periodic = (MAXm, MAXn, Lm, Ln): the periodic constructor (AProductCore.cpp:251-536)."""
         L = load()
         self.R = np.ascontiguousarray(np.asarray(R, dtype=np.int32).reshape(-1))
         self.N = self.R.size // 3
@@ -205,7 +209,13 @@ class AProductCore:
                         self.R.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), self.d, self.lam, self.nback,
                         _dptr(mat.view(np.float64)), mat.size, METHODS[method], int(max_rhs), int(device))
         h = ctypes.c_void_p()
-        _check(L.tdda_core_create(ctypes.byref(desc), ctypes.byref(h)), "tdda_core_create")
+        if periodic is None:
+            _check(L.tdda_core_create(ctypes.byref(desc), ctypes.byref(h)), "tdda_core_create")
+        else:
+            mm, mn_, Lm, Ln = periodic
+            _check(L.tdda_core_create_periodic(ctypes.byref(desc), int(mm), int(mn_), float(Lm), float(Ln),
+                                               ctypes.byref(h)), "tdda_core_create_periodic")
+        self.periodic = periodic
         self.h = h
         self.max_rhs = int(max_rhs)
         K = ctypes.c_double()
