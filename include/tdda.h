@@ -62,7 +62,7 @@ typedef struct tdda_core_desc {
     double nback;            /* background refractive index */
     const double* material;  /* nmat complex permittivities (re, im), host memory */
     int nmat;
-    int method;              /* TDDA_METHOD_LDR */
+    int method;              /* TDDA_METHOD_LDR or TDDA_METHOD_FCD */
     int max_rhs;             /* right-hand sides a batched solve may carry (>= 1) */
     int device;              /* CUDA device ordinal */
 } tdda_core_desc;
@@ -108,10 +108,16 @@ tdda_status tdda_core_info(const tdda_core* core, double* K, int* grid3, double*
  * AProductCore.cpp:697-758).  precision TDDA_FP32_REFINE runs the complex64
  * convolution once (no refinement) for error studies. */
 tdda_status tdda_aproduct(tdda_core* core, int precision, const double* b, double* y, int mem);
-/* The LDR interaction tensor at offset (x, y, z) in the units of d
+/* The LDR interaction tensor at the offset (x, y, z) nm
  * (AProductCore::LDR_inter, AProductCore.h:80): out12 = xx, xy, xz, yy, yz,
  * zz as (re, im).  Host arithmetic, as in the reference. */
 tdda_status tdda_core_ldr_inter(const tdda_core* core, double x, double y, double z, double* out12);
+/* AProductCore::A_dic_generator(x, y, z) (AProductCore.cpp:560-571): the
+ * core's interaction tensor at the offset (x, y, z) nm, LDR or FCD
+ * (AProductCore.cpp:625-695, Si/Ci interpolated as SiCi.cpp:27-47 in tables
+ * of Si(0.1 k), Ci(0.1 k), k = 1 .. 999999); same output layout as
+ * tdda_core_ldr_inter. */
+tdda_status tdda_core_interaction(const tdda_core* core, double x, double y, double z, double* out12);
 
 /* model: incident field, polarisability and solve state ----------------- */
 /* Replaces DDAModel::DDAModel(Core, n_K, E0, n_E0) (DDAModel.h:34,

@@ -44,6 +44,11 @@ def lib() -> ctypes.CDLL:
         L.or_core_create_periodic.argtypes = [ctypes.c_int] * 4 + [ip] + [ctypes.c_double] * 3 + [
             ctypes.c_int, dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
             ctypes.c_int, ctypes.c_int]
+        L.or_core_create_method.restype = vp
+        L.or_core_create_method.argtypes = [ctypes.c_int] * 4 + [ip] + [ctypes.c_double] * 3 + [
+            ctypes.c_int, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+            ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.or_fcd_inter.argtypes = [ctypes.c_double] * 5 + [dp]
         L.or_core_destroy.argtypes = [vp]
         L.or_core_set_pruned.argtypes = [vp, ctypes.c_int]
         L.or_core_K.restype = ctypes.c_double
@@ -64,6 +69,7 @@ def lib() -> ctypes.CDLL:
         L.or_model_update_E_in_structure.argtypes = [vp]
         L.or_model_get.argtypes = [vp, ctypes.c_int, dp]
         L.or_model_field_at.argtypes = [vp, ctypes.c_int, dp, dp]
+        L.or_sici.argtypes = [ctypes.c_double, dp, dp]
         _LIB = L
     return _LIB
 
@@ -86,6 +92,20 @@ def ldr_inter(K: float, x: float, y: float, z: float) -> np.ndarray:
     return out
 
 
+def fcd_inter(K: float, d: float, x: float, y: float, z: float) -> np.ndarray:
+    """FCD tensor (AProductCore.cpp:625-695): xx, xy, xz, yy, yz, zz."""
+    out = np.zeros(12)
+    lib().or_fcd_inter(K, d, x, y, z, _dp(out))
+    return out.view(np.complex128)
+
+
+def sici(x: float):
+    """(Si(x), Ci(x)) for x > 0."""
+    s, c = ctypes.c_double(), ctypes.c_double()
+    lib().or_sici(float(x), ctypes.byref(s), ctypes.byref(c))
+    return s.value, c.value
+
+
 def get_alpha(lam, K, d, eps, nE0, nK) -> complex:
     out = np.zeros(2)
     nE0 = np.ascontiguousarray(nE0, np.float64)
@@ -105,13 +125,20 @@ def aproduct_direct(R: np.ndarray, d: float, K: float, b) -> np.ndarray:
 class OracleCore:
     """AProductCore restated (AProductCore.cpp:12-249, 697-758)."""
 
-    def __init__(self, Nx, Ny, Nz, R, d, lam, material, nback=1.0, grid=None, pruned=False, periodic=None):
-        """periodic = (MAXm, MAXn, Lm, Ln) selects the periodic constructor (AProductCore.cpp:251-536)."""
+    def __init__(self, Nx, Ny, Nz, R, d, lam, material, nback=1.0, grid=None, pruned=False, periodic=None,
+                 method="LDR"):
+        """periodic = (MAXm, MAXn, Lm, Ln) selects the periodic constructor (AProductCore.cpp:251-536);
+        method "LDR" or "FCD" the interaction tensor (AProductCore.cpp:560-571)."""
         self.R = np.ascontiguousarray(R, np.int32).reshape(-1)
         self.N = self.R.size // 3
         mat = _c128(material)
         M = grid or (0, 0, 0)
-        if periodic is None:
+        if method != "LDR":
+            mm, mn, Lm, Ln = periodic if periodic is not None else (0, 0, 0.0, 0.0)
+            h = lib().or_core_create_method(Nx, Ny, Nz, self.N, _ip(self.R), d, lam, nback, mat.size,
+                                            _dp(mat.view(np.float64)), {"FCD": 1}[method], int(periodic is not None),
+                                            int(mm), int(mn), float(Lm), float(Ln), int(M[0]), int(M[1]), int(M[2]))
+        elif periodic is None:
             h = lib().or_core_create(Nx, Ny, Nz, self.N, _ip(self.R), d, lam, nback, mat.size,
                                      _dp(mat.view(np.float64)), int(M[0]), int(M[1]), int(M[2]))
         else:

@@ -17,6 +17,8 @@
  *        mode 3 appends int32 npts; f64 pts[npts][3]
  *        mode 4 (A-products on the periodic core, AProductCore.cpp:251-536)
  *        appends int32 MAXm MAXn; f64 Lm Ln
+ *        mode 5: A-products with the FCD tensor (AProductCore.cpp:625-695); its
+ *        SiCi tables are read from the working directory (SiCi.cpp:8-25)
  *   out: see the per-mode writers below.
  */
 #include <cstdio>
@@ -127,7 +129,7 @@ int main(int argc, char** argv) {
     VectorXcd material(nmat);
     for (int i = 0; i < nmat; i++) material(i) = std::complex<double>(mat[2 * i], mat[2 * i + 1]);
     AProductCore Core = mode == 4 ? AProductCore(&CStr, lam, material, nback, MAXm, MAXn, Lm, Ln, "LDR")
-                                  : AProductCore(&CStr, lam, material, nback, "LDR");
+                                  : AProductCore(&CStr, lam, material, nback, mode == 5 ? "FCD" : "LDR");
 
     FILE* fo = std::fopen(argv[2], "wb");
     if (!fo) return 2;
@@ -154,7 +156,7 @@ int main(int argc, char** argv) {
         std::fwrite(&r, 4, 1, fo);
     }
     put_cvec(fo, *Model.get_al());
-    if (mode == 0 || mode == 4) {
+    if (mode == 0 || mode == 4 || mode == 5) {
         for (int v = 0; v < nvec; v++) {
             VectorXcd b = to_cvec(vecs, v * veclen, 3 * N);
             VectorXcd y = Core.Aproduct(b);

@@ -54,6 +54,127 @@ void or_ldr_inter(double K, double x, double y, double z, double* out12) {
     for (int l = 0; l < 6; l++) st(out12, l, c1 * t[l]);
 }
 
+/* Sine and cosine integrals Si(x) = int_0^x sin t / t dt and
+ * Ci(x) = gamma + ln x + int_0^x (cos t - 1) / t dt for x > 0, to double
+ * precision, from the formulas of Abramowitz & Stegun:
+ *  - x <= 4: the power series 5.2.14 and 5.2.16, summed until the terms no
+ *    longer change the sum;
+ *  - x > 4: E1(ix) = -Ci(x) + i (Si(x) - pi/2) (5.2.23), with E1(z) from its
+ *    even continued fraction 5.1.22, e^{-z} / (z + 1 - 1/(z + 3 - 4/(z + 5 - ...))),
+ *    evaluated by the modified Lentz method (W. J. Lentz, Appl. Opt. 15, 1976;
+ *    Thompson & Barnett, J. Comput. Phys. 64, 1986). */
+void or_sici(double x, double* si, double* ci) {
+    const double euler = 0.57721566490153286061;
+    if (x <= 4.0) {
+        double s = 0.0, c = 0.0, term = x; /* term = (-1)^k x^(2k+1) / (2k+1)! */
+        for (int k = 0; k < 60; k++) {
+            const double sk = term / (2 * k + 1);
+            s += sk;
+            const double tc = -term * x / (2 * k + 2); /* (-1)^(k+1) x^(2k+2) / (2k+2)! */
+            const double ck = tc / (2 * k + 2);
+            c += ck;
+            term = tc * x / (2 * k + 3);
+            if (fabs(sk) <= 1e-17 * fabs(s) && fabs(ck) <= 1e-17 * (fabs(c) + 1e-300)) break;
+        }
+        *si = s;
+        *ci = euler + log(x) + c;
+        return;
+    }
+    /* Lentz on f = b0 + a1/(b1 + a2/(b2 + ...)) with b_j = z + 2j + 1 and
+     * a_j = -j^2, then E1 = e^{-z} / f, z = i x */
+    const cd z = x * I;
+    const double tiny = 1e-300;
+    cd b = z + 1.0;
+    cd f = b, C = b, D = 0.0;
+    for (int j = 1; j < 1000; j++) {
+        const double a = -(double)j * (double)j;
+        b = b + 2.0;
+        D = b + a * D;
+        if (cabs(D) < tiny) D = tiny;
+        C = b + a / C;
+        if (cabs(C) < tiny) C = tiny;
+        D = 1.0 / D;
+        const cd delta = C * D;
+        f = f * delta;
+        if (cabs(delta - 1.0) < 1e-16) break;
+    }
+    const cd e1 = cexp(-z) / f;
+    *ci = -creal(e1);
+    *si = OR_PI / 2 + cimag(e1);
+}
+
+/* The Si/Ci tables of SiCi/SiCi.py (read by SiCi.cpp:8-25): the values at
+ * x = 0.1 k, k = 1 .. 999999, here evaluated with or_sici. */
+enum { SICI_N = 999999 };
+static const double SICI_DIS = 0.1;
+static double* g_si = NULL;
+static double* g_ci = NULL;
+static void sici_tables(void) {
+    if (g_si) return;
+    double* si = (double*)malloc(sizeof(double) * SICI_N);
+    double* ci = (double*)malloc(sizeof(double) * SICI_N);
+    for (int k = 0; k < SICI_N; k++) or_sici(SICI_DIS * (k + 1), &si[k], &ci[k]);
+    g_ci = ci;
+    g_si = si;
+}
+/* SiCi::get_Si / get_Ci (SiCi.cpp:27-47): linear interpolation between the
+ * nodes (floor(x/dis)) dis and (ceil(x/dis)) dis.  Where the reference divides
+ * 0 by 0 (x on a node) this returns the node value; below the first node and
+ * past the last it extends the end intervals (the reference reads outside
+ * its table there). */
+static double sici_interp(const double* tab, double x) {
+    double q = x / SICI_DIS;
+    if (!(q >= 0.0)) q = 0.0;
+    if (q > (double)SICI_N) q = (double)SICI_N;
+    int p1 = (int)floor(q) - 1, p2 = (int)ceil(q) - 1;
+    if (p1 < 0) p1 = 0, p2 = 1;
+    if (p2 > SICI_N - 1) p2 = SICI_N - 1, p1 = SICI_N - 2;
+    if (p1 == p2) return tab[p1];
+    const double v1 = tab[p1], v2 = tab[p2];
+    const double a1 = (p1 + 1) * SICI_DIS, a2 = (p2 + 1) * SICI_DIS;
+    return v1 + ((v2 - v1) / (a2 - a1)) * (x - a1);
+}
+
+/* AProductCore::FCD_inter (AProductCore.cpp:625-695): the filtered coupled
+ * dipole tensor with the cut-off Kf = pi / d. */
+void or_fcd_inter(double K, double d, double x, double y, double z, double* out12) {
+    sici_tables();
+    const double xs = x * x, ys = y * y, zs = z * z;
+    const double rn = sqrt(xs + ys + zs);
+    if (rn == 0.0) {
+        memset(out12, 0, 12 * sizeof(double));
+        return;
+    }
+    const double xy = x * y, yz = y * z, zx = z * x;
+    const double rsq = rn * rn, rcu = rn * rn * rn;
+    const double Kf = OR_PI / d;
+    const double Cz = sici_interp(g_ci, (Kf + K) * rn), Cf = sici_interp(g_ci, (Kf - K) * rn);
+    const double Sz = sici_interp(g_si, (Kf + K) * rn), Sf = sici_interp(g_si, (Kf - K) * rn);
+    const double Cz1 = cos((Kf + K) * rn) / rn, Cf1 = cos((Kf - K) * rn) / rn;
+    const double Sz1 = sin((Kf + K) * rn) / rn, Sf1 = sin((Kf - K) * rn) / rn;
+    const double Cz2 = (-((Kf + K) * rn) * sin((Kf + K) * rn) - cos((Kf + K) * rn)) / rsq;
+    const double Cf2 = (-((Kf - K) * rn) * sin((Kf - K) * rn) - cos((Kf - K) * rn)) / rsq;
+    const double Sz2 = (((Kf + K) * rn) * cos((Kf + K) * rn) - sin((Kf + K) * rn)) / rsq;
+    const double Sf2 = (((Kf - K) * rn) * cos((Kf - K) * rn) - sin((Kf - K) * rn)) / rsq;
+    const double kr = K * rn;
+    const double sikr = sin(kr), cskr = cos(kr);
+    const double sikfr = sin(Kf * rn), cskfr = cos(Kf * rn);
+    const cd CC = OR_PI * I + Cf - Cz;
+    const double C1C1 = Cf1 - Cz1, C2C2 = Cf2 - Cz2;
+    const double SS = Sz + Sf, S1S1 = Sz1 + Sf1, S2S2 = Sz2 + Sf2;
+    const cd gf = (sikr * CC + cskr * SS) / (OR_PI * rn);
+    const cd const1 = (kr * cskr - sikr) * CC - (kr * sikr + cskr) * SS + rn * sikr * C1C1 + rn * cskr * S1S1;
+    const cd const2 = (-K * kr * sikr) * CC - (K * kr * cskr) * SS + (2 * kr * cskr) * C1C1 - (2 * kr * sikr) * S1S1 +
+                      rn * sikr * C2C2 + rn * cskr * S2S2;
+    const cd gf1 = const1 / (OR_PI * rsq);
+    const cd gf2 = (rn * const2 - 2.0 * const1) / (OR_PI * rcu);
+    const double hr = (sikfr - Kf * rn * cskfr) / (2.0 * OR_PI * OR_PI * rcu);
+    const cd term1 = K * K * gf + gf1 / rn + (4.0 * OR_PI / 3.0) * hr;
+    const cd term2 = (gf2 - gf1 / rn) / rsq;
+    const cd t[6] = {term1 + xs * term2, xy * term2, zx * term2, term1 + ys * term2, yz * term2, term1 + zs * term2};
+    for (int l = 0; l < 6; l++) st(out12, l, -1.0 * t[l]);
+}
+
 /* tools.cpp:617-630: LDR polarisability.  The three lattice-dispersion
  * coefficients are the published LDR constants the reference uses. */
 void or_get_alpha(double lam, double K, double d, double eps_re, double eps_im,
@@ -81,6 +202,7 @@ struct or_core {
     int Mx, My, Mz;
     long M;
     int pruned;
+    int method;       /* 0 LDR, 1 FCD */
     oc_cplx* A[6];    /* spectra of xx, xy, xz, yy, yz, zz */
     oc_cplx* bg[3];   /* padded b grids */
     oc_plan1d *px, *py, *pz;
@@ -137,39 +259,56 @@ static void fft3(or_core* c, oc_cplx* g, int sign, int prune_in, int prune_out) 
 /* AProductCore::A_dic_generator(x, y, z, m, n) (AProductCore.cpp:573-586):
  * the LDR tensor of the image (m, n) of a lattice periodic in x and y with
  * periods Lm, Ln, damped by exp(-(gamma K r)^4), gamma = 0.01 */
-static void ldr_image(double K, double x, double y, double z, int m, int n, double Lm, double Ln, double* t) {
+/* AProductCore::A_dic_generator(x, y, z) (AProductCore.cpp:560-571) */
+static void a_dic(int method, double K, double d, double x, double y, double z, double* t) {
+    if (method == 1) or_fcd_inter(K, d, x, y, z, t);
+    else or_ldr_inter(K, x, y, z, t);
+}
+
+static void ldr_image(int method, double K, double d, double x, double y, double z, int m, int n, double Lm,
+                      double Ln, double* t) {
     const double gamma = 0.01;
     x = x + m * Lm;
     y = y + n * Ln;
-    or_ldr_inter(K, x, y, z, t);
+    a_dic(method, K, d, x, y, z, t);
     const double ph = exp(-pow(gamma * K * sqrt(x * x + y * y + z * z), 4));
     for (int l = 0; l < 12; l++) t[l] *= ph;
 }
 
 static or_core* core_create(int Nx, int Ny, int Nz, int N, const int* R, double d, double lam, double nback,
                             int nmat, const double* material, int Mx, int My, int Mz, int periodic, int MAXm,
-                            int MAXn, double Lm, double Ln);
+                            int MAXn, double Lm, double Ln, int method);
 
 or_core* or_core_create(int Nx, int Ny, int Nz, int N, const int* R, double d, double lam,
                         double nback, int nmat, const double* material, int Mx, int My, int Mz) {
-    return core_create(Nx, Ny, Nz, N, R, d, lam, nback, nmat, material, Mx, My, Mz, 0, 0, 0, 0.0, 0.0);
+    return core_create(Nx, Ny, Nz, N, R, d, lam, nback, nmat, material, Mx, My, Mz, 0, 0, 0, 0.0, 0.0, 0);
 }
 
 or_core* or_core_create_periodic(int Nx, int Ny, int Nz, int N, const int* R, double d, double lam, double nback,
                                  int nmat, const double* material, int MAXm, int MAXn, double Lm, double Ln,
                                  int Mx, int My, int Mz) {
     if (MAXm < 0 || MAXn < 0) return NULL;
-    return core_create(Nx, Ny, Nz, N, R, d, lam, nback, nmat, material, Mx, My, Mz, 1, MAXm, MAXn, Lm, Ln);
+    return core_create(Nx, Ny, Nz, N, R, d, lam, nback, nmat, material, Mx, My, Mz, 1, MAXm, MAXn, Lm, Ln, 0);
+}
+
+or_core* or_core_create_method(int Nx, int Ny, int Nz, int N, const int* R, double d, double lam, double nback,
+                               int nmat, const double* material, int method, int periodic, int MAXm, int MAXn,
+                               double Lm, double Ln, int Mx, int My, int Mz) {
+    if (method != 0 && method != 1) return NULL;
+    if (periodic && (MAXm < 0 || MAXn < 0)) return NULL;
+    return core_create(Nx, Ny, Nz, N, R, d, lam, nback, nmat, material, Mx, My, Mz, periodic, MAXm, MAXn, Lm, Ln,
+                       method);
 }
 
 static or_core* core_create(int Nx, int Ny, int Nz, int N, const int* R, double d, double lam, double nback,
                             int nmat, const double* material, int Mx, int My, int Mz, int periodic, int MAXm,
-                            int MAXn, double Lm, double Ln) {
+                            int MAXn, double Lm, double Ln, int method) {
     if (Nx < 1 || Ny < 1 || Nz < 1 || N < 0 || nmat < 1) return NULL;
     or_core* c = (or_core*)calloc(1, sizeof(or_core));
     if (!c) return NULL;
     c->Nx = Nx; c->Ny = Ny; c->Nz = Nz; c->N = N;
     c->d = d; c->lam = lam; c->nback = nback;
+    c->method = method;
     c->K = 2 * OR_PI / (lam / nback); /* AProductCore.cpp:17 */
     c->nmat = nmat;
     c->material = (double*)malloc(sizeof(double) * 2 * nmat);
@@ -216,11 +355,11 @@ static or_core* core_create(int Nx, int Ny, int Nz, int N, const int* R, double 
                     memset(t, 0, sizeof(t));
                     for (int m = -MAXm; m <= MAXm; m++)
                         for (int n = -MAXn; n <= MAXn; n++) {
-                            ldr_image(c->K, d * ox, d * oy, d * oz, m, n, Lm, Ln, ti);
+                            ldr_image(method, c->K, d, d * ox, d * oy, d * oz, m, n, Lm, Ln, ti);
                             for (int l = 0; l < 12; l++) t[l] = t[l] + ti[l];
                         }
                 } else {
-                    or_ldr_inter(c->K, d * ox, d * oy, d * oz, t);
+                    a_dic(method, c->K, d, d * ox, d * oy, d * oz, t);
                 }
                 long g = gidx(c, i, j, k);
                 for (int l = 0; l < 6; l++) {
@@ -521,7 +660,8 @@ void or_model_field_at(const or_model* m, int npts, const double* pts, double* E
         cd s[3];
         for (int j = 0; j < 3; j++) s[j] = (m->E0 * m->nE0[j]) * e;
         for (int i = 0; i < c->N; i++) {
-            or_ldr_inter(c->K, x - c->d * c->R[3 * i], y - c->d * c->R[3 * i + 1], z - c->d * c->R[3 * i + 2], A);
+            a_dic(c->method, c->K, c->d, x - c->d * c->R[3 * i], y - c->d * c->R[3 * i + 1], z - c->d * c->R[3 * i + 2],
+                  A);
             const cd a00 = A[0] + A[1] * I, a01 = A[2] + A[3] * I, a02 = A[4] + A[5] * I;
             const cd a11 = A[6] + A[7] * I, a12 = A[8] + A[9] * I, a22 = A[10] + A[11] * I;
             const cd px = m->P[3 * i], py = m->P[3 * i + 1], pz = m->P[3 * i + 2];

@@ -37,6 +37,10 @@ extern "C" {
 
 void or_normalize_material(int nmat, const double* mat_in, double nback, double* mat_out);
 void or_ldr_inter(double K, double x, double y, double z, double* out12);
+/* Si(x), Ci(x) for x > 0 (A&S 5.2.14, 5.2.16, 5.2.23, 5.1.22) */
+void or_sici(double x, double* si, double* ci);
+/* FCD tensor (AProductCore.cpp:625-695) with the interpolated Si/Ci tables */
+void or_fcd_inter(double K, double d, double x, double y, double z, double* out12);
 void or_get_alpha(double lam, double K, double d, double eps_re, double eps_im,
                   const double* nE0, const double* nK, double* out2);
 
@@ -52,6 +56,10 @@ or_core* or_core_create(int Nx, int Ny, int Nz, int N, const int* R, double d, d
 or_core* or_core_create_periodic(int Nx, int Ny, int Nz, int N, const int* R, double d, double lam, double nback,
                                  int nmat, const double* material, int MAXm, int MAXn, double Lm, double Ln,
                                  int Mx, int My, int Mz);
+/* general constructor: method 0 LDR, 1 FCD; periodic as or_core_create_periodic */
+or_core* or_core_create_method(int Nx, int Ny, int Nz, int N, const int* R, double d, double lam, double nback,
+                               int nmat, const double* material, int method, int periodic, int MAXm, int MAXn,
+                               double Lm, double Ln, int Mx, int My, int Mz);
 void or_core_destroy(or_core* c);
 void or_core_set_pruned(or_core* c, int pruned);
 double or_core_K(const or_core* c);

@@ -9,6 +9,8 @@ on seeded inputs.  Each fixture stores its inputs and the reference's outputs:
   aprod_*.npz      Aproduct / Aproductwithalb (AProductCore.cpp:697-758,
                    DDAModel.cpp:577-586) of seeded vectors
   aprodper_*.npz   the same on the periodic core (AProductCore.cpp:251-536)
+  aprodfcd_*.npz   the same with the FCD tensor (AProductCore.cpp:625-695); its
+                   Si/Ci tables are written the way SiCi/SiCi.py writes them
   solve_*.npz      bicgstab + update_E_in_structure (DDAModel.cpp:131-260,
                    567-575): ITERATION, the printed Error, P, Einternal
   field_*.npz      a solve, then the point-field objective
@@ -64,8 +66,25 @@ def write_input(path, mode, Nx, Ny, Nz, R, d, lam, nback, material, nK, E0, nE0,
             f.write(np.asarray(v).astype("<c16" if mode != 2 else "<f8").tobytes())
 
 
+def write_sici_tables(folder):
+    """The tables SiCi.cpp:8-25 reads (from .\\SiCi\\Si.txt and .\\SiCi\\Ci.txt relative to the
+    working directory, backslashes included), produced as SiCi/SiCi.py does: scipy's sici at
+    0.1, 0.2, ..., 0.1 * 999999, written with str()."""
+    from scipy.special import sici
+    number, dis = 1000000, 0.1
+    pos = np.linspace(dis, dis * (number - 1), number - 1)
+    si, ci = sici(pos)
+    for name, vals in (("Si", si), ("Ci", ci)):
+        with open(os.path.join(folder, ".\\SiCi\\%s.txt" % name), "w") as f:
+            f.write(str(number - 1) + "\n" + str(dis) + "\n")
+            f.write("\n".join(str(v) for v in vals.tolist()))
+            f.write("\n")
+
+
 def run(mode, points=None, periodic=None, **kw):
     with tempfile.TemporaryDirectory() as td:
+        if mode == 5:
+            write_sici_tables(td)
         fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
         write_input(fin, mode, **kw)
         if periodic is not None:
@@ -77,7 +96,7 @@ def run(mode, points=None, periodic=None, **kw):
             with open(fin, "ab") as f:
                 f.write(struct.pack("<i", pts.shape[0]))
                 f.write(pts.tobytes())
-        pr = subprocess.run([DRIVER, fin, fout], capture_output=True, text=True, check=True)
+        pr = subprocess.run([DRIVER, fin, fout], capture_output=True, text=True, check=True, cwd=td)
         with open(fout, "rb") as f:
             raw = f.read()
     return raw, pr.stdout
@@ -146,6 +165,24 @@ def gen_aprod(name, w: lattice.Workload, nvec, seed):
     np.savez_compressed(os.path.join(HERE, f"aprod_{name}.npz"), **inputs_dict(w), al=al, b=np.array(vecs),
              y=np.array(ys), y_alb=np.array(yws))
     print(f"aprod_{name}: N={N} |y|={np.linalg.norm(ys[0]):.6g}")
+
+
+def gen_aprod_fcd(name, w: lattice.Workload, nvec, seed):
+    N = w.N
+    vecs = [rand_vec(3 * N, seed + v) for v in range(nvec)]
+    raw, _ = run(5, **case_kw(w), vecs=vecs)
+    off = 12 * N
+    al = np.frombuffer(raw, "<c16", count=3 * N, offset=off)
+    off += 48 * N
+    ys, yws = [], []
+    for _ in range(nvec):
+        ys.append(np.frombuffer(raw, "<c16", count=3 * N, offset=off))
+        off += 48 * N
+        yws.append(np.frombuffer(raw, "<c16", count=3 * N, offset=off))
+        off += 48 * N
+    np.savez_compressed(os.path.join(HERE, f"aprodfcd_{name}.npz"), **inputs_dict(w), al=al, b=np.array(vecs),
+                        y=np.array(ys), y_alb=np.array(yws))
+    print(f"aprodfcd_{name}: N={N} |y|={np.linalg.norm(ys[0]):.6g}")
 
 
 def gen_aprod_periodic(name, w: lattice.Workload, periodic, nvec, seed):
@@ -233,6 +270,10 @@ def main():
     gen_aprod_periodic("cell6x5x3", small_workload("cell6x5x3", 6, 5, 3, 16), (3, 3, 60.0, 50.0), 2, 600)
     gen_aprod_periodic("sparse5x4x3", small_workload("sparse5x4x3", 5, 4, 3, 17, keep=0.7, shuffle=True),
                        (5, 2, 75.0, 52.0), 1, 700)
+    # the FCD tensor on a box and on a sparse lattice
+    gen_aprod_fcd("box6x5x4", small_workload("box6x5x4", 6, 5, 4, 11), 1, 800)
+    gen_aprod_fcd("sparse7x6x4", small_workload("sparse7x6x4", 7, 6, 4, 18, em=2.25 + 0.0j, lam=620.0, keep=0.6,
+                                                  shuffle=True), 1, 900)
     # the point field of the solved cfg 1 structure: above the centre (the topology objective's
     # point), beside, below, far off, and inside the box between lattice sites
     gen_field("cfg1", lattice.config(1), [[95.0, 95.0, 190.0], [-50.0, 95.0, 45.0], [95.0, 95.0, -80.0],

@@ -44,13 +44,15 @@ def test_core_create_rejects_bad_arguments_before_touching_a_device():
     assert b"invalid" in L.tdda_last_error()
 
 
-def test_fcd_method_is_reported_unsupported():
+def test_fcd_needs_the_spacing_inside_the_sici_tables():
+    """FCD evaluates Si/Ci at (pi/d - K) r >= pi - K d, and the tables start at 0.1."""
     import numpy as np
     R = tdda.lattice.bulk(2, 2, 2)
     mat = np.array([1.0, 4.0 + 0.1j])
     with pytest.raises(tdda.TddaError) as e:
-        tdda.AProductCore(2, 2, 2, R, 10.0, 500.0, mat, method="FCD")
+        tdda.AProductCore(2, 2, 2, R, 100.0, 200.0, mat, method="FCD")
     assert e.value.status == tdda.ERR_UNSUPPORTED
+    assert b"FCD" in tdda.load().tdda_last_error()
 
 
 def test_periodic_core_rejects_bad_images_before_touching_a_device():

@@ -278,3 +278,53 @@ def test_periodic_solve_matches_oracle():
         assert rel(m.get_P(), om.P) <= bound
         m.close()
     core.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["box6x5x4", "sparse7x6x4"])
+def test_fcd_aproduct_matches_reference(name):
+    """The FCD tensor on the device (Si/Ci tables built by k_sici_table, interpolated as
+    SiCi.cpp:27-47) against the reference's FCD A-products."""
+    g = golden(f"aprodfcd_{name}.npz")
+    Nx, Ny, Nz = (int(v) for v in g["box"])
+    core = tdda.AProductCore(Nx, Ny, Nz, g["R"], float(g["d"]), float(g["lam"]), g["material"], float(g["nback"]),
+                             method="FCD")
+    m = tdda.DDAModel(core, g["nK"], float(g["E0"]), g["nE0"], g["diel_old"])
+    for b, y, yw in zip(g["b"], g["y"], g["y_alb"]):
+        assert rel(core.Aproduct(b), y) <= 1e-12
+        assert rel(core.Aproduct(b, tdda.FP32_REFINE), y) <= 1e-5
+        assert rel(m.Aproductwithalb(b), yw) <= 1e-12
+    m.close()
+    core.close()
+
+
+@pytest.mark.gpu
+def test_fcd_tensor_field_and_solve_match_oracle():
+    """A_dic_generator, the off-lattice field and an FP64 solve on an FCD core (periodic
+    images included) against the oracle."""
+    Nx, Ny, Nz, d, lam = 6, 5, 3, 12.0, 560.0
+    R = tdda.lattice.bulk(Nx, Ny, Nz)
+    rho = np.repeat(0.5 + 0.5 * np.sin(0.33 * np.arange(Nx * Ny * Nz)), 3)
+    mat = np.array([1.0, 3.0 + 0.05j])
+    oc = O.OracleCore(Nx, Ny, Nz, R, d, lam, mat, method="FCD")
+    core = tdda.AProductCore(Nx, Ny, Nz, R, d, lam, mat, method="FCD")
+    for p in ((12.0, 0.0, 0.0), (24.0, -12.0, 36.0), (7.3, 15.1, -3.3)):
+        t = O.fcd_inter(oc.K, d, *p)
+        full = np.array([[t[0], t[1], t[2]], [t[1], t[3], t[4]], [t[2], t[4], t[5]]])
+        assert np.max(np.abs(core.A_dic_generator(*p) - full)) <= 1e-13 * np.max(np.abs(full))
+    om = O.OracleModel(oc, [0, 0, 1], 1.0, [1, 0, 0], rho)
+    assert om.bicgstab(10000, 1e-12) == O.CONVERGED
+    m = tdda.DDAModel(core, [0, 0, 1], 1.0, [1, 0, 0], rho)
+    assert m.bicgstab(10000, 1e-10)["status"] == 0
+    assert rel(m.get_P(), om.P) <= 1e-9
+    m.InitializeP(om.P)
+    pts = np.array([[30.0, 24.0, 90.0], [-20.0, 10.0, 18.0]])
+    assert rel(m.field_at(pts).ravel(), om.field_at(pts).ravel()) <= 1e-12
+    m.close()
+    core.close()
+    per = (2, 2, Nx * d, Ny * d)
+    opc = O.OracleCore(Nx, Ny, Nz, R, d, lam, mat, method="FCD", periodic=per)
+    pcore = tdda.AProductCore(Nx, Ny, Nz, R, d, lam, mat, method="FCD", periodic=per)
+    b = (np.cos(np.arange(3 * R.size // 3)) + 1j * np.sin(0.5 * np.arange(3 * R.size // 3))).astype(np.complex128)
+    assert rel(pcore.Aproduct(b), opc.Aproduct(b)) <= 1e-12
+    pcore.close()

@@ -131,3 +131,30 @@ def test_periodic_aproduct_matches_reference(name):
     for b, y, yw in zip(g["b"], g["y"], g["y_alb"]):
         assert rel(core.Aproduct(b), y) <= 1e-14
         assert rel(model.Aproductwithalb(b), yw) <= 1e-14
+
+
+def test_sici_matches_scipy():
+    """Si, Ci of the restatement (A&S series and continued fraction) against scipy's."""
+    special = pytest.importorskip("scipy.special")
+    xs = np.concatenate([np.linspace(0.1, 4.0, 391), np.linspace(4.0, 60.0, 561), np.geomspace(60.0, 1e5, 300)])
+    S, C = special.sici(xs)
+    for x, s_ref, c_ref in zip(xs, S, C):
+        s, c = O.sici(float(x))
+        assert abs(s - s_ref) <= 2e-15 * max(1.0, abs(s_ref))
+        assert abs(c - c_ref) <= 2e-15 * max(1.0, abs(c_ref))
+
+
+@pytest.mark.parametrize("name", ["box6x5x4", "sparse7x6x4"])
+def test_fcd_aproduct_matches_reference(name):
+    """The FCD tensor (AProductCore.cpp:625-695) with interpolated Si/Ci tables: the oracle's
+    tables are its own Si/Ci at the nodes; the reference's were written by scipy, as
+    SiCi/SiCi.py does."""
+    g = golden(f"aprodfcd_{name}.npz")
+    Nx, Ny, Nz = (int(v) for v in g["box"])
+    core = O.OracleCore(Nx, Ny, Nz, g["R"], float(g["d"]), float(g["lam"]), g["material"], float(g["nback"]),
+                        method="FCD")
+    model = O.OracleModel(core, g["nK"], float(g["E0"]), g["nE0"], g["diel_old"])
+    assert rel(model.al, g["al"]) <= 1e-15
+    for b, y, yw in zip(g["b"], g["y"], g["y_alb"]):
+        assert rel(core.Aproduct(b), y) <= 1e-13
+        assert rel(model.Aproductwithalb(b), yw) <= 1e-13

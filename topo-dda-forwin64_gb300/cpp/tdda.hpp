@@ -135,8 +135,13 @@ class AProductCore {
         for (int l = 0; l < 6; l++) a[l] = cplx(t[2 * l], t[2 * l + 1]);
         return {{{a[0], a[1], a[2]}, {a[1], a[3], a[4]}, {a[2], a[4], a[5]}}};
     }
+    // Matrix3cd A_dic_generator(double x, double y, double z)     AProductCore.cpp:560-571 (LDR or FCD)
     std::array<std::array<cplx, 3>, 3> A_dic_generator(double x, double y, double z) const {
-        return LDR_inter(x, y, z);
+        double t[12];
+        check(tdda_core_interaction(h_, x, y, z, t), "A_dic_generator");
+        cplx a[6];
+        for (int l = 0; l < 6; l++) a[l] = cplx(t[2 * l], t[2 * l + 1]);
+        return {{{a[0], a[1], a[2]}, {a[1], a[3], a[4]}, {a[2], a[4], a[5]}}};
     }
     // Matrix3cd A_dic_generator(double x, double y, double z, int m, int n)     AProductCore.cpp:573-586
     std::array<std::array<cplx, 3>, 3> A_dic_generator(double x, double y, double z, int m, int n) const {

@@ -178,6 +178,7 @@ struct tdda_core_s {
     std::vector<void*> allocs;
     bool is_periodic = false;
     tdda::PeriodicImages periodic{};
+    tdda::Interaction inter{};  // LDR, or FCD with this device's Si/Ci tables
 };
 
 struct tdda_model_s {
@@ -712,7 +713,37 @@ int tdda_device_count(void) {
 
 namespace {
 tdda_status core_create(const tdda_core_desc* desc, const tdda::PeriodicImages* pi, tdda_core** out);
+
+// The FCD tensor's Si/Ci tables, built once per device by k_sici_table and
+// kept for the life of the process (2 x 8 MB).
+std::mutex g_sici_mu;
+double* g_sici[64][2];
+tdda_status sici_tables(int device, cudaStream_t stream, const double** si, const double** ci) {
+    std::lock_guard<std::mutex> lk(g_sici_mu);
+    if (device < 0 || device >= 64) {
+        set_err("device %d out of range", device);
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    if (!g_sici[device][0]) {
+        double *a = nullptr, *b = nullptr;
+        cudaError_t e = cudaMalloc((void**)&a, sizeof(double) * tdda::kSiCiN);
+        if (e == cudaSuccess) e = cudaMalloc((void**)&b, sizeof(double) * tdda::kSiCiN);
+        if (e == cudaSuccess) e = tdda::launch_sici_table(a, b, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) {
+            if (a) cudaFree(a);
+            if (b) cudaFree(b);
+            return cuda_fail(e, "Si/Ci tables");
+        }
+        count_launches(1);
+        g_sici[device][0] = a;
+        g_sici[device][1] = b;
+    }
+    *si = g_sici[device][0];
+    *ci = g_sici[device][1];
+    return TDDA_OK;
 }
+}  // namespace
 
 tdda_status tdda_core_create(const tdda_core_desc* desc, tdda_core** out) { return core_create(desc, nullptr, out); }
 
@@ -746,9 +777,18 @@ tdda_status core_create(const tdda_core_desc* desc, const tdda::PeriodicImages* 
         set_err("at most %d materials", tdda::kMaxMaterials);
         return TDDA_ERR_UNSUPPORTED;
     }
-    if (desc->method != TDDA_METHOD_LDR) {
-        set_err("only the LDR interaction tensor is built (FCD needs the Si/Ci tables)");
-        return TDDA_ERR_UNSUPPORTED;
+    if (desc->method != TDDA_METHOD_LDR && desc->method != TDDA_METHOD_FCD) {
+        set_err("unknown interaction method %d", desc->method);
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    if (desc->method == TDDA_METHOD_FCD) {
+        // the smallest Si/Ci argument is (pi/d - K) d = pi - K d (nearest neighbours), and
+        // the reference's tables start at 0.1 (SiCi.cpp:27-47)
+        const double Kd = 2 * kPi / (desc->lam / desc->nback) * desc->d;
+        if (!(kPi - Kd >= tdda::kSiCiDis)) {
+            set_err("FCD needs K d <= pi - 0.1 (K d = %g): the spacing is too coarse for the wavelength", Kd);
+            return TDDA_ERR_UNSUPPORTED;
+        }
     }
     if ((long long)desc->Nx * desc->Ny * desc->Nz > (1LL << 28)) {
         set_err("lattice box too large");
@@ -895,6 +935,8 @@ tdda_status core_create(const tdda_core_desc* desc, const tdda::PeriodicImages* 
     TDDA_CORE_CK(cudaMemcpyAsync(c->rhs64 + c->max_rhs, &p64, sizeof(p64), cudaMemcpyHostToDevice, c->stream));
     TDDA_CORE_CK(cudaMemcpyAsync(c->rhs32 + c->max_rhs, &p32, sizeof(p32), cudaMemcpyHostToDevice, c->stream));
     TDDA_CORE_TRY(configure_once(c->device));
+    c->inter.fcd = c->method == TDDA_METHOD_FCD;
+    if (c->inter.fcd) TDDA_CORE_TRY(sici_tables(c->device, c->stream, &c->inter.si, &c->inter.ci));
     // Green spectrum (AProductCore.cpp:53-229; periodic: :300-520), on a temporary full grid
     double2* full6 = nullptr;
     double2* oct = nullptr;
@@ -902,7 +944,7 @@ tdda_status core_create(const tdda_core_desc* desc, const tdda::PeriodicImages* 
     if (pi) TDDA_CORE_CK(cudaMallocAsync((void**)&oct, sizeof(double2) * 6 * (size_t)g.Nx * g.Ny * g.Nz, c->stream));
     count_launches(pi ? 6 : 5);
     cudaError_t ge = tdda::launch_green(g, c->K, c->d, c->tw64[0], c->tw64[1], c->tw64[2], full6, c->green64,
-                                        c->green32, c->stream, pi, oct);
+                                        c->green32, c->stream, c->inter, pi, oct);
     cudaError_t fe = cudaFreeAsync(full6, c->stream);
     if (oct && fe == cudaSuccess) fe = cudaFreeAsync(oct, c->stream);
     TDDA_CORE_CK(ge);
@@ -961,6 +1003,21 @@ tdda_status tdda_core_ldr_inter(const tdda_core* c, double x, double y, double z
     for (int l = 0; l < 6; l++) {
         out12[2 * l] = t[l].real();
         out12[2 * l + 1] = t[l].imag();
+    }
+    return TDDA_OK;
+}
+
+tdda_status tdda_core_interaction(const tdda_core* c, double x, double y, double z, double* out12) {
+    if (!c || !out12) {
+        set_err("null argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    double2 t[6];
+    tdda::Interaction it{c->inter.fcd, nullptr, nullptr};  // host: Si/Ci node values evaluated directly
+    tdda::interaction_tensor(it, c->K, c->d, x, y, z, t);
+    for (int l = 0; l < 6; l++) {
+        out12[2 * l] = t[l].x;
+        out12[2 * l + 1] = t[l].y;
     }
     return TDDA_OK;
 }
@@ -1268,7 +1325,7 @@ tdda_status tdda_model_field_at(tdda_model* m, int npts, const double* points, d
         }
         count_launches(2 * ((npts + 32767) / 32768));
         if (e == cudaSuccess)
-            e = tdda::launch_field_at(c->N, c->Rdev, c->d, c->K, m->P, npts, dpts, make_double3(m->nK[0], m->nK[1], m->nK[2]),
+            e = tdda::launch_field_at(c->N, c->Rdev, c->d, c->K, c->inter, m->P, npts, dpts, make_double3(m->nK[0], m->nK[1], m->nK[2]),
                                       make_double3(m->nE0[0], m->nE0[1], m->nE0[2]), m->E0, part, dE, c->stream);
         if (e == cudaSuccess && mem != TDDA_MEM_DEVICE)
             e = cudaMemcpyAsync(E, dE, sizeof(double2) * 3 * (size_t)npts, cudaMemcpyDeviceToHost, c->stream);

@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include "tdda_fft.cuh"
+#include "tdda_tensor.cuh"
 
 namespace tdda {
 
@@ -144,8 +145,10 @@ struct PeriodicImages {
 // FFT, fold, scale.
 cudaError_t launch_green(const Geom& g, double K, double d, const double2* tw64x, const double2* tw64y,
                          const double2* tw64z, double2* full6 /* 6*Mx*My*Mz scratch */, double2* green64,
-                         float2* green32, cudaStream_t stream, const PeriodicImages* pi = nullptr,
-                         double2* oct = nullptr);
+                         float2* green32, cudaStream_t stream, const Interaction& it,
+                         const PeriodicImages* pi = nullptr, double2* oct = nullptr);
+// the FCD Si/Ci tables (kSiCiN entries each)
+cudaError_t launch_sici_table(double* si, double* ci, cudaStream_t stream);
 
 // One A-product over nrhs right-hand sides.  rhs[] lives in device memory.
 // ev, when given, holds 6 events recorded before K1..K5 and after K5; with
@@ -199,8 +202,9 @@ cudaError_t launch_model_incident(int N, const int* R, double3 nK, double3 nE0, 
 // E at npts points (nm): E_ext - sum_i A(r - d R_i) P_i, FP64 (ObjDDAModel.cpp:42-96).
 // part holds 3 * field_blocks(N, npts) * npts double2.
 int field_blocks(int N, int npts);
-cudaError_t launch_field_at(int N, const int* R, double d, double K, const double2* P, int npts, const double* pts,
-                            double3 nK, double3 nE0, double E0, double2* part, double2* E, cudaStream_t stream);
+cudaError_t launch_field_at(int N, const int* R, double d, double K, const Interaction& it, const double2* P, int npts,
+                            const double* pts, double3 nK, double3 nE0, double E0, double2* part, double2* E,
+                            cudaStream_t stream);
 
 // Adjoint sensitivity per design parameter (EvoDDAModel.cpp:610-638):
 //   s_i = sum_{q in [off_i, off_i+1)} Re( sum_c lam_{3j+c} dal_j/drho_j P_{3j+c} ), j = dip_q,

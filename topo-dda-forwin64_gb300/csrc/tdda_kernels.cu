@@ -23,6 +23,7 @@
 #include <algorithm>
 
 #include "tdda_device.cuh"
+#include "tdda_tensor.cuh"
 
 namespace tdda {
 
@@ -108,34 +109,7 @@ __global__ void __launch_bounds__(kNT) k_solve_begin(int n3, const RhsVecs<T>* _
 }
 
 // ================================================================ K0 green
-// LDR_inter (AProductCore.cpp:588-623) at the offset (x, y, z) nm: the six
-// components xx, xy, xz, yy, yz, zz; r = 0 gives the zero tensor
-__device__ __forceinline__ void ldr_tensor(double K, double x, double y, double z, double2 (&t)[6]) {
-    const double xs = x * x, ys = y * y, zs = z * z;
-    const double rn = sqrt(xs + ys + zs);
-    if (rn == 0.0) {
-#pragma unroll
-        for (int l = 0; l < 6; l++) t[l] = make_double2(0.0, 0.0);
-        return;
-    }
-    const double rsq = rn * rn, rcu = rn * rn * rn;
-    double sn, cs;
-    sincos(K * rn, &sn, &cs);
-    const double2 c1 = make_double2(cs / rcu, sn / rcu);        // e^{iKr} / r^3
-    const double2 c2 = make_double2(1.0 / rsq, -(K * rn) / rsq);  // (1 - iKr) / r^2
-    const double2 c3 = make_double2(K * K - 3.0 * c2.x, -3.0 * c2.y);
-    double2 v[6];
-    v[0] = make_double2(c2.x * (rsq - 3 * xs) - K * K * (ys + zs), c2.y * (rsq - 3 * xs));
-    v[1] = make_double2(x * y * c3.x, x * y * c3.y);
-    v[2] = make_double2(z * x * c3.x, z * x * c3.y);
-    v[3] = make_double2(c2.x * (rsq - 3 * ys) - K * K * (zs + xs), c2.y * (rsq - 3 * ys));
-    v[4] = make_double2(y * z * c3.x, y * z * c3.y);
-    v[5] = make_double2(c2.x * (rsq - 3 * zs) - K * K * (xs + ys), c2.y * (rsq - 3 * zs));
-#pragma unroll
-    for (int l = 0; l < 6; l++) t[l] = dmul(c1, v[l]);
-}
-
-__global__ void k_green_real(Geom g, double K, double d, double2* __restrict__ full6) {
+__global__ void k_green_real(Geom g, double K, double d, Interaction it, double2* __restrict__ full6) {
     const int Mx = g.px.M, My = g.py.M, Mz = g.pz.M;
     const long long M = (long long)Mx * My * Mz;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < M; e += (long long)gridDim.x * blockDim.x) {
@@ -148,7 +122,7 @@ __global__ void k_green_real(Geom g, double K, double d, double2* __restrict__ f
         int oz = k < g.Nz ? k : (k > Mz - g.Nz ? k - Mz : INT32_MIN);
         double2 t[6];
         if (ox != INT32_MIN && oy != INT32_MIN && oz != INT32_MIN) {
-            ldr_tensor(K, d * ox, d * oy, d * oz, t);
+            interaction_tensor(it, K, d, d * ox, d * oy, d * oz, t);
         } else {
 #pragma unroll
             for (int l = 0; l < 6; l++) t[l] = make_double2(0.0, 0.0);
@@ -165,15 +139,15 @@ __global__ void k_green_real(Geom g, double K, double d, double2* __restrict__ f
 // writes its three complex partials; pass 2 adds the nb partials of each point
 // in block order and subtracts them from the incident field.
 __global__ void __launch_bounds__(kNT) k_field_partial(int N, const int* __restrict__ R, double d, double K,
-                                                       const double2* __restrict__ P, const double* __restrict__ pts,
-                                                       double2* __restrict__ part) {
+                                                       Interaction it, const double2* __restrict__ P,
+                                                       const double* __restrict__ pts, double2* __restrict__ part) {
     __shared__ double sred[6 * kNT];
     const int p = blockIdx.y;
     const double x = pts[3 * p], y = pts[3 * p + 1], z = pts[3 * p + 2];
     double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
         double2 t[6];
-        ldr_tensor(K, x - d * R[3 * i], y - d * R[3 * i + 1], z - d * R[3 * i + 2], t);
+        interaction_tensor(it, K, d, x - d * R[3 * i], y - d * R[3 * i + 1], z - d * R[3 * i + 2], t);
         const double2 px = P[3 * i], py = P[3 * i + 1], pz = P[3 * i + 2];
         const double2 s0 = dmul(t[0], px), s1 = dmul(t[1], py), s2 = dmul(t[2], pz);
         const double2 u0 = dmul(t[1], px), u1 = dmul(t[3], py), u2 = dmul(t[4], pz);
@@ -219,7 +193,7 @@ __global__ void k_field_sum(int npts, int nb, const double2* __restrict__ part, 
 // free-space tensor and the octant o >= 0 determines the rest.  One block
 // per octant offset sums the (2 MAXm + 1)(2 MAXn + 1) images in a fixed order.
 __global__ void __launch_bounds__(kNT) k_green_periodic_octant(Geom g, double K, double d, PeriodicImages pi,
-                                                               double2* __restrict__ oct) {
+                                                               Interaction it, double2* __restrict__ oct) {
     __shared__ double sred[12 * kNT];
     const int o = blockIdx.x;  // (ox Ny + oy) Nz + oz
     const int oz = o % g.Nz, oy = (o / g.Nz) % g.Ny, ox = o / (g.Nz * g.Ny);
@@ -231,7 +205,7 @@ __global__ void __launch_bounds__(kNT) k_green_periodic_octant(Geom g, double K,
         const int m = q % nm - pi.MAXm, n = q / nm - pi.MAXn;
         const double x = d * ox + m * pi.Lm, y = d * oy + n * pi.Ln, z = d * oz;
         double2 t[6];
-        ldr_tensor(K, x, y, z, t);
+        interaction_tensor(it, K, d, x, y, z, t);
         const double gk = 0.01 * K * sqrt(x * x + y * y + z * z);
         const double g2 = gk * gk;
         const double ph = exp(-(g2 * g2));
@@ -274,6 +248,12 @@ __global__ void k_green_expand(Geom g, const double2* __restrict__ oct, double2*
 #pragma unroll
         for (int l = 0; l < 6; l++) full6[l * M + e] = t[l];
     }
+}
+
+// the Si/Ci tables of the FCD tensor: Si(0.1 k), Ci(0.1 k), k = 1 .. kSiCiN
+__global__ void k_sici_table(double* __restrict__ si, double* __restrict__ ci) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < kSiCiN; k += gridDim.x * blockDim.x)
+        sici(kSiCiDis * (k + 1), &si[k], &ci[k]);
 }
 
 // fold the spectrum to the octant, scale by 1/M, write FP64 and FP32 copies
@@ -529,19 +509,19 @@ cudaError_t fft_cols(double2* data, int nouter, int o1, long long s1, long long 
 
 cudaError_t launch_green(const Geom& g, double K, double d, const double2* twx, const double2* twy, const double2* twz,
                          double2* full6, double2* green64, float2* green32, cudaStream_t stream,
-                         const PeriodicImages* pi, double2* oct) {
+                         const Interaction& it, const PeriodicImages* pi, double2* oct) {
     const int Mx = g.px.M, My = g.py.M, Mz = g.pz.M;
     const long long M = (long long)Mx * My * Mz;
     cudaError_t err;
     if (pi) {
-        k_green_periodic_octant<<<g.Nx * g.Ny * g.Nz, kNT, 0, stream>>>(g, K, d, *pi, oct);
+        k_green_periodic_octant<<<g.Nx * g.Ny * g.Nz, kNT, 0, stream>>>(g, K, d, *pi, it, oct);
         err = cudaGetLastError();
         if (!err) {
             k_green_expand<<<grid1d(M, kNT), kNT, 0, stream>>>(g, oct, full6);
             err = cudaGetLastError();
         }
     } else {
-        k_green_real<<<grid1d(M, kNT), kNT, 0, stream>>>(g, K, d, full6);
+        k_green_real<<<grid1d(M, kNT), kNT, 0, stream>>>(g, K, d, it, full6);
         err = cudaGetLastError();
     }
     // the six components form a (6 Mx, My, Mz) array for the z and y axes;
@@ -625,20 +605,26 @@ cudaError_t launch_residual_is_rhs(const Geom& g, int nrhs, const RhsVecs<T>* rh
     return cudaGetLastError();
 }
 
+cudaError_t launch_sici_table(double* si, double* ci, cudaStream_t stream) {
+    k_sici_table<<<grid1d(kSiCiN, 128), 128, 0, stream>>>(si, ci);
+    return cudaGetLastError();
+}
+
 int field_blocks(int N, int npts) {
     const int per_point = std::max(1, (N + kNT - 1) / kNT);
     const int fill = std::max(1, (152 * 8) / std::max(1, npts));
     return std::min(per_point, fill);
 }
 
-cudaError_t launch_field_at(int N, const int* R, double d, double K, const double2* P, int npts, const double* pts,
-                            double3 nK, double3 nE0, double E0, double2* part, double2* E, cudaStream_t stream) {
+cudaError_t launch_field_at(int N, const int* R, double d, double K, const Interaction& it, const double2* P, int npts,
+                            const double* pts, double3 nK, double3 nE0, double E0, double2* part, double2* E,
+                            cudaStream_t stream) {
     const int nb = field_blocks(N, npts);
     constexpr int kChunk = 32768;  // points per launch (gridDim.y <= 65535)
     for (int p0 = 0; p0 < npts; p0 += kChunk) {
         const int np = std::min(kChunk, npts - p0);
         double2* pp = part + 3LL * nb * p0;
-        k_field_partial<<<dim3(nb, np), kNT, 0, stream>>>(N, R, d, K, P, pts + 3LL * p0, pp);
+        k_field_partial<<<dim3(nb, np), kNT, 0, stream>>>(N, R, d, K, it, P, pts + 3LL * p0, pp);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         k_field_sum<<<grid1d(np, 128), 128, 0, stream>>>(np, nb, pp, pts + 3LL * p0, nK, nE0, E0, K, E + 3LL * p0);

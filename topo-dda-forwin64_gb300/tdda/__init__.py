@@ -38,6 +38,7 @@ METHODS = {"LDR": 0, "FCD": 1}
 # every entry point declared in include/tdda.h
 EXPORTS = [
     "tdda_abi_version", "tdda_last_error", "tdda_device_count", "tdda_core_create", "tdda_core_create_periodic",
+    "tdda_core_interaction",
     "tdda_core_destroy",
     "tdda_core_info", "tdda_aproduct", "tdda_core_ldr_inter", "tdda_model_create", "tdda_model_destroy",
     "tdda_model_update_alpha", "tdda_model_update_alpha_single", "tdda_model_change_E", "tdda_model_reset_E",
@@ -137,6 +138,7 @@ def load() -> ctypes.CDLL:
         "tdda_model_iterations": (i, [vp]),
         "tdda_model_field_at": (i, [vp, i, vp, vp, i]),
         "tdda_core_create_periodic": (i, [ctypes.POINTER(CoreDesc), i, i, d, d, ctypes.POINTER(vp)]),
+        "tdda_core_interaction": (i, [vp, d, d, d, dp]),
         "tdda_model_density_gradient": (i, [vp, i, vp, vp, i, vp, vp, vp]),
         "tdda_solve_batch": (i, [ctypes.POINTER(vp), i, i, i, d, ctypes.POINTER(SolveInfo)]),
         "tdda_fft3d": (i, [vp, i, i, i, i]),
@@ -287,6 +289,13 @@ class AProductCore:
     def LDR_inter(self, x, y, z) -> np.ndarray:
         out = np.zeros(6, np.complex128)
         _check(load().tdda_core_ldr_inter(self.h, x, y, z, _dptr(out.view(np.float64))), "tdda_core_ldr_inter")
+        a = out
+        return np.array([[a[0], a[1], a[2]], [a[1], a[3], a[4]], [a[2], a[4], a[5]]])
+
+    def A_dic_generator(self, x, y, z) -> np.ndarray:
+        """The core's interaction tensor, LDR or FCD (AProductCore.cpp:560-571), 3 x 3."""
+        out = np.zeros(6, np.complex128)
+        _check(load().tdda_core_interaction(self.h, x, y, z, _dptr(out.view(np.float64))), "tdda_core_interaction")
         a = out
         return np.array([[a[0], a[1], a[2]], [a[1], a[3], a[4]], [a[2], a[4], a[5]]])
 
