@@ -19,9 +19,14 @@
  *        appends int32 MAXm MAXn; f64 Lm Ln
  *        mode 5: A-products with the FCD tensor (AProductCore.cpp:625-695); its
  *        SiCi tables are read from the working directory (SiCi.cpp:8-25)
+ *        mode 6: a solve, then the reference's text writers into the working
+ *        directory: CoreStructure::output_to_file (CoreStructure.cpp:155-185,
+ *        both modes), DDAModel::output_to_file (DDAModel.cpp:589-697) and the
+ *        commondata.txt lines of main.cpp:282-289
  *   out: see the per-mode writers below.
  */
 #include <cstdio>
+#include <fstream>
 #include <cstdint>
 #include <iostream>
 #include <stdexcept>
@@ -164,7 +169,7 @@ int main(int argc, char** argv) {
             VectorXcd yw = Model.Aproductwithalb(b);
             put_cvec(fo, yw);
         }
-    } else {
+    } else {  // modes 1, 3, 6
         if (nvec >= 1) {
             VectorXcd P0 = to_cvec(vecs, 0, 3 * N);
             Model.InitializeP(P0);
@@ -176,6 +181,19 @@ int main(int argc, char** argv) {
         std::fwrite(&it, 4, 1, fo);
         put_cvec(fo, *Model.get_P());
         put_cvec(fo, *Model.get_Einternal());
+        if (mode == 6) {
+            CStr.output_to_file("", 7, "normal");   // CoreStructure7.txt
+            CStr.output_to_file("s", 8, "simple");  // sCoreStructure8.txt
+            Model.solve_E();                        // EResult = Einternal (DDAModel.cpp:560-562)
+            Model.output_to_file("", 3, 1);         // Model_results1it3.txt
+            std::ofstream Common("commondata.txt");  // main.cpp:282-289
+            Common << CStr.get_Nx() << std::endl << CStr.get_Ny() << std::endl << CStr.get_Nz() << std::endl
+                   << CStr.get_N() << std::endl;
+            Common << (spacepara.get_geometry()) << std::endl;
+            Common << d << std::endl;
+            Common << nE0 << std::endl;
+            Common << nK << std::endl;
+        }
         if (mode == 3) {
             // ObjDDAModel.cpp:20-96: |E| at each point from the solved P
             for (size_t p = 0; p + 2 < pts.size(); p += 3) {

@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <string>
 #include <vector>
 
 #include "../../topo-dda-forwin64_gb300/cpp/tdda.hpp"
@@ -84,6 +85,7 @@ int main(int argc, char** argv) {
     std::fwrite(TestModel.get_P()->data(), 16, TestModel.get_P()->size(), f);
     std::fwrite(TestModel.get_Einternal()->data(), 16, TestModel.get_Einternal()->size(), f);
     std::fwrite(TestModel.get_EResult()->data(), 16, TestModel.get_EResult()->size(), f);
+    TestModel.output_to_file(std::string(argv[10]) + ".", 3, 1);  // <out>.Model_results1it3.txt
     // the periodic constructor on the same structure (AProductCore.cpp:251-536): the product of
     // the solved P and one image tensor
     tdda::AProductCore PCore(&S, lam, material, 1.0, 2, 1, S.Nx * S.d, S.Ny * S.d, "LDR");

@@ -13,6 +13,9 @@ on seeded inputs.  Each fixture stores its inputs and the reference's outputs:
                    Si/Ci tables are written the way SiCi/SiCi.py writes them
   solve_*.npz      bicgstab + update_E_in_structure (DDAModel.cpp:131-260,
                    567-575): ITERATION, the printed Error, P, Einternal
+  text_*/          the reference's text files of a solved structure
+                   (CoreStructure.cpp:155-185, DDAModel.cpp:589-697,
+                   main.cpp:282-289) with text_*.npz holding what they print
   field_*.npz      a solve, then the point-field objective
                    ObjPointEDDAModel::GetVal (ObjDDAModel.cpp:20-96) at
                    off-lattice points: |E_ext(r) - sum_i A(r - d R_i) P_i|
@@ -81,7 +84,7 @@ def write_sici_tables(folder):
             f.write("\n")
 
 
-def run(mode, points=None, periodic=None, **kw):
+def run(mode, points=None, periodic=None, keep=None, **kw):
     with tempfile.TemporaryDirectory() as td:
         if mode == 5:
             write_sici_tables(td)
@@ -99,6 +102,12 @@ def run(mode, points=None, periodic=None, **kw):
         pr = subprocess.run([DRIVER, fin, fout], capture_output=True, text=True, check=True, cwd=td)
         with open(fout, "rb") as f:
             raw = f.read()
+        if keep is not None:  # copy the files the reference wrote into its working directory
+            import shutil
+            os.makedirs(keep, exist_ok=True)
+            for name in os.listdir(td):
+                if name.endswith(".txt") and "SiCi" not in name:
+                    shutil.copy(os.path.join(td, name), os.path.join(keep, name))
     return raw, pr.stdout
 
 
@@ -165,6 +174,22 @@ def gen_aprod(name, w: lattice.Workload, nvec, seed):
     np.savez_compressed(os.path.join(HERE, f"aprod_{name}.npz"), **inputs_dict(w), al=al, b=np.array(vecs),
              y=np.array(ys), y_alb=np.array(yws))
     print(f"aprod_{name}: N={N} |y|={np.linalg.norm(ys[0]):.6g}")
+
+
+def gen_text(name, w: lattice.Workload):
+    N = w.N
+    folder = os.path.join(HERE, f"text_{name}")
+    raw, _ = run(6, keep=folder, **case_kw(w), vecs=[])
+    off = 12 * N + 48 * N
+    it = struct.unpack_from("<i", raw, off)[0]
+    off += 4
+    P = np.frombuffer(raw, "<c16", count=3 * N, offset=off)
+    off += 48 * N
+    Ein = np.frombuffer(raw, "<c16", count=3 * N, offset=off)
+    inc = w.incidences[0]
+    np.savez_compressed(os.path.join(HERE, f"text_{name}.npz"), box=np.array([w.Nx, w.Ny, w.Nz], np.int32),
+                        R=w.R, diel_old=w.diel_old, d=w.d, nK=inc.nK, nE0=inc.nE0, P=P, Einternal=Ein)
+    print(f"text_{name}: N={N} files={sorted(os.listdir(folder))}")
 
 
 def gen_aprod_fcd(name, w: lattice.Workload, nvec, seed):
@@ -274,6 +299,9 @@ def main():
     gen_aprod_fcd("box6x5x4", small_workload("box6x5x4", 6, 5, 4, 11), 1, 800)
     gen_aprod_fcd("sparse7x6x4", small_workload("sparse7x6x4", 7, 6, 4, 18, em=2.25 + 0.0j, lam=620.0, keep=0.6,
                                                   shuffle=True), 1, 900)
+    # the reference's text files of a small solved structure (densities with many digits, a
+    # shuffled sparse lattice)
+    gen_text("sparse4x3x2", small_workload("sparse4x3x2", 4, 3, 2, 19, keep=0.8, shuffle=True))
     # the point field of the solved cfg 1 structure: above the centre (the topology objective's
     # point), beside, below, far off, and inside the box between lattice sites
     gen_field("cfg1", lattice.config(1), [[95.0, 95.0, 190.0], [-50.0, 95.0, 45.0], [95.0, 95.0, -80.0],

@@ -64,6 +64,10 @@ def test_mirror_solve_matches_oracle(tmp_path, precision, tol, bound):
     assert rel(P, om.P) <= bound
     assert rel(Ein, om.Einternal) <= bound
     assert rel(EResult, om.field_at(d * RResult).ravel()) <= bound
+    # DDAModel::output_to_file: the same bytes as the reference's writer (tdda.io, pinned to it)
+    ref_txt = str(tmp_path / "ref.txt")
+    tdda.io.write_model_results(ref_txt, EResult, P)
+    assert open(out + ".Model_results1it3.txt", "rb").read() == open(ref_txt, "rb").read()
     # periodic core (MAXm 2, MAXn 1, periods of the box): the product of the solved P, and the
     # image tensor A_dic_generator(10, 20, 5, m=1, n=-1)
     off = 4 + 96 * N + 12 * 16

@@ -32,6 +32,7 @@
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <fstream>
 #include <functional>
 #include <iostream>
 #include <stdexcept>
@@ -200,6 +201,8 @@ template <class VectorXcd = std::vector<cplx>> class DDAModelT {
         P_ = VectorXcd(n3_);
         Einternal_ = VectorXcd(n3_);
         al_ = VectorXcd(n3_);
+        EResult_ = VectorXcd(n3_);  // VectorXcd::Zero(N*3) until solve_E (DDAModel.cpp:46)
+        for (size_t i = 0; i < n3_; i++) EResult_[i] = cplx(0.0, 0.0);
         fetch(TDDA_FIELD_AL, al_);
     }
     // DDAModel(AProductCore*, Vector3d n_K, double E0, Vector3d n_E0, VectorXi* RResult,
@@ -263,6 +266,20 @@ template <class VectorXcd = std::vector<cplx>> class DDAModelT {
     }
     VectorXcd* get_EResult() { return &EResult_; }
 
+    // DDAModel::output_to_file(string save_position, int iteration, int ModelLabel)   DDAModel.cpp:618-656:
+    // EResult then P, one "re+imj" / "re-imj" per line
+    void output_to_file(const std::string& save_position, int iteration, int ModelLabel) {
+        std::ofstream fout(save_position + "Model_results" + std::to_string(ModelLabel) + "it" +
+                           std::to_string(iteration) + ".txt");
+        write_complex(fout, EResult_);
+        write_complex(fout, P_);
+    }
+    // DDAModel::output_to_file(string save_position, int iteration)   DDAModel.cpp:658-697: EResult only
+    void output_to_file(const std::string& save_position, int iteration) {
+        std::ofstream fout(save_position + "Model_results" + "it" + std::to_string(iteration) + ".txt");
+        write_complex(fout, EResult_);
+    }
+
     VectorXcd* get_P() { return &P_; }
     VectorXcd* get_Einternal() { return &Einternal_; }
     VectorXcd* get_al() { return &al_; }
@@ -276,6 +293,14 @@ template <class VectorXcd = std::vector<cplx>> class DDAModelT {
    private:
     std::vector<double> rresult_;  // d * RResult, nm
     VectorXcd EResult_;
+    static void write_complex(std::ostream& f, const VectorXcd& v) {
+        for (size_t i = 0; i < (size_t)v.size(); i++) {
+            if (v[i].imag() < 0)
+                f << v[i].real() << v[i].imag() << "j" << std::endl;
+            else
+                f << v[i].real() << "+" << v[i].imag() << "j" << std::endl;
+        }
+    }
     void fetch(int field, VectorXcd& out) {
         check(tdda_model_get(h_, field, dptr(out), TDDA_MEM_HOST), "DDAModel get");
     }
