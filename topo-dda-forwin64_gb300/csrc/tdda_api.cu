@@ -361,32 +361,53 @@ template <> struct Prec<float> {
 template <typename T> int product_kernels(const tdda_core* c) { return tdda::zy_fused(c->g, sizeof(T) == 4) ? 3 : 5; }
 
 template <typename T>
-cudaError_t aprod(tdda_core* c, int src, int snk, int n, const RhsVecs<T>* rhs, cudaEvent_t* ev = nullptr) {
+cudaError_t aprod(tdda_core* c, int src, int snk, int n, const RhsVecs<T>* rhs, cudaEvent_t* ev = nullptr,
+                  int slot = 0) {
     count_launches(product_kernels<T>(c));
     return tdda::launch_aproduct<T>(c->g, src, snk, n, rhs, Prec<T>::green(c), Prec<T>::tw(c, 0), Prec<T>::tw(c, 1),
-                                    Prec<T>::tw(c, 2), c->cellmap, Prec<T>::grid(c), c->stream, ev);
+                                    Prec<T>::tw(c, 2), c->cellmap, Prec<T>::grid(c), c->stream, ev, slot);
 }
 
 // One BiCGSTAB step.  FP64 (the drop-in): the reference's recurrence with its
 // three reductions, the update of P and r in k_update.  FP32 (the inner solve
 // of the mixed form): the update is deferred into the next step's gather and
 // r0.r, |r|^2 follow from sums taken with At (SNK_AT_DEF), so a step is two
-// products and no separate update kernel.
+// products and no separate update kernel.  The FP32 sink passes only publish
+// block partials; the next gather forms alpha, or the end of the previous step
+// (zeta, r0.r, convergence, beta), in every block, and its block 0 records
+// them in the state slots of the step's parity `slot`.
 template <typename T> constexpr bool kDeferred = sizeof(T) == 4;
 
 template <typename T> int step_kernels(const tdda_core* c) { return 2 * product_kernels<T>(c) + (kDeferred<T> ? 0 : 1); }
 
-template <typename T> cudaError_t enqueue_iteration(tdda_core* c, int n) {
+template <typename T> cudaError_t enqueue_iteration(tdda_core* c, int n, int slot) {
     const RhsVecs<T>* rhs = Prec<T>::rhs(c);
     cudaError_t e;
-    if (kDeferred<T>) {
-        if ((e = aprod<T>(c, tdda::SRC_PUPD_DEF, tdda::SNK_AP, n, rhs))) return e;  // update, p, Ap, alpha
-        return aprod<T>(c, tdda::SRC_TUPD, tdda::SNK_AT_DEF, n, rhs);              // t, At, zeta, rho, beta
+    if constexpr (kDeferred<T>) {
+        // update, p, Ap
+        if ((e = aprod<T>(c, tdda::SRC_PUPD_DEF, tdda::SNK_AP, n, rhs, nullptr, slot))) return e;
+        return aprod<T>(c, tdda::SRC_TUPD, tdda::SNK_AT_DEF, n, rhs, nullptr, slot);  // alpha, t, At
+    } else {
+        if ((e = aprod<T>(c, tdda::SRC_PUPD, tdda::SNK_AP, n, rhs))) return e;  // p, Ap, alpha
+        if ((e = aprod<T>(c, tdda::SRC_TUPD, tdda::SNK_AT, n, rhs))) return e;  // t, At, zeta
+        count_launches(1);
+        return tdda::launch_update<T>(c->g, n, rhs, 0, c->stream);  // u, P, r, rho, beta
     }
-    if ((e = aprod<T>(c, tdda::SRC_PUPD, tdda::SNK_AP, n, rhs))) return e;  // p, Ap, alpha
-    if ((e = aprod<T>(c, tdda::SRC_TUPD, tdda::SNK_AT, n, rhs))) return e;  // t, At, zeta
-    count_launches(1);
-    return tdda::launch_update<T>(c->g, n, rhs, 0, c->stream);              // u, P, r, rho, beta
+}
+
+// kChunk steps (parities 0, 1, 0, 1 ...); FP32 ends the chunk with the step
+// end for the next step (parity 0), so the state the host polls is current
+template <typename T> cudaError_t enqueue_chunk(tdda_core* c, int n) {
+    for (int k = 0; k < kChunk; k++) {
+        count_launches(step_kernels<T>(c));
+        cudaError_t e = enqueue_iteration<T>(c, n, k & 1);
+        if (e != cudaSuccess) return e;
+    }
+    if constexpr (kDeferred<T>) {
+        count_launches(1);
+        return tdda::launch_step_end(c->g, n, Prec<T>::rhs(c), 0, c->stream);
+    }
+    return cudaSuccess;
 }
 
 template <typename T> tdda_status get_iteration_graph(tdda_core* c, int n, cudaGraphExec_t* out) {
@@ -395,10 +416,10 @@ template <typename T> tdda_status get_iteration_graph(tdda_core* c, int n, cudaG
         cudaGraph_t gr = nullptr;
         TDDA_CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         t_capturing = true;
-        cudaError_t e = enqueue_iteration<T>(c, n);
+        cudaError_t e = enqueue_chunk<T>(c, n);
         t_capturing = false;
         cudaError_t e2 = cudaStreamEndCapture(c->stream, &gr);
-        if (e != cudaSuccess) return cuda_fail(e, "capture of one BiCGSTAB iteration");
+        if (e != cudaSuccess) return cuda_fail(e, "capture of the BiCGSTAB steps");
         if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
         e = cudaGraphInstantiate(&ex, gr, 0);
         cudaGraphDestroy(gr);
@@ -418,10 +439,11 @@ template <typename T> tdda_status krylov(tdda_core* c, int n, bool p_zero, int m
         TDDA_CK1(tdda::launch_solve_begin<T>(c->g, n, rhs, c->stream));
         TDDA_CK(aprod<T>(c, tdda::SRC_P, tdda::SNK_RES, n, rhs));  // r = r0 = p = E - A P
     }
-    TDDA_CK(aprod<T>(c, tdda::SRC_IN, tdda::SNK_AP, n, rhs));    // Ap0, alpha
-    if (kDeferred<T>) {
-        TDDA_CK(aprod<T>(c, tdda::SRC_TUPD, tdda::SNK_AT_DEF, n, rhs));  // t, At0, zeta, rho, beta
+    if (kDeferred<T>) {  // the initial products are step -1 (parity 1)
+        TDDA_CK(aprod<T>(c, tdda::SRC_IN, tdda::SNK_AP, n, rhs, nullptr, 1));     // Ap0
+        TDDA_CK(aprod<T>(c, tdda::SRC_TUPD, tdda::SNK_AT_DEF, n, rhs, nullptr, 1));  // alpha, t, At0
     } else {
+        TDDA_CK(aprod<T>(c, tdda::SRC_IN, tdda::SNK_AP, n, rhs));  // Ap0, alpha
         TDDA_CK(aprod<T>(c, tdda::SRC_TUPD, tdda::SNK_AT, n, rhs));  // t, At0, zeta
         TDDA_CK1(tdda::launch_update<T>(c->g, n, rhs, 1, c->stream));
     }
@@ -434,10 +456,8 @@ template <typename T> tdda_status krylov(tdda_core* c, int n, bool p_zero, int m
         bool running = false;
         for (int i = 0; i < n; i++) running |= c->hst[i].status == tdda::ST_RUNNING;
         if (!running || done_it > max_it) break;
-        for (int k = 0; k < kChunk; k++) {
-            count_launches(step_kernels<T>(c));
-            TDDA_CK(cudaGraphLaunch(ex, c->stream));
-        }
+        count_launches(kChunk * step_kernels<T>(c) + (kDeferred<T> ? 1 : 0));
+        TDDA_CK(cudaGraphLaunch(ex, c->stream));
         done_it += kChunk;
     }
     if (kDeferred<T>) TDDA_CK1(tdda::launch_finish<T>(c->g, n, rhs, c->stream));  // the last step's update
@@ -463,6 +483,8 @@ SolveState fresh_state(double tol, int max_it, int iterations) {
     s.status = tdda::ST_RUNNING;
     s.init = 1;
     s.tol32 = (float)tol;
+    s.init32[1] = 1;  // the FP32 initial products are step -1 (slot 1)
+    s.last_slot = -1;
     return s;
 }
 

@@ -302,67 +302,110 @@ __device__ __forceinline__ float2 fdiv2(float2 a, float2 b) {
     return make_float2((a.x * r + a.y) / den, (a.y * r - a.x) / den);
 }
 
-// finish_step for the FP32 state
-__device__ __forceinline__ void finish_step_f32(SolveState* st, float2 rho, float rn2, bool is_init) {
-    st->rho_prev32 = st->rho32;
-    st->rho32 = rho;
-    const float err = sqrtf(rn2) / st->Enorm32;
-    if (!is_init) {
-        st->it += 1;
-        if (err <= st->tol32) {  // DDAModel.cpp:232-235
-            st->status = ST_CONVERGED;
-            st->iterations = st->it;
-            st->error = err;
-            return;
-        }
-    }
-    if (st->it >= st->max_it) {
-        st->status = ST_MAXITER;
-        st->error = err;
-        return;
-    }
-    if (st->rho_prev32.x == 0.f && st->rho_prev32.y == 0.f) {  // DDAModel.cpp:193-215
-        st->status = ST_BREAKDOWN;
-        st->iterations = st->it + 1;
-        st->error = err;
-        return;
-    }
-    const float2 beta = fdiv2(fmul2(fdiv2(st->alpha32, st->zeta32), rho), st->rho_prev32);  // DDAModel.cpp:218
-    st->beta32 = beta;
-    if (!isfinite(rho.x) || !isfinite(rho.y) || !isfinite(err) || !isfinite(beta.x) || !isfinite(beta.y)) {
-        st->status = ST_NAN;
-        st->error = err;
+// ---- the FP32 deferred step, formed by the consuming kernels ---------------
+// The sink passes of an FP32 step only publish block partials (publish_partials).
+// Every block of the next gather sums them (sum_partials) and forms the step
+// scalars itself; block 0 records them in the state slot of the step.
+
+// Block partials as double-float pairs into part slots k * nblk + bid (thread 0).
+template <int NV>
+__device__ __forceinline__ void publish_partials(float (&v)[NV], double* part, int nblk, int bid, double* sred) {
+    float2 a[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++) a[k] = make_float2(v[k], 0.f);
+    block_sum<NV>(a, reinterpret_cast<float2*>(sred));
+    if (threadIdx.x == 0) {
+        float2* part2 = reinterpret_cast<float2*>(part);
+#pragma unroll
+        for (int k = 0; k < NV; k++) part2[k * nblk + bid] = a[k];
     }
 }
 
-// The deferred step end (SNK_AT_DEF) on FP32 state: zeta = At.t / At.At in
-// FP32 (the value the update applies), then for r = t - zeta At
-// r0.r = r0.t - zeta r0.At and |r|^2 = t.t - 2 Re(conj(zeta) At.t) + |zeta|^2 At.At
-// as FP64 multiply-adds on the double-float totals: these differences cancel
-// as r becomes small next to t, and no FP64 division or root is needed.
+// The totals of nblk published partials, in block order (every thread).  sred:
+// 32 * NV float2 of shared scratch.
+template <int NV>
+__device__ __forceinline__ void sum_partials(const double* part, int nblk, float2* sred, float2 (&tot)[NV]) {
+    const float2* part2 = reinterpret_cast<const float2*>(part);
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        float2 q = make_float2(0.f, 0.f);
+        for (int i = threadIdx.x; i < nblk; i += blockDim.x) q = df_add(q, __ldcg(part2 + k * nblk + i));
+        tot[k] = q;
+    }
+    block_sum<NV>(tot, sred);
+}
+
+// The end of step k - 1 as seen by step k (parity p): zeta = At.t / At.At in
+// FP32; r0.r and |r|^2 of r = t - zeta At as FP64 multiply-adds on the
+// double-float totals (they cancel as r gets small next to t); then the
+// logic of DDAModel.cpp:218-255: convergence (not after the initial
+// products), the iteration limit, breakdown on r0.rl = 0, beta.
+struct StepEnd {
+    float2 zeta, rho, beta;
+    float err;
+    int it, stop, set_iterations, iterations;
+};
 __device__ __forceinline__ double df_d(float2 a) { return (double)a.x + (double)a.y; }
-__device__ __forceinline__ void finish_step_deferred_f32(SolveState* st, const float2 (&tot)[8]) {
-    const float2 zeta = fdiv2(make_float2(tot[0].x, tot[1].x), make_float2(tot[2].x, 0.f));  // DDAModel.cpp:225
-    st->zeta32 = zeta;
-    const double zx = zeta.x, zy = zeta.y;
+__device__ __forceinline__ StepEnd step_end_f32(const SolveState* st, const float2 (&tot)[8], int p) {
+    const int q = p ^ 1;
+    StepEnd e;
+    e.zeta = fdiv2(make_float2(tot[0].x, tot[1].x), make_float2(tot[2].x, 0.f));  // DDAModel.cpp:225
+    const double zx = e.zeta.x, zy = e.zeta.y;
     const double ax = df_d(tot[0]), ay = df_d(tot[1]), bb = df_d(tot[2]);
     const double tx = df_d(tot[3]), ty = df_d(tot[4]), ux = df_d(tot[5]), uy = df_d(tot[6]), cc = df_d(tot[7]);
-    const float2 rho = make_float2((float)(tx - (zx * ux - zy * uy)), (float)(ty - (zx * uy + zy * ux)));
+    e.rho = make_float2((float)(tx - (zx * ux - zy * uy)), (float)(ty - (zx * uy + zy * ux)));
     double rn2 = cc - 2.0 * (zx * ax + zy * ay) + (zx * zx + zy * zy) * bb;
     if (!(rn2 > 0.0)) rn2 = isnan(rn2) ? rn2 : 0.0;
-    const bool init = st->init != 0;
-    st->init = 0;
-    st->pending = 1;
-    finish_step_f32(st, rho, (float)rn2, init);
+    e.err = sqrtf((float)rn2) / st->Enorm32;
+    const bool init = st->init32[q] != 0;
+    e.it = st->it32[q] + (init ? 0 : 1);
+    e.stop = ST_RUNNING;
+    e.set_iterations = 0;
+    e.iterations = 0;
+    e.beta = make_float2(0.f, 0.f);
+    const float2 rho_prev = st->rho32[q];
+    if (!init && e.err <= st->tol32) {  // DDAModel.cpp:232-235
+        e.stop = ST_CONVERGED;
+        e.set_iterations = 1;
+        e.iterations = e.it;
+    } else if (e.it >= st->max_it) {  // the loop of DDAModel.cpp:186 ends
+        e.stop = ST_MAXITER;
+    } else if (rho_prev.x == 0.f && rho_prev.y == 0.f) {  // DDAModel.cpp:193-215
+        e.stop = ST_BREAKDOWN;
+        e.set_iterations = 1;
+        e.iterations = e.it + 1;
+    } else {
+        // beta = (alpha / zeta) * (r0 . r) / (r0 . rl)      DDAModel.cpp:218
+        e.beta = fdiv2(fmul2(fdiv2(st->alpha32[q], e.zeta), e.rho), rho_prev);
+        if (!isfinite(e.rho.x) || !isfinite(e.rho.y) || !isfinite(e.err) || !isfinite(e.beta.x) ||
+            !isfinite(e.beta.y))
+            e.stop = ST_NAN;
+    }
+    return e;
+}
+// records step_end_f32's result (one thread of one block)
+__device__ __forceinline__ void write_step_end(SolveState* st, const StepEnd& e, int p) {
+    const int q = p ^ 1;
+    st->zeta32[q] = e.zeta;
+    st->rho32[p] = e.rho;
+    st->beta32[p] = e.beta;
+    st->it32[p] = e.it;
+    st->init32[p] = 0;
+    st->it = e.it;
+    if (e.stop != ST_RUNNING) {
+        st->status = e.stop;
+        st->error = e.err;
+        st->last_slot = q;
+        if (e.set_iterations) st->iterations = e.iterations;
+    }
 }
 
 // The scalars a sink pass forms from its grid totals (thread 0 of the last block).
 template <typename T, int SNK, int NV> __device__ __forceinline__ void finalize_sink(SolveState* st, const tot_t<T> (&tot)[NV]) {
     if constexpr (sizeof(T) == 4) {
-        if constexpr (SNK == SNK_RES) st->rho32 = make_float2(tot[0].x, 0.f);
-        else if constexpr (SNK == SNK_AT_DEF) finish_step_deferred_f32(st, tot);
-        else if constexpr (SNK == SNK_AP) st->alpha32 = fdiv2(st->rho32, make_float2(tot[0].x, tot[1].x));
-        else if constexpr (SNK == SNK_AT) st->zeta32 = fdiv2(make_float2(tot[0].x, tot[1].x), make_float2(tot[2].x, 0.f));
+        // the FP32 step forms its scalars in the consuming kernels; the initial
+        // residual r0.r seeds slot 1 (the initial products are step -1)
+        if constexpr (SNK == SNK_RES) st->rho32[1] = make_float2(tot[0].x, 0.f);
     } else {
         if constexpr (SNK == SNK_RES) {
             st->rho = make_double2(tot[0], 0.0);  // r0 . r with r0 = r
@@ -378,14 +421,14 @@ template <typename T, int SNK, int NV> __device__ __forceinline__ void finalize_
 }
 
 // step scalars as the kernels of precision T use them
-template <typename T> __device__ __forceinline__ cx<T> st_alpha(const SolveState* s) {
-    if constexpr (sizeof(T) == 4) return s->alpha32; else return s->alpha;
+template <typename T> __device__ __forceinline__ cx<T> st_alpha(const SolveState* s, int slot = 0) {
+    if constexpr (sizeof(T) == 4) return s->alpha32[slot]; else return s->alpha;
 }
-template <typename T> __device__ __forceinline__ cx<T> st_beta(const SolveState* s) {
-    if constexpr (sizeof(T) == 4) return s->beta32; else return s->beta;
+template <typename T> __device__ __forceinline__ cx<T> st_beta(const SolveState* s, int slot = 0) {
+    if constexpr (sizeof(T) == 4) return s->beta32[slot]; else return s->beta;
 }
-template <typename T> __device__ __forceinline__ cx<T> st_zeta(const SolveState* s) {
-    if constexpr (sizeof(T) == 4) return s->zeta32; else return s->zeta;
+template <typename T> __device__ __forceinline__ cx<T> st_zeta(const SolveState* s, int slot = 0) {
+    if constexpr (sizeof(T) == 4) return s->zeta32[slot]; else return s->zeta;
 }
 
 __device__ __forceinline__ bool rhs_done(const SolveState* st) {

@@ -45,10 +45,15 @@ struct SolveState {
     int max_it;
     int iterations;    // ITERATION as the reference reports it
     int init;          // the next step finalisation is the initial one (no convergence check)
-    int pending;       // deferred update of P and r not yet applied (FP32 inner solve)
+    int pending;       // deferred update of P and r not yet applied (FP64 deferred form)
     // The FP32 inner solve keeps its step scalars in FP32 (its kernels use
-    // them so): no FP64 conversion or arithmetic on its critical path.
-    float2 alpha32, beta32, zeta32, rho32, rho_prev32;
+    // them so), in two slots: step k (parity p = k & 1) reads the slots q = p ^ 1
+    // of step k - 1 and writes slot p, so no kernel reads a field one of its own
+    // blocks writes (the scalars are formed by the consuming kernels).
+    float2 alpha32[2], beta32[2], zeta32[2], rho32[2];
+    int it32[2];       // completed steps after step k
+    int init32[2];     // slot q of the first step: the initial products (no convergence check)
+    int last_slot;     // slot of the step whose update is pending when the solve stopped, or -1
     float Enorm32, tol32;
 };
 
@@ -109,6 +114,8 @@ template <typename T> struct PassArgs {
     const int* cellmap;
     cx<T>* grid;
     cudaStream_t stream;
+    int slot;       // FP32 deferred step: parity of the step (state slots)
+    int prod_nblk;  // FP32 deferred step: blocks of the sink pass whose partials this gather reads
 };
 // mode: SrcMode for PASS_ZFWD, SnkMode for PASS_ZINV, unused otherwise
 template <typename T> cudaError_t pass_generic(int pass, int mode, const PassArgs<T>& a);
@@ -158,7 +165,15 @@ cudaError_t launch_sici_table(double* si, double* ci, cudaStream_t stream);
 template <typename T>
 cudaError_t launch_aproduct(const Geom& g, int src, int snk, int nrhs, const RhsVecs<T>* rhs,
                             const cx<T>* green, const cx<T>* twx, const cx<T>* twy, const cx<T>* twz,
-                            const int* cellmap, cx<T>* grid, cudaStream_t stream, cudaEvent_t* ev = nullptr);
+                            const int* cellmap, cx<T>* grid, cudaStream_t stream, cudaEvent_t* ev = nullptr,
+                            int slot = 0);
+// blocks of the last pass of an A-product at precision T (the producer of the
+// dot-product partials)
+template <typename T> int sink_blocks(const Geom& g);
+// FP32 deferred step: the step end formed from the At-pass partials for the
+// step of parity `slot` (the same computation as the next gather's prologue),
+// one block per right-hand side; keeps the host's status reads current.
+cudaError_t launch_step_end(const Geom& g, int nrhs, const RhsVecs<float>* rhs, int slot, cudaStream_t stream);
 
 // u = zeta Ap; z = zeta r - alpha u; P += alpha p + z; r = t - zeta At;
 // rho_prev = rho; rho = r0.r; convergence / breakdown / iteration limit;

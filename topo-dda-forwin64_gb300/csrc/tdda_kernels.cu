@@ -33,6 +33,7 @@ using namespace dev;
 // ================================================================ K6 update
 template <typename T>
 __global__ void __launch_bounds__(kNT) k_update(int n3, const RhsVecs<T>* __restrict__ rhs, int is_init) {
+    static_assert(sizeof(T) == 8, "the FP32 step is the deferred form");
     __shared__ double sred[sred_size<T, 4>()];
     const int b = blockIdx.y;
     const RhsVecs<T> R = rhs[b];
@@ -56,8 +57,7 @@ __global__ void __launch_bounds__(kNT) k_update(int n3, const RhsVecs<T>* __rest
     tot_t<T> tot[4];
     if (!last_block_total<4>(acc, R.part, gridDim.x, blockIdx.x, R.cnt + 3, sred, tot)) return;
     if (threadIdx.x != 0) return;
-    if constexpr (sizeof(T) == 4) finish_step_f32(R.st, make_float2(tot[0].x, tot[1].x), tot[2].x, is_init != 0);
-    else finish_step(R.st, make_double2(tot[0], tot[1]), tot[2], is_init != 0);
+    finish_step(R.st, make_double2(tot[0], tot[1]), tot[2], is_init != 0);
 }
 
 // The deferred update of the last step (SNK_AT_DEF) for every right-hand side
@@ -65,8 +65,18 @@ __global__ void __launch_bounds__(kNT) k_update(int n3, const RhsVecs<T>* __rest
 // r = t - zeta At.
 template <typename T> __global__ void __launch_bounds__(kNT) k_finish(int n3, const RhsVecs<T>* __restrict__ rhs) {
     const RhsVecs<T> R = rhs[blockIdx.y];
-    if (R.st == nullptr || !R.st->pending) return;
-    const cx<T> alpha = st_alpha<T>(R.st), zeta = st_zeta<T>(R.st);
+    if (R.st == nullptr) return;
+    cx<T> alpha, zeta;
+    if constexpr (sizeof(T) == 4) {
+        const int q = R.st->last_slot;  // the step whose update is pending
+        if (q < 0) return;
+        alpha = R.st->alpha32[q];
+        zeta = R.st->zeta32[q];
+    } else {
+        if (!R.st->pending) return;
+        alpha = R.st->alpha;
+        zeta = R.st->zeta;
+    }
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x) {
         const cx<T> u = cmul<T>(zeta, R.Ap[e]);
         const cx<T> r = R.r[e];
@@ -98,7 +108,7 @@ __global__ void __launch_bounds__(kNT) k_solve_begin(int n3, const RhsVecs<T>* _
     if (threadIdx.x != 0) return;
     if constexpr (sizeof(T) == 4) {
         R.st->Enorm32 = sqrtf(tot[0].x);
-        if (resid_is_rhs) R.st->rho32 = make_float2(tot[0].x, 0.f);
+        if (resid_is_rhs) R.st->rho32[1] = make_float2(tot[0].x, 0.f);  // r0.r of the initial products (step -1)
     } else {
         R.st->Enorm = sqrt(tot[0]);
         if (resid_is_rhs) {
@@ -106,6 +116,18 @@ __global__ void __launch_bounds__(kNT) k_solve_begin(int n3, const RhsVecs<T>* _
             R.st->rnorm2 = tot[0];
         }
     }
+}
+
+// The end of the FP32 step before a step of parity `slot`, from the At-pass
+// partials: the computation every block of the next gather repeats, here by
+// one block per right-hand side so that the state the host reads is current.
+__global__ void __launch_bounds__(kNT) k_step_end(const RhsVecs<float>* __restrict__ rhs, int slot, int prod_nblk) {
+    __shared__ float2 sred[32 * 8];
+    const RhsVecs<float> R = rhs[blockIdx.x];
+    if (rhs_done(R.st)) return;
+    float2 tot[8];
+    sum_partials<8>(R.part, prod_nblk, sred, tot);
+    if (threadIdx.x == 0) write_step_end(R.st, step_end_f32(R.st, tot, slot), slot);
 }
 
 // ================================================================ K0 green
@@ -548,8 +570,8 @@ cudaError_t launch_fft3d_f64(double2* data, const AxisPlan& p0, const AxisPlan& 
 template <typename T>
 cudaError_t launch_aproduct(const Geom& g, int src, int snk, int nrhs, const RhsVecs<T>* rhs, const cx<T>* green,
                             const cx<T>* twx, const cx<T>* twy, const cx<T>* twz, const int* cellmap, cx<T>* grid,
-                            cudaStream_t stream, cudaEvent_t* ev) {
-    const PassArgs<T> a{g, nrhs, rhs, green, twx, twy, twz, cellmap, grid, stream};
+                            cudaStream_t stream, cudaEvent_t* ev, int slot) {
+    const PassArgs<T> a{g, nrhs, rhs, green, twx, twy, twz, cellmap, grid, stream, slot, sink_blocks<T>(g)};
     if (zy_fused(g, sizeof(T) == 4)) {
         cudaError_t err = cudaSuccess;
         if (ev) cudaEventRecord(ev[0], stream);
@@ -575,6 +597,17 @@ cudaError_t launch_aproduct(const Geom& g, int src, int snk, int nrhs, const Rhs
     }
     if (ev) cudaEventRecord(ev[5], stream);
     return cudaSuccess;
+}
+
+template <typename T> int sink_blocks(const Geom& g) {
+    if (zy_fused(g, sizeof(T) == 4)) return 3 * g.Nx;  // one block per (x plane, component)
+    const int lz = z_lines<T>(g.pz.M);
+    return (g.Nx * g.Ny + lz - 1) / lz;
+}
+
+cudaError_t launch_step_end(const Geom& g, int nrhs, const RhsVecs<float>* rhs, int slot, cudaStream_t stream) {
+    k_step_end<<<nrhs, kNT, 0, stream>>>(rhs, slot, sink_blocks<float>(g));
+    return cudaGetLastError();
 }
 
 template <typename T>
@@ -671,8 +704,8 @@ template <typename T> cudaError_t launch_zero(long long n, cx<T>* v, cudaStream_
 #define TDDA_INST(T)                                                                                               \
     template cudaError_t launch_aproduct<T>(const Geom&, int, int, int, const RhsVecs<T>*, const cx<T>*,          \
                                             const cx<T>*, const cx<T>*, const cx<T>*, const int*, cx<T>*,         \
-                                            cudaStream_t, cudaEvent_t*);                                           \
-    template cudaError_t launch_update<T>(const Geom&, int, const RhsVecs<T>*, int, cudaStream_t);                 \
+                                            cudaStream_t, cudaEvent_t*, int);                                      \
+    template int sink_blocks<T>(const Geom&);                                                                      \
     template cudaError_t launch_finish<T>(const Geom&, int, const RhsVecs<T>*, cudaStream_t);                      \
     template cudaError_t launch_solve_begin<T>(const Geom&, int, const RhsVecs<T>*, cudaStream_t);                 \
     template cudaError_t launch_residual_is_rhs<T>(const Geom&, int, const RhsVecs<T>*, cudaStream_t);             \
@@ -680,5 +713,6 @@ template <typename T> cudaError_t launch_zero(long long n, cx<T>* v, cudaStream_
 TDDA_INST(float)
 TDDA_INST(double)
 #undef TDDA_INST
+template cudaError_t launch_update<double>(const Geom&, int, const RhsVecs<double>*, int, cudaStream_t);
 
 }  // namespace tdda

@@ -33,12 +33,54 @@ __device__ __forceinline__ cx<T> deferred_step(const RhsVecs<T>& R, long long o,
     return pn;
 }
 
+// The FP32 step's scalars in a gather pass (SRC_PUPD_DEF: the end of the
+// previous step from the At partials; SRC_TUPD: alpha from the Ap partials),
+// formed by every block from the partials the previous sink pass published;
+// block 0 records them.  scratch: 32 * 8 float2 of shared memory that is free
+// until the gather.  Returns false when the step ends the solve.
+template <int SRC>
+__device__ __forceinline__ bool fp32_step_scalars(const RhsVecs<float>& R, int slot, int prod_nblk, float2* scratch,
+                                                  float2& alpha, float2& beta, float2& zeta) {
+    __shared__ float2 s_sc[3];
+    __shared__ int s_stop;
+    if constexpr (SRC == SRC_PUPD_DEF) {
+        float2 tot[8];
+        sum_partials<8>(R.part, prod_nblk, scratch, tot);
+        if (threadIdx.x == 0) {
+            const StepEnd e = step_end_f32(R.st, tot, slot);
+            if (blockIdx.x == 0) write_step_end(R.st, e, slot);
+            s_sc[0] = e.zeta;
+            s_sc[1] = e.beta;
+            s_sc[2] = R.st->alpha32[slot ^ 1];
+            s_stop = e.stop;
+        }
+        __syncthreads();
+        if (s_stop != ST_RUNNING) return false;
+        zeta = s_sc[0];
+        beta = s_sc[1];
+        alpha = s_sc[2];
+    } else {
+        float2 tot[2];
+        sum_partials<2>(R.part, prod_nblk, scratch, tot);
+        if (threadIdx.x == 0) {
+            const float2 a = fdiv2(R.st->rho32[slot], make_float2(tot[0].x, tot[1].x));  // DDAModel.cpp:221
+            if (blockIdx.x == 0) R.st->alpha32[slot] = a;
+            s_sc[0] = a;
+        }
+        __syncthreads();
+        alpha = s_sc[0];
+    }
+    return true;
+}
+
 // ------------------------------------------------------------ K1 zfwd
 template <typename T, int SRC, int CM>
 __global__ void __launch_bounds__(kNT) k_zfwd(Geom g, const RhsVecs<T>* __restrict__ rhs,
                                               const cx<T>* __restrict__ twz, const int* __restrict__ cellmap,
-                                              cx<T>* __restrict__ grid) {
+                                              cx<T>* __restrict__ grid, int slot, int prod_nblk) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr bool kStep32 = sizeof(T) == 4 && (SRC == SRC_PUPD_DEF || SRC == SRC_TUPD);
+    __shared__ double s_scratch[kStep32 ? 32 * 8 : 1];
     const int b = blockIdx.y;
     const RhsVecs<T> R = rhs[b];
     if (rhs_done(R.st)) return;
@@ -55,9 +97,14 @@ __global__ void __launch_bounds__(kNT) k_zfwd(Geom g, const RhsVecs<T>* __restri
     const int nl = min(LZ, nlines - l0);
 
     cx<T> beta, alpha, zeta;
-    if (SRC == SRC_PUPD || SRC == SRC_PUPD_DEF) beta = st_beta<T>(R.st);
-    if (SRC == SRC_TUPD || SRC == SRC_PUPD_DEF) alpha = st_alpha<T>(R.st);
-    if (SRC == SRC_PUPD_DEF) zeta = st_zeta<T>(R.st);
+    if constexpr (kStep32) {
+        if (!fp32_step_scalars<SRC>(R, slot, prod_nblk, reinterpret_cast<float2*>(s_scratch), alpha, beta, zeta))
+            return;
+    } else {
+        if (SRC == SRC_PUPD || SRC == SRC_PUPD_DEF) beta = st_beta<T>(R.st);
+        if (SRC == SRC_TUPD || SRC == SRC_PUPD_DEF) alpha = st_alpha<T>(R.st);
+        if (SRC == SRC_PUPD_DEF) zeta = st_zeta<T>(R.st);
+    }
     const cx<T>* src = SRC == SRC_IN ? R.p : R.P;
     for (int e = threadIdx.x; e < nl * Nz; e += blockDim.x) {
         const int line = e / Nz, z = e - (e / Nz) * Nz;
@@ -435,6 +482,10 @@ __global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restri
         }
     }
     if (SNK == SNK_OUT || SNK == SNK_ALB) return;
+    if constexpr (sizeof(T) == 4 && (SNK == SNK_AP || SNK == SNK_AT_DEF)) {
+        publish_partials<NV>(acc, R.part, gridDim.x, blockIdx.x, sred);  // the next gather forms the scalars
+        return;
+    }
     tot_t<T> tot[NV];
     const int nblk = gridDim.x;
     const int slot = SNK == SNK_AP ? 0 : (SNK == SNK_AT || SNK == SNK_AT_DEF ? 1 : 2);
@@ -583,12 +634,15 @@ template <typename T, int MY, int MZ> struct ZyPlane {
 template <typename T, int SRC, int MY, int MZ>
 __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restrict__ rhs,
                                                const cx<T>* __restrict__ twy, const cx<T>* __restrict__ twz,
-                                               const int* __restrict__ cellmap, cx<T>* __restrict__ grid) {
+                                               const int* __restrict__ cellmap, cx<T>* __restrict__ grid, int slot,
+                                               int prod_nblk) {
+    constexpr bool kStep32 = sizeof(T) == 4 && (SRC == SRC_PUPD_DEF || SRC == SRC_TUPD);
     using PL = ZyPlane<T, MY, MZ>;
     constexpr int A1 = ct_radix(MZ, 0, true), A2 = ct_radix(MZ, 1, true);
     constexpr int B1 = ct_radix(MY, 0, true), B2 = ct_radix(MY, 1, true);
     static_assert(ct_nstages(MZ, true) == 2 && ct_nstages(MY, true) == 2, "two-stage plans");
     constexpr int ZP = PL::ZP, LY = PL::LY;
+    static_assert(!kStep32 || LY * ZP >= 32 * 8, "buffer B holds the scratch of the step scalars");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int b = blockIdx.y;
     const RhsVecs<T> R = rhs[b];
@@ -603,9 +657,13 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
     stage_tw<T>(stwz, twz, MZ);
 
     cx<T> beta, alpha, zeta;
-    if (SRC == SRC_PUPD || SRC == SRC_PUPD_DEF) beta = st_beta<T>(R.st);
-    if (SRC == SRC_TUPD || SRC == SRC_PUPD_DEF) alpha = st_alpha<T>(R.st);
-    if (SRC == SRC_PUPD_DEF) zeta = st_zeta<T>(R.st);
+    if constexpr (kStep32) {  // buffer B is free until the gather
+        if (!fp32_step_scalars<SRC>(R, slot, prod_nblk, reinterpret_cast<float2*>(sB), alpha, beta, zeta)) return;
+    } else {
+        if (SRC == SRC_PUPD || SRC == SRC_PUPD_DEF) beta = st_beta<T>(R.st);
+        if (SRC == SRC_TUPD || SRC == SRC_PUPD_DEF) alpha = st_alpha<T>(R.st);
+        if (SRC == SRC_PUPD_DEF) zeta = st_zeta<T>(R.st);
+    }
     const cx<T>* src = SRC == SRC_IN ? R.p : R.P;
     const int* cm = cellmap + (long long)x * Ny * Nz;
     const int ibase = x * Ny * Nz;
@@ -615,14 +673,14 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
     constexpr int LZ = PL::LZ, NCELL = LY * LZ, NE = (NCELL + kNT - 1) / kNT, CH = NE < 4 ? NE : 4;
 #pragma unroll
     for (int c0 = 0; c0 < NE; c0 += CH) {
-        int slot[CH];
+        int sidx[CH];
         long long o[CH];
 #pragma unroll
         for (int q = 0; q < CH; q++) {
             const int e = threadIdx.x + (c0 + q) * kNT;
             const int y = e / LZ, z = e - (e / LZ) * LZ;
             const bool cell = c0 + q < NE && e < NCELL;
-            slot[q] = cell ? y * ZP + z : -1;
+            sidx[q] = cell ? y * ZP + z : -1;
             int i = -1;
             if (cell && y < Ny && z < Nz) i = g.dense ? ibase + y * Nz + z : cm[y * Nz + z];
             o[q] = i >= 0 ? 3LL * i + c : -1LL;
@@ -631,7 +689,7 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
         gather_chunk<T, SRC, CH>(R, o, v, src, alpha, beta, zeta);
 #pragma unroll
         for (int q = 0; q < CH; q++)
-            if (slot[q] >= 0) sB[slot[q]] = v[q];
+            if (sidx[q] >= 0) sB[sidx[q]] = v[q];
     }
     __syncthreads();  // also publishes the twiddles
     // z stage 1: task (y < LY, j < A2) reads z = j + A2 r < LZ (columns past LZ
@@ -808,6 +866,10 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
         scatter_chunk<T, SRC, SNK, CH, NV>(R, o, vo, acc);
     }
     if (SNK == SNK_OUT || SNK == SNK_ALB) return;
+    if constexpr (sizeof(T) == 4 && (SNK == SNK_AP || SNK == SNK_AT_DEF)) {
+        publish_partials<NV>(acc, R.part, gridDim.x, blockIdx.x, sred);  // the next gather forms the scalars
+        return;
+    }
     tot_t<T> tot[NV];
     const int slot = SNK == SNK_AP ? 0 : (SNK == SNK_AT || SNK == SNK_AT_DEF ? 1 : 2);
     if (!last_block_total<NV>(acc, R.part, gridDim.x, blockIdx.x, R.cnt + slot, sred, tot)) return;
@@ -823,11 +885,11 @@ template <typename T, int MY, int MZ> struct ZyLaunch {
         const Geom& g = a.g;
         if (pass == PASS_ZFWD) {
             switch (mode) {
-                case SRC_IN: k_zyfwd<T, SRC_IN, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
-                case SRC_PUPD: k_zyfwd<T, SRC_PUPD, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
-                case SRC_TUPD: k_zyfwd<T, SRC_TUPD, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
-                case SRC_PUPD_DEF: k_zyfwd<T, SRC_PUPD_DEF, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
-                default: k_zyfwd<T, SRC_P, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
+                case SRC_IN: k_zyfwd<T, SRC_IN, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid, a.slot, a.prod_nblk); break;
+                case SRC_PUPD: k_zyfwd<T, SRC_PUPD, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid, a.slot, a.prod_nblk); break;
+                case SRC_TUPD: k_zyfwd<T, SRC_TUPD, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid, a.slot, a.prod_nblk); break;
+                case SRC_PUPD_DEF: k_zyfwd<T, SRC_PUPD_DEF, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid, a.slot, a.prod_nblk); break;
+                default: k_zyfwd<T, SRC_P, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid, a.slot, a.prod_nblk); break;
             }
         } else {
             switch (mode) {
@@ -873,11 +935,11 @@ template <typename T, int CM> struct PassLaunch {
             const size_t sm = zsmem<T>(Mz);
             if (pass == PASS_ZFWD) {
                 switch (mode) {
-                    case SRC_IN: k_zfwd<T, SRC_IN, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid); break;
-                    case SRC_PUPD: k_zfwd<T, SRC_PUPD, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid); break;
-                    case SRC_TUPD: k_zfwd<T, SRC_TUPD, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid); break;
-                    case SRC_PUPD_DEF: k_zfwd<T, SRC_PUPD_DEF, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid); break;
-                    default: k_zfwd<T, SRC_P, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid); break;
+                    case SRC_IN: k_zfwd<T, SRC_IN, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid, a.slot, a.prod_nblk); break;
+                    case SRC_PUPD: k_zfwd<T, SRC_PUPD, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid, a.slot, a.prod_nblk); break;
+                    case SRC_TUPD: k_zfwd<T, SRC_TUPD, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid, a.slot, a.prod_nblk); break;
+                    case SRC_PUPD_DEF: k_zfwd<T, SRC_PUPD_DEF, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid, a.slot, a.prod_nblk); break;
+                    default: k_zfwd<T, SRC_P, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid, a.slot, a.prod_nblk); break;
                 }
             } else {
                 switch (mode) {
