@@ -321,18 +321,54 @@ __device__ __forceinline__ void publish_partials(float (&v)[NV], double* part, i
     }
 }
 
-// The totals of nblk published partials, in block order (every thread).  sred:
-// 32 * NV float2 of shared scratch.
+// The totals of nblk published partials (every thread).  Warp k adds value k:
+// lane l takes the partials l, l + 32, ... (loads issued eight at a time), then
+// a shuffle tree; one barrier.  The order is fixed.  sred: NV float2 of shared
+// scratch.
 template <int NV>
 __device__ __forceinline__ void sum_partials(const double* part, int nblk, float2* sred, float2 (&tot)[NV]) {
+    static_assert(NV <= kNT / 32, "one warp per summed value");
     const float2* part2 = reinterpret_cast<const float2*>(part);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (warp < NV) {
+        const float2* src = part2 + (long long)warp * nblk;
+        float2 a = make_float2(0.f, 0.f);
+        for (int i0 = lane; i0 < nblk; i0 += 32 * 8) {
+            float2 v[8];
 #pragma unroll
-    for (int k = 0; k < NV; k++) {
-        float2 q = make_float2(0.f, 0.f);
-        for (int i = threadIdx.x; i < nblk; i += blockDim.x) q = df_add(q, __ldcg(part2 + k * nblk + i));
-        tot[k] = q;
+            for (int u = 0; u < 8; u++) v[u] = i0 + 32 * u < nblk ? __ldcg(src + i0 + 32 * u) : make_float2(0.f, 0.f);
+#pragma unroll
+            for (int u = 0; u < 8; u++) a = df_add(a, v[u]);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            a = df_add(a, make_float2(__shfl_down_sync(0xffffffffu, a.x, o), __shfl_down_sync(0xffffffffu, a.y, o)));
+        if (lane == 0) sred[warp] = a;
     }
-    block_sum<NV>(tot, sred);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; k++) tot[k] = sred[k];
+}
+
+// The state fields the end of step k - 1 reads, loaded together ahead of the
+// partial sums (one round trip instead of a chain of dependent ones).
+struct StepIn {
+    float2 alpha, rho;  // alpha and r0.r of step k - 1
+    int it, init, status, max_it;
+    float Enorm, tol;
+};
+__device__ __forceinline__ StepIn load_step_in(const SolveState* st, int p) {
+    const int q = p ^ 1;
+    StepIn s;
+    s.alpha = st->alpha32[q];
+    s.rho = st->rho32[q];
+    s.it = st->it32[q];
+    s.init = st->init32[q];
+    s.status = st->status;
+    s.max_it = st->max_it;
+    s.Enorm = st->Enorm32;
+    s.tol = st->tol32;
+    return s;
 }
 
 // The end of step k - 1 as seen by step k (parity p): zeta = At.t / At.At in
@@ -346,8 +382,7 @@ struct StepEnd {
     int it, stop, set_iterations, iterations;
 };
 __device__ __forceinline__ double df_d(float2 a) { return (double)a.x + (double)a.y; }
-__device__ __forceinline__ StepEnd step_end_f32(const SolveState* st, const float2 (&tot)[8], int p) {
-    const int q = p ^ 1;
+__device__ __forceinline__ StepEnd step_end_f32(const StepIn& st, const float2 (&tot)[8]) {
     StepEnd e;
     e.zeta = fdiv2(make_float2(tot[0].x, tot[1].x), make_float2(tot[2].x, 0.f));  // DDAModel.cpp:225
     const double zx = e.zeta.x, zy = e.zeta.y;
@@ -356,19 +391,19 @@ __device__ __forceinline__ StepEnd step_end_f32(const SolveState* st, const floa
     e.rho = make_float2((float)(tx - (zx * ux - zy * uy)), (float)(ty - (zx * uy + zy * ux)));
     double rn2 = cc - 2.0 * (zx * ax + zy * ay) + (zx * zx + zy * zy) * bb;
     if (!(rn2 > 0.0)) rn2 = isnan(rn2) ? rn2 : 0.0;
-    e.err = sqrtf((float)rn2) / st->Enorm32;
-    const bool init = st->init32[q] != 0;
-    e.it = st->it32[q] + (init ? 0 : 1);
+    e.err = sqrtf((float)rn2) / st.Enorm;
+    const bool init = st.init != 0;
+    e.it = st.it + (init ? 0 : 1);
     e.stop = ST_RUNNING;
     e.set_iterations = 0;
     e.iterations = 0;
     e.beta = make_float2(0.f, 0.f);
-    const float2 rho_prev = st->rho32[q];
-    if (!init && e.err <= st->tol32) {  // DDAModel.cpp:232-235
+    const float2 rho_prev = st.rho;
+    if (!init && e.err <= st.tol) {  // DDAModel.cpp:232-235
         e.stop = ST_CONVERGED;
         e.set_iterations = 1;
         e.iterations = e.it;
-    } else if (e.it >= st->max_it) {  // the loop of DDAModel.cpp:186 ends
+    } else if (e.it >= st.max_it) {  // the loop of DDAModel.cpp:186 ends
         e.stop = ST_MAXITER;
     } else if (rho_prev.x == 0.f && rho_prev.y == 0.f) {  // DDAModel.cpp:193-215
         e.stop = ST_BREAKDOWN;
@@ -376,7 +411,7 @@ __device__ __forceinline__ StepEnd step_end_f32(const SolveState* st, const floa
         e.iterations = e.it + 1;
     } else {
         // beta = (alpha / zeta) * (r0 . r) / (r0 . rl)      DDAModel.cpp:218
-        e.beta = fdiv2(fmul2(fdiv2(st->alpha32[q], e.zeta), e.rho), rho_prev);
+        e.beta = fdiv2(fmul2(fdiv2(st.alpha, e.zeta), e.rho), rho_prev);
         if (!isfinite(e.rho.x) || !isfinite(e.rho.y) || !isfinite(e.err) || !isfinite(e.beta.x) ||
             !isfinite(e.beta.y))
             e.stop = ST_NAN;

@@ -95,14 +95,41 @@ template <int SIGN, typename T> struct Bfly<4, SIGN, T> {
     }
 };
 
-template <int SIGN, typename T> struct Bfly<8, SIGN, T> {
-    // split into even / odd 4-point DFTs, combine with W8^q
+// DFT of length R whose inputs v[NIN .. R) are zero: they are neither read
+// nor added (the zero-padded half of a first stage).  Pruned forms for NIN =
+// R / 2 with R = 4, 8, 16 (the first radices of the two-stage plans); any
+// other NIN runs the full butterfly on zeros.
+template <int R, int SIGN, typename T, int NIN> struct BflyIn {
+    static __device__ __forceinline__ void run(cx<T>* v) {
+#pragma unroll
+        for (int r = NIN; r < R; r++) v[r] = czero<T>();
+        Bfly<R, SIGN, T>::run(v);
+    }
+};
+template <int SIGN, typename T> struct BflyIn<4, SIGN, T, 4> {
+    static __device__ __forceinline__ void run(cx<T>* v) { Bfly<4, SIGN, T>::run(v); }
+};
+template <int SIGN, typename T> struct BflyIn<4, SIGN, T, 2> {
+    // v[0] + W^q v[1], W = exp(SIGN i pi / 2)
+    static __device__ __forceinline__ void run(cx<T>* v) {
+        const cx<T> a = v[0], b = v[1], wb = cmul_i<SIGN, T>(b);
+        v[0] = cadd<T>(a, b);
+        v[1] = cadd<T>(a, wb);
+        v[2] = csub<T>(a, b);
+        v[3] = csub<T>(a, wb);
+    }
+};
+
+// Radix 8: even / odd 4-point DFTs combined with W8^q.  NIN4 < 4: only the
+// first NIN4 inputs of each 4-point DFT (v[0 .. 2 NIN4)) are non-zero.
+template <int SIGN, typename T, int NIN4> struct Bfly8 {
     static __device__ __forceinline__ void run(cx<T>* v) {
         const T h = T(0.70710678118654752440084436210484904);  // sqrt(1/2)
-        cx<T> e[4] = {v[0], v[2], v[4], v[6]};
-        cx<T> o[4] = {v[1], v[3], v[5], v[7]};
-        Bfly<4, SIGN, T>::run(e);
-        Bfly<4, SIGN, T>::run(o);
+        cx<T> e[4], o[4];
+#pragma unroll
+        for (int k = 0; k < NIN4; k++) e[k] = v[2 * k], o[k] = v[2 * k + 1];
+        BflyIn<4, SIGN, T, NIN4>::run(e);
+        BflyIn<4, SIGN, T, NIN4>::run(o);
         // W8^1 = (1 + SIGN i) sqrt(1/2), W8^2 = SIGN i, W8^3 = (-1 + SIGN i) sqrt(1/2)
         cx<T> o1 = mk<T>((o[1].x - T(SIGN) * o[1].y) * h, (o[1].y + T(SIGN) * o[1].x) * h);
         cx<T> o2 = cmul_i<SIGN, T>(o[2]);
@@ -117,6 +144,7 @@ template <int SIGN, typename T> struct Bfly<8, SIGN, T> {
         v[7] = csub<T>(e[3], o3);
     }
 };
+template <int SIGN, typename T> struct Bfly<8, SIGN, T> : Bfly8<SIGN, T, 4> {};
 
 // odd prime radices: V[q] = v0 + sum_{r=1}^{(R-1)/2} [ c_{rq} (v_r + v_{R-r}) + SIGN i s_{rq} (v_r - v_{R-r}) ]
 // with c_m = cos(2 pi m / R), s_m = sin(2 pi m / R)
@@ -228,7 +256,9 @@ template <> struct RootTab<16> {
     }
 };
 
-template <int R1, int R2, int SIGN, typename T> struct BflyComp {
+// NIN1 < R1: only inputs n1 < NIN1 of each inner DFT (v[0 .. R2 NIN1)) are
+// non-zero.
+template <int R1, int R2, int SIGN, typename T, int NIN1 = R1> struct BflyComp {
     static __device__ __forceinline__ void run(cx<T>* v) {
         constexpr int R = R1 * R2;
         cx<T> y[R2][R1];
@@ -236,8 +266,8 @@ template <int R1, int R2, int SIGN, typename T> struct BflyComp {
         for (int n2 = 0; n2 < R2; n2++) {
             cx<T> a[R1];
 #pragma unroll
-            for (int n1 = 0; n1 < R1; n1++) a[n1] = v[R2 * n1 + n2];
-            Bfly<R1, SIGN, T>::run(a);
+            for (int n1 = 0; n1 < NIN1; n1++) a[n1] = v[R2 * n1 + n2];
+            BflyIn<R1, SIGN, T, NIN1>::run(a);
 #pragma unroll
             for (int k1 = 0; k1 < R1; k1++) {
                 if (n2 > 0 && k1 > 0) {
@@ -259,6 +289,8 @@ template <int R1, int R2, int SIGN, typename T> struct BflyComp {
     }
 };
 template <int SIGN, typename T> struct Bfly<16, SIGN, T> : BflyComp<4, 4, SIGN, T> {};
+template <int SIGN, typename T> struct BflyIn<8, SIGN, T, 4> : Bfly8<SIGN, T, 2> {};
+template <int SIGN, typename T> struct BflyIn<16, SIGN, T, 8> : BflyComp<4, 4, SIGN, T, 2> {};
 template <int SIGN, typename T> struct Bfly<12, SIGN, T> : BflyComp<4, 3, SIGN, T> {};
 template <int SIGN, typename T> struct Bfly<10, SIGN, T> : BflyComp<2, 5, SIGN, T> {};
 

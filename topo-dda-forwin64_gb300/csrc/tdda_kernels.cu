@@ -122,12 +122,13 @@ __global__ void __launch_bounds__(kNT) k_solve_begin(int n3, const RhsVecs<T>* _
 // partials: the computation every block of the next gather repeats, here by
 // one block per right-hand side so that the state the host reads is current.
 __global__ void __launch_bounds__(kNT) k_step_end(const RhsVecs<float>* __restrict__ rhs, int slot, int prod_nblk) {
-    __shared__ float2 sred[32 * 8];
+    __shared__ float2 sred[8];
     const RhsVecs<float> R = rhs[blockIdx.x];
-    if (rhs_done(R.st)) return;
+    StepIn in;
+    if (threadIdx.x == 0) in = load_step_in(R.st, slot);
     float2 tot[8];
     sum_partials<8>(R.part, prod_nblk, sred, tot);
-    if (threadIdx.x == 0) write_step_end(R.st, step_end_f32(R.st, tot, slot), slot);
+    if (threadIdx.x == 0 && in.status == ST_RUNNING) write_step_end(R.st, step_end_f32(in, tot), slot);
 }
 
 // ================================================================ K0 green

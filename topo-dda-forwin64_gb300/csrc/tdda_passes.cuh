@@ -36,23 +36,31 @@ __device__ __forceinline__ cx<T> deferred_step(const RhsVecs<T>& R, long long o,
 // The FP32 step's scalars in a gather pass (SRC_PUPD_DEF: the end of the
 // previous step from the At partials; SRC_TUPD: alpha from the Ap partials),
 // formed by every block from the partials the previous sink pass published;
-// block 0 records them.  scratch: 32 * 8 float2 of shared memory that is free
-// until the gather.  Returns false when the step ends the solve.
+// block 0 records them.  The state is read here, with the partials: a
+// right-hand side whose solve has stopped returns false without writing.
+// scratch: 8 float2 of shared memory that is free until the gather.  Returns
+// false when the solve does not continue.
 template <int SRC>
 __device__ __forceinline__ bool fp32_step_scalars(const RhsVecs<float>& R, int slot, int prod_nblk, float2* scratch,
                                                   float2& alpha, float2& beta, float2& zeta) {
     __shared__ float2 s_sc[3];
     __shared__ int s_stop;
     if constexpr (SRC == SRC_PUPD_DEF) {
+        StepIn in;
+        if (threadIdx.x == 0) in = load_step_in(R.st, slot);
         float2 tot[8];
         sum_partials<8>(R.part, prod_nblk, scratch, tot);
         if (threadIdx.x == 0) {
-            const StepEnd e = step_end_f32(R.st, tot, slot);
-            if (blockIdx.x == 0) write_step_end(R.st, e, slot);
-            s_sc[0] = e.zeta;
-            s_sc[1] = e.beta;
-            s_sc[2] = R.st->alpha32[slot ^ 1];
-            s_stop = e.stop;
+            if (in.status != ST_RUNNING) {
+                s_stop = in.status;
+            } else {
+                const StepEnd e = step_end_f32(in, tot);
+                if (blockIdx.x == 0) write_step_end(R.st, e, slot);
+                s_sc[0] = e.zeta;
+                s_sc[1] = e.beta;
+                s_sc[2] = in.alpha;
+                s_stop = e.stop;
+            }
         }
         __syncthreads();
         if (s_stop != ST_RUNNING) return false;
@@ -60,14 +68,19 @@ __device__ __forceinline__ bool fp32_step_scalars(const RhsVecs<float>& R, int s
         beta = s_sc[1];
         alpha = s_sc[2];
     } else {
+        float2 rho;
+        int status;
+        if (threadIdx.x == 0) rho = R.st->rho32[slot], status = R.st->status;
         float2 tot[2];
         sum_partials<2>(R.part, prod_nblk, scratch, tot);
         if (threadIdx.x == 0) {
-            const float2 a = fdiv2(R.st->rho32[slot], make_float2(tot[0].x, tot[1].x));  // DDAModel.cpp:221
-            if (blockIdx.x == 0) R.st->alpha32[slot] = a;
+            const float2 a = fdiv2(rho, make_float2(tot[0].x, tot[1].x));  // DDAModel.cpp:221
+            if (status == ST_RUNNING && blockIdx.x == 0) R.st->alpha32[slot] = a;
             s_sc[0] = a;
+            s_stop = status;
         }
         __syncthreads();
+        if (s_stop != ST_RUNNING) return false;
         alpha = s_sc[0];
     }
     return true;
@@ -80,10 +93,12 @@ __global__ void __launch_bounds__(kNT) k_zfwd(Geom g, const RhsVecs<T>* __restri
                                               cx<T>* __restrict__ grid, int slot, int prod_nblk) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr bool kStep32 = sizeof(T) == 4 && (SRC == SRC_PUPD_DEF || SRC == SRC_TUPD);
-    __shared__ double s_scratch[kStep32 ? 32 * 8 : 1];
+    __shared__ double s_scratch[kStep32 ? 8 : 1];
     const int b = blockIdx.y;
     const RhsVecs<T> R = rhs[b];
-    if (rhs_done(R.st)) return;
+    if constexpr (!kStep32) {  // the FP32 step reads the status with its scalars
+        if (rhs_done(R.st)) return;
+    }
     constexpr int cLZ = CM > 0 ? z_lines<T>(CM) : 1;
     constexpr int cMzP = CM > 0 ? pad_odd(CM) : 1;
     const int Mz = CM > 0 ? CM : g.pz.M, Nz = g.Nz;
@@ -301,18 +316,21 @@ __global__ void __launch_bounds__(ZT * ct_radix(M, 0, true), MINB) k_xpass2(Geom
     stage_tw<T>(stw, twx, M);
     cx<T>* gp = grid + (long long)b * g.sb + (long long)y * g.sy + z0;
 
-    // forward stage 1: radix R1 over x = j + R2 r < Nx, grid -> s[j R1 + q][line]
+    // forward stage 1: radix R1 over x = j + R2 r < Nx, grid -> s[j R1 + q][line].
+    // Nx <= M / 2, so the inputs r >= R1 / 2 are zero padding: not read, not added.
+    static_assert(R1 % 2 == 0, "even first radix");
+    constexpr int RH = R1 / 2;
     for (int w = threadIdx.x; w < W * R2; w += NT) {
         const int l = w % W, j = w / W;
         const int c = l / ZT, zl = l - c * ZT;
         const cx<T>* src = gp + c * g.sc + zl;
         cx<T> v[R1];
 #pragma unroll
-        for (int r = 0; r < R1; r++) {
+        for (int r = 0; r < RH; r++) {
             const int xx = j + R2 * r;
             v[r] = (zl < zn && xx < Nx) ? src[(long long)xx * g.sx] : czero<T>();
         }
-        Bfly<R1, -1, T>::run(v);
+        BflyIn<R1, -1, T, RH>::run(v);
 #pragma unroll
         for (int q = 0; q < R1; q++) s[(j * R1 + q) * WP + l] = v[q];
     }
@@ -378,7 +396,7 @@ __global__ void __launch_bounds__(ZT * ct_radix(M, 0, true), MINB) k_xpass2(Geom
         Bfly<R1, +1, T>::run(v);
         cx<T>* dst = gp + c * g.sc + zz;
 #pragma unroll
-        for (int q = 0; q < R1; q++) {
+        for (int q = 0; q < RH; q++) {  // outputs x >= M / 2 >= Nx are never stored
             const int xx = jj + R2 * q;
             if (zz < zn && xx < Nx) dst[(long long)xx * g.sx] = v[q];
         }
@@ -504,60 +522,66 @@ __global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restri
 // row stride ZP.  Lattice data occupies rows y < Ny <= LY and columns
 // z < Nz <= LZ (M >= 2N - 1 on every axis).
 // Gather of CH entries of one component: o[q] = 3 i + c of the dipole in
-// cell q, or -1 for an empty or padding cell (v[q] = 0).  All loads come before the
+// cell q, or -1 for an empty or padding cell (v[q] = 0).  GatherIn holds the
+// vectors a gather reads: load() issues every load, combine() forms the grid
+// values with the step scalars and stores the updated vectors, so a kernel can
+// form the scalars while the loads are in flight.  All loads come before the
 // first store.
+template <typename T, int SRC, int CH> struct GatherIn {
+    static constexpr int NL = SRC == SRC_PUPD_DEF ? 6 : (SRC == SRC_PUPD ? 3 : (SRC == SRC_TUPD ? 2 : 1));
+    cx<T> a[NL][CH];
+    __device__ __forceinline__ void load(const RhsVecs<T>& R, const long long (&o)[CH], const cx<T>* src) {
+#pragma unroll
+        for (int q = 0; q < CH; q++) {
+            if (o[q] < 0) continue;
+            const long long i = o[q];
+            if constexpr (SRC == SRC_PUPD_DEF) {
+                a[0][q] = R.Ap[i]; a[1][q] = R.r[i]; a[2][q] = R.p[i];
+                a[3][q] = R.t[i]; a[4][q] = R.At[i]; a[5][q] = R.P[i];
+            } else if constexpr (SRC == SRC_PUPD) {
+                a[0][q] = R.p[i]; a[1][q] = R.u[i]; a[2][q] = R.r[i];
+            } else if constexpr (SRC == SRC_TUPD) {
+                a[0][q] = R.r[i]; a[1][q] = R.Ap[i];
+            } else {
+                a[0][q] = src[i];
+            }
+        }
+    }
+    __device__ __forceinline__ void combine(const RhsVecs<T>& R, const long long (&o)[CH], cx<T> (&v)[CH], cx<T> alpha,
+                                            cx<T> beta, cx<T> zeta) const {
+#pragma unroll
+        for (int q = 0; q < CH; q++) {
+            v[q] = czero<T>();
+            if (o[q] < 0) continue;
+            const long long i = o[q];
+            if constexpr (SRC == SRC_PUPD_DEF) {
+                // the previous step's update (DDAModel.cpp:226-230), then p (DDAModel.cpp:219)
+                const cx<T> Ap = a[0][q], r = a[1][q], p = a[2][q], t = a[3][q], At = a[4][q], P = a[5][q];
+                const cx<T> u = cmul<T>(zeta, Ap);
+                const cx<T> z = csub<T>(cmul<T>(zeta, r), cmul<T>(alpha, u));
+                R.P[i] = cadd<T>(cadd<T>(P, cmul<T>(alpha, p)), z);
+                const cx<T> rn = csub<T>(t, cmul<T>(zeta, At));
+                R.r[i] = rn;
+                v[q] = cadd<T>(rn, cmul<T>(beta, csub<T>(p, u)));
+                R.p[i] = v[q];
+            } else if constexpr (SRC == SRC_PUPD) {
+                v[q] = cadd<T>(a[2][q], cmul<T>(beta, csub<T>(a[0][q], a[1][q])));  // p = r + beta (p - u)
+                R.p[i] = v[q];
+            } else if constexpr (SRC == SRC_TUPD) {
+                v[q] = csub<T>(a[0][q], cmul<T>(alpha, a[1][q]));  // t = r - alpha Ap
+                R.t[i] = v[q];
+            } else {
+                v[q] = a[0][q];
+            }
+        }
+    }
+};
 template <typename T, int SRC, int CH>
 __device__ __forceinline__ void gather_chunk(const RhsVecs<T>& R, const long long (&o)[CH], cx<T> (&v)[CH],
                                              const cx<T>* src, cx<T> alpha, cx<T> beta, cx<T> zeta) {
-    if constexpr (SRC == SRC_PUPD_DEF) {
-        cx<T> Ap[CH], r[CH], p[CH], t[CH], At[CH], P[CH];
-#pragma unroll
-        for (int q = 0; q < CH; q++)
-            if (o[q] >= 0) {
-                Ap[q] = R.Ap[o[q]]; r[q] = R.r[o[q]]; p[q] = R.p[o[q]];
-                t[q] = R.t[o[q]]; At[q] = R.At[o[q]]; P[q] = R.P[o[q]];
-            }
-#pragma unroll
-        for (int q = 0; q < CH; q++) {
-            v[q] = czero<T>();
-            if (o[q] < 0) continue;
-            // the previous step's update (DDAModel.cpp:226-230), then p (DDAModel.cpp:219)
-            const cx<T> u = cmul<T>(zeta, Ap[q]);
-            const cx<T> z = csub<T>(cmul<T>(zeta, r[q]), cmul<T>(alpha, u));
-            R.P[o[q]] = cadd<T>(cadd<T>(P[q], cmul<T>(alpha, p[q])), z);
-            const cx<T> rn = csub<T>(t[q], cmul<T>(zeta, At[q]));
-            R.r[o[q]] = rn;
-            v[q] = cadd<T>(rn, cmul<T>(beta, csub<T>(p[q], u)));
-            R.p[o[q]] = v[q];
-        }
-    } else if constexpr (SRC == SRC_PUPD) {
-        cx<T> p[CH], u[CH], r[CH];
-#pragma unroll
-        for (int q = 0; q < CH; q++)
-            if (o[q] >= 0) { p[q] = R.p[o[q]]; u[q] = R.u[o[q]]; r[q] = R.r[o[q]]; }
-#pragma unroll
-        for (int q = 0; q < CH; q++) {
-            v[q] = czero<T>();
-            if (o[q] < 0) continue;
-            v[q] = cadd<T>(r[q], cmul<T>(beta, csub<T>(p[q], u[q])));
-            R.p[o[q]] = v[q];
-        }
-    } else if constexpr (SRC == SRC_TUPD) {
-        cx<T> r[CH], ap[CH];
-#pragma unroll
-        for (int q = 0; q < CH; q++)
-            if (o[q] >= 0) { r[q] = R.r[o[q]]; ap[q] = R.Ap[o[q]]; }
-#pragma unroll
-        for (int q = 0; q < CH; q++) {
-            v[q] = czero<T>();
-            if (o[q] < 0) continue;
-            v[q] = csub<T>(r[q], cmul<T>(alpha, ap[q]));
-            R.t[o[q]] = v[q];
-        }
-    } else {
-#pragma unroll
-        for (int q = 0; q < CH; q++) v[q] = o[q] >= 0 ? src[o[q]] : czero<T>();
-    }
+    GatherIn<T, SRC, CH> in;
+    in.load(R, o, src);
+    in.combine(R, o, v, alpha, beta, zeta);
 }
 
 // Scatter of CH entries of one component (A v in val[q], dipole entry o[q] or
@@ -642,11 +666,13 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
     constexpr int B1 = ct_radix(MY, 0, true), B2 = ct_radix(MY, 1, true);
     static_assert(ct_nstages(MZ, true) == 2 && ct_nstages(MY, true) == 2, "two-stage plans");
     constexpr int ZP = PL::ZP, LY = PL::LY;
-    static_assert(!kStep32 || LY * ZP >= 32 * 8, "buffer B holds the scratch of the step scalars");
+    static_assert(!kStep32 || LY * ZP >= 8, "buffer B holds the scratch of the step scalars");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int b = blockIdx.y;
     const RhsVecs<T> R = rhs[b];
-    if (rhs_done(R.st)) return;
+    if constexpr (!kStep32) {  // the FP32 step reads the status with its scalars
+        if (rhs_done(R.st)) return;
+    }
     const int x = blockIdx.x / 3, c = blockIdx.x - 3 * (blockIdx.x / 3);
     const int Ny = g.Ny, Nz = g.Nz;
     cx<T>* stwy = reinterpret_cast<cx<T>*>(smem_raw);
@@ -657,9 +683,7 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
     stage_tw<T>(stwz, twz, MZ);
 
     cx<T> beta, alpha, zeta;
-    if constexpr (kStep32) {  // buffer B is free until the gather
-        if (!fp32_step_scalars<SRC>(R, slot, prod_nblk, reinterpret_cast<float2*>(sB), alpha, beta, zeta)) return;
-    } else {
+    if constexpr (!kStep32) {
         if (SRC == SRC_PUPD || SRC == SRC_PUPD_DEF) beta = st_beta<T>(R.st);
         if (SRC == SRC_TUPD || SRC == SRC_PUPD_DEF) alpha = st_alpha<T>(R.st);
         if (SRC == SRC_PUPD_DEF) zeta = st_zeta<T>(R.st);
@@ -685,8 +709,17 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
             if (cell && y < Ny && z < Nz) i = g.dense ? ibase + y * Nz + z : cm[y * Nz + z];
             o[q] = i >= 0 ? 3LL * i + c : -1LL;
         }
+        GatherIn<T, SRC, CH> in;
+        in.load(R, o, src);
+        if constexpr (kStep32) {
+            // the FP32 step scalars, formed while the first chunk's loads are in
+            // flight (buffer B is free until the chunk's stores)
+            if (c0 == 0 &&
+                !fp32_step_scalars<SRC>(R, slot, prod_nblk, reinterpret_cast<float2*>(sB), alpha, beta, zeta))
+                return;
+        }
         cx<T> v[CH];
-        gather_chunk<T, SRC, CH>(R, o, v, src, alpha, beta, zeta);
+        in.combine(R, o, v, alpha, beta, zeta);
 #pragma unroll
         for (int q = 0; q < CH; q++)
             if (sidx[q] >= 0) sB[sidx[q]] = v[q];
@@ -699,8 +732,8 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
         const int y = w % LY, j = w / LY;
         cx<T> v[A1];
 #pragma unroll
-        for (int r = 0; r < A1; r++) v[r] = (r < RV && j + A2 * r < LZ) ? sB[y * ZP + j + A2 * r] : czero<T>();
-        Bfly<A1, -1, T>::run(v);
+        for (int r = 0; r < RV; r++) v[r] = j + A2 * r < LZ ? sB[y * ZP + j + A2 * r] : czero<T>();
+        BflyIn<A1, -1, T, RV>::run(v);
 #pragma unroll
         for (int q = 0; q < A1; q++) sA[y * ZP + j * A1 + q] = v[q];
     }
@@ -720,16 +753,18 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
         for (int q = 0; q < A2; q++) sB[y * ZP + j + A1 * q] = v[q];
     }
     __syncthreads();
-    // y stage 1: task (kz < Mz, j < B2) reads rows y = j + B2 r < Ny
+    // y stage 1: task (kz < Mz, j < B2) reads rows y = j + B2 r < Ny (r < RY:
+    // Ny <= LY)
+    constexpr int RY = (LY + B2 - 1) / B2;
     for (int w = threadIdx.x; w < MZ * B2; w += kNT) {
         const int kz = w % MZ, j = w / MZ;
         cx<T> v[B1];
 #pragma unroll
-        for (int r = 0; r < B1; r++) {
+        for (int r = 0; r < RY; r++) {
             const int y = j + B2 * r;
             v[r] = y < Ny ? sB[y * ZP + kz] : czero<T>();
         }
-        Bfly<B1, -1, T>::run(v);
+        BflyIn<B1, -1, T, RY>::run(v);
 #pragma unroll
         for (int q = 0; q < B1; q++) sA[(j * B1 + q) * ZP + kz] = v[q];
     }
@@ -802,8 +837,9 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
             v[r] = t;
         }
         Bfly<B2, +1, T>::run(v);
+        constexpr int QY = (LY + B1 - 1) / B1;  // rows past LY >= Ny are never kept
 #pragma unroll
-        for (int q = 0; q < B2; q++) {
+        for (int q = 0; q < QY; q++) {
             const int y = j + B1 * q;
             if (y < Ny) sB[y * ZP + kz] = v[q];
         }
