@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(ZT * ct_radix(M, 0, true), MINB) k_xpass2(Geom
     cx<T>* stw = reinterpret_cast<cx<T>*>(smem_raw);
     cx<T>* s = stw + M;  // [M][WP]
     const int b = blockIdx.y;
-    if (rhs_done(rhs[b].st)) return;
+    const SolveState* st = rhs[b].st;
     const int My = g.py.M, Mz = g.pz.M, Nx = g.Nx;
     const int nzt = (Mz + ZT - 1) / ZT;
     const int y = blockIdx.x / nzt, z0 = (blockIdx.x - y * nzt) * ZT;
@@ -334,6 +334,9 @@ __global__ void __launch_bounds__(ZT * ct_radix(M, 0, true), MINB) k_xpass2(Geom
 #pragma unroll
         for (int q = 0; q < R1; q++) s[(j * R1 + q) * WP + l] = v[q];
     }
+    // a stopped solve is checked here, after the first loads are issued: nothing
+    // has been written to global memory yet
+    if (rhs_done(st)) return;
     __syncthreads();
 
     // forward stage 2, spectral product, inverse stage 1: task (zl, j), j < R1
@@ -800,7 +803,6 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
     __shared__ double sred[sred_size<T, NV>()];
     const int b = blockIdx.y;
     const RhsVecs<T> R = rhs[b];
-    if (rhs_done(R.st)) return;
     const int x = blockIdx.x / 3, c = blockIdx.x - 3 * (blockIdx.x / 3);
     const int Ny = g.Ny, Nz = g.Nz;
     cx<T>* stwy = reinterpret_cast<cx<T>*>(smem_raw);
@@ -821,6 +823,9 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
 #pragma unroll
         for (int q = 0; q < B1; q++) sA[(j * B1 + q) * ZP + kz] = v[q];
     }
+    // a stopped solve is checked here, after the plane's loads are issued:
+    // nothing has been written to global memory yet
+    if (rhs_done(R.st)) return;
     __syncthreads();  // also publishes the twiddles
     // y stage 2: task (kz, j < B1), twiddles conj(w^(r j)), rows j + B1 q < Ny kept
     for (int w = threadIdx.x; w < MZ * B1; w += kNT) {
