@@ -38,12 +38,20 @@ __host__ __device__ constexpr int ct_nrad(int M, int which, bool big = false) {
 __host__ __device__ constexpr int ct_nstages(int M, bool big) { return ct_nrad(M, -1, big); }
 __host__ __device__ constexpr int ct_radix(int M, int st, bool big) { return ct_nrad(M, st, big); }
 
-template <int R, int SIGN, typename T, int M, int NS, int L, int LS, int MS, int NT>
+// PIN (first stage only): the inputs idx >= M / 2 are zero padding (nvalid
+// <= M / 2), so the butterfly inputs r >= (R + 1) / 2 are neither read nor
+// added.  POUT (last stage only): outputs idx >= M / 2 are never stored (nout
+// <= M / 2), so the butterfly outputs q >= (R + 1) / 2 are not formed.
+template <int R, int SIGN, typename T, int M, int NS, int L, int LS, int MS, int NT, bool PIN, bool POUT>
 __device__ __forceinline__ void ct_stage(const cx<T>* __restrict__ x, cx<T>* __restrict__ y, const cx<T>* tw,
                                          int nvalid, int nout) {
     constexpr int m = M / R;
     constexpr int nb = L * m;
     constexpr int twstep = M / (NS * R);
+    static_assert(!PIN || NS == 1, "input pruning on the first stage");
+    static_assert(!POUT || NS * R == M, "output pruning on the last stage");
+    constexpr int RIN = PIN ? (R + 1) / 2 : R;
+    constexpr int ROUT = POUT ? (R + 1) / 2 : R;
 #pragma unroll 4
     for (int w = threadIdx.x; w < nb; w += NT) {
         const int j = w / L;
@@ -51,7 +59,7 @@ __device__ __forceinline__ void ct_stage(const cx<T>* __restrict__ x, cx<T>* __r
         const cx<T>* xb = x + l * LS;
         cx<T> v[R];
 #pragma unroll
-        for (int r = 0; r < R; r++) {
+        for (int r = 0; r < RIN; r++) {
             const int idx = j + r * m;
             v[r] = idx < nvalid ? xb[idx * MS] : czero<T>();
         }
@@ -64,11 +72,11 @@ __device__ __forceinline__ void ct_stage(const cx<T>* __restrict__ x, cx<T>* __r
                 v[r] = cmul<T>(v[r], t);
             }
         }
-        Bfly<R, SIGN, T>::run(v);
+        BflyIn<R, SIGN, T, RIN>::run(v);
         cx<T>* yb = y + l * LS;
         const int ob = (j - k) * R + k;
 #pragma unroll
-        for (int q = 0; q < R; q++) {
+        for (int q = 0; q < ROUT; q++) {
             const int idx = ob + q * NS;
             if (idx < nout) yb[idx * MS] = v[q];
         }
@@ -76,16 +84,21 @@ __device__ __forceinline__ void ct_stage(const cx<T>* __restrict__ x, cx<T>* __r
     __syncthreads();
 }
 
-template <int SIGN, typename T, int M, int L, int LS, int MS, int NT, int ST = 0, int NS = 1>
+// HIN: nvalid <= M / 2 (a zero-padded forward input); HOUT: nout <= M / 2 (an
+// inverse whose upper half is discarded).  M even for either.
+template <int SIGN, typename T, int M, int L, int LS, int MS, int NT, bool HIN = false, bool HOUT = false, int ST = 0,
+          int NS = 1>
 __device__ __forceinline__ cx<T>* ct_fft(cx<T>* a, cx<T>* b, const cx<T>* tw, int nvalid, int nout) {
     constexpr bool big = sizeof(T) == 4;
+    static_assert(!(HIN || HOUT) || M % 2 == 0, "halving needs an even length");
     if constexpr (ST == ct_nstages(M, big)) {
         return a;
     } else {
         constexpr int R = ct_radix(M, ST, big);
-        ct_stage<R, SIGN, T, M, NS, L, LS, MS, NT>(a, b, tw, ST == 0 ? nvalid : M,
-                                                   ST == ct_nstages(M, big) - 1 ? nout : M);
-        return ct_fft<SIGN, T, M, L, LS, MS, NT, ST + 1, NS * R>(b, a, tw, nvalid, nout);
+        constexpr bool last = ST == ct_nstages(M, big) - 1;
+        ct_stage<R, SIGN, T, M, NS, L, LS, MS, NT, HIN && ST == 0, HOUT && last>(a, b, tw, ST == 0 ? nvalid : M,
+                                                                                 last ? nout : M);
+        return ct_fft<SIGN, T, M, L, LS, MS, NT, HIN, HOUT, ST + 1, NS * R>(b, a, tw, nvalid, nout);
     }
 }
 

@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(kNT) k_zfwd(Geom g, const RhsVecs<T>* __restri
     }
     __syncthreads();
     const cx<T>* res;
-    if constexpr (CM > 0) res = ct_fft<-1, T, CM, 3 * cLZ, cMzP, 1, kNT>(s, s2, stw, Nz, CM);
+    if constexpr (CM > 0) res = ct_fft<-1, T, CM, 3 * cLZ, cMzP, 1, kNT, true, false>(s, s2, stw, Nz, CM);
     else res = smem_fft<-1, T>(s, s2, 3 * LZ, MzP, 1, g.pz, stw, Nz, Mz);
     cx<T>* gb = grid + (long long)b * g.sb;
     for (int e = threadIdx.x; e < 3 * nl * Mz; e += blockDim.x) {
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(kNT) k_ypass(Geom g, const RhsVecs<T>* __restr
     }
     __syncthreads();
     const cx<T>* res;
-    if constexpr (CM > 0) res = ct_fft<SIGN, T, CM, cZT, 1, cZT + 1, kNT>(s, s2, stw, nin, nout);
+    if constexpr (CM > 0) res = ct_fft<SIGN, T, CM, cZT, 1, cZT + 1, kNT, (SIGN < 0), (SIGN > 0)>(s, s2, stw, nin, nout);
     else res = smem_fft<SIGN, T>(s, s2, ZT, 1, ZP, g.py, stw, nin, nout);
     for (int e = threadIdx.x; e < nout * ZT; e += blockDim.x) {
         const int y = e / ZT, zl = e - (e / ZT) * ZT;
@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(kNT) k_xpass(Geom g, const RhsVecs<T>* __restr
     }
     __syncthreads();
     cx<T>* res;
-    if constexpr (CM > 0) res = ct_fft<-1, T, CM, 3 * cZT, 1, 3 * cZT + 1, kNT>(s, s2, stw, Nx, CM);
+    if constexpr (CM > 0) res = ct_fft<-1, T, CM, 3 * cZT, 1, 3 * cZT + 1, kNT, true, false>(s, s2, stw, Nx, CM);
     else res = smem_fft<-1, T>(s, s2, W, 1, WP, g.px, stw, Nx, Mx);
 
     // spectral product: C = A b with the symmetric 3x3 Green tensor
@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(kNT) k_xpass(Geom g, const RhsVecs<T>* __restr
     __syncthreads();
     cx<T>* other = res == s ? s2 : s;
     const cx<T>* out;
-    if constexpr (CM > 0) out = ct_fft<+1, T, CM, 3 * cZT, 1, 3 * cZT + 1, kNT>(res, other, stw, CM, Nx);
+    if constexpr (CM > 0) out = ct_fft<+1, T, CM, 3 * cZT, 1, 3 * cZT + 1, kNT, false, true>(res, other, stw, CM, Nx);
     else out = smem_fft<+1, T>(res, other, W, 1, WP, g.px, stw, Mx, Nx);
     for (int e = threadIdx.x; e < Nx * W; e += blockDim.x) {
         const int x = e / W, r = e - (e / W) * W;
@@ -452,7 +452,7 @@ __global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restri
     }
     __syncthreads();
     const cx<T>* res;
-    if constexpr (CM > 0) res = ct_fft<+1, T, CM, 3 * cLZ, cMzP, 1, kNT>(s, s2, stw, CM, Nz);
+    if constexpr (CM > 0) res = ct_fft<+1, T, CM, 3 * cLZ, cMzP, 1, kNT, false, true>(s, s2, stw, CM, Nz);
     else res = smem_fft<+1, T>(s, s2, 3 * LZ, MzP, 1, g.pz, stw, Mz, Nz);
 
     // scatter to the dipoles, fused diagonal term and dot products
