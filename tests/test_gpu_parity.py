@@ -151,6 +151,24 @@ def test_mixed_precision_reaches_tolerance_with_fp64_residual():
     assert rel(m.get_P(), g["P"]) <= 2e-4
 
 
+@pytest.mark.parametrize("steps", [1, 2, 3, 4, 5, 6, 9])
+def test_mixed_inner_steps_follow_the_reference_recurrence(steps):
+    """The FP32 inner solve stopped by its step limit: the first correction after k steps
+    is the reference's BiCGSTAB iterate after k iterations from P = 0 (DDAModel.cpp:164-255),
+    up to FP32 rounding (tolerance 1e-3; a step applied one iteration early or late moves P
+    by O(1) here).  Limits inside and at the end of the 4-step launch chunks."""
+    g = golden("solve_cfg1.npz")
+    c = _core(g)
+    m = _model(g, c)
+    info = m.solve_mixed(steps, 1e-12)
+    assert info["status"] == tdda.NOT_CONVERGED
+    assert info["inner_iterations"] == steps and info["outer_iterations"] == 1
+    oc = _ocore(g)
+    om = O.OracleModel(oc, g["nK"], float(g["E0"]), g["nE0"], g["diel_old"])
+    om.bicgstab(steps, 1e-12)
+    assert rel(m.get_P(), om.P) <= 1e-3
+
+
 def test_batch_equals_alone():
     w = tdda.lattice.config(1)
     incs = [tdda.lattice.XPOL_Z,
