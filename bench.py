@@ -280,6 +280,11 @@ def pinned_c128(n: int) -> np.ndarray:
     return torch.zeros(n, dtype=torch.complex128, pin_memory=True).numpy()
 
 
+def pinned_f64(n: int) -> np.ndarray:
+    import torch
+    return torch.zeros(n, dtype=torch.float64, pin_memory=True).numpy()
+
+
 def time_batch(tdda, torch, w, incs, precision, steps, dev, flush_l2):
     """Solve len(incs) right-hand sides of one lattice in one batched solve per step."""
     core = tdda.AProductCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material, w.nback, max_rhs=len(incs), device=dev)
@@ -454,8 +459,10 @@ def run_ours(args, dist: Dist):
     ms64 = [r[0] for r in r64]
     fp64_value = dist.world * k64 / (dist.max(sum(ms64)) / 1000.0)
 
-    # end to end through the C ABI with host buffers: new densities in, P out
-    rho_host = np.ascontiguousarray(w.diel_old)
+    # end to end through the C ABI with pinned host buffers: new densities and P0 in, P out
+    rho_host = pinned_f64(n3)
+    rho_host[:] = w.diel_old
+    zero = pinned_c128(n3)
     h2d = n3 * 8 + n3 * 16    # the 3N densities uploaded by UpdateAlpha, P0 by InitializeP
     d2h = n3 * 16             # P
     for _ in range(1):

@@ -217,6 +217,27 @@ def test_iteration_limit_keeps_previous_iteration_count():
     assert m2.get_ITERATION() == it
 
 
+def test_densities_outside_the_material_table_are_rejected():
+    """A density whose interpolation would index outside material (DDAModel.cpp:54-63)
+    is refused before anything changes: 0 <= rho < len(material), NaN refused."""
+    g = golden("aprod_box6x5x4.npz")
+    c = _core(g)
+    m = _model(g, c)
+    al0 = m.get_al()
+    for bad in (-0.1, 2.0, np.nan):
+        d = g["diel_old"].copy()
+        d[7] = bad
+        with pytest.raises(tdda.TddaError):
+            m.UpdateAlpha(d)
+        assert np.array_equal(m.get_al(), al0)
+        with pytest.raises(tdda.TddaError):
+            tdda.DDAModel(c, g["nK"], float(g["E0"]), g["nE0"], d)
+    d = g["diel_old"].copy()
+    d[7] = np.nextafter(2.0, 0.0)  # the last density inside the table
+    m.UpdateAlpha(d)
+    assert np.isfinite(m.get_al()).all()
+
+
 def test_update_alpha_matches_oracle():
     g = golden("aprod_box6x5x4.npz")
     c = _core(g)

@@ -171,6 +171,8 @@ struct tdda_core_s {
     SolveState* st64 = nullptr;        // device, max_rhs
     SolveState* st32 = nullptr;
     SolveState* hst = nullptr;         // pinned host, max_rhs
+    unsigned int* flag = nullptr;      // device: result of launch_scan
+    unsigned int* hflag = nullptr;     // pinned host copy of it
     double* part = nullptr;
     unsigned int* cnt = nullptr;
     Graphs<double> g64;
@@ -309,18 +311,8 @@ tdda_status model_upload_fields(tdda_model* m, bool field_E, bool field_al) {
         TDDA_CK(cudaStreamSynchronize(c->stream));
     }
     if (field_al) {
-        // eps and al on the device (DDAModel.cpp:54-63, tools.cpp:617-630); the
-        // density range is checked here so that the kernel never indexes
-        // outside the material table
-        for (int i = 0; i < 3 * N; i++) {
-            const double v = m->diel_old[i];
-            const int lf = (int)std::floor(v);
-            const int ln = lf >= 1 ? lf : lf + 1;
-            if (!(v == v) || lf < 0 || lf >= c->nmat || ln >= c->nmat) {
-                set_err("density %g of entry %d is outside the material table", v, i);
-                return TDDA_ERR_INVALID_ARGUMENT;
-            }
-        }
+        // eps and al on the device (DDAModel.cpp:54-63, tools.cpp:617-630) from
+        // the densities the caller checked with densities_in_table
         const tdda::AlphaParams ap = alpha_params(m);
         TDDA_CK(cudaMemcpyAsync(m->dold, m->diel_old.data(), sizeof(double) * 3 * (size_t)N, cudaMemcpyHostToDevice,
                                 c->stream));
@@ -329,6 +321,29 @@ tdda_status model_upload_fields(tdda_model* m, bool field_E, bool field_al) {
     }
     return TDDA_OK;
 }
+
+// Every density indexes the material table of the interpolation of
+// DDAModel.cpp:54-63: with lf = floor(v) and ln = (lf >= 1 ? lf : lf + 1), both
+// lf and ln lie in [0, nmat), which holds exactly when nmat >= 2 and
+// 0 <= v < nmat (NaN fails).  Checked in branch-free chunks the compiler
+// vectorises; on failure *bad is the first offending entry.
+bool densities_in_table(const double* v, size_t n, int nmat, size_t* bad) {
+    const double hi = (double)nmat;
+    constexpr size_t kChunk = 4096;
+    for (size_t i0 = 0; i0 < n; i0 += kChunk) {
+        const size_t i1 = std::min(n, i0 + kChunk);
+        int ok = nmat >= 2;
+        for (size_t i = i0; i < i1; i++) ok &= (v[i] >= 0.0) & (v[i] < hi);
+        if (!ok) {
+            size_t i = i0;
+            while (i < i1 && nmat >= 2 && v[i] >= 0.0 && v[i] < hi) i++;
+            *bad = std::min(i, i1 - 1);
+            return false;
+        }
+    }
+    return true;
+}
+
 
 tdda_status model_alloc_f32(tdda_model* m) {
     if (m->fP) return TDDA_OK;
@@ -933,6 +948,8 @@ tdda_status core_create(const tdda_core_desc* desc, const tdda::PeriodicImages* 
     TDDA_CORE_TRY(dalloc_c(c, &c->part, (size_t)c->max_rhs * tdda::kPartSlots * c->maxblk));
     TDDA_CORE_TRY(dalloc_c(c, &c->cnt, (size_t)c->max_rhs * tdda::kCounters));
     TDDA_CORE_CK(cudaMallocHost((void**)&c->hst, sizeof(SolveState) * c->max_rhs));
+    TDDA_CORE_TRY(dalloc_c(c, &c->flag, 1));
+    TDDA_CORE_CK(cudaMallocHost((void**)&c->hflag, sizeof(unsigned int)));
     TDDA_CORE_CK(cudaMemsetAsync(c->cnt, 0, sizeof(unsigned int) * c->max_rhs * tdda::kCounters, c->stream));
     TDDA_CORE_CK(cudaMemcpyAsync(c->cellmap, cellmap.data(), sizeof(int) * cellmap.size(), cudaMemcpyHostToDevice,
                                  c->stream));
@@ -991,6 +1008,7 @@ tdda_status tdda_core_destroy(tdda_core* c) {
     free_all(c->allocs, c->stream);
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->hst) cudaFreeHost(c->hst);
+    if (c->hflag) cudaFreeHost(c->hflag);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return TDDA_OK;
@@ -1072,6 +1090,13 @@ tdda_status tdda_model_create(tdda_core* c, const double* nK, double E0, const d
         return TDDA_ERR_INVALID_ARGUMENT;
     }
     *out = nullptr;
+    {
+        size_t bad = 0;
+        if (!densities_in_table(diel_old, 3 * (size_t)c->N, c->nmat, &bad)) {
+            set_err("density %g of entry %zu is outside the material table", diel_old[bad], bad);
+            return TDDA_ERR_INVALID_ARGUMENT;
+        }
+    }
     TDDA_TRY(set_device(c->device));
     tdda_model* m = new tdda_model_s();
     m->core = c;
@@ -1127,11 +1152,26 @@ tdda_status tdda_model_update_alpha(tdda_model* m, const double* diel_old) {
         return TDDA_ERR_INVALID_ARGUMENT;
     }
     TDDA_TRY(set_device(m->core->device));
-    std::vector<double> keep = m->diel_old;
-    m->diel_old.assign(diel_old, diel_old + 3 * (size_t)m->core->N);
-    tdda_status s = model_upload_fields(m, false, true);
-    if (s != TDDA_OK) m->diel_old = keep;
-    return s;
+    tdda_core* c = m->core;
+    const size_t n3 = 3 * (size_t)c->N;
+    // upload, then check the range on the device before anything that depends
+    // on the densities changes (the host scan below only names the entry)
+    TDDA_CK(cudaMemcpyAsync(m->dold, diel_old, sizeof(double) * n3, cudaMemcpyHostToDevice, c->stream));
+    TDDA_CK1(tdda::launch_scan((long long)n3, m->dold, 1, (double)c->nmat, c->flag, c->stream));
+    TDDA_CK(cudaMemcpyAsync(c->hflag, c->flag, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
+    TDDA_CK(cudaStreamSynchronize(c->stream));
+    if (*c->hflag || c->nmat < 2) {
+        size_t bad = 0;
+        densities_in_table(diel_old, n3, c->nmat, &bad);
+        TDDA_CK(cudaMemcpyAsync(m->dold, m->diel_old.data(), sizeof(double) * n3, cudaMemcpyHostToDevice, c->stream));
+        TDDA_CK(cudaStreamSynchronize(c->stream));  // the model keeps its densities
+        set_err("density %g of entry %zu is outside the material table", diel_old[bad], bad);
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    TDDA_CK1(tdda::launch_model_alpha((int)n3, m->dold, alpha_params(m), m->diel, m->al, m->fal, c->stream));
+    m->diel_old.assign(diel_old, diel_old + n3);  // while the kernel runs
+    TDDA_CK(cudaStreamSynchronize(c->stream));
+    return TDDA_OK;
 }
 
 tdda_status tdda_model_update_alpha_single(tdda_model* m, int idx, double value) {
@@ -1177,10 +1217,12 @@ tdda_status tdda_model_initialize_P(tdda_model* m, const double* P, int mem) {
         m->P_zero = true;
         return TDDA_OK;
     }
-    TDDA_CK(cudaMemcpyAsync(m->P, P, sizeof(double) * n, kind_in(mem), m->core->stream));
-    bool zero = mem == TDDA_MEM_HOST;
-    for (size_t i = 0; zero && i < n; i++) zero = P[i] == 0.0;
-    TDDA_CK(cudaStreamSynchronize(m->core->stream));
+    tdda_core* c = m->core;
+    TDDA_CK(cudaMemcpyAsync(m->P, P, sizeof(double) * n, kind_in(mem), c->stream));
+    TDDA_CK1(tdda::launch_scan((long long)n, reinterpret_cast<const double*>(m->P), 0, 0.0, c->flag, c->stream));
+    TDDA_CK(cudaMemcpyAsync(c->hflag, c->flag, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
+    TDDA_CK(cudaStreamSynchronize(c->stream));
+    const bool zero = *c->hflag == 0;
     m->P_zero = zero;  // A 0 = 0 exactly, so the solve may skip its first product
     return TDDA_OK;
 }

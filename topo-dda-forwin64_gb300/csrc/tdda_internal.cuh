@@ -239,6 +239,9 @@ cudaError_t launch_einternal(int n3, const double2* al, const double2* P, const 
 
 // mixed precision helpers: dst32 = (float) src64 ; P64 += (double) d32 ; zero
 cudaError_t launch_to_f32(int n3, const double2* src, float2* dst, cudaStream_t stream);
+// *flag = 1 when one of the n values is not +-0 (mode 0), or lies outside
+// [0, hi) or is NaN (mode 1); else 0
+cudaError_t launch_scan(long long n, const double* v, int mode, double hi, unsigned int* flag, cudaStream_t stream);
 cudaError_t launch_accumulate(int n3, const float2* d, double2* P, cudaStream_t stream);
 template <typename T> cudaError_t launch_zero(long long n, cx<T>* v, cudaStream_t stream);
 

@@ -359,30 +359,58 @@ __global__ void __launch_bounds__(kNT) k_fft_cols(double2* __restrict__ data, in
 __device__ __forceinline__ double2 dadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 dscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
 
+// eps and al = 1 / alpha_LDR(eps) of one density (DDAModel.cpp:54-63, tools.cpp:617-630)
+__device__ __forceinline__ void model_alpha_one(double v, const AlphaParams& ap, double2& eps, double2& inv) {
+    const double b1 = -1.891531, b2 = 0.1648469, b3 = -1.7700004;  // LDR coefficients (tools.cpp:618-620)
+    int lf = (int)floor(v);
+    int ln = lf + 1;
+    if (lf >= 1) ln = lf;
+    lf = lf < 0 ? 0 : (lf >= ap.nmat ? ap.nmat - 1 : lf);  // the host checked the range
+    ln = ln >= ap.nmat ? ap.nmat - 1 : ln;
+    const double2 mf = ap.mat[lf], mn = ap.mat[ln];
+    const double w = v - (double)lf;
+    eps = make_double2(mf.x + w * (mn.x - mf.x), mf.y + w * (mn.y - mf.y));
+    // a1 = (3 d^3 / (4 pi)) (eps - 1) / (eps + 2)
+    const double2 a1 = cdiv(dscale(make_double2(eps.x - 1.0, eps.y), ap.a1c), make_double2(eps.x + 2.0, eps.y));
+    // result = 1 + (a1 / d^3) ((b1 + eps b2 + eps b3 S) (K d)^2 - i (2/3)(K d)^3)
+    const double2 q = dadd(dadd(make_double2(b1, 0.0), dscale(eps, b2)), dscale(dscale(eps, b3), ap.S));
+    const double2 t = make_double2(q.x * ap.Kd2, q.y * ap.Kd2 - ap.rad);
+    const double2 res = dadd(make_double2(1.0, 0.0), dmul(make_double2(a1.x / ap.d3, a1.y / ap.d3), t));
+    const double2 alpha = cdiv(a1, res);
+    inv = cdiv(make_double2(1.0, 0.0), alpha);
+}
+
+// *flag |= 1 when an entry is neither +0 nor -0 (mode 0: A 0 = 0 exactly), or
+// when a density lies outside [0, hi) or is NaN (mode 1: the material table,
+// DDAModel.cpp:54-63).  An OR, so the result does not depend on the order.
+__global__ void k_scan(long long n, const double* __restrict__ v, int mode, double hi, unsigned int* __restrict__ flag) {
+    unsigned int any = 0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const double x = v[e];
+        if (mode == 0) any |= (__double_as_longlong(x) & 0x7fffffffffffffffll) != 0;
+        else any |= !(x >= 0.0 && x < hi);
+    }
+    any = __any_sync(0xffffffffu, any);
+    if (any && (threadIdx.x & 31) == 0) atomicOr(flag, 1u);
+}
+
+// One thread per dipole: the three entries of a dipole normally hold the same
+// density (CoreStructure.cpp:22-27), whose values are formed once.
 __global__ void k_model_alpha(int n3, const double* __restrict__ diel_old, AlphaParams ap, double2* __restrict__ diel,
                               double2* __restrict__ al, float2* __restrict__ fal) {
-    const double b1 = -1.891531, b2 = 0.1648469, b3 = -1.7700004;  // LDR coefficients (tools.cpp:618-620)
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x) {
-        const double v = diel_old[e];
-        int lf = (int)floor(v);
-        int ln = lf + 1;
-        if (lf >= 1) ln = lf;
-        lf = lf < 0 ? 0 : (lf >= ap.nmat ? ap.nmat - 1 : lf);  // the host checked the range
-        ln = ln >= ap.nmat ? ap.nmat - 1 : ln;
-        const double2 mf = ap.mat[lf], mn = ap.mat[ln];
-        const double w = v - (double)lf;
-        const double2 eps = make_double2(mf.x + w * (mn.x - mf.x), mf.y + w * (mn.y - mf.y));
-        // a1 = (3 d^3 / (4 pi)) (eps - 1) / (eps + 2)
-        const double2 a1 = cdiv(dscale(make_double2(eps.x - 1.0, eps.y), ap.a1c), make_double2(eps.x + 2.0, eps.y));
-        // result = 1 + (a1 / d^3) ((b1 + eps b2 + eps b3 S) (K d)^2 - i (2/3)(K d)^3)
-        const double2 q = dadd(dadd(make_double2(b1, 0.0), dscale(eps, b2)), dscale(dscale(eps, b3), ap.S));
-        const double2 t = make_double2(q.x * ap.Kd2, q.y * ap.Kd2 - ap.rad);
-        const double2 res = dadd(make_double2(1.0, 0.0), dmul(make_double2(a1.x / ap.d3, a1.y / ap.d3), t));
-        const double2 alpha = cdiv(a1, res);
-        const double2 inv = cdiv(make_double2(1.0, 0.0), alpha);
-        diel[e] = eps;
-        al[e] = inv;
-        if (fal) fal[e] = make_float2((float)inv.x, (float)inv.y);
+    const int n = n3 / 3;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double2 eps, inv;
+        double vprev = 0.0;
+        for (int c = 0; c < 3; c++) {
+            const int e = 3 * i + c;
+            const double v = diel_old[e];
+            if (c == 0 || !(v == vprev)) model_alpha_one(v, ap, eps, inv);
+            vprev = v;
+            diel[e] = eps;
+            al[e] = inv;
+            if (fal) fal[e] = make_float2((float)inv.x, (float)inv.y);
+        }
     }
 }
 
@@ -673,9 +701,15 @@ cudaError_t launch_einternal(int n3, const double2* al, const double2* P, const 
     k_einternal<<<grid1d(n3, kNT), kNT, 0, stream>>>(n3, al, P, diel, Ein);
     return cudaGetLastError();
 }
+cudaError_t launch_scan(long long n, const double* v, int mode, double hi, unsigned int* flag, cudaStream_t stream) {
+    cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(unsigned int), stream);
+    if (e != cudaSuccess) return e;
+    k_scan<<<std::min(grid1d(n, kNT), 152 * 8), kNT, 0, stream>>>(n, v, mode, hi, flag);
+    return cudaGetLastError();
+}
 cudaError_t launch_model_alpha(int n3, const double* diel_old, const AlphaParams& ap, double2* diel, double2* al,
                                float2* fal, cudaStream_t stream) {
-    k_model_alpha<<<grid1d(n3, kNT), kNT, 0, stream>>>(n3, diel_old, ap, diel, al, fal);
+    k_model_alpha<<<grid1d(n3 / 3, kNT), kNT, 0, stream>>>(n3, diel_old, ap, diel, al, fal);
     return cudaGetLastError();
 }
 cudaError_t launch_density_gradient(int nparam, const int* off, const int* dip, const double2* P, const double2* eps,
