@@ -143,7 +143,7 @@ void ldr_host(double K, double x, double y, double z, cd out[6]) {
 }
 
 template <typename T> struct Graphs {
-    cudaGraphExec_t iter[65] = {};  // one iteration, by batch width
+    cudaGraphExec_t iter[65] = {};  // the steps of a solve, by batch width
 };
 
 }  // namespace
@@ -411,31 +411,59 @@ template <typename T> cudaError_t enqueue_iteration(tdda_core* c, int n, int slo
 }
 
 // kChunk steps (parities 0, 1, 0, 1 ...); FP32 ends the chunk with the step
-// end for the next step (parity 0), so the state the host polls is current
-template <typename T> cudaError_t enqueue_chunk(tdda_core* c, int n) {
+// end for the next step (parity 0) and the condition of the device-side loop
+template <typename T> cudaError_t enqueue_chunk(tdda_core* c, int n, cudaGraphConditionalHandle loop) {
     for (int k = 0; k < kChunk; k++) {
-        count_launches(step_kernels<T>(c));
         cudaError_t e = enqueue_iteration<T>(c, n, k & 1);
         if (e != cudaSuccess) return e;
     }
-    if constexpr (kDeferred<T>) {
-        count_launches(1);
-        return tdda::launch_step_end(c->g, n, Prec<T>::rhs(c), 0, c->stream);
-    }
+    if constexpr (kDeferred<T>) return tdda::launch_chunk_end(c->g, n, Prec<T>::rhs(c), 0, loop, c->stream);
     return cudaSuccess;
 }
+template <typename T> int chunk_kernels(const tdda_core* c) { return kChunk * step_kernels<T>(c) + (kDeferred<T> ? 1 : 0); }
 
+// The graph of the steps.  FP64: one chunk, launched by the host until the
+// states it reads stop.  FP32: a conditional WHILE node whose body is one
+// chunk; k_chunk_end sets its condition, so the inner solve runs to its end
+// without a host round trip (at most chunk_limit chunks).
 template <typename T> tdda_status get_iteration_graph(tdda_core* c, int n, cudaGraphExec_t* out) {
     cudaGraphExec_t& ex = Prec<T>::graph(c, n);
     if (!ex) {
         cudaGraph_t gr = nullptr;
-        TDDA_CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-        t_capturing = true;
-        cudaError_t e = enqueue_chunk<T>(c, n);
-        t_capturing = false;
-        cudaError_t e2 = cudaStreamEndCapture(c->stream, &gr);
-        if (e != cudaSuccess) return cuda_fail(e, "capture of the BiCGSTAB steps");
-        if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+        cudaError_t e = cudaSuccess, e2 = cudaSuccess;
+        if constexpr (kDeferred<T>) {
+            TDDA_CK(cudaGraphCreate(&gr, 0));
+            cudaGraphConditionalHandle loop = 0;
+            e = cudaGraphConditionalHandleCreate(&loop, gr, 1, cudaGraphCondAssignDefault);
+            cudaGraphNodeParams cp{};
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = loop;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            cudaGraphNode_t node = nullptr;
+            if (e == cudaSuccess) e = cudaGraphAddNode(&node, gr, nullptr, nullptr, 0, &cp);
+            if (e != cudaSuccess) {
+                cudaGraphDestroy(gr);
+                return cuda_fail(e, "conditional node of the inner solve");
+            }
+            cudaGraph_t body = cp.conditional.phGraph_out[0];
+            TDDA_CK(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+            t_capturing = true;
+            e = enqueue_chunk<T>(c, n, loop);
+            t_capturing = false;
+            cudaGraph_t captured = nullptr;
+            e2 = cudaStreamEndCapture(c->stream, &captured);
+        } else {
+            TDDA_CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            t_capturing = true;
+            e = enqueue_chunk<T>(c, n, 0);
+            t_capturing = false;
+            e2 = cudaStreamEndCapture(c->stream, &gr);
+        }
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+            if (gr) cudaGraphDestroy(gr);
+            return cuda_fail(e != cudaSuccess ? e : e2, "capture of the BiCGSTAB steps");
+        }
         e = cudaGraphInstantiate(&ex, gr, 0);
         cudaGraphDestroy(gr);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
@@ -464,6 +492,14 @@ template <typename T> tdda_status krylov(tdda_core* c, int n, bool p_zero, int m
     }
     cudaGraphExec_t ex;
     TDDA_TRY(get_iteration_graph<T>(c, n, &ex));
+    if constexpr (kDeferred<T>) {  // the device-side loop runs the whole inner solve
+        TDDA_CK(cudaGraphLaunch(ex, c->stream));
+        TDDA_CK1(tdda::launch_finish<T>(c->g, n, rhs, c->stream));  // the last step's update
+        TDDA_CK(cudaMemcpyAsync(c->hst, Prec<T>::st(c), sizeof(SolveState) * n, cudaMemcpyDeviceToHost, c->stream));
+        TDDA_CK(cudaStreamSynchronize(c->stream));
+        count_launches(c->hst[0].chunks * chunk_kernels<T>(c));
+        return TDDA_OK;
+    }
     int done_it = 0;
     for (;;) {
         TDDA_CK(cudaMemcpyAsync(c->hst, Prec<T>::st(c), sizeof(SolveState) * n, cudaMemcpyDeviceToHost, c->stream));
@@ -471,11 +507,10 @@ template <typename T> tdda_status krylov(tdda_core* c, int n, bool p_zero, int m
         bool running = false;
         for (int i = 0; i < n; i++) running |= c->hst[i].status == tdda::ST_RUNNING;
         if (!running || done_it > max_it) break;
-        count_launches(kChunk * step_kernels<T>(c) + (kDeferred<T> ? 1 : 0));
+        count_launches(chunk_kernels<T>(c));
         TDDA_CK(cudaGraphLaunch(ex, c->stream));
         done_it += kChunk;
     }
-    if (kDeferred<T>) TDDA_CK1(tdda::launch_finish<T>(c->g, n, rhs, c->stream));  // the last step's update
     return TDDA_OK;
 }
 
@@ -500,6 +535,8 @@ SolveState fresh_state(double tol, int max_it, int iterations) {
     s.tol32 = (float)tol;
     s.init32[1] = 1;  // the FP32 initial products are step -1 (slot 1)
     s.last_slot = -1;
+    s.chunks = 0;
+    s.chunk_limit = max_it / kChunk + 2;  // max_it steps and the chunk that detects the stop
     return s;
 }
 
@@ -644,6 +681,8 @@ tdda_status solve_mixed(tdda_model* const* ms, int n, int max_it, double tol, td
             TDDA_CK1(tdda::launch_to_f32(3 * c->N, m->r, m->fE, c->stream));
             TDDA_CK1(tdda::launch_zero<float>(3LL * c->N, m->fP, c->stream));
         }
+        // the device-side loop reads its limit from the first state: the largest of the batch
+        for (int i = 1; i < n; i++) c->hst[0].chunk_limit = std::max(c->hst[0].chunk_limit, c->hst[i].chunk_limit);
         TDDA_CK(cudaMemcpyAsync(c->st32, c->hst, sizeof(SolveState) * n, cudaMemcpyHostToDevice, c->stream));
         TDDA_TRY(krylov<float>(c, n, true, max_it));
         for (int i = 0; i < n; i++) {

@@ -55,6 +55,9 @@ struct SolveState {
     int init32[2];     // slot q of the first step: the initial products (no convergence check)
     int last_slot;     // slot of the step whose update is pending when the solve stopped, or -1
     float Enorm32, tol32;
+    // the device-side loop of the FP32 inner solve (kept in the state of the
+    // first right-hand side of a batch): chunks of steps run, and the limit
+    int chunks, chunk_limit;
 };
 
 // per right-hand side: the vectors of one solve (AoS [x,y,z] per dipole)
@@ -170,10 +173,13 @@ cudaError_t launch_aproduct(const Geom& g, int src, int snk, int nrhs, const Rhs
 // blocks of the last pass of an A-product at precision T (the producer of the
 // dot-product partials)
 template <typename T> int sink_blocks(const Geom& g);
-// FP32 deferred step: the step end formed from the At-pass partials for the
-// step of parity `slot` (the same computation as the next gather's prologue),
-// one block per right-hand side; keeps the host's status reads current.
-cudaError_t launch_step_end(const Geom& g, int nrhs, const RhsVecs<float>* rhs, int slot, cudaStream_t stream);
+// FP32 deferred step, end of a chunk of steps inside the device-side loop: one
+// block forms the step end of every right-hand side for the step of parity
+// `slot` (the computation the next gather repeats), counts the chunk and sets
+// the loop's condition: another chunk while a right-hand side is running and
+// fewer than chunk_limit chunks have run.
+cudaError_t launch_chunk_end(const Geom& g, int nrhs, const RhsVecs<float>* rhs, int slot,
+                             cudaGraphConditionalHandle loop, cudaStream_t stream);
 
 // u = zeta Ap; z = zeta r - alpha u; P += alpha p + z; r = t - zeta At;
 // rho_prev = rho; rho = r0.r; convergence / breakdown / iteration limit;

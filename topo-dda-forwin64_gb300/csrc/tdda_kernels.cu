@@ -118,17 +118,34 @@ __global__ void __launch_bounds__(kNT) k_solve_begin(int n3, const RhsVecs<T>* _
     }
 }
 
-// The end of the FP32 step before a step of parity `slot`, from the At-pass
-// partials: the computation every block of the next gather repeats, here by
-// one block per right-hand side so that the state the host reads is current.
-__global__ void __launch_bounds__(kNT) k_step_end(const RhsVecs<float>* __restrict__ rhs, int slot, int prod_nblk) {
+// The end of a chunk of FP32 steps: for each right-hand side the step end
+// before the step of parity `slot`, from the At-pass partials (the computation
+// every block of the next gather repeats, so the state the host reads after
+// the loop is current), then the condition of the device-side loop.  One block.
+__global__ void __launch_bounds__(kNT) k_chunk_end(const RhsVecs<float>* __restrict__ rhs, int nrhs, int slot,
+                                                   int prod_nblk, cudaGraphConditionalHandle loop) {
     __shared__ float2 sred[8];
-    const RhsVecs<float> R = rhs[blockIdx.x];
-    StepIn in;
-    if (threadIdx.x == 0) in = load_step_in(R.st, slot);
-    float2 tot[8];
-    sum_partials<8>(R.part, prod_nblk, sred, tot);
-    if (threadIdx.x == 0 && in.status == ST_RUNNING) write_step_end(R.st, step_end_f32(in, tot), slot);
+    __shared__ int s_running;
+    if (threadIdx.x == 0) s_running = 0;
+    for (int b = 0; b < nrhs; b++) {
+        const RhsVecs<float> R = rhs[b];
+        StepIn in;
+        if (threadIdx.x == 0) in = load_step_in(R.st, slot);
+        float2 tot[8];
+        sum_partials<8>(R.part, prod_nblk, sred, tot);
+        if (threadIdx.x == 0 && in.status == ST_RUNNING) {
+            const StepEnd e = step_end_f32(in, tot);
+            write_step_end(R.st, e, slot);
+            if (e.stop == ST_RUNNING) s_running = 1;
+        }
+        __syncthreads();  // sred is reused for the next right-hand side
+    }
+    if (threadIdx.x == 0) {
+        SolveState* st0 = rhs[0].st;
+        const int chunks = st0->chunks + 1;
+        st0->chunks = chunks;
+        cudaGraphSetConditional(loop, (s_running && chunks < st0->chunk_limit) ? 1u : 0u);
+    }
 }
 
 // ================================================================ K0 green
@@ -634,8 +651,9 @@ template <typename T> int sink_blocks(const Geom& g) {
     return (g.Nx * g.Ny + lz - 1) / lz;
 }
 
-cudaError_t launch_step_end(const Geom& g, int nrhs, const RhsVecs<float>* rhs, int slot, cudaStream_t stream) {
-    k_step_end<<<nrhs, kNT, 0, stream>>>(rhs, slot, sink_blocks<float>(g));
+cudaError_t launch_chunk_end(const Geom& g, int nrhs, const RhsVecs<float>* rhs, int slot,
+                             cudaGraphConditionalHandle loop, cudaStream_t stream) {
+    k_chunk_end<<<1, kNT, 0, stream>>>(rhs, nrhs, slot, sink_blocks<float>(g), loop);
     return cudaGetLastError();
 }
 
