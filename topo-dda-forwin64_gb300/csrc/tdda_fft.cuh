@@ -256,6 +256,17 @@ template <> struct RootTab<16> {
     }
 };
 
+template <> struct RootTab<24> {
+    static __device__ __forceinline__ double c(int m) {
+        constexpr double t[24] = {1.0, 0.9659258262890683, 0.8660254037844387, 0.7071067811865476, 0.5000000000000001, 0.25881904510252074, 6.123233995736766e-17, -0.25881904510252063, -0.4999999999999998, -0.7071067811865475, -0.8660254037844387, -0.9659258262890682, -1.0, -0.9659258262890683, -0.8660254037844388, -0.7071067811865479, -0.5000000000000004, -0.25881904510252063, -1.8369701987210297e-16, 0.2588190451025203, 0.5000000000000001, 0.7071067811865474, 0.8660254037844384, 0.9659258262890681};
+        return t[m % 24];
+    }
+    static __device__ __forceinline__ double s(int m) {
+        constexpr double t[24] = {0.0, 0.25881904510252074, 0.49999999999999994, 0.7071067811865475, 0.8660254037844386, 0.9659258262890683, 1.0, 0.9659258262890683, 0.8660254037844387, 0.7071067811865476, 0.49999999999999994, 0.258819045102521, 1.2246467991473532e-16, -0.2588190451025208, -0.4999999999999997, -0.7071067811865471, -0.8660254037844384, -0.9659258262890683, -1.0, -0.9659258262890684, -0.8660254037844386, -0.7071067811865477, -0.5000000000000004, -0.25881904510252157};
+        return t[m % 24];
+    }
+};
+
 // NIN1 < R1: only inputs n1 < NIN1 of each inner DFT (v[0 .. R2 NIN1)) are
 // non-zero.
 template <int R1, int R2, int SIGN, typename T, int NIN1 = R1> struct BflyComp {
@@ -291,6 +302,8 @@ template <int R1, int R2, int SIGN, typename T, int NIN1 = R1> struct BflyComp {
 template <int SIGN, typename T> struct Bfly<16, SIGN, T> : BflyComp<4, 4, SIGN, T> {};
 template <int SIGN, typename T> struct BflyIn<8, SIGN, T, 4> : Bfly8<SIGN, T, 2> {};
 template <int SIGN, typename T> struct BflyIn<16, SIGN, T, 8> : BflyComp<4, 4, SIGN, T, 2> {};
+template <int SIGN, typename T> struct Bfly<24, SIGN, T> : BflyComp<8, 3, SIGN, T> {};
+template <int SIGN, typename T> struct BflyIn<24, SIGN, T, 12> : BflyComp<8, 3, SIGN, T, 4> {};
 template <int SIGN, typename T> struct Bfly<12, SIGN, T> : BflyComp<4, 3, SIGN, T> {};
 template <int SIGN, typename T> struct Bfly<10, SIGN, T> : BflyComp<2, 5, SIGN, T> {};
 

@@ -36,6 +36,14 @@ __host__ __device__ constexpr int ct_nrad(int M, int which, bool big = false) {
     return which < 0 ? n : r[which];
 }
 __host__ __device__ constexpr int ct_nstages(int M, bool big) { return ct_nrad(M, -1, big); }
+// The two-stage plan of the register-form x pass, M = R1 R2: the FP32 plan,
+// except 192 = 24 x 8.  Its first and last stages have 3 ZT R2 tasks for ZT R1
+// threads, one each when R1 = 3 R2, and the spectra of its second stage take
+// 3 R2 complex registers.
+__host__ __device__ constexpr int x2_radix(int M, int which) {
+    if (M == 192) return which == 0 ? 24 : 8;
+    return ct_nrad(M, which, true);
+}
 __host__ __device__ constexpr int ct_radix(int M, int st, bool big) { return ct_nrad(M, st, big); }
 
 // PIN (first stage only): the inputs idx >= M / 2 are zero padding (nvalid

@@ -8,11 +8,11 @@ bool ct_has_xy(int M) { return M == 40 || M == 128 || M == 160 || M == 192; }
 bool xpass2_length(int M) { return ct_has_xy(M); }
 
 // z-columns per block of the register-form x pass (k_xpass2), per length
-template <int M> constexpr int xpass2_tile() { return (M == 128 || M == 192) ? 16 : 8; }
+template <int M> constexpr int xpass2_tile() { return M == 128 ? 16 : 8; }
 // blocks per SM the register form is compiled for: 16 warps per SM (a
 // register cap of 128 per thread), 24 for M = 128, whose spectra fit in 85
 template <int M> constexpr int xpass2_minb() {
-    return (M == 128 ? 24 : 16) * 32 / (xpass2_tile<M>() * ct_radix(M, 0, true));
+    return (M == 128 || M == 192 ? 24 : 16) * 32 / (xpass2_tile<M>() * x2_radix(M, 0));
 }
 
 template <typename T> bool pass_ct_xy(int pass, int mode, const PassArgs<T>& a, cudaError_t* err) {

@@ -297,12 +297,12 @@ __global__ void __launch_bounds__(kNT) k_xpass(Geom g, const RhsVecs<T>* __restr
 // six, three barriers.  One block: ZT z-columns of one y row, NT = ZT R1
 // threads (one register-stage task each).
 template <typename T, int M, int ZT, int MINB>
-__global__ void __launch_bounds__(ZT * ct_radix(M, 0, true), MINB) k_xpass2(Geom g, const RhsVecs<T>* __restrict__ rhs,
+__global__ void __launch_bounds__(ZT * x2_radix(M, 0), MINB) k_xpass2(Geom g, const RhsVecs<T>* __restrict__ rhs,
                                                                    const cx<T>* __restrict__ green,
                                                                    const cx<T>* __restrict__ twx,
                                                                    cx<T>* __restrict__ grid) {
-    constexpr int R1 = ct_radix(M, 0, true), R2 = ct_radix(M, 1, true);
-    static_assert(ct_nstages(M, true) == 2 && R1 * R2 == M, "two-stage plan");
+    constexpr int R1 = x2_radix(M, 0), R2 = x2_radix(M, 1);
+    static_assert(R1 * R2 == M, "two-stage plan");
     constexpr int NT = ZT * R1, W = 3 * ZT, WP = W + 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<T>* stw = reinterpret_cast<cx<T>*>(smem_raw);
@@ -407,7 +407,7 @@ __global__ void __launch_bounds__(ZT * ct_radix(M, 0, true), MINB) k_xpass2(Geom
 }
 
 template <typename T, int M, int ZT, int MINB = 1> struct XLaunch2 {
-    static constexpr int NT = ZT * ct_radix(M, 0, true);
+    static constexpr int NT = ZT * x2_radix(M, 0);
     static constexpr size_t smem = sizeof(cx<T>) * (size_t)(M + M * (3 * ZT + 1));
     static cudaError_t run(const PassArgs<T>& a) {
         const Geom& g = a.g;
