@@ -169,6 +169,22 @@ def test_mixed_inner_steps_follow_the_reference_recurrence(steps):
     assert rel(m.get_P(), om.P) <= 1e-3
 
 
+def test_mixed_residual_in_double_float_matches_the_fp64_product():
+    """The refinement's residual on the 64x64x16 lattice comes from the double-float
+    product (FP32 pairs, about 44 bits).  It equals |E - (A P + al P)| / |E| formed with
+    the FP64 product to 1e-6 of itself: the double-float error is ~1e-13 |E|."""
+    w = tdda.lattice.config(2)
+    c = tdda.AProductCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material, w.nback)
+    inc = w.incidences[0]
+    m = tdda.DDAModel(c, inc.nK, inc.E0, inc.nE0, w.diel_old)
+    info = m.solve_mixed(10000, 1e-5)
+    assert info["status"] == tdda.OK
+    E = m.get_E()
+    res64 = np.linalg.norm(E - m.Aproductwithalb(m.get_P())) / np.linalg.norm(E)
+    assert res64 <= 1e-5
+    assert abs(info["true_residual"] - res64) <= 1e-6 * res64
+
+
 def test_batch_equals_alone():
     w = tdda.lattice.config(1)
     incs = [tdda.lattice.XPOL_Z,

@@ -27,6 +27,8 @@ using tdda::AxisPlan;
 using tdda::Geom;
 using tdda::RhsVecs;
 using tdda::SolveState;
+using tdda::dd;
+using tdda::dd2;
 using cd = std::complex<double>;
 
 namespace {
@@ -159,6 +161,8 @@ struct tdda_core_s {
     int* cellmap = nullptr;
     int* Rdev = nullptr;  // 3N lattice indices
     double2* green64 = nullptr;
+    dd2* green_dd = nullptr;            // double-float copies for the residual product (on first use)
+    dd2* tw_dd[3] = {nullptr, nullptr, nullptr};
     float2* green32 = nullptr;
     double2* tw64[3] = {nullptr, nullptr, nullptr};
     float2* tw32[3] = {nullptr, nullptr, nullptr};
@@ -472,6 +476,30 @@ template <typename T> tdda_status get_iteration_graph(tdda_core* c, int n, cudaG
     return TDDA_OK;
 }
 
+// The FP64 residual r = E - (A P + al P) of the refinement: the double-float
+// product (about 44 bits, on the FP32 pipes) where its passes are compiled,
+// else the FP64 passes.  The double-float spectrum and twiddles are split from
+// the FP64 ones on first use.
+tdda_status residual_product(tdda_core* c, int n) {
+    if (tdda::dd_lengths(c->g)) {
+        if (!c->green_dd) {
+            const long long H6 = 6LL * c->g.Hx * c->g.Hy * c->g.Hz;
+            const int M[3] = {c->g.px.M, c->g.py.M, c->g.pz.M};
+            TDDA_TRY(dalloc_c(c, &c->green_dd, (size_t)H6));
+            for (int a = 0; a < 3; a++) TDDA_TRY(dalloc_c(c, &c->tw_dd[a], (size_t)M[a]));
+            TDDA_CK1(tdda::launch_to_dd(H6, c->green64, c->green_dd, c->stream));
+            for (int a = 0; a < 3; a++) TDDA_CK1(tdda::launch_to_dd(M[a], c->tw64[a], c->tw_dd[a], c->stream));
+        }
+        count_launches(5);
+        TDDA_CK1(tdda::launch_residual_dd(c->g, n, reinterpret_cast<const RhsVecs<dd>*>(c->rhs64), c->green_dd,
+                                          c->tw_dd[0], c->tw_dd[1], c->tw_dd[2], c->cellmap,
+                                          reinterpret_cast<dd2*>(c->grid64), c->stream));
+        return TDDA_OK;
+    }
+    TDDA_CK(aprod<double>(c, tdda::SRC_P, tdda::SNK_RES, n, c->rhs64));
+    return TDDA_OK;
+}
+
 // BiCGSTAB on n right-hand sides whose RhsVecs<T> and states are uploaded.
 // DDAModel.cpp:164-255.  p_zero: every P is zero, so r = E without a product.
 template <typename T> tdda_status krylov(tdda_core* c, int n, bool p_zero, int max_it) {
@@ -638,7 +666,7 @@ tdda_status solve_mixed(tdda_model* const* ms, int n, int max_it, double tol, td
             TDDA_CK1(tdda::launch_residual_is_rhs<double>(c->g, n, c->rhs64, c->stream));
         } else {
             TDDA_CK1(tdda::launch_solve_begin<double>(c->g, n, c->rhs64, c->stream));
-            TDDA_CK(aprod<double>(c, tdda::SRC_P, tdda::SNK_RES, n, c->rhs64));
+            TDDA_TRY(residual_product(c, n));
         }
         TDDA_CK(cudaMemcpyAsync(c->hst, c->st64, sizeof(SolveState) * n, cudaMemcpyDeviceToHost, c->stream));
         TDDA_CK(cudaStreamSynchronize(c->stream));

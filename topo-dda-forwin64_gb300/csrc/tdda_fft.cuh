@@ -21,6 +21,55 @@ template <typename T> struct cplx_t;
 template <> struct cplx_t<float> { typedef float2 type; };
 template <> struct cplx_t<double> { typedef double2 type; };
 
+// Double-float scalar: an unevaluated sum hi + lo of two FP32 values (about 44
+// significant bits), for products that need more than FP32 and run on the
+// FP32 pipes.  Addition is the TwoSum of the high parts with the low parts
+// added (D. E. Knuth, TAOCP vol. 2, 4.2.2; the "sloppy" double-double add of
+// Hida, Li and Bailey's QD library): its error is bounded by about 2^-44 of
+// |a| + |b|, the bound an FFT needs.  Multiplication takes the exact error of
+// hi*hi from one FMA (Dekker's product with a fused multiply-add).  Every
+// operation is rounded explicitly, so no contraction or reordering applies.
+struct dd {
+    float hi, lo;
+    __host__ __device__ dd() {}
+    __host__ __device__ constexpr dd(float h, float l) : hi(h), lo(l) {}
+    __host__ __device__ dd(double v) : hi((float)v), lo((float)(v - (double)(float)v)) {}
+    __host__ __device__ dd(int v) : dd((double)v) {}
+    __host__ __device__ operator double() const { return (double)hi + (double)lo; }
+};
+__device__ __forceinline__ dd dd_fast2sum(float a, float b) {  // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return dd(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ dd operator+(dd a, dd b) {
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bp = __fsub_rn(s, a.hi);
+    const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bp)), __fsub_rn(b.hi, bp));
+    return dd_fast2sum(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ dd operator-(dd a) { return dd(-a.hi, -a.lo); }
+__device__ __forceinline__ dd operator-(dd a, dd b) { return a + (-b); }
+__device__ __forceinline__ dd operator*(dd a, dd b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return dd_fast2sum(p, e);
+}
+__device__ __forceinline__ dd& operator+=(dd& a, dd b) { return a = a + b; }
+// complex double-float: 16 bytes, (re.hi, re.lo, im.hi, im.lo)
+struct __align__(16) dd2 {
+    dd x, y;
+    __host__ __device__ dd2() {}
+    __host__ __device__ dd2(dd re, dd im) : x(re), y(im) {}
+    __host__ __device__ dd2(double2 v) : x(v.x), y(v.y) {}
+    __host__ __device__ explicit dd2(float4 v) : x(v.x, v.y), y(v.z, v.w) {}
+    __host__ __device__ double2 to_double2() const { return make_double2((double)x, (double)y); }
+};
+template <> struct cplx_t<dd> { typedef dd2 type; };
+template <typename T> constexpr bool is_dd = false;
+template <> constexpr bool is_dd<dd> = true;
+
 template <typename T> using cx = typename cplx_t<T>::type;
 
 template <typename T> __host__ __device__ __forceinline__ cx<T> mk(T re, T im) {

@@ -131,6 +131,15 @@ template <typename T> bool pass_ct_xy(int pass, int mode, const PassArgs<T>& a, 
 template <typename T> bool pass_zy(int pass, int mode, const PassArgs<T>& a, cudaError_t* err);
 bool zy_fused(const Geom& g, bool fp32);
 cudaError_t configure_pass_zy();
+// the double-float A-product (tdda_pass_dd.cu): residual r = E - (A P + al P)
+// of the FP64 vectors of rhs (laid out as RhsVecs<double>), for the grids
+// dd_lengths() accepts
+bool dd_lengths(const Geom& g);
+cudaError_t launch_residual_dd(const Geom& g, int nrhs, const RhsVecs<dd>* rhs, const dd2* green, const dd2* twx,
+                               const dd2* twy, const dd2* twz, const int* cellmap, dd2* grid, cudaStream_t stream);
+cudaError_t configure_pass_dd();
+// dst = src split into double-float pairs
+cudaError_t launch_to_dd(long long n, const double2* src, dd2* dst, cudaStream_t stream);
 cudaError_t configure_pass_generic();
 cudaError_t configure_pass_ct_z();
 cudaError_t configure_pass_ct_xy();

@@ -397,6 +397,11 @@ __device__ __forceinline__ void model_alpha_one(double v, const AlphaParams& ap,
     inv = cdiv(make_double2(1.0, 0.0), alpha);
 }
 
+__global__ void k_to_dd(long long n, const double2* __restrict__ src, dd2* __restrict__ dst) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        dst[e] = dd2(src[e]);
+}
+
 // *flag |= 1 when an entry is neither +0 nor -0 (mode 0: A 0 = 0 exactly), or
 // when a density lies outside [0, hi) or is NaN (mode 1: the material table,
 // DDAModel.cpp:54-63).  An OR, so the result does not depend on the order.
@@ -531,6 +536,7 @@ cudaError_t configure_kernels() {
     if (e == cudaSuccess) e = configure_pass_ct_z();
     if (e == cudaSuccess) e = configure_pass_ct_xy();
     if (e == cudaSuccess) e = configure_pass_zy();
+    if (e == cudaSuccess) e = configure_pass_dd();
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute((const void*)k_fft_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxPassSmem);
     if (e == cudaSuccess)
@@ -739,6 +745,10 @@ cudaError_t launch_density_gradient(int nparam, const int* off, const int* dip, 
 cudaError_t launch_model_incident(int N, const int* R, double3 nK, double3 nE0, double E0, double K, double d,
                                   double2* E, cudaStream_t stream) {
     k_model_incident<<<grid1d(N, kNT), kNT, 0, stream>>>(N, R, nK, nE0, E0, K, d, E);
+    return cudaGetLastError();
+}
+cudaError_t launch_to_dd(long long n, const double2* src, dd2* dst, cudaStream_t stream) {
+    k_to_dd<<<std::min(grid1d(n, kNT), 152 * 8), kNT, 0, stream>>>(n, src, dst);
     return cudaGetLastError();
 }
 cudaError_t launch_to_f32(int n3, const double2* src, float2* dst, cudaStream_t stream) {

@@ -20,6 +20,26 @@ namespace dev {
 // previous step (DDAModel.cpp:226-230: u = zeta Ap, z = zeta r - alpha u,
 // P += alpha p + z, r = t - zeta At), then the new direction
 // p = r + beta (p - u) (DDAModel.cpp:219), which is returned.
+// Vector access of the pass kernels.  The double-float product reads and
+// writes the FP64 vectors (double2 in memory) and converts at the gather and
+// the scatter; the other precisions load and store their own type.
+template <typename T> __device__ __forceinline__ cx<T> ldv(const cx<T>* p, long long i) {
+    if constexpr (is_dd<T>) return dd2(reinterpret_cast<const double2*>(p)[i]);
+    else return p[i];
+}
+template <typename T> __device__ __forceinline__ void stv(cx<T>* p, long long i, cx<T> v) {
+    if constexpr (is_dd<T>) reinterpret_cast<double2*>(p)[i] = v.to_double2();
+    else p[i] = v;
+}
+template <typename T> __device__ __forceinline__ acc_t<T> cnorm2(cx<T> v) {
+    if constexpr (is_dd<T>) {
+        const double2 d = v.to_double2();
+        return d.x * d.x + d.y * d.y;
+    } else {
+        return v.x * v.x + v.y * v.y;
+    }
+}
+
 template <typename T>
 __device__ __forceinline__ cx<T> deferred_step(const RhsVecs<T>& R, long long o, cx<T> alpha, cx<T> zeta, cx<T> beta) {
     const cx<T> Ap = R.Ap[o], r = R.r[o], p = R.p[o], t = R.t[o], At = R.At[o];
@@ -140,7 +160,7 @@ __global__ void __launch_bounds__(kNT) k_zfwd(Geom g, const RhsVecs<T>* __restri
                     v[c] = csub<T>(rc, cmul<T>(alpha, ac));
                     R.t[o + c] = v[c];
                 } else {
-                    v[c] = src[o + c];
+                    v[c] = ldv<T>(src, o + c);
                 }
             }
         } else {
@@ -208,7 +228,11 @@ __device__ __forceinline__ int fold(int k, int M) { return 2 * k > M ? M - k : k
 template <typename T>
 __device__ __forceinline__ void load_green6(const cx<T>* gg, cx<T>& a0, cx<T>& a1, cx<T>& a2, cx<T>& a3, cx<T>& a4,
                                             cx<T>& a5) {
-    if constexpr (sizeof(cx<T>) == 8) {
+    if constexpr (is_dd<T>) {
+        const float4* q = reinterpret_cast<const float4*>(gg);
+        a0 = dd2(__ldg(q)); a1 = dd2(__ldg(q + 1)); a2 = dd2(__ldg(q + 2));
+        a3 = dd2(__ldg(q + 3)); a4 = dd2(__ldg(q + 4)); a5 = dd2(__ldg(q + 5));
+    } else if constexpr (sizeof(cx<T>) == 8) {
         const float4* q = reinterpret_cast<const float4*>(gg);
         const float4 u = __ldg(q), v = __ldg(q + 1), w = __ldg(q + 2);
         a0 = mk<T>(u.x, u.y); a1 = mk<T>(u.z, u.w);
@@ -470,8 +494,8 @@ __global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restri
                 R.Ap[o + c] = val;
                 continue;
             }
-            const cx<T> vv = vsrc[o + c];
-            const cx<T> w = cadd<T>(val, cmul<T>(vv, R.al[o + c]));
+            const cx<T> vv = ldv<T>(vsrc, o + c);
+            const cx<T> w = cadd<T>(val, cmul<T>(vv, ldv<T>(R.al, o + c)));
             if (SNK == SNK_ALB) {
                 R.Ap[o + c] = w;
             } else if (SNK == SNK_AP) {
@@ -494,11 +518,11 @@ __global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restri
                     acc[7] += tt.x * tt.x + tt.y * tt.y;
                 }
             } else if (SNK == SNK_RES) {
-                const cx<T> res = csub<T>(R.E[o + c], w);
-                R.r[o + c] = res;
-                R.r0[o + c] = res;
-                R.p[o + c] = res;
-                acc[0] += res.x * res.x + res.y * res.y;
+                const cx<T> res = csub<T>(ldv<T>(R.E, o + c), w);
+                stv<T>(R.r, o + c, res);
+                stv<T>(R.r0, o + c, res);
+                stv<T>(R.p, o + c, res);
+                acc[0] += cnorm2<T>(res);
             }
         }
     }
@@ -974,6 +998,15 @@ template <typename T, int CM> struct PassLaunch {
             const int LZ = z_lines<T>(Mz);
             const dim3 grid((g.Nx * g.Ny + LZ - 1) / LZ, a.nrhs);
             const size_t sm = zsmem<T>(Mz);
+            if constexpr (is_dd<T>) {  // the double-float product forms residuals only
+                if (pass == PASS_ZFWD) {
+                    k_zfwd<T, SRC_P, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid, a.slot,
+                                                                      a.prod_nblk);
+                } else {
+                    k_zinv<T, SRC_P, SNK_RES, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid);
+                }
+                return cudaGetLastError();
+            }
             if (pass == PASS_ZFWD) {
                 switch (mode) {
                     case SRC_IN: k_zfwd<T, SRC_IN, CM><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twz, a.cellmap, a.grid, a.slot, a.prod_nblk); break;
@@ -1023,6 +1056,10 @@ template <typename T, int CM> struct PassLaunch {
         return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxPassSmem);
     }
     static cudaError_t configure_z() {
+        if constexpr (is_dd<T>) {
+            cudaError_t e = set_attr((const void*)k_zfwd<T, SRC_P, CM>);
+            return e != cudaSuccess ? e : set_attr((const void*)k_zinv<T, SRC_P, SNK_RES, CM>);
+        }
         const void* ks[] = {(const void*)k_zfwd<T, SRC_IN, CM>, (const void*)k_zfwd<T, SRC_PUPD, CM>,
                             (const void*)k_zfwd<T, SRC_TUPD, CM>, (const void*)k_zfwd<T, SRC_P, CM>,
                             (const void*)k_zfwd<T, SRC_PUPD_DEF, CM>, (const void*)k_zinv<T, SRC_TUPD, SNK_AT_DEF, CM>,
