@@ -242,6 +242,37 @@ tdda_status configure_once(int device) {
     return TDDA_OK;
 }
 
+// Small pinned host buffers (solve states, flags) come from a process-wide
+// free list by size class and go back to it: freeing pinned memory
+// synchronises the whole device, so a core destroyed while other streams run
+// solves would wait for all of their queued work.
+std::mutex g_pin_mu;
+std::vector<std::pair<size_t, void*>> g_pin_free;
+size_t pin_class(size_t bytes) {
+    size_t c = 256;
+    while (c < bytes) c *= 2;
+    return c;
+}
+cudaError_t pinned_get(void** p, size_t bytes) {
+    const size_t cls = pin_class(bytes);
+    {
+        std::lock_guard<std::mutex> lk(g_pin_mu);
+        for (size_t i = 0; i < g_pin_free.size(); i++) {
+            if (g_pin_free[i].first == cls) {
+                *p = g_pin_free[i].second;
+                g_pin_free.erase(g_pin_free.begin() + (long)i);
+                return cudaSuccess;
+            }
+        }
+    }
+    return cudaMallocHost(p, cls);
+}
+void pinned_put(void* p, size_t bytes) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lk(g_pin_mu);
+    g_pin_free.emplace_back(pin_class(bytes), p);
+}
+
 // keep freed pool memory cached for reuse instead of returning it to the
 // driver at every synchronisation (once per device)
 std::mutex g_pool_mu;
@@ -520,12 +551,18 @@ template <typename T> tdda_status krylov(tdda_core* c, int n, bool p_zero, int m
     }
     cudaGraphExec_t ex;
     TDDA_TRY(get_iteration_graph<T>(c, n, &ex));
-    if constexpr (kDeferred<T>) {  // the device-side loop runs the whole inner solve
-        TDDA_CK(cudaGraphLaunch(ex, c->stream));
-        TDDA_CK1(tdda::launch_finish<T>(c->g, n, rhs, c->stream));  // the last step's update
-        TDDA_CK(cudaMemcpyAsync(c->hst, Prec<T>::st(c), sizeof(SolveState) * n, cudaMemcpyDeviceToHost, c->stream));
-        TDDA_CK(cudaStreamSynchronize(c->stream));
+    if constexpr (kDeferred<T>) {  // device-side loop, up to kLoopChunks chunks per launch
+        for (;;) {
+            TDDA_CK(cudaGraphLaunch(ex, c->stream));
+            TDDA_CK(cudaMemcpyAsync(c->hst, Prec<T>::st(c), sizeof(SolveState) * n, cudaMemcpyDeviceToHost,
+                                    c->stream));
+            TDDA_CK(cudaStreamSynchronize(c->stream));
+            bool running = false;
+            for (int i = 0; i < n; i++) running |= c->hst[i].status == tdda::ST_RUNNING;
+            if (!running || c->hst[0].chunks >= c->hst[0].chunk_limit) break;
+        }
         count_launches(c->hst[0].chunks * chunk_kernels<T>(c));
+        TDDA_CK1(tdda::launch_finish<T>(c->g, n, rhs, c->stream));  // the last step's update
         return TDDA_OK;
     }
     int done_it = 0;
@@ -1014,9 +1051,9 @@ tdda_status core_create(const tdda_core_desc* desc, const tdda::PeriodicImages* 
     TDDA_CORE_TRY(dalloc_c(c, &c->st32, (size_t)c->max_rhs));
     TDDA_CORE_TRY(dalloc_c(c, &c->part, (size_t)c->max_rhs * tdda::kPartSlots * c->maxblk));
     TDDA_CORE_TRY(dalloc_c(c, &c->cnt, (size_t)c->max_rhs * tdda::kCounters));
-    TDDA_CORE_CK(cudaMallocHost((void**)&c->hst, sizeof(SolveState) * c->max_rhs));
+    TDDA_CORE_CK(pinned_get((void**)&c->hst, sizeof(SolveState) * c->max_rhs));
     TDDA_CORE_TRY(dalloc_c(c, &c->flag, 1));
-    TDDA_CORE_CK(cudaMallocHost((void**)&c->hflag, sizeof(unsigned int)));
+    TDDA_CORE_CK(pinned_get((void**)&c->hflag, sizeof(unsigned int)));
     TDDA_CORE_CK(cudaMemsetAsync(c->cnt, 0, sizeof(unsigned int) * c->max_rhs * tdda::kCounters, c->stream));
     TDDA_CORE_CK(cudaMemcpyAsync(c->cellmap, cellmap.data(), sizeof(int) * cellmap.size(), cudaMemcpyHostToDevice,
                                  c->stream));
@@ -1074,8 +1111,8 @@ tdda_status tdda_core_destroy(tdda_core* c) {
         if (e) cudaGraphExecDestroy(e);
     free_all(c->allocs, c->stream);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    if (c->hst) cudaFreeHost(c->hst);
-    if (c->hflag) cudaFreeHost(c->hflag);
+    pinned_put(c->hst, sizeof(SolveState) * c->max_rhs);
+    pinned_put(c->hflag, sizeof(unsigned int));
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return TDDA_OK;

@@ -182,11 +182,16 @@ cudaError_t launch_aproduct(const Geom& g, int src, int snk, int nrhs, const Rhs
 // blocks of the last pass of an A-product at precision T (the producer of the
 // dot-product partials)
 template <typename T> int sink_blocks(const Geom& g);
+// chunks of FP32 steps one launch of the device-side loop runs at most.  A
+// bounded launch keeps the host in the loop now and then: while a device-side
+// loop runs, driver operations of other streams on the GPU (graph
+// instantiation and destruction, module loads) can wait for it.
+constexpr int kLoopChunks = 8;
 // FP32 deferred step, end of a chunk of steps inside the device-side loop: one
 // block forms the step end of every right-hand side for the step of parity
 // `slot` (the computation the next gather repeats), counts the chunk and sets
-// the loop's condition: another chunk while a right-hand side is running and
-// fewer than chunk_limit chunks have run.
+// the loop's condition: another chunk while a right-hand side is running, fewer
+// than chunk_limit chunks have run, and this launch has not run kLoopChunks.
 cudaError_t launch_chunk_end(const Geom& g, int nrhs, const RhsVecs<float>* rhs, int slot,
                              cudaGraphConditionalHandle loop, cudaStream_t stream);
 

@@ -144,7 +144,10 @@ __global__ void __launch_bounds__(kNT) k_chunk_end(const RhsVecs<float>* __restr
         SolveState* st0 = rhs[0].st;
         const int chunks = st0->chunks + 1;
         st0->chunks = chunks;
-        cudaGraphSetConditional(loop, (s_running && chunks < st0->chunk_limit) ? 1u : 0u);
+        // another chunk inside this launch, unless the launch has run its
+        // kLoopChunks (the host then reads the states and launches again)
+        const bool more = s_running && chunks < st0->chunk_limit && chunks % kLoopChunks != 0;
+        cudaGraphSetConditional(loop, more ? 1u : 0u);
     }
 }
 
