@@ -7,8 +7,9 @@ Workload (one step = one converged solve): the mixed-precision single-solve latt
 seeded then 3x3x3 box filtered, eps_m = 6.25+0.05i, x-polarised plane wave along +z,
 LDR polarisability, BiCGSTAB to |r|/|E| <= 1e-5.  Data are seeded synthetic (no dataset).
 
-ours       FP32 FFT convolution + Krylov vectors, FP64 dots / scalars, FP64 residual
-           with iterative refinement (value); the plain FP64 solve of the same lattice is
+ours       FP32 FFT convolution + Krylov vectors, double-float dot sums, the residual of
+           the FP64 vectors from a double-float (~44-bit) product, iterative refinement
+           (value); the plain FP64 solve of the same lattice is
            timed beside it (fp64).  Inputs are resident in HBM in the device-timed region;
            `e2e` is the same solve through the C ABI with host buffers.
 reference  the reference's solve path run on the host cores (the oracle port of

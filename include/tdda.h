@@ -42,8 +42,10 @@ typedef enum tdda_method { TDDA_METHOD_LDR = 0, TDDA_METHOD_FCD = 1 } tdda_metho
 typedef enum tdda_memory { TDDA_MEM_HOST = 0, TDDA_MEM_DEVICE = 1 } tdda_memory;
 typedef enum tdda_precision {
     TDDA_FP64 = 0,       /* complex128 FFT convolution and Krylov vectors */
-    TDDA_FP32_REFINE = 1 /* complex64 FFT and Krylov vectors, FP64 dots, scalars and an outer
-                            FP64 residual with iterative refinement */
+    TDDA_FP32_REFINE = 1 /* complex64 FFT and Krylov vectors, double-float dot sums, and an
+                            outer residual of the FP64 vectors (double-float product, ~44 bits,
+                            on the compiled grids; FP64 product elsewhere) with iterative
+                            refinement */
 } tdda_precision;
 typedef enum tdda_field {
     TDDA_FIELD_P = 0,
