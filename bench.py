@@ -148,7 +148,7 @@ def measured_peaks() -> dict:
 def pass_bytes(grid, Nx, Ny, Nz, N, s, fused=False):
     """Algorithmic bytes of the five A-product passes for one right-hand side.
 
-    Pass model of the survey's canonical count, on the grid (Mx, My, Mz) actually used:
+    The canonical pass model, on the grid (Mx, My, Mz) actually used:
     the z-forward pass reads the 3N vector and writes 3 Nx Ny Mz grid entries, the
     y-forward pass reads those and writes 3 Nx My Mz, the x pass reads and writes
     3 Nx My Mz and reads the six Green components on the full grid (6 Mx My Mz,
