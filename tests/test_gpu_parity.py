@@ -185,6 +185,49 @@ def test_mixed_residual_in_double_float_matches_the_fp64_product():
     assert abs(info["true_residual"] - res64) <= 1e-6 * res64
 
 
+def test_mixed_solve_on_a_lattice_with_holes_uses_the_double_float_residual():
+    """A sphere of dipoles inside a 20x20x10 box (grid 40x40x20, a double-float grid): the
+    gather and scatter go through the cell map.  The refined solve reaches tol by the
+    oracle's FP64 product, and its reported residual equals that product's."""
+    Nx, Ny, Nz = 20, 20, 10
+    x, y, z = np.meshgrid(np.arange(Nx), np.arange(Ny), np.arange(Nz), indexing="ij")
+    keep = ((x - 9.5) / 9.5) ** 2 + ((y - 9.5) / 9.5) ** 2 + ((z - 4.5) / 4.5) ** 2 <= 1.0
+    R = np.stack([x[keep], y[keep], z[keep]], axis=1).astype(np.int32).ravel()
+    N = R.size // 3
+    rho = np.repeat(np.random.Generator(np.random.PCG64(11)).random(N), 3)
+    mat = np.array([1.0, 4.0 + 0.1j])
+    c = tdda.AProductCore(Nx, Ny, Nz, R, 10.0, 500.0, mat)
+    assert tuple(c.grid) == (40, 40, 20)
+    m = tdda.DDAModel(c, (0.0, 0.0, 1.0), 1.0, (1.0, 0.0, 0.0), rho)
+    info = m.solve_mixed(10000, 1e-5)
+    assert info["status"] == tdda.OK
+    oc = O.OracleCore(Nx, Ny, Nz, R, 10.0, 500.0, mat, grid=c.grid)
+    om = O.OracleModel(oc, (0.0, 0.0, 1.0), 1.0, (1.0, 0.0, 0.0), rho)
+    E = om.E
+    res = np.linalg.norm(E - om.Aproductwithalb(m.get_P())) / np.linalg.norm(E)
+    assert res <= 1e-5
+    assert abs(info["true_residual"] - res) <= 1e-6 * res
+
+
+def test_host_launched_chunks_equal_the_device_side_loop(monkeypatch):
+    """TDDA_DEVICE_LOOP=0 (cores created while it is set) launches each 4-step chunk from the
+    host instead of the conditional graph node: the same kernels in the same order, so P and
+    the step counts are bit-identical."""
+    w = tdda.lattice.config(1)
+    out = []
+    for mode in ("1", "0"):
+        monkeypatch.setenv("TDDA_DEVICE_LOOP", mode)
+        c = tdda.AProductCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material, max_rhs=2)
+        ms = [tdda.DDAModel(c, inc.nK, 1.0, inc.nE0, w.diel_old)
+              for inc in (tdda.lattice.XPOL_Z,
+                          tdda.lattice.Incidence(np.array([0.0, 0.0, 1.0]), np.array([0.0, 1.0, 0.0])))]
+        infos = tdda.solve_batch(ms, tdda.FP32_REFINE, 10000, 1e-5)
+        out.append(([m.get_P() for m in ms], [i["inner_iterations"] for i in infos]))
+    assert out[0][1] == out[1][1]
+    for a, b in zip(out[0][0], out[1][0]):
+        assert np.array_equal(a, b)
+
+
 def test_batch_equals_alone():
     w = tdda.lattice.config(1)
     incs = [tdda.lattice.XPOL_Z,

@@ -16,6 +16,7 @@
 #include <complex>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -161,6 +162,10 @@ struct tdda_core_s {
     int* cellmap = nullptr;
     int* Rdev = nullptr;  // 3N lattice indices
     double2* green64 = nullptr;
+    // FP32 inner solve as a device-side loop (conditional graph node); TDDA_DEVICE_LOOP=0 in the
+    // environment makes the host launch each chunk instead (profilers see the kernels of a
+    // host-launched graph, not those of a device-side loop's body)
+    bool device_loop = true;
     dd2* green_dd = nullptr;            // double-float copies for the residual product (on first use)
     dd2* tw_dd[3] = {nullptr, nullptr, nullptr};
     float2* green32 = nullptr;
@@ -447,12 +452,13 @@ template <typename T> cudaError_t enqueue_iteration(tdda_core* c, int n, int slo
 
 // kChunk steps (parities 0, 1, 0, 1 ...); FP32 ends the chunk with the step
 // end for the next step (parity 0) and the condition of the device-side loop
-template <typename T> cudaError_t enqueue_chunk(tdda_core* c, int n, cudaGraphConditionalHandle loop) {
+template <typename T>
+cudaError_t enqueue_chunk(tdda_core* c, int n, cudaGraphConditionalHandle loop, bool in_loop) {
     for (int k = 0; k < kChunk; k++) {
         cudaError_t e = enqueue_iteration<T>(c, n, k & 1);
         if (e != cudaSuccess) return e;
     }
-    if constexpr (kDeferred<T>) return tdda::launch_chunk_end(c->g, n, Prec<T>::rhs(c), 0, loop, c->stream);
+    if constexpr (kDeferred<T>) return tdda::launch_chunk_end(c->g, n, Prec<T>::rhs(c), 0, loop, in_loop, c->stream);
     return cudaSuccess;
 }
 template <typename T> int chunk_kernels(const tdda_core* c) { return kChunk * step_kernels<T>(c) + (kDeferred<T> ? 1 : 0); }
@@ -466,7 +472,7 @@ template <typename T> tdda_status get_iteration_graph(tdda_core* c, int n, cudaG
     if (!ex) {
         cudaGraph_t gr = nullptr;
         cudaError_t e = cudaSuccess, e2 = cudaSuccess;
-        if constexpr (kDeferred<T>) {
+        if (kDeferred<T> && c->device_loop) {
             TDDA_CK(cudaGraphCreate(&gr, 0));
             cudaGraphConditionalHandle loop = 0;
             e = cudaGraphConditionalHandleCreate(&loop, gr, 1, cudaGraphCondAssignDefault);
@@ -484,14 +490,14 @@ template <typename T> tdda_status get_iteration_graph(tdda_core* c, int n, cudaG
             cudaGraph_t body = cp.conditional.phGraph_out[0];
             TDDA_CK(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
             t_capturing = true;
-            e = enqueue_chunk<T>(c, n, loop);
+            e = enqueue_chunk<T>(c, n, loop, true);
             t_capturing = false;
             cudaGraph_t captured = nullptr;
             e2 = cudaStreamEndCapture(c->stream, &captured);
         } else {
             TDDA_CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
             t_capturing = true;
-            e = enqueue_chunk<T>(c, n, 0);
+            e = enqueue_chunk<T>(c, n, 0, false);
             t_capturing = false;
             e2 = cudaStreamEndCapture(c->stream, &gr);
         }
@@ -551,7 +557,7 @@ template <typename T> tdda_status krylov(tdda_core* c, int n, bool p_zero, int m
     }
     cudaGraphExec_t ex;
     TDDA_TRY(get_iteration_graph<T>(c, n, &ex));
-    if constexpr (kDeferred<T>) {  // device-side loop, up to kLoopChunks chunks per launch
+    if constexpr (kDeferred<T>) {  // device-side loop, up to kLoopChunks chunks per launch (else one)
         for (;;) {
             TDDA_CK(cudaGraphLaunch(ex, c->stream));
             TDDA_CK(cudaMemcpyAsync(c->hst, Prec<T>::st(c), sizeof(SolveState) * n, cudaMemcpyDeviceToHost,
@@ -1027,6 +1033,10 @@ tdda_status core_create(const tdda_core_desc* desc, const tdda::PeriodicImages* 
     } while (0)
 
     TDDA_CORE_CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    {
+        const char* v = std::getenv("TDDA_DEVICE_LOOP");
+        c->device_loop = !(v && v[0] == '0');
+    }
     const size_t n3 = 3 * (size_t)g.N;
     const long long H6 = 6LL * g.Hx * g.Hy * g.Hz;
     const long long Mfull = (long long)g.px.M * g.py.M * g.pz.M;

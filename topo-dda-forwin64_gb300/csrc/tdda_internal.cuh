@@ -192,8 +192,10 @@ constexpr int kLoopChunks = 8;
 // `slot` (the computation the next gather repeats), counts the chunk and sets
 // the loop's condition: another chunk while a right-hand side is running, fewer
 // than chunk_limit chunks have run, and this launch has not run kLoopChunks.
+// in_loop: launched inside the conditional node of the device-side loop (else
+// the host launches each chunk and the condition is not set)
 cudaError_t launch_chunk_end(const Geom& g, int nrhs, const RhsVecs<float>* rhs, int slot,
-                             cudaGraphConditionalHandle loop, cudaStream_t stream);
+                             cudaGraphConditionalHandle loop, bool in_loop, cudaStream_t stream);
 
 // u = zeta Ap; z = zeta r - alpha u; P += alpha p + z; r = t - zeta At;
 // rho_prev = rho; rho = r0.r; convergence / breakdown / iteration limit;

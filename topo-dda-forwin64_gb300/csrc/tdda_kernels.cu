@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(kNT) k_solve_begin(int n3, const RhsVecs<T>* _
 // every block of the next gather repeats, so the state the host reads after
 // the loop is current), then the condition of the device-side loop.  One block.
 __global__ void __launch_bounds__(kNT) k_chunk_end(const RhsVecs<float>* __restrict__ rhs, int nrhs, int slot,
-                                                   int prod_nblk, cudaGraphConditionalHandle loop) {
+                                                   int prod_nblk, cudaGraphConditionalHandle loop, int in_loop) {
     __shared__ float2 sred[8];
     __shared__ int s_running;
     if (threadIdx.x == 0) s_running = 0;
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(kNT) k_chunk_end(const RhsVecs<float>* __restr
         // another chunk inside this launch, unless the launch has run its
         // kLoopChunks (the host then reads the states and launches again)
         const bool more = s_running && chunks < st0->chunk_limit && chunks % kLoopChunks != 0;
-        cudaGraphSetConditional(loop, more ? 1u : 0u);
+        if (in_loop) cudaGraphSetConditional(loop, more ? 1u : 0u);
     }
 }
 
@@ -661,8 +661,8 @@ template <typename T> int sink_blocks(const Geom& g) {
 }
 
 cudaError_t launch_chunk_end(const Geom& g, int nrhs, const RhsVecs<float>* rhs, int slot,
-                             cudaGraphConditionalHandle loop, cudaStream_t stream) {
-    k_chunk_end<<<1, kNT, 0, stream>>>(rhs, nrhs, slot, sink_blocks<float>(g), loop);
+                             cudaGraphConditionalHandle loop, bool in_loop, cudaStream_t stream) {
+    k_chunk_end<<<1, kNT, 0, stream>>>(rhs, nrhs, slot, sink_blocks<float>(g), loop, in_loop ? 1 : 0);
     return cudaGetLastError();
 }
 
