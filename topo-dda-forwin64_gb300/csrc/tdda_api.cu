@@ -740,10 +740,12 @@ tdda_status solve_mixed(tdda_model* const* ms, int n, int max_it, double tol, td
         }
         if (!open) break;
         // FP32 correction: A d = r, d0 = 0, to a relative tolerance that brings
-        // the true residual under tol with margin
+        // the true residual under tol with margin (0.8 tol: the FP32 recurrence
+        // residual tracks the true one to ~1e-8 of |E| at these tolerances; the
+        // outer check catches the rest)
         for (int i = 0; i < n; i++) {
             tdda_model* m = ms[i];
-            double tin = std::min(0.5, std::max(2e-6, 0.5 * tol / std::max(res[i], 1e-300)));
+            double tin = std::min(0.5, std::max(2e-6, 0.8 * tol / std::max(res[i], 1e-300)));
             c->hst[i] = fresh_state(tin, max_it - inner[i], 0);
             if (done[i]) {
                 c->hst[i].status = tdda::ST_CONVERGED;
