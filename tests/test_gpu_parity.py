@@ -97,6 +97,28 @@ def test_aproduct_config_shapes_against_oracle():
         assert rel(c.Aproduct(b, precision=tdda.FP32_REFINE), y) <= 1e-5
 
 
+@pytest.mark.parametrize("box,grid", [((16, 24, 32), (32, 48, 64)), ((40, 48, 28), (80, 96, 64)),
+                                      ((110, 10, 10), (256, 20, 20)), ((30, 60, 12), (64, 128, 24))])
+def test_rounded_up_lengths_against_oracle(box, grid):
+    """Axes rounded up to the further compiled lengths (32, 48, 64, 80, 96, 256; z 64):
+    products in both precisions against the oracle on the same grid, and a refined solve."""
+    Nx, Ny, Nz = box
+    R = tdda.lattice.bulk(Nx, Ny, Nz)
+    mat = np.array([1.0, 4.0 + 0.1j])
+    c = tdda.AProductCore(Nx, Ny, Nz, R, 8.0, 550.0, mat)
+    assert tuple(c.grid) == grid
+    oc = O.OracleCore(Nx, Ny, Nz, R, 8.0, 550.0, mat, grid=c.grid, pruned=True)
+    rng = np.random.Generator(np.random.PCG64(sum(box)))
+    b = rng.standard_normal(R.size) + 1j * rng.standard_normal(R.size)
+    y = oc.Aproduct(b)
+    assert rel(c.Aproduct(b), y) <= 1e-12
+    assert rel(c.Aproduct(b, precision=tdda.FP32_REFINE), y) <= 1e-5
+    rho = np.repeat(rng.random(R.size // 3), 3)
+    m = tdda.DDAModel(c, (0.0, 0.0, 1.0), 1.0, (1.0, 0.0, 0.0), rho)
+    info = m.solve_mixed(10000, 1e-5)
+    assert info["status"] == tdda.OK and info["true_residual"] <= 1e-5
+
+
 def _model(g, core):
     m = tdda.DDAModel(core, g["nK"], float(g["E0"]), g["nE0"], g["diel_old"])
     if "P0" in g:

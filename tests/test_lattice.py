@@ -39,3 +39,14 @@ def test_configs_are_seeded_and_in_range():
     assert len(lattice.config(3).incidences) == 8
     w4 = lattice.config(4).rho.reshape(80, 80, 20)
     assert np.allclose(w4, w4[::-1, :, :]) and np.allclose(w4, w4[:, ::-1, :])
+
+
+def test_fft_lengths_round_up_to_compiled_lengths():
+    """The core's axis lengths: the compiled length when it costs at most 25% more points."""
+    assert [lattice.fft_length(n, False) for n in (20, 64, 80, 96)] == [40, 128, 160, 192]
+    assert [lattice.fft_length(n, True) for n in (10, 16, 20, 24)] == [20, 32, 40, 48]
+    assert lattice.fft_length(32, True) == 64        # 63 -> 64
+    assert lattice.fft_length(18, False) == 40       # 35 -> 40
+    assert lattice.fft_length(50, False) == 100      # 99 -> 100: 128 is 28% more
+    assert lattice.fft_length(110, False) == 256     # 219 -> 224 -> 256
+    assert lattice.fft_length(6, False) == 12 and lattice.fft_length(4, True) == 7

@@ -83,6 +83,20 @@ int smooth_size(int n) {
     while (!smooth7(m)) m++;
     return m;
 }
+// FFT length of an axis of N cells: the smallest 7-smooth length >= 2N - 1,
+// or the next length with compiled passes when that holds at most 25% more
+// points.  Any length >= 2N - 1 gives the same linear convolution
+// (AProductCore.cpp:41-43 uses 2N - 1).
+int fft_length(int N, bool z_axis) {
+    static const int kZ[] = {20, 32, 40, 48, 64};
+    static const int kXY[] = {32, 40, 48, 64, 80, 96, 128, 160, 192, 256};
+    const int m = smooth_size(2 * N - 1);
+    const int* f = z_axis ? kZ : kXY;
+    const int nf = z_axis ? 5 : 10;
+    for (int k = 0; k < nf; k++)
+        if (f[k] >= m) return 4 * f[k] <= 5 * m ? f[k] : m;
+    return m;
+}
 
 // radix plan: 8s and 4s (no lone 2 unless the power of two is 2), then 3, 5, 7
 bool make_plan(int M, AxisPlan* ap) {
@@ -991,9 +1005,8 @@ tdda_status core_create(const tdda_core_desc* desc, const tdda::PeriodicImages* 
     }
     g.dense = 1;
     for (size_t k = 0; k < cellmap.size() && g.dense; k++) g.dense = cellmap[k] == (int)k;
-    // FFT length per axis: smallest 7-smooth >= 2N-1 (the reference's
-    // 2N-1, AProductCore.cpp:41-43, gives the same linear convolution)
-    int Ms[3] = {smooth_size(2 * g.Nx - 1), smooth_size(2 * g.Ny - 1), smooth_size(2 * g.Nz - 1)};
+    // FFT length per axis (fft_length)
+    int Ms[3] = {fft_length(g.Nx, false), fft_length(g.Ny, false), fft_length(g.Nz, true)};
     AxisPlan* plans[3] = {&g.px, &g.py, &g.pz};
     for (int a = 0; a < 3; a++) {
         if (!make_plan(Ms[a], plans[a])) {
@@ -1652,7 +1665,7 @@ tdda_status tdda_aproduct_noalloc(tdda_core* c, const double* b, double* y) {
 
 double tdda_request_bytes(int Nx, int Ny, int Nz, int N, int nrhs, int precision) {
     if (Nx < 1 || Ny < 1 || Nz < 1 || N < 1 || nrhs < 1) return 0.0;
-    const double Mx = smooth_size(2 * Nx - 1), My = smooth_size(2 * Ny - 1), Mz = smooth_size(2 * Nz - 1);
+    const double Mx = fft_length(Nx, false), My = fft_length(Ny, false), Mz = fft_length(Nz, true);
     const double H = (Mx / 2 + 1) * (My / 2 + 1) * (Mz / 2 + 1);
     const double n3 = 3.0 * N;
     const double grid = 3.0 * Nx * My * Mz * nrhs;  // FFT work grid entries

@@ -353,6 +353,7 @@ template <int SIGN, typename T> struct BflyIn<8, SIGN, T, 4> : Bfly8<SIGN, T, 2>
 template <int SIGN, typename T> struct BflyIn<16, SIGN, T, 8> : BflyComp<4, 4, SIGN, T, 2> {};
 template <int SIGN, typename T> struct Bfly<24, SIGN, T> : BflyComp<8, 3, SIGN, T> {};
 template <int SIGN, typename T> struct BflyIn<24, SIGN, T, 12> : BflyComp<8, 3, SIGN, T, 4> {};
+template <int SIGN, typename T> struct BflyIn<12, SIGN, T, 6> : BflyComp<4, 3, SIGN, T, 2> {};
 template <int SIGN, typename T> struct Bfly<12, SIGN, T> : BflyComp<4, 3, SIGN, T> {};
 template <int SIGN, typename T> struct Bfly<10, SIGN, T> : BflyComp<2, 5, SIGN, T> {};
 

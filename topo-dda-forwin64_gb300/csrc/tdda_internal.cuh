@@ -148,6 +148,11 @@ bool ct_has_z(int Mz);
 bool ct_has_xy(int M);
 // FFT x lengths whose FP32 x pass is the register form (k_xpass2)
 bool xpass2_length(int M);
+// the further x / y lengths of tdda_pass_xy2.cu
+template <typename T> bool pass_ct_xy2(int pass, int mode, const PassArgs<T>& a, cudaError_t* err);
+bool ct_has_xy2(int M);
+bool xpass2_length2(int M);
+cudaError_t configure_pass_ct_xy2();
 constexpr size_t kMaxPassSmem = 200 * 1024;
 
 // -------------------------------------------------------------- launchers

@@ -538,6 +538,7 @@ cudaError_t configure_kernels() {
     cudaError_t e = configure_pass_generic();
     if (e == cudaSuccess) e = configure_pass_ct_z();
     if (e == cudaSuccess) e = configure_pass_ct_xy();
+    if (e == cudaSuccess) e = configure_pass_ct_xy2();
     if (e == cudaSuccess) e = configure_pass_zy();
     if (e == cudaSuccess) e = configure_pass_dd();
     if (e == cudaSuccess)
@@ -646,7 +647,8 @@ cudaError_t launch_aproduct(const Geom& g, int src, int snk, int nrhs, const Rhs
     for (int k = 0; k < 5; k++) {
         if (ev) cudaEventRecord(ev[k], stream);
         cudaError_t err = cudaSuccess;
-        const bool done = pass_ct_z<T>(passes[k], modes[k], a, &err) || pass_ct_xy<T>(passes[k], modes[k], a, &err);
+        const bool done = pass_ct_z<T>(passes[k], modes[k], a, &err) || pass_ct_xy<T>(passes[k], modes[k], a, &err) ||
+                          pass_ct_xy2<T>(passes[k], modes[k], a, &err);
         if (!done) err = pass_generic<T>(passes[k], modes[k], a);
         if (err != cudaSuccess) return err;
     }

@@ -5,7 +5,7 @@
 namespace tdda {
 
 bool ct_has_xy(int M) { return M == 40 || M == 128 || M == 160 || M == 192; }
-bool xpass2_length(int M) { return ct_has_xy(M); }
+bool xpass2_length(int M) { return ct_has_xy(M) || xpass2_length2(M); }
 
 // z-columns per block of the register-form x pass (k_xpass2), per length
 template <int M> constexpr int xpass2_tile() { return M == 128 ? 16 : 8; }

@@ -1,0 +1,76 @@
+// tdda_pass_xy2.cu -- y and x passes compiled for the further x / y FFT lengths
+// a core rounds its axes up to (32, 48, 64, 80, 96, 256; the lattices of a
+// served request stream), beside tdda_pass_xy.cu's lengths of the common
+// lattices.  FP32 x passes take the register form on the two-stage plans
+// (not 256, whose 16 x 16 spectra would not fit the registers).
+#include "tdda_passes.cuh"
+
+namespace tdda {
+
+bool ct_has_xy2(int M) { return M == 32 || M == 48 || M == 64 || M == 80 || M == 96 || M == 256; }
+bool xpass2_length2(int M) { return M == 32 || M == 48 || M == 64 || M == 80 || M == 96; }
+
+namespace {
+constexpr int kTile2 = 8;  // z-columns per block of the register form
+// blocks per SM the register form is compiled for: 16 warps (128 registers a thread)
+template <int M> constexpr int minb2() { return 16 * 32 / (kTile2 * x2_radix(M, 0)) > 0 ? 16 * 32 / (kTile2 * x2_radix(M, 0)) : 1; }
+}  // namespace
+
+template <typename T> bool pass_ct_xy2(int pass, int mode, const PassArgs<T>& a, cudaError_t* err) {
+    (void)mode;
+    const bool y = pass == PASS_YFWD || pass == PASS_YINV;
+    if (!y && pass != PASS_XPASS) return false;
+    if constexpr (sizeof(T) == 4) {
+        if (!y) {
+            switch (a.g.px.M) {
+#define TDDA_X2(M)                                                         \
+    case M: *err = dev::XLaunch2<T, M, kTile2, minb2<M>()>::run(a); return true;
+                TDDA_X2(32)
+                TDDA_X2(48)
+                TDDA_X2(64)
+                TDDA_X2(80)
+                TDDA_X2(96)
+#undef TDDA_X2
+                default: break;
+            }
+        }
+    }
+    switch (y ? a.g.py.M : a.g.px.M) {
+#define TDDA_XY(M)                                                                                      \
+    case M:                                                                                             \
+        *err = y ? dev::PassLaunch<T, M>::run_y(pass, a) : dev::PassLaunch<T, M>::run_x(a);              \
+        return true;
+        TDDA_XY(32)
+        TDDA_XY(48)
+        TDDA_XY(64)
+        TDDA_XY(80)
+        TDDA_XY(96)
+        TDDA_XY(256)
+#undef TDDA_XY
+        default: return false;
+    }
+}
+template bool pass_ct_xy2<float>(int, int, const PassArgs<float>&, cudaError_t*);
+template bool pass_ct_xy2<double>(int, int, const PassArgs<double>&, cudaError_t*);
+
+cudaError_t configure_pass_ct_xy2() {
+    cudaError_t e = cudaSuccess;
+#define TDDA_CFG(M)                                                                   \
+    if (!e) e = dev::PassLaunch<float, M>::configure_xy();                            \
+    if (!e) e = dev::PassLaunch<double, M>::configure_xy();
+    TDDA_CFG(32)
+    TDDA_CFG(48)
+    TDDA_CFG(64)
+    TDDA_CFG(80)
+    TDDA_CFG(96)
+    TDDA_CFG(256)
+#undef TDDA_CFG
+    if (!e) e = dev::XLaunch2<float, 32, kTile2, minb2<32>()>::configure();
+    if (!e) e = dev::XLaunch2<float, 48, kTile2, minb2<48>()>::configure();
+    if (!e) e = dev::XLaunch2<float, 64, kTile2, minb2<64>()>::configure();
+    if (!e) e = dev::XLaunch2<float, 80, kTile2, minb2<80>()>::configure();
+    if (!e) e = dev::XLaunch2<float, 96, kTile2, minb2<96>()>::configure();
+    return e;
+}
+
+}  // namespace tdda

@@ -38,6 +38,20 @@ def smooth_size(n: int) -> int:
         m += 1
 
 
+FAST_Z = (20, 32, 40, 48, 64)
+FAST_XY = (32, 40, 48, 64, 80, 96, 128, 160, 192, 256)
+
+
+def fft_length(n: int, z_axis: bool) -> int:
+    """FFT length a core uses for an axis of n cells: smooth_size(2n-1), or the next length
+    with compiled passes (FAST_Z / FAST_XY) when that holds at most 25% more points."""
+    m = smooth_size(2 * n - 1)
+    for f in (FAST_Z if z_axis else FAST_XY):
+        if f >= m:
+            return f if 4 * f <= 5 * m else m
+    return m
+
+
 def n_e_perp_in_xz(theta: float, phi: float = 0.0) -> np.ndarray:
     """Unit polarisation perpendicular to k in the xz-plane (tools.cpp:686-704)."""
     tmp = math.cos(theta) / math.sqrt(math.sin(theta) ** 2 * math.cos(phi) ** 2 + math.cos(theta) ** 2)
