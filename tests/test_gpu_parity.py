@@ -97,10 +97,12 @@ def test_aproduct_config_shapes_against_oracle():
         assert rel(c.Aproduct(b, precision=tdda.FP32_REFINE), y) <= 1e-5
 
 
-@pytest.mark.parametrize("box,grid", [((16, 24, 32), (32, 48, 64)), ((40, 48, 28), (80, 96, 64)),
-                                      ((110, 10, 10), (256, 20, 20)), ((30, 60, 12), (64, 128, 24))])
+@pytest.mark.parametrize("box,grid", [((16, 24, 32), (32, 48, 64)), ((40, 48, 28), (80, 96, 56)),
+                                      ((120, 10, 10), (256, 20, 20)), ((30, 60, 12), (64, 128, 24)),
+                                      ((25, 50, 25), (56, 112, 56)), ((100, 8, 8), (224, 15, 15))])
 def test_rounded_up_lengths_against_oracle(box, grid):
-    """Axes rounded up to the further compiled lengths (32, 48, 64, 80, 96, 256; z 64):
+    """Axes rounded up to the further compiled lengths (32, 48, 56, 64, 80, 96, 112, 224,
+    256; z 56, 64):
     products in both precisions against the oracle on the same grid, and a refined solve."""
     Nx, Ny, Nz = box
     R = tdda.lattice.bulk(Nx, Ny, Nz)

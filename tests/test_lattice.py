@@ -47,6 +47,10 @@ def test_fft_lengths_round_up_to_compiled_lengths():
     assert [lattice.fft_length(n, True) for n in (10, 16, 20, 24)] == [20, 32, 40, 48]
     assert lattice.fft_length(32, True) == 64        # 63 -> 64
     assert lattice.fft_length(18, False) == 40       # 35 -> 40
-    assert lattice.fft_length(50, False) == 100      # 99 -> 100: 128 is 28% more
-    assert lattice.fft_length(110, False) == 256     # 219 -> 224 -> 256
+    assert lattice.fft_length(50, False) == 112      # 99 -> 100 -> 112
+    assert lattice.fft_length(25, False) == 56 and lattice.fft_length(25, True) == 56  # 49 -> 56
+    assert lattice.fft_length(100, False) == 224     # 199 -> 200 -> 224
+    assert lattice.fft_length(66, False) == 160      # 131 -> 135 -> 160 (18% more)
+    assert lattice.fft_length(110, False) == 224     # 219 -> 224
+    assert lattice.fft_length(120, False) == 256     # 239 -> 240 -> 256
     assert lattice.fft_length(6, False) == 12 and lattice.fft_length(4, True) == 7

@@ -88,11 +88,11 @@ int smooth_size(int n) {
 // points.  Any length >= 2N - 1 gives the same linear convolution
 // (AProductCore.cpp:41-43 uses 2N - 1).
 int fft_length(int N, bool z_axis) {
-    static const int kZ[] = {20, 32, 40, 48, 64};
-    static const int kXY[] = {32, 40, 48, 64, 80, 96, 128, 160, 192, 256};
+    static const int kZ[] = {20, 32, 40, 48, 56, 64};
+    static const int kXY[] = {32, 40, 48, 56, 64, 80, 96, 112, 128, 160, 192, 224, 256};
     const int m = smooth_size(2 * N - 1);
     const int* f = z_axis ? kZ : kXY;
-    const int nf = z_axis ? 5 : 10;
+    const int nf = z_axis ? 6 : 13;
     for (int k = 0; k < nf; k++)
         if (f[k] >= m) return 4 * f[k] <= 5 * m ? f[k] : m;
     return m;

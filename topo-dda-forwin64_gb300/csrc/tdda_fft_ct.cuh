@@ -23,7 +23,9 @@ __host__ __device__ constexpr int ct_nrad(int M, int which, bool big = false) {
     if (big && M == 192) return which < 0 ? 2 : (which == 0 ? 16 : 12);
     if (big && M == 160) return which < 0 ? 2 : (which == 0 ? 16 : 10);
     if (big && M == 48) return which < 0 ? 2 : (which == 0 ? 16 : 3);
+    if (big && M == 56) return which < 0 ? 2 : (which == 0 ? 8 : 7);
     if (big && M == 80) return which < 0 ? 2 : (which == 0 ? 16 : 5);
+    if (big && M == 112) return which < 0 ? 2 : (which == 0 ? 16 : 7);
     if (big && M == 96) return which < 0 ? 2 : (which == 0 ? 12 : 8);
     int m = M, a = 0;
     while (m % 2 == 0) { m /= 2; a++; }

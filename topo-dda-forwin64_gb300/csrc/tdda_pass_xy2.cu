@@ -1,14 +1,16 @@
 // tdda_pass_xy2.cu -- y and x passes compiled for the further x / y FFT lengths
-// a core rounds its axes up to (32, 48, 64, 80, 96, 256; the lattices of a
-// served request stream), beside tdda_pass_xy.cu's lengths of the common
-// lattices.  FP32 x passes take the register form on the two-stage plans
-// (not 256, whose 16 x 16 spectra would not fit the registers).
+// a core rounds its axes up to (32, 48, 56, 64, 80, 96, 112, 224, 256; the
+// lattices of a served request stream), beside tdda_pass_xy.cu's lengths of
+// the common lattices.  FP32 x passes take the register form on the two-stage
+// plans (not 224 and 256, which have none that fits the registers).
 #include "tdda_passes.cuh"
 
 namespace tdda {
 
-bool ct_has_xy2(int M) { return M == 32 || M == 48 || M == 64 || M == 80 || M == 96 || M == 256; }
-bool xpass2_length2(int M) { return M == 32 || M == 48 || M == 64 || M == 80 || M == 96; }
+bool ct_has_xy2(int M) {
+    return M == 32 || M == 48 || M == 56 || M == 64 || M == 80 || M == 96 || M == 112 || M == 224 || M == 256;
+}
+bool xpass2_length2(int M) { return M == 32 || M == 48 || M == 56 || M == 64 || M == 80 || M == 96 || M == 112; }
 
 namespace {
 constexpr int kTile2 = 8;  // z-columns per block of the register form
@@ -27,9 +29,11 @@ template <typename T> bool pass_ct_xy2(int pass, int mode, const PassArgs<T>& a,
     case M: *err = dev::XLaunch2<T, M, kTile2, minb2<M>()>::run(a); return true;
                 TDDA_X2(32)
                 TDDA_X2(48)
+                TDDA_X2(56)
                 TDDA_X2(64)
                 TDDA_X2(80)
                 TDDA_X2(96)
+                TDDA_X2(112)
 #undef TDDA_X2
                 default: break;
             }
@@ -42,9 +46,12 @@ template <typename T> bool pass_ct_xy2(int pass, int mode, const PassArgs<T>& a,
         return true;
         TDDA_XY(32)
         TDDA_XY(48)
+        TDDA_XY(56)
         TDDA_XY(64)
         TDDA_XY(80)
         TDDA_XY(96)
+        TDDA_XY(112)
+        TDDA_XY(224)
         TDDA_XY(256)
 #undef TDDA_XY
         default: return false;
@@ -60,9 +67,12 @@ cudaError_t configure_pass_ct_xy2() {
     if (!e) e = dev::PassLaunch<double, M>::configure_xy();
     TDDA_CFG(32)
     TDDA_CFG(48)
+    TDDA_CFG(56)
     TDDA_CFG(64)
     TDDA_CFG(80)
     TDDA_CFG(96)
+    TDDA_CFG(112)
+    TDDA_CFG(224)
     TDDA_CFG(256)
 #undef TDDA_CFG
     if (!e) e = dev::XLaunch2<float, 32, kTile2, minb2<32>()>::configure();
@@ -70,6 +80,8 @@ cudaError_t configure_pass_ct_xy2() {
     if (!e) e = dev::XLaunch2<float, 64, kTile2, minb2<64>()>::configure();
     if (!e) e = dev::XLaunch2<float, 80, kTile2, minb2<80>()>::configure();
     if (!e) e = dev::XLaunch2<float, 96, kTile2, minb2<96>()>::configure();
+    if (!e) e = dev::XLaunch2<float, 56, kTile2, minb2<56>()>::configure();
+    if (!e) e = dev::XLaunch2<float, 112, kTile2, minb2<112>()>::configure();
     return e;
 }
 

@@ -1,10 +1,10 @@
 // tdda_pass_z.cu -- z-axis passes (K1, K5) compiled for the z FFT lengths of
-// the common lattices (Nz = 10, 16, 20, 24 -> Mz = 20, 32, 40, 48) and 64.
+// the common lattices (Nz = 10, 16, 20, 24 -> Mz = 20, 32, 40, 48), 56 and 64.
 #include "tdda_passes.cuh"
 
 namespace tdda {
 
-bool ct_has_z(int Mz) { return Mz == 20 || Mz == 32 || Mz == 40 || Mz == 48 || Mz == 64; }
+bool ct_has_z(int Mz) { return Mz == 20 || Mz == 32 || Mz == 40 || Mz == 48 || Mz == 56 || Mz == 64; }
 
 template <typename T> bool pass_ct_z(int pass, int mode, const PassArgs<T>& a, cudaError_t* err) {
     if (pass != PASS_ZFWD && pass != PASS_ZINV) return false;
@@ -13,6 +13,7 @@ template <typename T> bool pass_ct_z(int pass, int mode, const PassArgs<T>& a, c
         case 32: *err = dev::PassLaunch<T, 32>::run_z(pass, mode, a); return true;
         case 40: *err = dev::PassLaunch<T, 40>::run_z(pass, mode, a); return true;
         case 48: *err = dev::PassLaunch<T, 48>::run_z(pass, mode, a); return true;
+        case 56: *err = dev::PassLaunch<T, 56>::run_z(pass, mode, a); return true;
         case 64: *err = dev::PassLaunch<T, 64>::run_z(pass, mode, a); return true;
         default: return false;
     }
@@ -26,11 +27,13 @@ cudaError_t configure_pass_ct_z() {
     if (!e) e = dev::PassLaunch<float, 32>::configure_z();
     if (!e) e = dev::PassLaunch<float, 40>::configure_z();
     if (!e) e = dev::PassLaunch<float, 48>::configure_z();
+    if (!e) e = dev::PassLaunch<float, 56>::configure_z();
     if (!e) e = dev::PassLaunch<float, 64>::configure_z();
     if (!e) e = dev::PassLaunch<double, 20>::configure_z();
     if (!e) e = dev::PassLaunch<double, 32>::configure_z();
     if (!e) e = dev::PassLaunch<double, 40>::configure_z();
     if (!e) e = dev::PassLaunch<double, 48>::configure_z();
+    if (!e) e = dev::PassLaunch<double, 56>::configure_z();
     if (!e) e = dev::PassLaunch<double, 64>::configure_z();
     return e;
 }

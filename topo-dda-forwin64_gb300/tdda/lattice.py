@@ -38,8 +38,8 @@ def smooth_size(n: int) -> int:
         m += 1
 
 
-FAST_Z = (20, 32, 40, 48, 64)
-FAST_XY = (32, 40, 48, 64, 80, 96, 128, 160, 192, 256)
+FAST_Z = (20, 32, 40, 48, 56, 64)
+FAST_XY = (32, 40, 48, 56, 64, 80, 96, 112, 128, 160, 192, 224, 256)
 
 
 def fft_length(n: int, z_axis: bool) -> int:
