@@ -99,10 +99,11 @@ def test_aproduct_config_shapes_against_oracle():
 
 @pytest.mark.parametrize("box,grid", [((16, 24, 32), (32, 48, 64)), ((40, 48, 28), (80, 96, 56)),
                                       ((120, 10, 10), (256, 20, 20)), ((30, 60, 12), (64, 128, 24)),
-                                      ((25, 50, 25), (56, 112, 56)), ((100, 8, 8), (224, 15, 15))])
+                                      ((25, 50, 25), (56, 112, 56)), ((100, 8, 8), (224, 15, 15)),
+                                      ((28, 64, 16), (56, 128, 32)), ((40, 80, 20), (80, 160, 40))])
 def test_rounded_up_lengths_against_oracle(box, grid):
     """Axes rounded up to the further compiled lengths (32, 48, 56, 64, 80, 96, 112, 224,
-    256; z 56, 64):
+    256; z 56, 64), also as the x length beside fused (My, Mz) planes:
     products in both precisions against the oracle on the same grid, and a refined solve."""
     Nx, Ny, Nz = box
     R = tdda.lattice.bulk(Nx, Ny, Nz)

@@ -634,7 +634,8 @@ cudaError_t launch_aproduct(const Geom& g, int src, int snk, int nrhs, const Rhs
         if (!pass_zy<T>(PASS_ZFWD, src, a, &err)) return cudaErrorInvalidValue;
         if (err != cudaSuccess) return err;
         if (ev) cudaEventRecord(ev[1], stream), cudaEventRecord(ev[2], stream);
-        if (!pass_ct_xy<T>(PASS_XPASS, 0, a, &err)) err = pass_generic<T>(PASS_XPASS, 0, a);
+        if (!pass_ct_xy<T>(PASS_XPASS, 0, a, &err) && !pass_ct_xy2<T>(PASS_XPASS, 0, a, &err))
+            err = pass_generic<T>(PASS_XPASS, 0, a);
         if (err != cudaSuccess) return err;
         if (ev) cudaEventRecord(ev[3], stream);
         if (!pass_zy<T>(PASS_ZINV, snk, a, &err)) return cudaErrorInvalidValue;
