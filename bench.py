@@ -289,6 +289,7 @@ def pinned_f64(n: int) -> np.ndarray:
 def time_batch(tdda, torch, w, incs, precision, steps, dev, flush_l2):
     """Solve len(incs) right-hand sides of one lattice in one batched solve per step."""
     core = tdda.AProductCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material, w.nback, max_rhs=len(incs), device=dev)
+    tune = core.autotune(nrhs=len(incs), reps=10) if precision == tdda.FP32_REFINE else None
     models = [tdda.DDAModel(core, inc.nK, inc.E0, inc.nE0, w.diel_old) for inc in incs]
     stream = torch.cuda.ExternalStream(core.stream(), device=dev)
     zero = pinned_c128(3 * w.N)
@@ -316,6 +317,8 @@ def time_batch(tdda, torch, w, incs, precision, steps, dev, flush_l2):
     out = {"rhs": len(incs), "value": len(incs) * steps / (sum(ms) / 1000.0), "unit": UNIT, "steps": steps,
            "ms_per_batch": sum(ms) / steps, "iterations": [i["iterations"] for i in infos],
            "pass_ms": prof, "kernels": pass_names(core, precision), "grid": list(core.grid)}
+    if tune:
+        out["x_pass_autotune"] = tune
     for m in models:
         m.close()
     core.close()
@@ -445,6 +448,7 @@ def run_ours(args, dist: Dist):
     inc = w.incidences[0]
     n3 = 3 * w.N
     core = tdda.AProductCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material, w.nback, max_rhs=1, device=dev)
+    tune = core.autotune(nrhs=1, reps=20)  # the FP32 x pass's form and tile, timed on this core
     model = tdda.DDAModel(core, inc.nK, inc.E0, inc.nE0, w.diel_old)
     stream = torch.cuda.ExternalStream(core.stream(), device=dev)
     zero = pinned_c128(n3)
@@ -595,7 +599,7 @@ def run_ours(args, dist: Dist):
                          "pass_ms_fp32": prof32, "pass_ms_fp64": prof64,
                          "kernels_fp32": pass_names(core, tdda.FP32_REFINE),
                          "kernels_fp64": pass_names(core, tdda.FP64),
-                         "passes_fp32": passes32, "aproduct_fp32": whole32},
+                         "passes_fp32": passes32, "aproduct_fp32": whole32, "x_pass_autotune": tune},
             "batched": batched,
             "serving": serving,
             "topo": topo_line,

@@ -294,6 +294,27 @@ int tdda_core_pass_count(const tdda_core* core, int precision);
  * that a fused kernel covers; NULL for an invalid argument.  Static string. */
 const char* tdda_core_pass_name(const tdda_core* core, int precision, int pass);
 
+/* The FP32 x pass (x FFT, spectral product, inverse x FFT) of a core runs in
+ * one of two forms: the register form on a two-stage radix plan (k_xpass2;
+ * compiled for x lengths 32-192) with 8 or 16 z-columns a block, or the
+ * shared-memory form on the length's compiled plan (k_xpass).  The tile does
+ * not change results; the form changes the FFT's rounding (FP32 level).
+ * form 0: register form where compiled, tile 8, 16 or 0 (built-in: 16 for
+ * x length 128, else 8); form 1: shared-memory form, tile 0.  Captured FP32
+ * solve steps of the core are dropped and captured again on next use; the
+ * call waits for the core's stream first. */
+tdda_status tdda_core_set_xpass(tdda_core* core, int form, int tile);
+typedef struct {
+    int x_form, x_tile;  /* the chosen configuration (now set on the core) */
+    int ncand;           /* candidates timed: 3, or 1 where the x length has no register form */
+    int form[4], tile[4];
+    double ms[4];        /* average ms of one FP32 A-product of nrhs right-hand sides, per candidate */
+} tdda_xpass_tune;
+/* Autotuner of the FP32 x pass: times `reps` plain FP32 A-products of nrhs
+ * right-hand sides (CUDA events on the core's stream, after one warm-up) for
+ * every candidate form and tile, and sets the fastest on the core. */
+tdda_status tdda_core_autotune(tdda_core* core, int nrhs, int reps, tdda_xpass_tune* out);
+
 #ifdef __cplusplus
 }
 #endif

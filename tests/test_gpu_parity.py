@@ -122,6 +122,52 @@ def test_rounded_up_lengths_against_oracle(box, grid):
     assert info["status"] == tdda.OK and info["true_residual"] <= 1e-5
 
 
+def test_xpass_tile_and_form_and_the_autotuner():
+    """The FP32 x pass's z-tile changes no result (products and refined solves bit-identical,
+    the captured solve steps taken again), the shared-memory form matches the oracle at the
+    FP32 level, and the autotuner keeps its fastest timed candidate."""
+    Nx, Ny, Nz = 64, 64, 16
+    R = tdda.lattice.bulk(Nx, Ny, Nz)
+    mat = np.array([1.0, 6.25 + 0.05j])
+    c = tdda.AProductCore(Nx, Ny, Nz, R, 10.0, 600.0, mat)
+    oc = O.OracleCore(Nx, Ny, Nz, R, 10.0, 600.0, mat, grid=c.grid, pruned=True)
+    rng = np.random.Generator(np.random.PCG64(77))
+    b = rng.standard_normal(R.size) + 1j * rng.standard_normal(R.size)
+    y = oc.Aproduct(b)
+    rho = np.repeat(rng.random(R.size // 3), 3)
+    m = tdda.DDAModel(c, (0.0, 0.0, 1.0), 1.0, (1.0, 0.0, 0.0), rho)
+    zero = np.zeros(R.size, np.complex128)
+    out = {}
+    for form, tile in ((0, 8), (0, 16), (1, 0)):
+        c.set_xpass(form, tile)
+        assert c.pass_names(tdda.FP32_REFINE)[2] == ("k_xpass2" if form == 0 else "k_xpass")
+        yk = c.Aproduct(b, precision=tdda.FP32_REFINE)
+        assert rel(yk, y) <= 1e-5
+        m.InitializeP(zero)
+        info = m.solve_mixed(10000, 1e-5)
+        assert info["status"] == tdda.OK and info["true_residual"] <= 1e-5
+        out[(form, tile)] = (yk, m.get_P(), info["inner_iterations"])
+    assert np.array_equal(out[(0, 8)][0], out[(0, 16)][0])
+    assert np.array_equal(out[(0, 8)][1], out[(0, 16)][1])
+    assert out[(0, 8)][2] == out[(0, 16)][2]
+    t = c.autotune(nrhs=1, reps=3)
+    cands = t["candidates"]
+    assert [(k["form"], k["tile"]) for k in cands] == [(0, 8), (0, 16), (1, 0)]
+    assert all(k["ms"] > 0 for k in cands)
+    fastest = min(cands, key=lambda k: k["ms"])
+    assert (t["x_form"], t["x_tile"]) == (fastest["form"], fastest["tile"])
+    m.InitializeP(zero)
+    info = m.solve_mixed(10000, 1e-5)
+    assert info["status"] == tdda.OK and info["true_residual"] <= 1e-5
+    assert np.array_equal(m.get_P(), out[(t["x_form"], t["x_tile"])][1])
+    with pytest.raises(tdda.TddaError):
+        c.set_xpass(1, 8)
+    # an x length without a two-stage plan has one candidate, the shared-memory form
+    c2 = tdda.AProductCore(100, 8, 8, tdda.lattice.bulk(100, 8, 8), 8.0, 550.0, np.array([1.0, 4.0 + 0.1j]))
+    t2 = c2.autotune(nrhs=1, reps=2)
+    assert [(k["form"], k["tile"]) for k in t2["candidates"]] == [(1, 0)] and t2["x_form"] == 1
+
+
 def _model(g, core):
     m = tdda.DDAModel(core, g["nK"], float(g["E0"]), g["nE0"], g["diel_old"])
     if "P0" in g:

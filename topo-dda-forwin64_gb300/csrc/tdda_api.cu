@@ -1583,7 +1583,7 @@ const char* tdda_core_pass_name(const tdda_core* c, int precision, int pass) {
     switch (pass) {
         case 0: return fused ? "k_zyfwd" : "k_zfwd";
         case 1: return fused ? "" : "k_ypass";
-        case 2: return fp32 && tdda::xpass2_length(c->g.px.M) ? "k_xpass2" : "k_xpass";
+        case 2: return fp32 && c->g.x_form == 0 && tdda::xpass2_length(c->g.px.M) ? "k_xpass2" : "k_xpass";
         case 3: return fused ? "k_yzinv" : "k_ypass";
         default: return fused ? "" : "k_zinv";
     }
@@ -1594,13 +1594,9 @@ int tdda_core_pass_count(const tdda_core* c, int precision) {
     return tdda::zy_fused(c->g, precision == TDDA_FP32_REFINE) ? 3 : 5;
 }
 
-tdda_status tdda_profile_aproduct(tdda_core* c, int precision, int nrhs, int reps, double* ms5) {
-    if (!c || !ms5 || reps < 1 || nrhs < 1 || nrhs > c->max_rhs ||
-        (precision != TDDA_FP64 && precision != TDDA_FP32_REFINE)) {
-        set_err("invalid argument");
-        return TDDA_ERR_INVALID_ARGUMENT;
-    }
-    TDDA_TRY(set_device(c->device));
+namespace {
+// the five pass times of `reps` plain products (arguments checked by the caller)
+tdda_status profile_products(tdda_core* c, int precision, int nrhs, int reps, double* ms5) {
     // nrhs plain products on the core's input / output vectors (the same
     // vectors for every right-hand side: the passes read and write the
     // grid slot of each right-hand side separately)
@@ -1635,6 +1631,72 @@ tdda_status tdda_profile_aproduct(tdda_core* c, int precision, int nrhs, int rep
     for (auto& e : ev) cudaEventDestroy(e);
     for (int k = 0; k < 5; k++) ms5[k] = acc[k] / reps;
     return st;
+}
+
+// A captured solve step holds its pass kernels and their Geom: a new FP32 x-pass
+// configuration drops the FP32 step graphs (captured again on next use).
+tdda_status set_xpass(tdda_core* c, int form, int tile) {
+    if (c->g.x_form == form && c->g.x_tile == tile) return TDDA_OK;
+    TDDA_CK(cudaStreamSynchronize(c->stream));
+    for (auto& e : c->g32.iter)
+        if (e) cudaGraphExecDestroy(e), e = nullptr;
+    c->g.x_form = form;
+    c->g.x_tile = tile;
+    return TDDA_OK;
+}
+}  // namespace
+
+tdda_status tdda_profile_aproduct(tdda_core* c, int precision, int nrhs, int reps, double* ms5) {
+    if (!c || !ms5 || reps < 1 || nrhs < 1 || nrhs > c->max_rhs ||
+        (precision != TDDA_FP64 && precision != TDDA_FP32_REFINE)) {
+        set_err("invalid argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    TDDA_TRY(set_device(c->device));
+    return profile_products(c, precision, nrhs, reps, ms5);
+}
+
+tdda_status tdda_core_set_xpass(tdda_core* c, int form, int tile) {
+    if (!c || (form != 0 && form != 1) || (tile != 0 && tile != 8 && tile != 16) || (form == 1 && tile != 0)) {
+        set_err("invalid argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    TDDA_TRY(set_device(c->device));
+    return set_xpass(c, form, tile);
+}
+
+tdda_status tdda_core_autotune(tdda_core* c, int nrhs, int reps, tdda_xpass_tune* out) {
+    if (!c || !out || reps < 1 || nrhs < 1 || nrhs > c->max_rhs) {
+        set_err("invalid argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    TDDA_TRY(set_device(c->device));
+    *out = tdda_xpass_tune{};
+    // candidates: the register form with 8 and 16 z-columns a block, where the
+    // x length has a two-stage plan, and the shared-memory form
+    int nc = 0;
+    if (tdda::xpass2_length(c->g.px.M)) {
+        out->form[nc] = 0, out->tile[nc++] = 8;
+        out->form[nc] = 0, out->tile[nc++] = 16;
+    }
+    out->form[nc] = 1, out->tile[nc++] = 0;
+    out->ncand = nc;
+    const int form0 = c->g.x_form, tile0 = c->g.x_tile;
+    int best = -1;
+    for (int k = 0; k < nc; k++) {
+        double ms5[5];
+        tdda_status st = set_xpass(c, out->form[k], out->tile[k]);
+        if (st == TDDA_OK) st = profile_products(c, TDDA_FP32_REFINE, nrhs, reps, ms5);
+        if (st != TDDA_OK) {
+            set_xpass(c, form0, tile0);
+            return st;
+        }
+        out->ms[k] = ms5[0] + ms5[1] + ms5[2] + ms5[3] + ms5[4];
+        if (best < 0 || out->ms[k] < out->ms[best]) best = k;
+    }
+    out->x_form = out->form[best];
+    out->x_tile = out->tile[best];
+    return set_xpass(c, out->x_form, out->x_tile);
 }
 
 tdda_status tdda_aproduct_noalloc(tdda_core* c, const double* b, double* y) {

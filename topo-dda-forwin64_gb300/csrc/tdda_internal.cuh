@@ -26,6 +26,11 @@ struct Geom {
     long long sy, sx, sc, sb;  // grid strides (y, x, component, rhs) in elements
     int dense;         // 1: the full box in build_a_bulk order, dipole (x Ny + y) Nz + z
                        // in every cell (tools.cpp:497-510), so no cellmap lookup
+    // FP32 x pass (set by tdda_core_set_xpass / tdda_core_autotune):
+    int x_form;        // 0: the register form on a two-stage plan where one is compiled,
+                       // 1: the shared-memory form on the length's compiled plan
+    int x_tile;        // z-columns per block of the register form: 8, 16, or 0 for
+                       // the built-in choice (16 for M = 128, else 8)
 };
 
 // solver status values (mirrored in include/tdda.h)

@@ -12,21 +12,15 @@ bool ct_has_xy2(int M) {
 }
 bool xpass2_length2(int M) { return M == 32 || M == 48 || M == 56 || M == 64 || M == 80 || M == 96 || M == 112; }
 
-namespace {
-constexpr int kTile2 = 8;  // z-columns per block of the register form
-// blocks per SM the register form is compiled for: 16 warps (128 registers a thread)
-template <int M> constexpr int minb2() { return 16 * 32 / (kTile2 * x2_radix(M, 0)) > 0 ? 16 * 32 / (kTile2 * x2_radix(M, 0)) : 1; }
-}  // namespace
-
 template <typename T> bool pass_ct_xy2(int pass, int mode, const PassArgs<T>& a, cudaError_t* err) {
     (void)mode;
     const bool y = pass == PASS_YFWD || pass == PASS_YINV;
     if (!y && pass != PASS_XPASS) return false;
     if constexpr (sizeof(T) == 4) {
-        if (!y) {
+        if (!y && a.g.x_form == 0) {
             switch (a.g.px.M) {
 #define TDDA_X2(M)                                                         \
-    case M: *err = dev::XLaunch2<T, M, kTile2, minb2<M>()>::run(a); return true;
+    case M: *err = dev::X2Launch<T, M>::run(a); return true;
                 TDDA_X2(32)
                 TDDA_X2(48)
                 TDDA_X2(56)
@@ -75,13 +69,13 @@ cudaError_t configure_pass_ct_xy2() {
     TDDA_CFG(224)
     TDDA_CFG(256)
 #undef TDDA_CFG
-    if (!e) e = dev::XLaunch2<float, 32, kTile2, minb2<32>()>::configure();
-    if (!e) e = dev::XLaunch2<float, 48, kTile2, minb2<48>()>::configure();
-    if (!e) e = dev::XLaunch2<float, 64, kTile2, minb2<64>()>::configure();
-    if (!e) e = dev::XLaunch2<float, 80, kTile2, minb2<80>()>::configure();
-    if (!e) e = dev::XLaunch2<float, 96, kTile2, minb2<96>()>::configure();
-    if (!e) e = dev::XLaunch2<float, 56, kTile2, minb2<56>()>::configure();
-    if (!e) e = dev::XLaunch2<float, 112, kTile2, minb2<112>()>::configure();
+    if (!e) e = dev::X2Launch<float, 32>::configure();
+    if (!e) e = dev::X2Launch<float, 48>::configure();
+    if (!e) e = dev::X2Launch<float, 64>::configure();
+    if (!e) e = dev::X2Launch<float, 80>::configure();
+    if (!e) e = dev::X2Launch<float, 96>::configure();
+    if (!e) e = dev::X2Launch<float, 56>::configure();
+    if (!e) e = dev::X2Launch<float, 112>::configure();
     return e;
 }
 

@@ -445,6 +445,28 @@ template <typename T, int M, int ZT, int MINB = 1> struct XLaunch2 {
     }
 };
 
+// blocks per SM the register form is compiled for: 16 warps per SM (a register
+// cap of 128 a thread), 24 for M = 128 and 192, whose spectra fit in 85
+template <int M, int ZT> constexpr int x2_minb() {
+    constexpr int n = ((M == 128 || M == 192) ? 24 : 16) * 32 / (ZT * x2_radix(M, 0));
+    return n > 0 ? n : 1;
+}
+// The register form with 8 or 16 z-columns a block (Geom::x_tile; 0 takes 16
+// for M = 128, else 8).  The tile changes only which block transforms a column:
+// results are bit-identical.
+template <typename T, int M> struct X2Launch {
+    using Narrow = XLaunch2<T, M, 8, x2_minb<M, 8>()>;
+    using Wide = XLaunch2<T, M, 16, x2_minb<M, 16>()>;
+    static cudaError_t run(const PassArgs<T>& a) {
+        const bool wide = a.g.x_tile ? a.g.x_tile == 16 : M == 128;
+        return wide ? Wide::run(a) : Narrow::run(a);
+    }
+    static cudaError_t configure() {
+        const cudaError_t e = Narrow::configure();
+        return e != cudaSuccess ? e : Wide::configure();
+    }
+};
+
 // ------------------------------------------------------------ K5 zinv
 template <typename T, int SRC, int SNK, int CM>
 __global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restrict__ rhs,

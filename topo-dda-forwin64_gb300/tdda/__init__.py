@@ -47,7 +47,7 @@ EXPORTS = [
     "tdda_model_density_gradient",
     "tdda_solve_batch",
     "tdda_fft3d", "tdda_core_stream", "tdda_kernel_launches", "tdda_profile_aproduct", "tdda_core_pass_count",
-    "tdda_core_pass_name",
+    "tdda_core_pass_name", "tdda_core_set_xpass", "tdda_core_autotune",
     "tdda_aproduct_noalloc", "tdda_server_create", "tdda_server_submit", "tdda_server_result",
     "tdda_server_stats", "tdda_server_clock", "tdda_server_destroy", "tdda_request_bytes",
 ]
@@ -66,6 +66,11 @@ class CoreDesc(ctypes.Structure):
                 ("nback", ctypes.c_double), ("material", ctypes.POINTER(ctypes.c_double)),
                 ("nmat", ctypes.c_int), ("method", ctypes.c_int), ("max_rhs", ctypes.c_int),
                 ("device", ctypes.c_int)]
+
+
+class XpassTune(ctypes.Structure):
+    _fields_ = [("x_form", ctypes.c_int), ("x_tile", ctypes.c_int), ("ncand", ctypes.c_int),
+                ("form", ctypes.c_int * 4), ("tile", ctypes.c_int * 4), ("ms", ctypes.c_double * 4)]
 
 
 class SolveInfo(ctypes.Structure):
@@ -147,6 +152,8 @@ def load() -> ctypes.CDLL:
         "tdda_profile_aproduct": (i, [vp, i, i, i, dp]),
         "tdda_core_pass_count": (i, [vp, i]),
         "tdda_core_pass_name": (ctypes.c_char_p, [vp, i, i]),
+        "tdda_core_set_xpass": (i, [vp, i, i]),
+        "tdda_core_autotune": (i, [vp, i, i, ctypes.POINTER(XpassTune)]),
         "tdda_aproduct_noalloc": (i, [vp, vp, vp]),
         "tdda_server_create": (i, [ctypes.POINTER(ServerDesc), ctypes.POINTER(vp)]),
         "tdda_server_submit": (i, [vp, ctypes.POINTER(RequestDesc), ctypes.POINTER(ctypes.c_ulonglong)]),
@@ -272,6 +279,18 @@ class AProductCore:
                 raise ValueError(f"pass_names: invalid precision {precision}")
             out.append(n.decode())
         return out
+
+    def set_xpass(self, form: int, tile: int = 0):
+        """FP32 x-pass configuration: form 0 = register form (tile 8, 16, or 0 for the
+        built-in choice), form 1 = shared-memory form (tile 0)."""
+        _check(load().tdda_core_set_xpass(self.h, int(form), int(tile)), "tdda_core_set_xpass")
+
+    def autotune(self, nrhs: int = 1, reps: int = 10) -> dict:
+        """Time the FP32 x-pass candidates on this core's A-product and keep the fastest."""
+        t = XpassTune()
+        _check(load().tdda_core_autotune(self.h, int(nrhs), int(reps), ctypes.byref(t)), "tdda_core_autotune")
+        return {"x_form": t.x_form, "x_tile": t.x_tile,
+                "candidates": [{"form": t.form[k], "tile": t.tile[k], "ms": t.ms[k]} for k in range(t.ncand)]}
 
     def profile_aproduct(self, precision: int = FP32_REFINE, nrhs: int = 1, reps: int = 10) -> list:
         """Average ms of the five passes of one A-product (CUDA events on the core stream)."""
