@@ -344,7 +344,13 @@ __global__ void __launch_bounds__(ZT * x2_radix(M, 0), MINB) k_xpass2(Geom g, co
     // Nx <= M / 2, so the inputs r >= R1 / 2 are zero padding: not read, not added.
     static_assert(R1 % 2 == 0, "even first radix");
     constexpr int RH = R1 / 2;
-    for (int w = threadIdx.x; w < W * R2; w += NT) {
+    // a compile-time count of tasks per thread, so the loads of all of a
+    // thread's tasks can be issued before the first butterfly
+    constexpr int T1 = (W * R2 + NT - 1) / NT;
+#pragma unroll
+    for (int k = 0; k < T1; k++) {
+        const int w = threadIdx.x + k * NT;
+        if (T1 * NT > W * R2 && w >= W * R2) break;
         const int l = w % W, j = w / W;
         const int c = l / ZT, zl = l - c * ZT;
         const cx<T>* src = gp + c * g.sc + zl;
