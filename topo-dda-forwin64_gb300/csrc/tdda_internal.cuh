@@ -65,7 +65,11 @@ struct SolveState {
     int chunks, chunk_limit;
 };
 
-// per right-hand side: the vectors of one solve (AoS [x,y,z] per dipole)
+// per right-hand side: the vectors of one solve.  FP64 vectors (and the
+// double-float residual product, which reads them) are AoS [x,y,z] per dipole,
+// the layout of the C ABI; the FP32 vectors of the inner solve, internal to
+// the library, are SoA [c][dipole], so the gather and scatter of a pass block
+// (one component of one x-plane) read and write whole sectors.
 template <typename T> struct RhsVecs {
     cx<T>* P;
     cx<T>* E;
@@ -81,6 +85,11 @@ template <typename T> struct RhsVecs {
     double* part;        // reduction partials, kPartSlots x maxblk doubles
     unsigned int* cnt;   // last-block counters, kCounters
 };
+// entry of component c of dipole i in a vector of N dipoles
+template <typename T> __host__ __device__ __forceinline__ long long vec_index(long long i, int c, int N) {
+    if constexpr (sizeof(T) == 4) return (long long)c * N + i;
+    return 3 * i + c;
+}
 constexpr int kPartSlots = 8;
 constexpr int kCounters = 8;
 

@@ -434,7 +434,7 @@ __global__ void k_model_alpha(int n3, const double* __restrict__ diel_old, Alpha
             vprev = v;
             diel[e] = eps;
             al[e] = inv;
-            if (fal) fal[e] = make_float2((float)inv.x, (float)inv.y);
+            if (fal) fal[(long long)c * n + i] = make_float2((float)inv.x, (float)inv.y);  // FP32: SoA
         }
     }
 }
@@ -493,13 +493,23 @@ __global__ void k_einternal(int n3, const double2* al, const double2* P, const d
         Ein[e] = cdiv(dmul(al[e], P[e]), lf);
     }
 }
+// FP64 AoS vector -> FP32 SoA vector (the layouts of RhsVecs<double> and <float>)
 __global__ void k_to_f32(int n3, const double2* src, float2* dst) {
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x)
-        dst[e] = make_float2((float)src[e].x, (float)src[e].y);
+    const int n = n3 / 3;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x) {
+        const int c = e / n, i = e - c * n;  // consecutive threads write consecutive entries
+        const double2 v = src[3LL * i + c];
+        dst[e] = make_float2((float)v.x, (float)v.y);
+    }
 }
+// P (FP64 AoS) += d (FP32 SoA)
 __global__ void k_accumulate(int n3, const float2* d, double2* P) {
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x)
-        P[e] = make_double2(P[e].x + (double)d[e].x, P[e].y + (double)d[e].y);
+    const int n = n3 / 3;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x) {
+        const int i = e / 3, c = e - 3 * i;
+        const float2 v = d[(long long)c * n + i];
+        P[e] = make_double2(P[e].x + (double)v.x, P[e].y + (double)v.y);
+    }
 }
 template <typename T> __global__ void k_zero(long long n, cx<T>* v) {
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)

@@ -146,21 +146,21 @@ __global__ void __launch_bounds__(kNT) k_zfwd(Geom g, const RhsVecs<T>* __restri
         const int i = cellmap[(long long)(l0 + line) * Nz + z];
         cx<T> v[3];
         if (i >= 0) {
-            const long long o = 3LL * i;
 #pragma unroll
             for (int c = 0; c < 3; c++) {
+                const long long o = vec_index<T>(i, c, g.N);
                 if (SRC == SRC_PUPD) {
-                    cx<T> pc = R.p[o + c], uc = R.u[o + c], rc = R.r[o + c];
+                    cx<T> pc = R.p[o], uc = R.u[o], rc = R.r[o];
                     v[c] = cadd<T>(rc, cmul<T>(beta, csub<T>(pc, uc)));
-                    R.p[o + c] = v[c];
+                    R.p[o] = v[c];
                 } else if (SRC == SRC_PUPD_DEF) {
-                    v[c] = deferred_step<T>(R, o + c, alpha, zeta, beta);
+                    v[c] = deferred_step<T>(R, o, alpha, zeta, beta);
                 } else if (SRC == SRC_TUPD) {
-                    cx<T> rc = R.r[o + c], ac = R.Ap[o + c];
+                    cx<T> rc = R.r[o], ac = R.Ap[o];
                     v[c] = csub<T>(rc, cmul<T>(alpha, ac));
-                    R.t[o + c] = v[c];
+                    R.t[o] = v[c];
                 } else {
-                    v[c] = ldv<T>(src, o + c);
+                    v[c] = ldv<T>(src, o);
                 }
             }
         } else {
@@ -514,31 +514,31 @@ __global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restri
         const int line = e / Nz, z = e - (e / Nz) * Nz;
         const int i = cellmap[(long long)(l0 + line) * Nz + z];
         if (i < 0) continue;
-        const long long o = 3LL * i;
 #pragma unroll
         for (int c = 0; c < 3; c++) {
+            const long long o = vec_index<T>(i, c, g.N);
             cx<T> val = res[(c * LZ + line) * MzP + z];
             if (SNK == SNK_OUT) {
-                R.Ap[o + c] = val;
+                R.Ap[o] = val;
                 continue;
             }
-            const cx<T> vv = ldv<T>(vsrc, o + c);
-            const cx<T> w = cadd<T>(val, cmul<T>(vv, ldv<T>(R.al, o + c)));
+            const cx<T> vv = ldv<T>(vsrc, o);
+            const cx<T> w = cadd<T>(val, cmul<T>(vv, ldv<T>(R.al, o)));
             if (SNK == SNK_ALB) {
-                R.Ap[o + c] = w;
+                R.Ap[o] = w;
             } else if (SNK == SNK_AP) {
-                R.Ap[o + c] = w;
-                const cx<T> q = R.r0[o + c];  // r0 . Ap
+                R.Ap[o] = w;
+                const cx<T> q = R.r0[o];  // r0 . Ap
                 acc[0] += q.x * w.x + q.y * w.y;
                 acc[1] += q.x * w.y - q.y * w.x;
             } else if (SNK == SNK_AT || SNK == SNK_AT_DEF) {
-                R.At[o + c] = w;
+                R.At[o] = w;
                 const cx<T> tt = vv;  // At . t and At . At
                 acc[0] += w.x * tt.x + w.y * tt.y;
                 acc[1] += w.x * tt.y - w.y * tt.x;
                 acc[2] += w.x * w.x + w.y * w.y;
                 if constexpr (SNK == SNK_AT_DEF) {  // r0 . t, r0 . At, t . t
-                    const cx<T> q = R.r0[o + c];
+                    const cx<T> q = R.r0[o];
                     acc[3] += q.x * tt.x + q.y * tt.y;
                     acc[4] += q.x * tt.y - q.y * tt.x;
                     acc[5] += q.x * w.x + q.y * w.y;
@@ -546,10 +546,10 @@ __global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restri
                     acc[7] += tt.x * tt.x + tt.y * tt.y;
                 }
             } else if (SNK == SNK_RES) {
-                const cx<T> res = csub<T>(ldv<T>(R.E, o + c), w);
-                stv<T>(R.r, o + c, res);
-                stv<T>(R.r0, o + c, res);
-                stv<T>(R.p, o + c, res);
+                const cx<T> res = csub<T>(ldv<T>(R.E, o), w);
+                stv<T>(R.r, o, res);
+                stv<T>(R.r0, o, res);
+                stv<T>(R.p, o, res);
                 acc[0] += cnorm2<T>(res);
             }
         }
@@ -762,7 +762,7 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
             sidx[q] = cell ? y * ZP + z : -1;
             int i = -1;
             if (cell && y < Ny && z < Nz) i = g.dense ? ibase + y * Nz + z : cm[y * Nz + z];
-            o[q] = i >= 0 ? 3LL * i + c : -1LL;
+            o[q] = i >= 0 ? vec_index<T>(i, c, g.N) : -1LL;
         }
         GatherIn<T, SRC, CH> in;
         in.load(R, o, src);
@@ -953,7 +953,7 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
             const bool cell = c0 + q < NE && e < NCELL && y < Ny && z < Nz;
             int i = -1;
             if (cell) i = g.dense ? ibase + y * Nz + z : cm[y * Nz + z];
-            o[q] = i >= 0 ? 3LL * i + c : -1LL;
+            o[q] = i >= 0 ? vec_index<T>(i, c, g.N) : -1LL;
             vo[q] = i >= 0 ? sB[y * ZP + z] : czero<T>();
         }
         scatter_chunk<T, SRC, SNK, CH, NV>(R, o, vo, acc);
