@@ -941,7 +941,9 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
     const int* cm = cellmap + (long long)x * Ny * Nz;
     const int ibase = x * Ny * Nz;
     acc_t<T> acc[NV] = {};
-    constexpr int NCELL = LY * LZ, NE = (NCELL + kNT - 1) / kNT, CH = NE < 4 ? NE : 4;
+    // the sink's operand loads of all the thread's cells at once, up to 9 cells
+    constexpr int NCELL = LY * LZ, NE = (NCELL + kNT - 1) / kNT;
+    constexpr int CH = (SNK != SNK_OUT && NE <= 9) || NE < 4 ? NE : 4;
 #pragma unroll
     for (int c0 = 0; c0 < NE; c0 += CH) {
         long long o[CH];
