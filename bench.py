@@ -624,6 +624,27 @@ def run_aprod_only(args):
                       "precision": args.aprod_precision, "pass_ms": ms}), flush=True)
 
 
+def run_solve_only(args):
+    """Only solves of one workload (for launch-list captures): --solve-only CFG runs two
+    batched FP32+refine solves of all of the workload's right-hand sides."""
+    import tdda
+
+    w = lattice.config(args.solve_only)
+    core = tdda.AProductCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material, w.nback, max_rhs=len(w.incidences))
+    models = [tdda.DDAModel(core, i.nK, i.E0, i.nE0, w.diel_old) for i in w.incidences]
+    zero = np.zeros(3 * w.N, np.complex128)
+    for _ in range(2):
+        for m in models:
+            m.InitializeP(zero)
+        infos = tdda.solve_batch(models, tdda.FP32_REFINE, MAX_IT, TOL)
+    print(json.dumps({"solve_only": f"cfg{args.solve_only}", "rhs": len(models),
+                      "inner_iterations": [i["inner_iterations"] for i in infos],
+                      "outer_iterations": [i["outer_iterations"] for i in infos]}), flush=True)
+    for m in models:
+        m.close()
+    core.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -641,11 +662,15 @@ def main():
     ap.add_argument("--aprod-only", type=int, default=0)
     ap.add_argument("--aprod-precision", choices=["fp32", "fp64"], default="fp32")
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--solve-only", type=int, default=0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.aprod_only:
         run_aprod_only(args)
+        return
+    if args.solve_only:
+        run_solve_only(args)
         return
     dist = Dist()
     try:
