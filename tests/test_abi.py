@@ -44,6 +44,14 @@ def test_core_create_rejects_bad_arguments_before_touching_a_device():
     assert b"invalid" in L.tdda_last_error()
 
 
+def test_xpass_tuning_rejects_bad_arguments_before_touching_a_device():
+    L = tdda.load()
+    t = tdda.XpassTune()
+    assert L.tdda_core_set_xpass(None, 0, 0) == tdda.ERR_INVALID_ARGUMENT
+    assert L.tdda_core_autotune(None, 1, 1, ctypes.byref(t)) == tdda.ERR_INVALID_ARGUMENT
+    assert b"invalid" in L.tdda_last_error()
+
+
 def test_fcd_needs_the_spacing_inside_the_sici_tables():
     """FCD evaluates Si/Ci at (pi/d - K) r >= pi - K d, and the tables start at 0.1."""
     import numpy as np
