@@ -167,6 +167,13 @@ class AProductCore {
     const std::vector<int>* get_R() const { return &R_; }
     std::array<int, 3> grid() const { return grid_; }
     tdda_core* handle() const { return h_; }
+    // Not in the reference: times the FP32 x pass's forms and tiles on this core's
+    // A-product of nrhs right-hand sides and keeps the fastest (tdda_core_autotune).
+    tdda_xpass_tune autotune(int nrhs = 1, int reps = 10) {
+        tdda_xpass_tune t{};
+        check(tdda_core_autotune(h_, nrhs, reps, &t), "autotune");
+        return t;
+    }
     // the structure's current densities (CoreStructure::get_diel_old)
     void read_diel_old(std::vector<double>& out) const { diel_old_(out); }
 
