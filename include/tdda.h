@@ -265,11 +265,21 @@ tdda_status tdda_fft3d(double* data, int n0, int n1, int n2, int sign);
  * in device memory.  The FFT work grid is a static 64 MiB device array that
  * every GPU loading the library holds until exit, so the core's grid
  * 3 x Nx x My x Mz must be at most 4,194,304 complex128 entries, else
- * TDDA_ERR_UNSUPPORTED.  The first call on a device looks the array up
- * (cudaGetSymbolAddress); make that first call before any stream capture.
- * All calls share the array, so calls that overlap on the GPU (two threads, or
- * two cores on different streams) race; each call fully rewrites what it
- * reads, so nothing needs clearing between calls. */
+ * TDDA_ERR_UNSUPPORTED.  The product runs on the core's own stream
+ * (tdda_core_stream) and the call returns when it has finished; like
+ * tdda_aproduct with TDDA_MEM_DEVICE, it does not wait for other streams, so
+ * the work that produces b must have finished on the device before the call
+ * (a cudaStreamSynchronize of the producer's stream, or an event the core's
+ * stream waits on).  The call synchronises the core's stream, so it cannot be
+ * captured into a CUDA graph.  The first call on a device looks the array's
+ * device address up (cudaGetSymbolAddress, which may load the library's
+ * module): that first call must not overlap a global-mode stream capture in
+ * another thread.  The address is kept for the life of the process, so this
+ * entry point must not be used after a cudaDeviceReset of that device (the
+ * reset also invalidates every core made before it).  All calls share the
+ * array, so calls that overlap on the GPU (two threads, or two cores on
+ * different streams) race; each call fully rewrites what it reads, so nothing
+ * needs clearing between calls. */
 tdda_status tdda_aproduct_noalloc(tdda_core* core, const double* b, double* y);
 
 /* measurement hooks (no counterpart in the reference) ------------------- */

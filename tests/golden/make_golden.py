@@ -1,7 +1,8 @@
 """Generate the golden fixtures in this folder from the reference itself.
 
 Builds oracle/_ref/ref_driver -- the reference's own AProductCore.cpp,
-DDAModel.cpp, tools.cpp, ... compiled unchanged from /root/reference with the
+DDAModel.cpp, tools.cpp, ... compiled unchanged from the reference checkout
+(oracle/Makefile's REF_ROOT, which the environment may set) with the
 CPU stand-ins for cuFFT and the CUDA runtime in oracle/ref_shim -- and runs it
 on seeded inputs.  Each fixture stores its inputs and the reference's outputs:
 
@@ -21,7 +22,7 @@ on seeded inputs.  Each fixture stores its inputs and the reference's outputs:
                    off-lattice points: |E_ext(r) - sum_i A(r - d R_i) P_i|
 
 Run from the repository root:  python tests/golden/make_golden.py
-It needs /root/reference, so it runs in the development container only; the
+It needs the reference checkout, so it runs where that checkout exists; the
 fixtures it writes are committed and travel with the tests.
 """
 from __future__ import annotations

@@ -3,7 +3,8 @@
 tests/cpp/mirror_solve.cpp builds a structure with the reference CoreStructure's getters,
 constructs AProductCore / DDAModel (with RResult points), runs bicgstab +
 update_E_in_structure + solve_E and dumps the results; here they are compared with the oracle.  Compiling is a CPU test; running is a
-GPU test.
+GPU test.  tests/cpp/dropin_reference.cpp compiles the reference's own callers (its
+ObjDDAModel.cpp and structure classes, unchanged) against the drop-in with Eigen types.
 """
 import math
 import os
@@ -34,6 +35,22 @@ def _build(tmp_path) -> str:
 def test_mirror_header_compiles_against_the_abi(tmp_path):
     tdda.load()  # libtdda.so must exist to link
     assert os.path.exists(_build(tmp_path))
+
+
+def test_reference_callers_compile_against_the_dropin():
+    """The reference's ObjDDAModel.cpp, CoreStructure.cpp, Space*.cpp, Structure.cpp, tools.cpp
+    and FilterOption.cpp, unchanged, with the drop-in in place of AProductCore.h / DDAModel.h
+    (tests/cpp/dropin_reference.cpp: the "DDA input" sequence of main.cpp:165-251 and the
+    point objective), built and linked with libtdda.  Matrix3cd A = Core.A_dic_generator(...)
+    (ObjDDAModel.cpp:60) and R = Core.get_R() into a VectorXi* (ObjDDAModel.cpp:37) compile.
+    Skipped where the reference checkout is absent; running it needs a CUDA device."""
+    tdda.load()
+    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "dropin-if-present"], capture_output=True,
+                       text=True)
+    if "reference sources absent" in r.stdout:
+        pytest.skip("reference checkout absent")
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert os.path.exists(os.path.join(ROOT, "oracle", "_ref", "dropin_reference"))
 
 
 @pytest.mark.gpu

@@ -6,8 +6,10 @@ Every call goes through libtdda's C ABI.  Tolerances:
   * A-product, FP32 convolution: 1e-5 relative;
   * FP64 solve at the reference's tolerance 1e-5: converged, |E - A P|/|E| <= 1e-5 checked
     with the oracle, P and Einternal within 2e-4 of the reference's and the iteration
-    count within 15% -- the reference's own solve moves by O(1e-5) and several
-    iterations under a rounding-level change of its product (test_oracle_golden.py);
+    count inside the spread the reference's own count shows under rounding-level changes
+    (measured: cfg 1 55-71 around the reference's 61; tests/golden/iters_spread.npz) -- the
+    reference's own solve moves by O(1e-5) and several iterations under a rounding-level
+    change of its product (test_oracle_golden.py);
   * FP64 solve at 1e-10: P and Einternal within 1e-9 of the reference's run at 1e-10.
 """
 import numpy as np
@@ -193,7 +195,14 @@ def test_fp64_solve_matches_reference_at_its_tolerance(name):
     assert info["status"] == tdda.OK
     assert info["error"] <= float(g["max_err"])
     it_ref = int(g["iterations"])
-    assert abs(m.get_ITERATION() - it_ref) <= max(1, int(0.15 * it_ref))
+    # the window is the measured spread of the reference's own count under rounding-level
+    # changes (its 2N-1 grid and the GPU's grid, E and 16 one-ulp perturbations of E each;
+    # tests/golden/make_golden_configs.py)
+    spread = golden("iters_spread.npz")[name][:, 2]
+    print(f"\n{name}: GPU FP64 {m.get_ITERATION()} iterations, reference {it_ref}, "
+          f"reference under rounding changes {int(spread.min())}-{int(spread.max())}")
+    assert int(spread.min()) <= it_ref <= int(spread.max())
+    assert int(spread.min()) <= m.get_ITERATION() <= int(spread.max())
     assert _true_residual(g, m.get_P(), m.get_E()) <= 1.5 * float(g["max_err"])
     assert rel(m.get_P(), g["P"]) <= 2e-4
     assert rel(m.get_Einternal(), g["Einternal"]) <= 2e-4

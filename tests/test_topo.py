@@ -2,10 +2,12 @@
 
 CPU: the LDR tensor restated with numpy equals the oracle's; the design map's transpose
 is its adjoint; dal/deps equals a finite difference of 1/alpha_LDR; the optimiser moments
-follow EvoDDAModel.cpp:673-731.  GPU: the device objective and sensitivity equal their host
+follow EvoDDAModel.cpp:673-731; the projection and its beta schedule follow
+FilterOption.cpp:23-62, and the reference's diagonal chain form restates gradients_filtered
+(EvoDDAModel.cpp:1177-1225).  GPU: the device objective and sensitivity equal their host
 restatement from the downloaded fields; the adjoint gradient (forward + 3 basis adjoints
-batched) equals central finite differences of the objective; gradient ascent raises the
-objective.
+batched) equals central finite differences of the objective, also through the projection;
+gradient ascent raises the objective.
 """
 import math
 from types import SimpleNamespace
@@ -133,4 +135,104 @@ def test_device_glue_equals_host_restatement():
     g_dip = -2.0 * np.real((lam * dal * P).reshape(-1, 3).sum(axis=1))
     g_host = dm.grad_theta(g_dip.reshape(Nx, Ny, Nz).sum(axis=2))
     assert rel(r.grad_theta, g_host) <= 1e-10
+    loop.close()
+
+
+def _smooth_density_restated(x, ita, beta):
+    """FilterOption::SmoothDensity (FilterOption.cpp:48-62), one value at a time."""
+    if 0.0 <= x <= ita:
+        return ita * (math.exp(-beta * (1 - x / ita)) - (1 - x / ita) * math.exp(-beta))
+    if ita < x <= 1.0:
+        return (1 - ita) * (1 - math.exp(-beta * (x - ita) / (1 - ita)) + (x - ita) / (1 - ita) * math.exp(-beta)) + ita
+    raise ValueError
+
+
+def test_projection_follows_the_reference():
+    for ita in (0.5, 0.3):
+        p = topo.Projection(1.0, 40.0, ita, "exp")
+        for it in (0, 37, 99):
+            beta = p.update_beta(it, 99)
+            assert beta == pytest.approx(1.0 + 39.0 * math.exp(it / 99 - 1.0), rel=1e-15)
+            x = np.linspace(0.0, 1.0, 41)
+            h = p(x)
+            assert np.allclose(h, [_smooth_density_restated(v, ita, beta) for v in x], rtol=1e-14, atol=1e-15)
+            assert h[0] == pytest.approx(0.0, abs=1e-15) and h[-1] == pytest.approx(1.0, abs=1e-15)
+            xi = np.linspace(0.01, 0.99, 17)
+            xi = xi[np.abs(xi - ita) > 1e-3]
+            fd = (p(xi + 1e-7) - p(xi - 1e-7)) / 2e-7
+            assert np.allclose(p.derivative(xi), fd, rtol=1e-6)
+    with pytest.raises(ValueError):
+        topo.Projection(1.0, 10.0)(np.array([1.2]))
+    with pytest.raises(ValueError):
+        topo.Projection(1.0, 10.0, kind="cubic")
+    # tools.cpp:780-798
+    assert topo.beta_schedule("piecewise", 50, 100, 1, 41) == 1
+    assert topo.beta_schedule("piecewise", 60, 100, 1, 41) == 3
+    assert topo.beta_schedule("piecewise", 75, 100, 1, 41) == 5
+    assert topo.beta_schedule("piecewise", 81, 100, 1, 41) == 41
+    assert topo.beta_schedule("linear", 25, 100, 1, 41) == 11
+    # fixit: the schedule runs over MAX_ITERATION_FIXED steps (FilterOption.cpp:23-27)
+    pf = topo.Projection(1.0, 41.0, kind="linear", fixed_steps=50)
+    assert pf.update_beta(25, 200) == 21
+
+
+def test_reference_chain_form_restates_gradients_filtered():
+    """The "reference" chain rule against a literal restatement of gradients_filtered's loops
+    (EvoDDAModel.cpp:1177-1225) over the design map's filter weights, one free parameter per
+    (x, y) column and no mirror (a 1 x 1 quadrant would hide the structure, so the map's mirror
+    is bypassed by comparing before mirror_t)."""
+    Nx, Ny = 7, 6
+    dm = topo.DesignMap(Nx, Ny, 2.0)
+    rng = np.random.Generator(np.random.PCG64(12))
+    rf = rng.uniform(0.05, 0.95, (Nx, Ny))
+    g = rng.standard_normal((Nx, Ny))
+    proj = topo.Projection(2.0, 30.0, 0.5)
+    proj.update_beta(10, 99)
+    # FreeWeight[i]: (position, weight) of the parameters filtered into parameter i
+    free_weight = []
+    for x in range(Nx):
+        for y in range(Ny):
+            lst = []
+            for dx, dy, w in dm.taps:
+                xs, ys = x + dx, y + dy
+                if 0 <= xs < Nx and 0 <= ys < Ny:
+                    lst.append((xs * Ny + ys, w))
+            free_weight.append(lst)
+    n = Nx * Ny
+    result = np.zeros(n)
+    for lst in free_weight:
+        s = sum(w for _, w in lst)
+        for pos, w in lst:
+            result[pos] += w / s
+    gf = g.ravel()
+    for i in range(n):
+        result[i] = result[i] * proj.derivative(rf.ravel()[i]) * gf[i]
+    colsum = dm.filter_t(np.ones((Nx, Ny)))
+    ours = colsum * proj.derivative(rf) * g
+    assert np.allclose(ours.ravel(), result, rtol=1e-13, atol=1e-15)
+
+
+@pytest.mark.gpu
+def test_adjoint_gradient_through_the_projection_equals_finite_differences():
+    if tdda.device_count() < 1:
+        pytest.skip("no CUDA device")
+    Nx, Ny, Nz, d = 6, 6, 4, 10.0
+    rng = np.random.Generator(np.random.PCG64(18))
+    th0 = 0.3 + 0.4 * rng.random((3, 3))
+    r_obs = (d * (Nx - 1) / 2, d * (Ny - 1) / 2, d * (Nz - 1) + 100.0)
+    proj = topo.Projection(2.0, 20.0, 0.5, "exp")
+    loop = topo.TopoLoop(Nx, Ny, Nz, d, 500.0, np.array([1.0, 4.0 + 0.1j]), th0, r_obs, precision=tdda.FP64,
+                         tol=1e-12, projection=proj, max_steps=50)
+    loop.iteration = 30  # beta = update_beta(29, 49), well above beta_min
+    g = loop.evaluate().grad_theta
+    assert loop.projection.beta == pytest.approx(2.0 + 18.0 * math.exp(29 / 49 - 1.0))
+    h = 1e-6
+    for (i, j) in ((0, 0), (1, 2), (2, 1)):
+        fs = []
+        for s in (+1, -1):
+            loop.theta = th0.copy()
+            loop.theta[i, j] += s * h
+            fs.append(loop.evaluate().objective)
+        fd = (fs[0] - fs[1]) / (2 * h)
+        assert abs(g[i, j] - fd) <= 1e-5 * max(abs(fd), 1e-30) + 1e-12, (i, j, g[i, j], fd)
     loop.close()

@@ -42,6 +42,35 @@ def test_noalloc_matches_allocating_product_twice(idx):
     core.close()
 
 
+def test_noalloc_smaller_grid_after_a_larger_one():
+    """The static array keeps the last call's contents.  A product on the 64x64x16 grid
+    fills it with values laid out for that grid's strides; the next product, on the
+    20x20x10 grid and then on a sparse lattice, must read only entries it wrote itself."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.Generator(np.random.PCG64(300))
+    big = tdda.lattice.config(2)
+    small = tdda.lattice.config(1)
+    keep = rng.random(small.N) < 0.6
+    Rs = small.R.reshape(-1, 3)[keep].ravel()
+    cases = [(big.Nx, big.Ny, big.Nz, big.R, big.d, big.lam, big.material),
+             (small.Nx, small.Ny, small.Nz, small.R, small.d, small.lam, small.material),
+             (big.Nx, big.Ny, big.Nz, big.R, big.d, big.lam, big.material),
+             (small.Nx, small.Ny, small.Nz, Rs, small.d, small.lam, small.material)]
+    for k, (Nx, Ny, Nz, R, d, lam, mat) in enumerate(cases):
+        core = tdda.AProductCore(Nx, Ny, Nz, R, d, lam, mat)
+        n3 = R.size
+        b = rng.standard_normal(n3) + 1j * rng.standard_normal(n3)
+        ref = core.Aproduct(b)
+        bd = torch.from_numpy(b).to("cuda")
+        yd = torch.full_like(bd, complex(np.nan, np.nan))
+        torch.cuda.synchronize()
+        core.Aproduct_noalloc(bd.data_ptr(), yd.data_ptr())
+        y = yd.cpu().numpy()
+        assert np.all(np.isfinite(y)), f"case {k}"
+        assert rel(y, ref) <= 1e-12, f"case {k}"
+        core.close()
+
+
 def test_noalloc_rejects_grids_beyond_its_static_size():
     torch = pytest.importorskip("torch")
     Nx, Ny, Nz = 128, 128, 32  # grid 3 x 128 x 256 x 64 entries > 4,194,304

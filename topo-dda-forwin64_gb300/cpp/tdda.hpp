@@ -19,13 +19,23 @@
 //     with data()/size() and a size constructor (Eigen::VectorXcd,
 //     std::vector<std::complex<double>>), chosen by DDAModelT's parameter.
 //
+// With Eigen (included before this header, as the reference's own headers do
+// through Tools.h, or TDDA_WITH_EIGEN defined with Eigen on the include path)
+// the getters and tensors take the reference's Eigen types, so its callers
+// compile unchanged: A_dic_generator / LDR_inter return Matrix3cd, get_R()
+// VectorXi*, get_diel_old() VectorXd*, get_material() VectorXcd*, and
+// DDAModel::get_nK / get_nE0 Vector3d (AProductCore.h:51-80, DDAModel.h:34-74;
+// ObjDDAModel.cpp:20-60 uses them so).  Without Eigen they are std::array /
+// std::vector.
+//
 // Behaviour matches the reference where it is observable: the material is
 // normalised and a vacuum permittivity bumped to 1.01 (AProductCore.cpp:19-24);
 // bicgstab prints its progress when verbose and leaves get_ITERATION()
 // unchanged when it does not converge (DDAModel.cpp:256-259); an unknown
 // method string throws std::invalid_argument (AProductCore.cpp:567-569).  CUDA
 // or argument errors, which the reference never checks, throw
-// std::runtime_error.  The FCD tensor is not built and is rejected.
+// std::runtime_error.  The method string selects the interaction tensor:
+// "LDR" or "FCD" (AProductCore.cpp:560-571), both built on the device.
 #pragma once
 
 #include <array>
@@ -37,13 +47,51 @@
 #include <iostream>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "tdda.h"
 
+#if defined(TDDA_WITH_EIGEN) && !defined(EIGEN_WORLD_VERSION)
+#include <Eigen/Core>
+#endif
+#if defined(EIGEN_WORLD_VERSION)
+#define TDDA_EIGEN_TYPES 1
+#else
+#define TDDA_EIGEN_TYPES 0
+#endif
+
 namespace tdda {
 
 using cplx = std::complex<double>;
+
+// the reference's value types (Eigen), or their plain stand-ins
+#if TDDA_EIGEN_TYPES
+using Tensor3 = Eigen::Matrix3cd;
+using IndexVec = Eigen::VectorXi;
+using RealVec = Eigen::VectorXd;
+using MaterialVec = Eigen::VectorXcd;
+using Vec3 = Eigen::Vector3d;
+inline Tensor3 make_tensor(const cplx (&a)[6]) {
+    Tensor3 m;
+    m << a[0], a[1], a[2], a[1], a[3], a[4], a[2], a[4], a[5];
+    return m;
+}
+inline Vec3 make_vec3(const double (&v)[3]) { return Vec3(v[0], v[1], v[2]); }
+inline void scale(Tensor3& m, double f) { m *= f; }
+#else
+using Tensor3 = std::array<std::array<cplx, 3>, 3>;
+using IndexVec = std::vector<int>;
+using RealVec = std::vector<double>;
+using MaterialVec = std::vector<cplx>;
+using Vec3 = std::array<double, 3>;
+inline Tensor3 make_tensor(const cplx (&a)[6]) { return {{{a[0], a[1], a[2]}, {a[1], a[3], a[4]}, {a[2], a[4], a[5]}}}; }
+inline Vec3 make_vec3(const double (&v)[3]) { return {v[0], v[1], v[2]}; }
+inline void scale(Tensor3& m, double f) {
+    for (auto& row : m)
+        for (auto& v : row) v *= f;
+}
+#endif
 
 inline void check(tdda_status st, const char* where) {
     if (st != TDDA_OK) throw std::runtime_error(std::string(where) + ": " + tdda_last_error());
@@ -87,12 +135,16 @@ class AProductCore {
         d_ = CStr->get_d();
         const auto* R = CStr->get_R();
         R_.resize(3 * (size_t)N_);
-        for (size_t i = 0; i < R_.size(); i++) R_[i] = (int)(*R)(i);
+        for (size_t i = 0; i < (size_t)R_.size(); i++) R_[i] = (int)(*R)(i);
         diel_old_ = [CStr](std::vector<double>& out) {
             const auto* dv = CStr->get_diel_old();
             out.resize((size_t)dv->size());
             for (size_t i = 0; i < out.size(); i++) out[i] = (*dv)(i);
         };
+        // get_diel_old() hands out the structure's own vector, as the reference does
+        // (AProductCore::get_diel_old returns CStr->get_diel_old())
+        if constexpr (std::is_convertible<decltype(CStr->get_diel_old()), RealVec*>::value)
+            diel_ptr_ = [CStr]() -> RealVec* { return CStr->get_diel_old(); };
         std::vector<double> mat(2 * (size_t)material.size());
         for (size_t i = 0; i < (size_t)material.size(); i++) {
             mat[2 * i] = std::real(material[i]);
@@ -129,29 +181,27 @@ class AProductCore {
         return y;
     }
     // Matrix3cd LDR_inter(double x, double y, double z)     AProductCore.cpp:588-623
-    std::array<std::array<cplx, 3>, 3> LDR_inter(double x, double y, double z) const {
+    Tensor3 LDR_inter(double x, double y, double z) const {
         double t[12];
         check(tdda_core_ldr_inter(h_, x, y, z, t), "LDR_inter");
         cplx a[6];
         for (int l = 0; l < 6; l++) a[l] = cplx(t[2 * l], t[2 * l + 1]);
-        return {{{a[0], a[1], a[2]}, {a[1], a[3], a[4]}, {a[2], a[4], a[5]}}};
+        return make_tensor(a);
     }
     // Matrix3cd A_dic_generator(double x, double y, double z)     AProductCore.cpp:560-571 (LDR or FCD)
-    std::array<std::array<cplx, 3>, 3> A_dic_generator(double x, double y, double z) const {
+    Tensor3 A_dic_generator(double x, double y, double z) const {
         double t[12];
         check(tdda_core_interaction(h_, x, y, z, t), "A_dic_generator");
         cplx a[6];
         for (int l = 0; l < 6; l++) a[l] = cplx(t[2 * l], t[2 * l + 1]);
-        return {{{a[0], a[1], a[2]}, {a[1], a[3], a[4]}, {a[2], a[4], a[5]}}};
+        return make_tensor(a);
     }
     // Matrix3cd A_dic_generator(double x, double y, double z, int m, int n)     AProductCore.cpp:573-586
-    std::array<std::array<cplx, 3>, 3> A_dic_generator(double x, double y, double z, int m, int n) const {
+    Tensor3 A_dic_generator(double x, double y, double z, int m, int n) const {
         x = x + m * Lm_;
         y = y + n * Ln_;
-        auto r = A_dic_generator(x, y, z);
-        const double ph = std::exp(-std::pow(0.01 * K_ * std::sqrt(x * x + y * y + z * z), 4));
-        for (auto& row : r)
-            for (auto& v : row) v *= ph;
+        Tensor3 r = A_dic_generator(x, y, z);
+        scale(r, std::exp(-std::pow(0.01 * K_ * std::sqrt(x * x + y * y + z * z), 4)));
         return r;
     }
 
@@ -163,8 +213,21 @@ class AProductCore {
     double get_lam() const { return lam_; }
     double get_K() const { return K_; }
     double get_nback() const { return nback_; }
-    const std::vector<cplx>* get_material() const { return &material_; }
-    const std::vector<int>* get_R() const { return &R_; }
+    double get_Lm() const { return Lm_; }
+    double get_Ln() const { return Ln_; }
+    // VectorXcd* get_material(), VectorXi* get_R(), VectorXd* get_diel_old()   AProductCore.h:66-75
+    MaterialVec* get_material() { return &material_; }
+    const MaterialVec* get_material() const { return &material_; }
+    IndexVec* get_R() { return &R_; }
+    const IndexVec* get_R() const { return &R_; }
+    RealVec* get_diel_old() {
+        if (diel_ptr_) return diel_ptr_();
+        std::vector<double> tmp;
+        diel_old_(tmp);
+        diel_copy_.resize(tmp.size());
+        for (size_t i = 0; i < tmp.size(); i++) diel_copy_[i] = tmp[i];
+        return &diel_copy_;
+    }
     std::array<int, 3> grid() const { return grid_; }
     tdda_core* handle() const { return h_; }
     // Not in the reference: times the FP32 x pass's forms and tiles on this core's
@@ -181,10 +244,12 @@ class AProductCore {
     tdda_core* h_ = nullptr;
     int N_ = 0, Nx_ = 0, Ny_ = 0, Nz_ = 0;
     double d_ = 0, lam_ = 0, nback_ = 1, K_ = 0;
-    std::vector<int> R_;
-    std::vector<cplx> material_;
+    IndexVec R_;
+    MaterialVec material_;
     std::array<int, 3> grid_{{0, 0, 0}};
     std::function<void(std::vector<double>&)> diel_old_;
+    std::function<RealVec*()> diel_ptr_;
+    RealVec diel_copy_;  // get_diel_old() of a structure whose vector is of another type
     int MAXm_ = 0, MAXn_ = 0;  // periodic images (AProductCore.h members of the periodic ctor)
     double Lm_ = 0, Ln_ = 0;
 };
@@ -229,6 +294,9 @@ template <class VectorXcd = std::vector<cplx>> class DDAModelT {
 
     // void bicgstab(int MAX_ITERATION, double MAX_ERROR)     DDAModel.cpp:131-260
     void bicgstab(int MAX_ITERATION, double MAX_ERROR) { solve(MAX_ITERATION, MAX_ERROR, TDDA_FP64); }
+    // bicgstab(int, double, int EVOITERATION) (DDAModel.h:41, a debug overload that prints
+    // at one optimisation step): the same solve
+    void bicgstab(int MAX_ITERATION, double MAX_ERROR, int /*EVOITERATION*/) { bicgstab(MAX_ITERATION, MAX_ERROR); }
     // the same solve with the FP32 convolution and FP64 refinement
     void bicgstab_mixed(int MAX_ITERATION, double MAX_ERROR) { solve(MAX_ITERATION, MAX_ERROR, TDDA_FP32_REFINE); }
 
@@ -292,8 +360,21 @@ template <class VectorXcd = std::vector<cplx>> class DDAModelT {
     VectorXcd* get_al() { return &al_; }
     int get_ITERATION() const { return tdda_model_iterations(h_); }
     double get_E0() const { return E0_; }
+    // Vector3d get_nE0() / get_nK()   DDAModel.h:52-53
+    Vec3 get_nE0() const { return make_vec3(nE0_); }
+    Vec3 get_nK() const { return make_vec3(nK_); }
     AProductCore* get_Core() { return core_; }
+    // the core's getters, forwarded as DDAModel.h:63-73 declares them
     int get_N() const { return core_->get_N(); }
+    int get_Nx() const { return core_->get_Nx(); }
+    int get_Ny() const { return core_->get_Ny(); }
+    int get_Nz() const { return core_->get_Nz(); }
+    IndexVec* get_R() { return core_->get_R(); }
+    double get_d() const { return core_->get_d(); }
+    double get_lam() const { return core_->get_lam(); }
+    double get_K() const { return core_->get_K(); }
+    RealVec* get_diel_old() { return core_->get_diel_old(); }
+    MaterialVec* get_material() { return core_->get_material(); }
     const tdda_solve_info& last_info() const { return info_; }
     tdda_model* handle() const { return h_; }
 

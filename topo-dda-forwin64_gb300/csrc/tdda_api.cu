@@ -737,7 +737,8 @@ tdda_status solve_mixed(tdda_model* const* ms, int n, int max_it, double tol, td
                 continue;
             }
             Enorm[i] = s.Enorm;
-            res[i] = Enorm[i] > 0 ? std::sqrt(s.rnorm2) / Enorm[i] : 0.0;
+            // a NaN in E makes |E| NaN, which the zero-E test below would take for 0
+            res[i] = !std::isfinite(Enorm[i]) ? Enorm[i] : (Enorm[i] > 0 ? std::sqrt(s.rnorm2) / Enorm[i] : 0.0);
             if (!std::isfinite(res[i])) {
                 done[i] = 1;
                 stat[i] = TDDA_ERR_NAN;

@@ -226,6 +226,9 @@ class AProductCore:
                                                ctypes.byref(h)), "tdda_core_create_periodic")
         self.periodic = periodic
         self.h = h
+        # handles of the live models on this core: a model must be destroyed before its core,
+        # and the garbage collector may finalise a core and its models in any order
+        self._models = set()
         self.max_rhs = int(max_rhs)
         K = ctypes.c_double()
         g = (ctypes.c_int * 3)()
@@ -320,6 +323,9 @@ class AProductCore:
 
     def close(self):
         if getattr(self, "h", None):
+            for mh in list(getattr(self, "_models", ())):
+                load().tdda_model_destroy(ctypes.c_void_p(mh))
+            self._models = set()
             load().tdda_core_destroy(self.h)
             self.h = None
 
@@ -345,6 +351,7 @@ class DDAModel:
         _check(load().tdda_model_create(core.h, _dptr(nK), float(E0), _dptr(nE), _dptr(diel), ctypes.byref(h)),
                "tdda_model_create")
         self.h = h
+        core._models.add(h.value)
         self.last_info = None
 
     def _get(self, field: int, out: np.ndarray = None) -> np.ndarray:
@@ -432,8 +439,12 @@ class DDAModel:
         _check(load().tdda_model_update_E_in_structure(self.h), "update_E_in_structure")
 
     def close(self):
+        """Destroys the model; a no-op when its core was closed first (which destroyed it)."""
         if getattr(self, "h", None):
-            load().tdda_model_destroy(self.h)
+            live = getattr(self.core, "_models", set())
+            if self.h.value in live:
+                live.discard(self.h.value)
+                load().tdda_model_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -449,7 +460,8 @@ def solve_batch(models, precision: int = FP64, max_it: int = 10000, tol: float =
     arr = (ctypes.c_void_p * n)(*[m.h.value for m in models])
     infos = (SolveInfo * n)()
     st = load().tdda_solve_batch(arr, n, int(precision), int(max_it), float(tol), infos)
-    _check(st, "tdda_solve_batch", allowed=(OK, NOT_CONVERGED, BREAKDOWN))
+    # a right-hand side that stops without converging reports it in its own info
+    _check(st, "tdda_solve_batch", allowed=(OK, NOT_CONVERGED, BREAKDOWN, ERR_NAN))
     out = [infos[k].as_dict() for k in range(n)]
     for m, o in zip(models, out):
         m.last_info = o

@@ -23,6 +23,11 @@ transposed chain.  The step is gradient ascent: the gradient is scaled so that
 its mean magnitude is at least 0.1 (EvoDDAModel.cpp:734-738) and multiplied by
 epsilon = 0.1, so the mean step is 0.01; theta is clipped to [0, 1].
 
+With a Projection, rho = H_beta(filter(mirror4(theta))): the reference's smooth Heaviside
+(FilterOption::SmoothDensity, FilterOption.cpp:48-62) with beta on its exp / piecewise /
+linear schedule (FilterOption.cpp:23-46), and the gradient passes through H' on the way back
+(EvoDDAModel.cpp:1177-1225), either exactly or in the reference's diagonal form.
+
 The step follows EvoDDAModel.cpp:640-735: optional Adam / Adamdecay / Adagrad
 moments on the parameter gradient, the mean-magnitude normalisation and the
 step epsilon * g.
@@ -135,6 +140,69 @@ class DesignMap:
         return self.mirror_t(self.filter_t(g_xy))
 
 
+def beta_schedule(kind: str, x: float, x_max: float, beta_min: float, beta_max: float) -> float:
+    """The projection sharpness at optimisation step x of x_max (FilterOption::update_beta,
+    FilterOption.cpp:23-46, with tools.cpp:776-798): "exp", "piecewise" or "linear"."""
+    if kind == "exp":
+        return beta_min + (beta_max - beta_min) * math.exp(x / x_max - 1.0)
+    if kind == "piecewise":
+        if x <= 0.5 * x_max:
+            return beta_min
+        if x <= 0.7 * x_max:
+            return beta_min + (beta_max - beta_min) / 20
+        if x <= 0.8 * x_max:
+            return beta_min + (beta_max - beta_min) / 10
+        return beta_max
+    if kind == "linear":
+        return beta_min + (beta_max - beta_min) * x / x_max
+    raise ValueError(f"beta schedule {kind!r} is not defined")
+
+
+class Projection:
+    """Smooth Heaviside projection of the filtered density (FilterOption, FilterOption.cpp:5-62):
+
+        H(x) = ita (exp(-beta (1 - x/ita)) - (1 - x/ita) exp(-beta))                     x <= ita
+        H(x) = (1-ita) (1 - exp(-beta (x-ita)/(1-ita)) + (x-ita)/(1-ita) exp(-beta)) + ita  x > ita
+
+    for x in [0, 1] (SmoothDensity, :48-62), and its derivative
+    H'(x) = beta exp(-beta (1 - x/ita)) + exp(-beta) below ita, beta exp(-beta (x-ita)/(1-ita)) +
+    exp(-beta) above (PtoFderivative, EvoDDAModel.cpp:1163-1175).  beta follows the schedule of
+    update_beta from beta_min at step 0 to beta_max at step x_max; with fixit the schedule runs
+    over MAX_ITERATION_FIXED steps instead (FilterOption.cpp:23-27)."""
+
+    def __init__(self, beta_min: float, beta_max: float, ita: float = 0.5, kind: str = "exp",
+                 fixed_steps: int = 0):
+        beta_schedule(kind, 0.0, 1.0, beta_min, beta_max)  # rejects an unknown schedule
+        self.beta_min, self.beta_max, self.ita, self.kind = float(beta_min), float(beta_max), float(ita), kind
+        self.fixed_steps = int(fixed_steps)
+        self.beta = self.beta_min
+
+    def update_beta(self, iteration: int, max_iteration: int) -> float:
+        x_max = self.fixed_steps if self.fixed_steps > 0 else max_iteration
+        self.beta = beta_schedule(self.kind, float(iteration), float(x_max), self.beta_min, self.beta_max)
+        return self.beta
+
+    def _check(self, x):
+        x = np.asarray(x, np.float64)
+        if np.any(x < 0.0) or np.any(x > 1.0) or np.any(np.isnan(x)):
+            raise ValueError("SmoothDensity: input out of range [0, 1]")
+        return x
+
+    def __call__(self, x):
+        x = self._check(x)
+        b, it = self.beta, self.ita
+        lo = it * (np.exp(-b * (1 - x / it)) - (1 - x / it) * math.exp(-b))
+        hi = (1 - it) * (1 - np.exp(-b * (x - it) / (1 - it)) + (x - it) / (1 - it) * math.exp(-b)) + it
+        return np.where(x <= it, lo, hi)
+
+    def derivative(self, x):
+        x = self._check(x)
+        b, it = self.beta, self.ita
+        lo = b * np.exp(-b * (1 - x / it)) + math.exp(-b)
+        hi = b * np.exp(-b * (x - it) / (1 - it)) + math.exp(-b)
+        return np.where(x <= it, lo, hi)
+
+
 @dataclass
 class StepResult:
     objective: float
@@ -147,7 +215,13 @@ class TopoLoop:
 
     def __init__(self, Nx, Ny, Nz, d, lam, material, theta0, r_obs, precision=FP32_REFINE, tol=1e-5,
                  max_it=10000, nK=(0.0, 0.0, 1.0), nE0=(1.0, 0.0, 0.0), E0=1.0, filter_r=2.0, epsilon=0.1,
-                 method="grad"):
+                 method="grad", projection: Projection = None, max_steps: int = 200, chain: str = "exact"):
+        """projection: the smooth Heaviside applied after the filter, its beta scheduled over
+        max_steps steps (the reference's MAX_ITERATION_EVO); chain "exact" (the transposed
+        chain rule through filter and projection, checked against finite differences) or
+        "reference" (the reference's diagonal form of gradients_filtered,
+        EvoDDAModel.cpp:1177-1225: each column's gradient times the column sum of the
+        normalised filter weights and the projection's slope at that column)."""
         self.Nx, self.Ny, self.Nz, self.d = Nx, Ny, Nz, d
         self.R = lattice.bulk(Nx, Ny, Nz)
         self.map = DesignMap(Nx, Ny, filter_r)
@@ -155,6 +229,10 @@ class TopoLoop:
         self.precision, self.tol, self.max_it, self.epsilon = precision, tol, max_it, epsilon
         self.nK, self.nE0, self.E0 = np.array(nK, float), np.array(nE0, float), float(E0)
         self.r_obs = np.array(r_obs, float)
+        if chain not in ("exact", "reference"):
+            raise ValueError(f"unknown chain rule {chain!r}")
+        self.projection, self.max_steps, self.chain = projection, int(max_steps), chain
+        self.iteration = 0
         self.core = AProductCore(Nx, Ny, Nz, self.R, d, lam, material, max_rhs=4)
         self.K = self.core.K
         self.mat = self.core.get_material()  # normalised (vacuum -> 1.01)
@@ -176,12 +254,24 @@ class TopoLoop:
         if method not in ("grad", "Adam", "Adamdecay", "Adagrad"):
             raise ValueError(f"unknown optimiser {method!r}")
         self.method = method
-        self.iteration = 0
         self.V = self.S_ad = None
         self.gsq = np.zeros_like(self.theta)  # Adagrad accumulator (EvoDDAModel.cpp:36)
 
-    def _rho(self):
+    def _beta(self):
+        """The projection's beta for the current step: the structure of step it was projected
+        with update_beta(it - 1, MAX - 1) (CoreStructure.cpp:46, EvoDDAModel.cpp:750), and its
+        gradient uses the same beta (EvoDDAModel.cpp:645-648)."""
+        return self.projection.update_beta(max(self.iteration - 1, 0), self.max_steps - 1)
+
+    def _filtered(self):
         return np.clip(self.map.rho(self.theta), 0.0, 1.0)
+
+    def _rho(self):
+        rf = self._filtered()
+        if self.projection is None:
+            return rf
+        self._beta()
+        return self.projection(rf)
 
     def _diel(self):
         rho_xy = self._rho()
@@ -202,7 +292,20 @@ class TopoLoop:
         s = self.fwd.density_gradient(self.adj, np.conj(E_obs), self.col_off, self.col_dip)
         g_xy = (-2.0 * s).reshape(self.Nx, self.Ny)
         # rho is clipped to [0, 1]; the filter keeps it inside, so the clip is inactive
-        return StepResult(f, [i["iterations"] for i in infos], self.map.grad_theta(g_xy))
+        return StepResult(f, [i["iterations"] for i in infos], self.grad_theta(g_xy))
+
+    def grad_theta(self, g_xy):
+        """df/dtheta from df/drho per (x, y) column through projection, filter and mirror."""
+        if self.projection is None:
+            return self.map.grad_theta(g_xy)
+        rf = self._filtered()
+        self._beta()
+        slope = self.projection.derivative(rf)
+        if self.chain == "exact":
+            return self.map.mirror_t(self.map.filter_t(slope * g_xy))
+        # EvoDDAModel.cpp:1199-1221: result(p) = (sum_i w_ip / sum_j w_ij) H'(rho_f(p)) g(p)
+        colsum = self.map.filter_t(np.ones_like(g_xy))
+        return self.map.mirror_t(colsum * slope * g_xy)
 
     def _moments(self, g):
         """Adam / Adamdecay / Adagrad of EvoDDAModel.cpp:673-731 (beta1 = 0.9,
