@@ -13,8 +13,8 @@ ours       FP32 FFT convolution + Krylov vectors, double-float dot sums, the res
            timed beside it (fp64).  Inputs are resident in HBM in the device-timed region;
            `e2e` is the same solve through the C ABI with host buffers.
 reference  the reference's solve path run on the host cores (the oracle port of
-           AProductCore::Aproduct + DDAModel::bicgstab, all host threads, one solve per
-           thread), a bounded sample scaled to solves/s.
+           AProductCore::Aproduct + DDAModel::bicgstab, all host threads, one full converged
+           solve per thread per step), solves/s.
 
 Multi-GPU: the solve does not shard; N ranks run N independent replicas (weak scaling).
 """
@@ -43,9 +43,6 @@ UNIT = "solves/s"
 TOL = 1e-5
 MAX_IT = 10000
 WORKLOAD = "mixed-precision single solve 64x64x16 (cfg 2)"
-# iteration count of the oracle's FP64 BiCGSTAB on this lattice run to convergence
-# (tol 1e-5); scales the bounded CPU sample to a full solve
-ORACLE_FP64_ITERATIONS_CFG2 = 29
 
 
 # --------------------------------------------------------------------------- helpers
@@ -201,14 +198,35 @@ def pass_names(core, precision):
 
 
 # ------------------------------------------------------------------ CPU baseline
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu / /proc/cpuinfo), or the platform's machine name."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                if ln.lower().startswith(("model name", "cpu model")):
+                    return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
+
+
 class CpuBaseline:
-    """Bounded sample of the reference's solve path on the host cores: `threads`
-    independent solves of the workload (one per thread, the oracle's FP64 restatement of
-    AProductCore::Aproduct + DDAModel::bicgstab, FFT grid pruned to the lattice), each
-    stopped after its 3 initial products and `iters` BiCGSTAB iterations.  The time of a
-    full solve is that sample scaled by the product count (3 + 2 * iterations) of the
-    oracle's converged FP64 solve of the same lattice.  The operators (Green spectra) are
-    built once, outside the sample, as the GPU path builds its core once."""
+    """The reference's solve path on the host cores: `threads` independent solves of the
+    workload (one per thread, the oracle's FP64 restatement of AProductCore::Aproduct +
+    DDAModel::bicgstab, pinned bit-exact to the reference's own sources on the smaller
+    fixtures), each a full converged BiCGSTAB solve to tol 1e-5 from P = 0.  The FFT grid
+    is the smooth 2N grid with the zero halves pruned, which makes the port faster than
+    the reference's own host path (prime 2N-1 lengths and an O(M) host scatter/gather per
+    product, AProductCore.cpp:697-758).  The operators (Green spectra) are built once,
+    outside the sample, as the GPU path builds its core once."""
 
     def __init__(self, w, threads: int):
         import oracle as O
@@ -223,12 +241,17 @@ class CpuBaseline:
         self.models = [O.OracleModel(c, inc.nK, inc.E0, inc.nE0, w.diel_old) for c in self.cores]
         self.zero = np.zeros(3 * w.N, np.complex128)
 
-    def sample(self, iters: int) -> dict:
+    def sample(self, iters: int = 0) -> dict:
+        """One step: every thread runs one solve at once.  iters = 0: each solve runs to
+        convergence (the measured sample); iters > 0: each stops after `iters` iterations
+        (warm-up only)."""
         for m in self.models:
             m.InitializeP(self.zero)
+            m.ITERATION = 0
+        status = [None] * self.threads
 
         def run(k):
-            self.models[k].bicgstab(iters, TOL)  # ctypes releases the GIL for the call
+            status[k] = self.models[k].bicgstab(iters if iters > 0 else MAX_IT, TOL)  # releases the GIL
 
         th = [threading.Thread(target=run, args=(k,)) for k in range(self.threads)]
         t0 = time.perf_counter()
@@ -237,13 +260,15 @@ class CpuBaseline:
         for t in th:
             t.join()
         wall = time.perf_counter() - t0
-        full_its = ORACLE_FP64_ITERATIONS_CFG2
-        scale = (3 + 2 * full_its) / (3 + 2 * iters)
-        return {"value": self.threads / (wall * scale), "unit": UNIT, "cores": self.threads, "kind": "port",
-                "sample": (f"{self.threads} threads x one solve each of the same lattice, stopped after 3 "
-                           f"initial products + {iters} BiCGSTAB iterations ({wall:.2f} s wall), scaled to "
-                           f"the {full_its}-iteration converged FP64 solve of this lattice"),
-                "sample_wall_s": wall}
+        if iters == 0 and any(st != self.O.CONVERGED for st in status):
+            raise RuntimeError(f"CPU baseline solve did not converge: {status}")
+        its = self.models[0].ITERATION
+        return {"value": self.threads / wall, "unit": UNIT, "cores": self.threads, "kind": "port",
+                "cpu_model": cpu_model(),
+                "sample": (f"{self.threads} threads x one full FP64 BiCGSTAB solve each of the same lattice "
+                           f"to tol {TOL:g} ({its} iterations, {wall:.2f} s wall); the oracle port of "
+                           f"the reference's solve path on the 2N grid with pruned zero halves"),
+                "sample_wall_s": wall, "iterations": its}
 
 
 def run_reference(args, dist: Dist):
@@ -255,11 +280,11 @@ def run_reference(args, dist: Dist):
     iters = max(1, args.cpu_iters)
     cpu = CpuBaseline(w, threads)
     for _ in range(args.warmup):
-        cpu.sample(1)
+        cpu.sample(iters)
     vals = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        r = cpu.sample(iters)
+        r = cpu.sample(0)
         vals.append(r["value"])
     total = time.perf_counter() - t0
     v = statistics.median(vals)
@@ -270,7 +295,7 @@ def run_reference(args, dist: Dist):
             "config": {"workload": WORKLOAD, "lattice": [w.Nx, w.Ny, w.Nz], "dipoles": w.N, "tol": TOL,
                        "grid": [lattice.smooth_size(2 * n - 1) for n in (w.Nx, w.Ny, w.Nz)]},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": r["sample"]},
+                             "cpu_model": r["cpu_model"], "sample": r["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -286,8 +311,9 @@ def pinned_f64(n: int) -> np.ndarray:
     return torch.zeros(n, dtype=torch.float64, pin_memory=True).numpy()
 
 
-def time_batch(tdda, torch, w, incs, precision, steps, dev, flush_l2):
-    """Solve len(incs) right-hand sides of one lattice in one batched solve per step."""
+def time_batch(tdda, torch, w, incs, precision, steps, dev, flush_l2, keep_P=False):
+    """Solve len(incs) right-hand sides of one lattice in one batched solve per step
+    (keep_P: the result's polarisations in out["P"])."""
     core = tdda.AProductCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material, w.nback, max_rhs=len(incs), device=dev)
     tune = core.autotune(nrhs=len(incs), reps=10) if precision == tdda.FP32_REFINE else None
     models = [tdda.DDAModel(core, inc.nK, inc.E0, inc.nE0, w.diel_old) for inc in incs]
@@ -319,10 +345,27 @@ def time_batch(tdda, torch, w, incs, precision, steps, dev, flush_l2):
            "pass_ms": prof, "kernels": pass_names(core, precision), "grid": list(core.grid)}
     if tune:
         out["x_pass_autotune"] = tune
+    if keep_P:
+        out["P"] = [m.get_P() for m in models]
     for m in models:
         m.close()
     core.close()
     return out, prof, n32
+
+
+def required_bytes(grid, Nx, N, s, fused, nrhs):
+    """Bytes each kernel of one A-product over nrhs right-hand sides must move, as stored:
+    the same grid and vector terms as pass_bytes, but the x pass reads the folded Green
+    table (6 Hx Hy Hz entries, H = M/2 + 1) once per launch instead of the canonical
+    6 Mx My Mz.  Fused forms only (the compiled FP32 planes) and the five-pass form."""
+    Mx, My, Mz = grid
+    H = (Mx // 2 + 1) * (My // 2 + 1) * (Mz // 2 + 1)
+    plane = 3 * Nx * My * Mz
+    if fused:
+        zy = (3 * N + plane) * s * nrhs
+        return [zy, 0, (2 * plane * nrhs + 6 * H) * s, zy, 0]
+    per = pass_bytes(grid, Nx, 0, 0, N, s, False)
+    return [per[0] * nrhs, per[1] * nrhs, (2 * plane * nrhs + 6 * H) * s, per[3] * nrhs, per[4] * nrhs]
 
 
 def pass_bytes_batch(w, grid, s, fused, nrhs):
@@ -360,9 +403,11 @@ def batched_roofline(w, grid, prof, nrhs, s, peak, kernel, names):
     b = pass_bytes_batch(w, grid, s, True, nrhs)[2]
     t = prof[2]
     ach = b / (t * 1e-3) / 1e9
+    req = required_bytes(grid, w.Nx, w.N, s, True, nrhs)[2]
     passes, whole = pass_rooflines(w, grid, prof, names, s, names[1] == "-", nrhs, peak)
     return {"kernel": kernel, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-            "algorithmic_bytes": b, "avg_ms": t, "traffic": ncu_traffic(f"{kernel}:fp32:cfg3x{nrhs}"),
+            "algorithmic_bytes": b, "avg_ms": t, "required_bytes": req,
+            "frac_required": req / (t * 1e-3) / 1e9 / peak, "traffic": ncu_traffic(f"{kernel}:fp32:cfg3x{nrhs}"),
             "passes": passes, "aproduct": whole}
 
 
@@ -484,6 +529,7 @@ def run_ours(args, dist: Dist):
     info = runs[-1][1]
     t_max = dist.max(sum(ms))
     value = dist.world * args.steps / (t_max / 1000.0)
+    P32 = model.get_P()  # the last timed FP32+refine solve
 
     # the plain FP64 solve of the same lattice, same timing rules
     k64 = max(3, min(args.steps, args.fp64_steps))
@@ -491,6 +537,16 @@ def run_ours(args, dist: Dist):
     r64 = [solve(tdda.FP64) for _ in range(k64)]
     ms64 = [r[0] for r in r64]
     fp64_value = dist.world * k64 / (dist.max(sum(ms64)) / 1000.0)
+    # the FP32+refine result's error against the FP64 solution of the same lattice (FP64
+    # BiCGSTAB to 1e-10, untimed), beside the error the FP64 solve itself carries at tol 1e-5
+    P64_tol = model.get_P()
+    model.InitializeP(zero)
+    model.bicgstab(MAX_IT, 1e-10)
+    P64 = model.get_P()
+    n64 = np.linalg.norm(P64)
+    error_vs_fp64 = {"fp32_refine": float(np.linalg.norm(P32 - P64) / n64),
+                     "fp64_at_tol": float(np.linalg.norm(P64_tol - P64) / n64),
+                     "reference_solution": "FP64 BiCGSTAB of the same lattice to 1e-10"}
 
     # end to end through the C ABI with pinned host buffers: new densities and P0 in, P out
     rho_host = pinned_f64(n3)
@@ -526,6 +582,7 @@ def run_ours(args, dist: Dist):
     t_k = (prof32 if prec == "fp32" else prof64)[k]
     peaks = measured_peaks()
     achieved = bytes_k / (t_k * 1e-3) / 1e9
+    req_k = required_bytes(core.grid, w.Nx, w.N, s, fused, 1)[k]
     traffic = ncu_traffic(f"{names[k]}:{prec}:cfg2")
     names32 = pass_names(core, tdda.FP32_REFINE)
     passes32, whole32 = pass_rooflines(w, core.grid, prof32, names32, 8, core.pass_count(tdda.FP32_REFINE) == 3, 1,
@@ -544,10 +601,21 @@ def run_ours(args, dist: Dist):
     batched = None
     if not args.no_batched:
         w3 = lattice.config(3)
-        b32, prof_b, _ = time_batch(tdda, torch, w3, w3.incidences, tdda.FP32_REFINE, args.batched_steps, dev, flush_l2)
+        b32, prof_b, _ = time_batch(tdda, torch, w3, w3.incidences, tdda.FP32_REFINE, args.batched_steps, dev, flush_l2,
+                                    keep_P=True)
         b32["roofline"] = batched_roofline(w3, tuple(b32["grid"]), prof_b, len(w3.incidences), 8, peaks["hbm_gbs"],
                                            b32["kernels"][2], b32["kernels"])
         b64, _, _ = time_batch(tdda, torch, w3, w3.incidences, tdda.FP64, 1, dev, flush_l2)
+        # error of each FP32+refine result against the FP64 solution to 1e-10 (untimed)
+        c3 = tdda.AProductCore(w3.Nx, w3.Ny, w3.Nz, w3.R, w3.d, w3.lam, w3.material, w3.nback,
+                               max_rhs=len(w3.incidences), device=dev)
+        m3 = [tdda.DDAModel(c3, i.nK, i.E0, i.nE0, w3.diel_old) for i in w3.incidences]
+        tdda.solve_batch(m3, tdda.FP64, MAX_IT, 1e-10)
+        b32["error_vs_fp64"] = [float(np.linalg.norm(p32 - m.get_P()) / np.linalg.norm(m.get_P()))
+                                for p32, m in zip(b32.pop("P"), m3)]
+        for m in m3:
+            m.close()
+        c3.close()
         batched = {"workload": "batched 8 RHS 96x96x24 (cfg 3)", "dipoles": w3.N, "fp32_refine": b32,
                    "fp64": {"value": b64["value"], "unit": UNIT, "iterations": b64["iterations"],
                             "ms_per_batch": b64["ms_per_batch"]},
@@ -573,7 +641,8 @@ def run_ours(args, dist: Dist):
     cpu = None
     if dist.rank == 0:
         base = CpuBaseline(w, args.cpu_threads or (os.cpu_count() or 1))
-        cpu = base.sample(args.cpu_iters)
+        base.sample(1)  # warm-up
+        cpu = base.sample(0)
         cpu.pop("sample_wall_s", None)
     clocks = ck.summary()
     if dist.rank == 0:
@@ -586,7 +655,7 @@ def run_ours(args, dist: Dist):
                        "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{dist.world}"},
             "latency_ms": {"p50": float(np.percentile(ms, 50)), "p99": float(np.percentile(ms, 99))},
             "solve": {"inner_iterations": info["inner_iterations"], "outer_iterations": info["outer_iterations"],
-                      "true_residual": info["true_residual"]},
+                      "true_residual": info["true_residual"], "error_vs_fp64": error_vs_fp64},
             "fp64": {"value": fp64_value, "unit": UNIT, "steps": k64,
                      "latency_ms": {"p50": float(np.percentile(ms64, 50)), "p99": float(np.percentile(ms64, 99))},
                      "iterations": r64[-1][1]["iterations"], "speedup_fp32_refine": value / fp64_value,
@@ -595,6 +664,7 @@ def run_ours(args, dist: Dist):
             "roofline": {"kernel": f"{names[k]} ({prec})", "bound": "hbm", "achieved": achieved,
                          "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
                          "peak_source": peaks["source"], "algorithmic_bytes": bytes_k, "avg_ms": t_k,
+                         "required_bytes": req_k, "frac_required": req_k / (t_k * 1e-3) / 1e9 / peaks["hbm_gbs"],
                          "traffic": traffic,
                          "pass_ms_fp32": prof32, "pass_ms_fp64": prof64,
                          "kernels_fp32": pass_names(core, tdda.FP32_REFINE),
