@@ -184,6 +184,17 @@ tdda_status tdda_model_density_gradient(const tdda_model* fwd, int nadj, tdda_mo
 tdda_status tdda_solve_batch(tdda_model* const* models, int n, int precision, int max_it, double max_err,
                              tdda_solve_info* infos);
 
+/* cross-lattice batched solve: FP32+refine solves of n models whose cores
+ * hold different lattices (box, dipoles, spacing, wavelength, material) on one
+ * FFT grid shape (tdda_core_info's grid3) and one device.  The FP32 inner
+ * solves of all n run in one launch per pass kernel (each right-hand side reads
+ * its own lattice, cellmap and Green spectrum); each refinement residual runs
+ * on its model's own core.  The reference solves one structure at a time with
+ * one shared core (main.cpp:577-598); here each result is bit-identical to the
+ * model's tdda_model_solve_mixed alone.  1 <= n <= 64; infos may be NULL. */
+tdda_status tdda_solve_multi(tdda_model* const* models, int n, int max_it, double max_err,
+                             tdda_solve_info* infos);
+
 /* serving loop: continuous batching of solve requests ------------------- */
 /* Requests queue in arrival order.  A worker takes the first request whose
  * device memory fits the HBM budget that the requests in flight leave free,

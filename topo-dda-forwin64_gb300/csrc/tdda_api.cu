@@ -23,6 +23,7 @@
 
 #include "../../include/tdda.h"
 #include "tdda_internal.cuh"
+#include "tdda_session.h"
 
 using tdda::AxisPlan;
 using tdda::Geom;
@@ -861,6 +862,412 @@ tdda_status noalloc_setup(int device, NoAllocSlot* out) {
 
 }  // namespace
 
+
+// ============================================================ cross-lattice sessions
+// The FP32+refine solve of solve_mixed, one right-hand side per slot, on a
+// "shape" core: a core of one FFT grid shape with no lattice of its own
+// (Geom::multi), whose pass kernels read each slot's lattice, cellmap and Green
+// spectrum from its RhsVecs.  Each slot follows solve_mixed's sequence for its
+// model alone: the refinement residual on the model's own core, the inner
+// solve's start with that core's vector-length reductions, the steps of the
+// shape's batched launches, the end (k_finish) and the accumulation of the
+// correction; so its result is bit-identical to tdda_model_solve_mixed.
+namespace tdda_session {
+namespace {
+
+enum Phase : int { kFree = 0, kResidual = 1, kInner = 2 };
+
+struct Slot {
+    tdda_model* m = nullptr;
+    int phase = kFree;
+    int inner = 0, outer = 0, nres = 0, max_it = 0;
+    double tol = 0, res = 1.0, prev_res = 1e300;
+};
+
+}  // namespace
+
+struct Shape {
+    tdda_core* c = nullptr;   // the shape core (g.multi = 1, no lattice)
+    int cap = 0;
+    std::vector<Slot> slots;
+    std::vector<RhsVecs<float>> h32;  // the full-width slot array, host copy
+    RhsVecs<float>* rhs32c = nullptr;  // device: a subset of slots for one launch
+    bool dirty = true;                 // h32 differs from the device copy
+};
+
+void core_grid(const tdda_core* c, int grid[3]) {
+    grid[0] = c->g.px.M;
+    grid[1] = c->g.py.M;
+    grid[2] = c->g.pz.M;
+}
+int core_device(const tdda_core* c) { return c->device; }
+
+namespace {
+// The largest lattice a grid shape holds on each axis: M >= 2N - 1
+int cap_of(int M) { return (M + 1) / 2; }
+
+// Geometry of a shape core: the plans of its lengths, strides for the largest
+// lattice, and the cross-lattice flag
+bool shape_geom(const int grid[3], Geom* g) {
+    std::memset(g, 0, sizeof(*g));
+    AxisPlan* plans[3] = {&g->px, &g->py, &g->pz};
+    for (int a = 0; a < 3; a++)
+        if (grid[a] < 1 || !make_plan(grid[a], plans[a])) return false;
+    g->Nx = cap_of(grid[0]);
+    g->Ny = cap_of(grid[1]);
+    g->Nz = cap_of(grid[2]);
+    g->N = g->Nx * g->Ny * g->Nz;
+    g->Hx = g->px.M / 2 + 1;
+    g->Hy = g->py.M / 2 + 1;
+    g->Hz = g->pz.M / 2 + 1;
+    g->sy = g->pz.M;
+    g->sx = (long long)g->py.M * g->pz.M;
+    g->sc = (long long)g->Nx * g->sx;
+    g->sb = 3 * g->sc;
+    g->dense = 0;
+    g->multi = 1;
+    return true;
+}
+
+// the slot's entry of the shape's RhsVecs array: the model's FP32 vectors with
+// its own lattice, or an empty lattice (every pass block of a free slot returns)
+RhsVecs<float> slot_vecs(Shape* s, int k) {
+    RhsVecs<float> v{};
+    tdda_core* c = s->c;
+    v.st = c->st32 + k;
+    v.part = c->part + (size_t)k * tdda::kPartSlots * c->maxblk;
+    v.cnt = c->cnt + (size_t)k * tdda::kCounters;
+    const tdda_model* m = s->slots[k].m;
+    if (!m) return v;
+    const tdda_core* oc = m->core;
+    v = vecs32(c, const_cast<tdda_model*>(m), k);
+    v.cellmap = oc->cellmap;
+    v.green = oc->green32;
+    v.Nx = oc->g.Nx;
+    v.Ny = oc->g.Ny;
+    v.Nz = oc->g.Nz;
+    v.N = oc->g.N;
+    v.dense = oc->g.dense;
+    return v;
+}
+
+// the refinement residual r = E - (A P + al P) of the model on its own core
+// (solve_mixed's outer step for one right-hand side); the state read back
+tdda_status own_residual(tdda_model* m, SolveState* out) {
+    tdda_core* oc = m->core;
+    RhsVecs<double> v = vecs64(oc, m, 0);
+    oc->hst[0] = fresh_state(0.0, 0, 0);
+    TDDA_CK(cudaMemcpyAsync(oc->rhs64, &v, sizeof(v), cudaMemcpyHostToDevice, oc->stream));
+    TDDA_CK(cudaMemcpyAsync(oc->st64, oc->hst, sizeof(SolveState), cudaMemcpyHostToDevice, oc->stream));
+    if (m->P_zero) {
+        // P = 0: the residual is E exactly (A 0 = 0), no product needed
+        TDDA_CK1(tdda::launch_residual_is_rhs<double>(oc->g, 1, oc->rhs64, oc->stream));
+    } else {
+        TDDA_CK1(tdda::launch_solve_begin<double>(oc->g, 1, oc->rhs64, oc->stream));
+        TDDA_TRY(residual_product(oc, 1));
+    }
+    TDDA_CK(cudaMemcpyAsync(oc->hst, oc->st64, sizeof(SolveState), cudaMemcpyDeviceToHost, oc->stream));
+    TDDA_CK(cudaStreamSynchronize(oc->stream));
+    *out = oc->hst[0];
+    return TDDA_OK;
+}
+
+void finish_slot(Shape* s, int k, tdda_status st, std::vector<Done>* done) {
+    Slot& sl = s->slots[k];
+    tdda_model* m = sl.m;
+    m->P_zero = false;
+    if (st == TDDA_OK) {
+        m->ITERATION = sl.inner;
+        m->Error = sl.res;
+    }
+    Done d;
+    d.slot = k;
+    d.model = m;
+    d.info.status = st;
+    d.info.iterations = sl.inner;
+    d.info.error = sl.res;
+    d.info.true_residual = sl.res;
+    d.info.outer_iterations = sl.outer;
+    d.info.inner_iterations = sl.inner;
+    done->push_back(d);
+    sl = Slot{};
+    s->h32[k] = slot_vecs(s, k);
+    s->dirty = true;
+}
+
+tdda_status upload_subset(Shape* s, const std::vector<int>& ks) {
+    std::vector<RhsVecs<float>> v(ks.size());
+    for (size_t i = 0; i < ks.size(); i++) v[i] = s->h32[ks[i]];
+    TDDA_CK(cudaMemcpyAsync(s->rhs32c, v.data(), sizeof(RhsVecs<float>) * v.size(), cudaMemcpyHostToDevice,
+                            s->c->stream));
+    return TDDA_OK;
+}
+}  // namespace
+
+double shape_bytes(const int grid[3], int cap) {
+    Geom g;
+    if (!shape_geom(grid, &g)) return 0.0;
+    const double blk = tdda::max_blocks_per_rhs(g);
+    return (double)g.sb * cap * 8 + cap * (tdda::kPartSlots * blk * 8 + 2 * sizeof(SolveState) +
+                                           2 * sizeof(RhsVecs<float>) + tdda::kCounters * 4) +
+           8.0 * (grid[0] + grid[1] + grid[2]) + 1e5;
+}
+
+tdda_status shape_create(int device, const int grid[3], int cap, Shape** out) {
+    if (!out || !grid || cap < 1 || cap > 64) {
+        set_err("invalid shape");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    Geom g;
+    if (!shape_geom(grid, &g)) {
+        set_err("no radix plan for the FFT grid %dx%dx%d", grid[0], grid[1], grid[2]);
+        return TDDA_ERR_UNSUPPORTED;
+    }
+    if (tdda::max_pass_smem(g) > tdda::kMaxPassSmem) {
+        set_err("FFT grid %dx%dx%d needs more shared memory per tile than a block has", grid[0], grid[1], grid[2]);
+        return TDDA_ERR_UNSUPPORTED;
+    }
+    TDDA_TRY(set_device(device));
+    TDDA_TRY(ensure_pool(device));
+    TDDA_TRY(configure_once(device));
+    Shape* s = new Shape();
+    tdda_core* c = new tdda_core_s();
+    s->c = c;
+    s->cap = cap;
+    c->device = device;
+    c->max_rhs = cap;
+    c->g = g;
+    c->N = g.N;
+    c->maxblk = tdda::max_blocks_per_rhs(g);
+    auto fail = [&](tdda_status st) {
+        shape_destroy(s);
+        return st;
+    };
+#define TDDA_SHAPE_CK(call)                                \
+    do {                                                   \
+        cudaError_t e_ = (call);                           \
+        if (e_ != cudaSuccess) return fail(cuda_fail(e_, #call)); \
+    } while (0)
+#define TDDA_SHAPE_TRY(call)                    \
+    do {                                        \
+        tdda_status s_ = (call);                \
+        if (s_ != TDDA_OK) return fail(s_);     \
+    } while (0)
+    TDDA_SHAPE_CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    {
+        const char* v = std::getenv("TDDA_DEVICE_LOOP");
+        c->device_loop = !(v && v[0] == '0');
+    }
+    for (int a = 0; a < 3; a++) TDDA_SHAPE_TRY(dalloc_c(c, &c->tw32[a], (size_t)grid[a]));
+    TDDA_SHAPE_TRY(dalloc_c(c, &c->grid32, (size_t)(g.sb * cap)));
+    TDDA_SHAPE_TRY(dalloc_c(c, &c->rhs32, (size_t)cap + 1));
+    TDDA_SHAPE_TRY(dalloc_c(c, &s->rhs32c, (size_t)cap));
+    TDDA_SHAPE_TRY(dalloc_c(c, &c->st32, (size_t)cap));
+    TDDA_SHAPE_TRY(dalloc_c(c, &c->part, (size_t)cap * tdda::kPartSlots * c->maxblk));
+    TDDA_SHAPE_TRY(dalloc_c(c, &c->cnt, (size_t)cap * tdda::kCounters));
+    TDDA_SHAPE_CK(pinned_get((void**)&c->hst, sizeof(SolveState) * cap));
+    TDDA_SHAPE_CK(cudaMemsetAsync(c->cnt, 0, sizeof(unsigned int) * cap * tdda::kCounters, c->stream));
+    for (int a = 0; a < 3; a++) {
+        std::vector<double2> w64;
+        std::vector<float2> w32;
+        twiddles(grid[a], w64, w32);
+        TDDA_SHAPE_CK(cudaMemcpyAsync(c->tw32[a], w32.data(), sizeof(float2) * w32.size(), cudaMemcpyHostToDevice,
+                                      c->stream));
+        TDDA_SHAPE_CK(cudaStreamSynchronize(c->stream));
+    }
+    // every slot starts free: a stopped state, an empty lattice
+    s->slots.assign(cap, Slot{});
+    s->h32.resize(cap);
+    for (int k = 0; k < cap; k++) {
+        c->hst[k] = fresh_state(0.0, 0, 0);
+        c->hst[k].status = tdda::ST_CONVERGED;
+        s->h32[k] = slot_vecs(s, k);
+    }
+    TDDA_SHAPE_CK(cudaMemcpyAsync(c->st32, c->hst, sizeof(SolveState) * cap, cudaMemcpyHostToDevice, c->stream));
+    TDDA_SHAPE_CK(cudaMemcpyAsync(c->rhs32, s->h32.data(), sizeof(RhsVecs<float>) * cap, cudaMemcpyHostToDevice,
+                                  c->stream));
+    TDDA_SHAPE_CK(cudaStreamSynchronize(c->stream));
+    s->dirty = false;
+#undef TDDA_SHAPE_CK
+#undef TDDA_SHAPE_TRY
+    *out = s;
+    return TDDA_OK;
+}
+
+void shape_destroy(Shape* s) {
+    if (!s) return;
+    if (s->c) tdda_core_destroy(s->c);
+    delete s;
+}
+
+bool shape_accepts(const Shape* s, const tdda_model* m) {
+    if (!s || !m) return false;
+    const tdda_core* oc = m->core;
+    return oc->device == s->c->device && oc->g.px.M == s->c->g.px.M && oc->g.py.M == s->c->g.py.M &&
+           oc->g.pz.M == s->c->g.pz.M && oc->g.Nx <= s->c->g.Nx && oc->g.Ny <= s->c->g.Ny && oc->g.Nz <= s->c->g.Nz;
+}
+int shape_cap(const Shape* s) { return s ? s->cap : 0; }
+int shape_active(const Shape* s) {
+    int n = 0;
+    if (s)
+        for (const Slot& sl : s->slots) n += sl.phase != kFree;
+    return n;
+}
+
+tdda_status shape_admit(Shape* s, tdda_model* m, int max_it, double tol, int* slot) {
+    if (!shape_accepts(s, m)) {
+        set_err("the model's core does not share the shape's FFT grid");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    int k = 0;
+    while (k < s->cap && s->slots[k].phase != kFree) k++;
+    if (k == s->cap) {
+        set_err("no free slot");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    TDDA_TRY(set_device(s->c->device));
+    TDDA_TRY(model_alloc_f32(m));
+    TDDA_CK(cudaStreamSynchronize(m->core->stream));
+    Slot& sl = s->slots[k];
+    sl = Slot{};
+    sl.m = m;
+    sl.phase = kResidual;
+    sl.max_it = max_it;
+    sl.tol = tol;
+    s->h32[k] = slot_vecs(s, k);
+    s->dirty = true;
+    if (slot) *slot = k;
+    return TDDA_OK;
+}
+
+tdda_status shape_step(Shape* s, std::vector<Done>* done) {
+    tdda_core* c = s->c;
+    TDDA_TRY(set_device(c->device));
+    // the shape's previous round (accumulations of the corrections) before the
+    // residuals read P on the models' own streams
+    TDDA_CK(cudaStreamSynchronize(c->stream));
+    // 1. refinement residuals, on each model's own core (solve_mixed's outer step)
+    std::vector<int> start;
+    for (int k = 0; k < s->cap; k++) {
+        Slot& sl = s->slots[k];
+        if (sl.phase != kResidual) continue;
+        SolveState st;
+        TDDA_TRY(own_residual(sl.m, &st));
+        const int nres = sl.nres++;
+        if (st.status == tdda::ST_NAN) {
+            finish_slot(s, k, TDDA_ERR_NAN, done);
+            continue;
+        }
+        const double En = st.Enorm;
+        sl.res = !std::isfinite(En) ? En : (En > 0 ? std::sqrt(st.rnorm2) / En : 0.0);
+        tdda_status fin = TDDA_OK;
+        bool open = false;
+        if (!std::isfinite(sl.res)) fin = TDDA_ERR_NAN;
+        else if (sl.res <= sl.tol) fin = TDDA_OK;
+        else if (nres == kMaxOuter || sl.inner >= sl.max_it || sl.res >= sl.prev_res) fin = TDDA_NOT_CONVERGED;
+        else open = true;
+        sl.prev_res = sl.res;
+        if (!open) {
+            finish_slot(s, k, fin, done);
+            continue;
+        }
+        // 2. the inner solve's start: FP32 right-hand side r, correction 0, a fresh state
+        tdda_model* m = sl.m;
+        const double tin = std::min(0.5, std::max(2e-6, 0.8 * sl.tol / std::max(sl.res, 1e-300)));
+        c->hst[k] = fresh_state(tin, sl.max_it - sl.inner, 0);
+        TDDA_CK(cudaMemcpyAsync(c->st32 + k, &c->hst[k], sizeof(SolveState), cudaMemcpyHostToDevice, c->stream));
+        TDDA_CK1(tdda::launch_to_f32(3 * m->core->N, m->r, m->fE, c->stream));
+        TDDA_CK1(tdda::launch_zero<float>(3LL * m->core->N, m->fP, c->stream));
+        sl.phase = kInner;
+        start.push_back(k);
+    }
+    if (s->dirty) {
+        TDDA_CK(cudaMemcpyAsync(c->rhs32, s->h32.data(), sizeof(RhsVecs<float>) * s->cap, cudaMemcpyHostToDevice,
+                                c->stream));
+        s->dirty = false;
+    }
+    if (!start.empty()) {
+        // r = r0 = p = E (the FP32 right-hand side), |E| and r0.r, each with its own
+        // lattice's vector-length reduction, as its solve alone forms them
+        for (int k : start) {
+            TDDA_TRY(upload_subset(s, {k}));
+            TDDA_CK1(tdda::launch_residual_is_rhs<float>(s->slots[k].m->core->g, 1, s->rhs32c, c->stream));
+        }
+        // the initial products of the new inner solves (step -1, parity 1), in one launch per pass
+        TDDA_TRY(upload_subset(s, start));
+        const int n = (int)start.size();
+        TDDA_CK(aprod<float>(c, tdda::SRC_IN, tdda::SNK_AP, n, s->rhs32c, nullptr, 1));
+        TDDA_CK(aprod<float>(c, tdda::SRC_TUPD, tdda::SNK_AT_DEF, n, s->rhs32c, nullptr, 1));
+    }
+    bool any_inner = false;
+    for (const Slot& sl : s->slots) any_inner |= sl.phase == kInner;
+    if (!any_inner) return TDDA_OK;
+    // 3. one launch of the steps of every slot (the device-side loop: at most
+    // kLoopChunks chunks of kChunk steps, or one host-launched chunk); the chunk
+    // count of the launch restarts in the first slot's state
+    const int zero_limit[2] = {0, 1 << 30};
+    TDDA_CK(cudaMemcpyAsync(&c->st32[0].chunks, zero_limit, sizeof(zero_limit), cudaMemcpyHostToDevice, c->stream));
+    cudaGraphExec_t ex;
+    TDDA_TRY(get_iteration_graph<float>(c, s->cap, &ex));
+    TDDA_CK(cudaGraphLaunch(ex, c->stream));
+    TDDA_CK(cudaMemcpyAsync(c->hst, c->st32, sizeof(SolveState) * s->cap, cudaMemcpyDeviceToHost, c->stream));
+    TDDA_CK(cudaStreamSynchronize(c->stream));
+    count_launches(std::max(1, c->hst[0].chunks) * chunk_kernels<float>(c));
+    // 4. inner solves that stopped: the pending update, then P += the correction
+    std::vector<int> stopped;
+    for (int k = 0; k < s->cap; k++)
+        if (s->slots[k].phase == kInner && c->hst[k].status != tdda::ST_RUNNING) stopped.push_back(k);
+    if (stopped.empty()) return TDDA_OK;
+    TDDA_TRY(upload_subset(s, stopped));
+    TDDA_CK1(tdda::launch_finish<float>(c->g, (int)stopped.size(), s->rhs32c, c->stream));
+    for (int k : stopped) {
+        Slot& sl = s->slots[k];
+        const SolveState& st = c->hst[k];
+        sl.inner += st.it;
+        sl.outer += 1;
+        if (st.status == tdda::ST_NAN) {
+            finish_slot(s, k, TDDA_ERR_NAN, done);
+            continue;
+        }
+        TDDA_CK1(tdda::launch_accumulate(3 * sl.m->core->N, sl.m->fP, sl.m->P, c->stream));
+        sl.m->P_zero = false;
+        sl.phase = kResidual;
+    }
+    TDDA_CK(cudaStreamSynchronize(c->stream));
+    return TDDA_OK;
+}
+
+tdda_status model_reinit(tdda_model* m, const double* nK, double E0, const double* nE0, const double* diel_old) {
+    if (!m || !nK || !nE0 || !diel_old) {
+        set_err("null argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    tdda_core* c = m->core;
+    size_t bad = 0;
+    if (!densities_in_table(diel_old, 3 * (size_t)c->N, c->nmat, &bad)) {
+        set_err("density %g of entry %zu is outside the material table", diel_old[bad], bad);
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    TDDA_TRY(set_device(c->device));
+    for (int j = 0; j < 3; j++) {
+        m->nK[j] = nK[j];
+        m->nE0[j] = nE0[j];
+    }
+    m->E0 = E0;
+    m->diel_old.assign(diel_old, diel_old + 3 * (size_t)c->N);
+    const size_t n3 = 3 * (size_t)c->N;
+    TDDA_CK(cudaMemsetAsync(m->P, 0, sizeof(double2) * n3, c->stream));
+    TDDA_CK(cudaMemsetAsync(m->Ein, 0, sizeof(double2) * n3, c->stream));
+    TDDA_TRY(model_upload_fields(m, true, true));
+    m->P_zero = true;
+    m->ITERATION = 0;
+    m->Error = 0.0;
+    return TDDA_OK;
+}
+
+}  // namespace tdda_session
+
 // ======================================================================= ABI
 extern "C" {
 
@@ -1390,6 +1797,84 @@ tdda_status tdda_solve_batch(tdda_model* const* ms, int n, int precision, int ma
     TDDA_TRY(set_device(ms[0]->core->device));
     if (precision == TDDA_FP64) return solve_fp64(ms, n, max_it, max_err, infos);
     return solve_mixed(ms, n, max_it, max_err, infos);
+}
+
+namespace {
+// shapes of tdda_solve_multi, kept per (device, grid, width) for the next call
+struct ShapeKey {
+    int device, Mx, My, Mz, cap;
+    bool operator==(const ShapeKey& o) const {
+        return device == o.device && Mx == o.Mx && My == o.My && Mz == o.Mz && cap == o.cap;
+    }
+};
+std::mutex g_shape_mu;
+std::vector<std::pair<ShapeKey, tdda_session::Shape*>> g_shapes;  // idle shapes
+}  // namespace
+
+tdda_status tdda_solve_multi(tdda_model* const* ms, int n, int max_it, double max_err, tdda_solve_info* infos) {
+    g_err.clear();
+    if (!ms || n < 1 || n > 64 || !(max_err >= 0)) {
+        set_err("invalid batch, tolerance or size (1..64 right-hand sides)");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    for (int i = 0; i < n; i++) {
+        if (!ms[i]) {
+            set_err("null model");
+            return TDDA_ERR_INVALID_ARGUMENT;
+        }
+        for (int j = 0; j < i; j++)
+            if (ms[j] == ms[i]) {
+                set_err("a model appears twice in a batch");
+                return TDDA_ERR_INVALID_ARGUMENT;
+            }
+    }
+    int grid[3];
+    tdda_session::core_grid(ms[0]->core, grid);
+    const int device = ms[0]->core->device;
+    for (int i = 1; i < n; i++) {
+        int gi[3];
+        tdda_session::core_grid(ms[i]->core, gi);
+        if (ms[i]->core->device != device || gi[0] != grid[0] || gi[1] != grid[1] || gi[2] != grid[2]) {
+            set_err("models of a cross-lattice batch share one device and FFT grid shape (%dx%dx%d and %dx%dx%d)",
+                    grid[0], grid[1], grid[2], gi[0], gi[1], gi[2]);
+            return TDDA_ERR_INVALID_ARGUMENT;
+        }
+    }
+    const ShapeKey key{device, grid[0], grid[1], grid[2], n};
+    tdda_session::Shape* sh = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_shape_mu);
+        for (size_t k = 0; k < g_shapes.size(); k++)
+            if (g_shapes[k].first == key) {
+                sh = g_shapes[k].second;
+                g_shapes.erase(g_shapes.begin() + (long)k);
+                break;
+            }
+    }
+    if (!sh) TDDA_TRY(tdda_session::shape_create(device, grid, n, &sh));
+    tdda_status worst = TDDA_OK;
+    tdda_status st = TDDA_OK;
+    for (int i = 0; i < n && st == TDDA_OK; i++) st = tdda_session::shape_admit(sh, ms[i], max_it, max_err, nullptr);
+    std::vector<tdda_session::Done> done;
+    while (st == TDDA_OK && tdda_session::shape_active(sh) > 0) st = tdda_session::shape_step(sh, &done);
+    if (st != TDDA_OK) {
+        tdda_session::shape_destroy(sh);  // slots may hold models mid-solve
+        return st;
+    }
+    for (const auto& d : done) {
+        for (int i = 0; i < n; i++)
+            if (ms[i] == d.model && infos) infos[i] = d.info;
+        if (d.info.status != TDDA_OK && worst == TDDA_OK) worst = (tdda_status)d.info.status;
+    }
+    {
+        std::lock_guard<std::mutex> lk(g_shape_mu);
+        g_shapes.emplace_back(key, sh);
+        if (g_shapes.size() > 16) {  // keep a few shapes; the oldest goes
+            tdda_session::shape_destroy(g_shapes.front().second);
+            g_shapes.erase(g_shapes.begin());
+        }
+    }
+    return worst;
 }
 
 tdda_status tdda_model_bicgstab(tdda_model* m, int max_it, double max_err, tdda_solve_info* info) {

@@ -31,6 +31,9 @@ struct Geom {
                        // 1: the shared-memory form on the length's compiled plan
     int x_tile;        // z-columns per block of the register form: 8, 16, or 0 for
                        // the built-in choice (16 for M = 128, else 8)
+    int multi;         // 1: a cross-lattice batch -- every right-hand side brings its own
+                       // lattice (RhsVecs::Nx ... green); Nx, Ny, Nz, N above are the
+                       // largest the grid shape holds (the strides follow them)
 };
 
 // solver status values (mirrored in include/tdda.h)
@@ -84,7 +87,25 @@ template <typename T> struct RhsVecs {
     SolveState* st;
     double* part;        // reduction partials, kPartSlots x maxblk doubles
     unsigned int* cnt;   // last-block counters, kCounters
+    // Cross-lattice batches (the FP32 fused passes on one FFT grid shape): the
+    // lattice of this right-hand side when it is not the launch's own -- its
+    // box, dipole count, build_a_bulk flag, cellmap and folded Green spectrum.
+    // Read only when Geom::multi is set.
+    const int* cellmap;
+    const cx<T>* green;
+    int Nx, Ny, Nz, N, dense;
 };
+// the lattice a pass kernel works on for one right-hand side: its own (cross-lattice
+// batches) or the launch's
+struct Lat {
+    int Nx, Ny, Nz, N, dense;
+    const int* cellmap;
+};
+template <typename T>
+__host__ __device__ __forceinline__ Lat lattice_of(const Geom& g, const RhsVecs<T>& R, const int* cellmap) {
+    if (g.multi) return Lat{R.Nx, R.Ny, R.Nz, R.N, R.dense, R.cellmap};
+    return Lat{g.Nx, g.Ny, g.Nz, g.N, g.dense, cellmap};
+}
 // entry of component c of dipole i in a vector of N dipoles
 template <typename T> __host__ __device__ __forceinline__ long long vec_index(long long i, int c, int N) {
     if constexpr (sizeof(T) == 4) return (long long)c * N + i;

@@ -63,9 +63,11 @@ __global__ void __launch_bounds__(kNT) k_update(int n3, const RhsVecs<T>* __rest
 // The deferred update of the last step (SNK_AT_DEF) for every right-hand side
 // that has one pending: u = zeta Ap; P += alpha p + zeta r - alpha u;
 // r = t - zeta At.
-template <typename T> __global__ void __launch_bounds__(kNT) k_finish(int n3, const RhsVecs<T>* __restrict__ rhs) {
+template <typename T>
+__global__ void __launch_bounds__(kNT) k_finish(int n3, int multi, const RhsVecs<T>* __restrict__ rhs) {
     const RhsVecs<T> R = rhs[blockIdx.y];
     if (R.st == nullptr) return;
+    if (multi) n3 = 3 * R.N;  // a cross-lattice batch: this right-hand side's dipoles
     cx<T> alpha, zeta;
     if constexpr (sizeof(T) == 4) {
         const int q = R.st->last_slot;  // the step whose update is pending
@@ -88,11 +90,13 @@ template <typename T> __global__ void __launch_bounds__(kNT) k_finish(int n3, co
 
 // |E| of each right-hand side
 template <typename T>
-__global__ void __launch_bounds__(kNT) k_solve_begin(int n3, const RhsVecs<T>* __restrict__ rhs, int resid_is_rhs) {
+__global__ void __launch_bounds__(kNT) k_solve_begin(int n3, int multi, const RhsVecs<T>* __restrict__ rhs,
+                                                     int resid_is_rhs) {
     __shared__ double sred[sred_size<T, 4>()];
     const int b = blockIdx.y;
     const RhsVecs<T> R = rhs[b];
     if (rhs_done(R.st)) return;
+    if (multi) n3 = 3 * R.N;  // a cross-lattice batch: this right-hand side's dipoles
     acc_t<T> acc[4] = {0, 0, 0, 0};
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x) {
         const cx<T> v = R.E[e];
@@ -689,21 +693,21 @@ cudaError_t launch_update(const Geom& g, int nrhs, const RhsVecs<T>* rhs, int is
 template <typename T>
 cudaError_t launch_finish(const Geom& g, int nrhs, const RhsVecs<T>* rhs, cudaStream_t stream) {
     const dim3 gr(grid1d(3LL * g.N, kNT), nrhs);
-    k_finish<T><<<gr, kNT, 0, stream>>>(3 * g.N, rhs);
+    k_finish<T><<<gr, kNT, 0, stream>>>(3 * g.N, g.multi, rhs);
     return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_solve_begin(const Geom& g, int nrhs, const RhsVecs<T>* rhs, cudaStream_t stream) {
     const dim3 gr(grid_reduce(3LL * g.N, sizeof(T) == 4), nrhs);
-    k_solve_begin<T><<<gr, kNT, 0, stream>>>(3 * g.N, rhs, 0);
+    k_solve_begin<T><<<gr, kNT, 0, stream>>>(3 * g.N, g.multi, rhs, 0);
     return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_residual_is_rhs(const Geom& g, int nrhs, const RhsVecs<T>* rhs, cudaStream_t stream) {
     const dim3 gr(grid_reduce(3LL * g.N, sizeof(T) == 4), nrhs);
-    k_solve_begin<T><<<gr, kNT, 0, stream>>>(3 * g.N, rhs, 1);
+    k_solve_begin<T><<<gr, kNT, 0, stream>>>(3 * g.N, g.multi, rhs, 1);
     return cudaGetLastError();
 }
 

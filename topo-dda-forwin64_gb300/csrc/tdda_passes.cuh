@@ -121,15 +121,19 @@ __global__ void __launch_bounds__(kNT) k_zfwd(Geom g, const RhsVecs<T>* __restri
     }
     constexpr int cLZ = CM > 0 ? z_lines<T>(CM) : 1;
     constexpr int cMzP = CM > 0 ? pad_odd(CM) : 1;
-    const int Mz = CM > 0 ? CM : g.pz.M, Nz = g.Nz;
+    const int Mz = CM > 0 ? CM : g.pz.M, Nz = g.multi ? R.Nz : g.Nz;
     const int LZ = CM > 0 ? cLZ : z_lines<T>(Mz), MzP = CM > 0 ? cMzP : pad_odd(Mz);
     cx<T>* stw = reinterpret_cast<cx<T>*>(smem_raw);
     cx<T>* s = stw + Mz;
     cx<T>* s2 = s + 3 * LZ * MzP;
-    stage_tw<T>(stw, twz, Mz);
-    const int nlines = g.Nx * g.Ny;
+    // the lattice of this right-hand side (its own in a cross-lattice batch, whose
+    // blocks past its lines return: the grid shape's launch covers the largest)
+    const Lat L = lattice_of<T>(g, R, cellmap);
+    const int nlines = L.Nx * L.Ny;
     const int l0 = blockIdx.x * LZ;
     const int nl = min(LZ, nlines - l0);
+    if (nl <= 0) return;
+    stage_tw<T>(stw, twz, Mz);
 
     cx<T> beta, alpha, zeta;
     if constexpr (kStep32) {
@@ -143,12 +147,12 @@ __global__ void __launch_bounds__(kNT) k_zfwd(Geom g, const RhsVecs<T>* __restri
     const cx<T>* src = SRC == SRC_IN ? R.p : R.P;
     for (int e = threadIdx.x; e < nl * Nz; e += blockDim.x) {
         const int line = e / Nz, z = e - (e / Nz) * Nz;
-        const int i = cellmap[(long long)(l0 + line) * Nz + z];
+        const int i = L.cellmap[(long long)(l0 + line) * Nz + z];
         cx<T> v[3];
         if (i >= 0) {
 #pragma unroll
             for (int c = 0; c < 3; c++) {
-                const long long o = vec_index<T>(i, c, g.N);
+                const long long o = vec_index<T>(i, c, L.N);
                 if (SRC == SRC_PUPD) {
                     cx<T> pc = R.p[o], uc = R.u[o], rc = R.r[o];
                     v[c] = cadd<T>(rc, cmul<T>(beta, csub<T>(pc, uc)));
@@ -177,7 +181,7 @@ __global__ void __launch_bounds__(kNT) k_zfwd(Geom g, const RhsVecs<T>* __restri
     for (int e = threadIdx.x; e < 3 * nl * Mz; e += blockDim.x) {
         const int cl = e / Mz, z = e - (e / Mz) * Mz;
         const int c = cl / nl, line = cl - (cl / nl) * nl;
-        const int l = l0 + line, x = l / g.Ny, y = l - (l / g.Ny) * g.Ny;
+        const int l = l0 + line, x = l / L.Ny, y = l - (l / L.Ny) * L.Ny;
         gb[c * g.sc + x * g.sx + y * g.sy + z] = res[(c * LZ + line) * MzP + z];
     }
 }
@@ -194,6 +198,9 @@ __global__ void __launch_bounds__(kNT) k_ypass(Geom g, const RhsVecs<T>* __restr
     const int ZT = CM > 0 ? cZT : y_tile<T>(My);
     const int nzt = (Mz + ZT - 1) / ZT;
     const int x = blockIdx.x / nzt, z0 = (blockIdx.x - x * nzt) * ZT;
+    // a cross-lattice batch: this right-hand side's own x extent and rows
+    const int Ny = g.multi ? rhs[b].Ny : g.Ny;
+    if (g.multi && x >= rhs[b].Nx) return;
     const int c = blockIdx.y;
     const int zn = min(ZT, Mz - z0);
     cx<T>* stw = reinterpret_cast<cx<T>*>(smem_raw);
@@ -202,8 +209,8 @@ __global__ void __launch_bounds__(kNT) k_ypass(Geom g, const RhsVecs<T>* __restr
     cx<T>* s2 = s + My * ZP;
     stage_tw<T>(stw, twy, My);
     cx<T>* gp = grid + (long long)b * g.sb + c * g.sc + (long long)x * g.sx + z0;
-    const int nin = SIGN < 0 ? g.Ny : My;
-    const int nout = SIGN < 0 ? My : g.Ny;
+    const int nin = SIGN < 0 ? Ny : My;
+    const int nout = SIGN < 0 ? My : Ny;
     for (int e = threadIdx.x; e < nin * ZT; e += blockDim.x) {
         const int y = e / ZT, zl = e - (e / ZT) * ZT;
         if (zl < zn) s[y * ZP + zl] = gp[(long long)y * g.sy + zl];
@@ -252,7 +259,9 @@ __global__ void __launch_bounds__(kNT) k_xpass(Geom g, const RhsVecs<T>* __restr
     const int b = blockIdx.y;
     if (rhs_done(rhs[b].st)) return;
     constexpr int cZT = CM > 0 ? x_tile<T>(CM) : 1;
-    const int Mx = CM > 0 ? CM : g.px.M, My = g.py.M, Mz = g.pz.M, Nx = g.Nx;
+    // a right-hand side of a cross-lattice batch brings its own box and spectrum
+    const int Mx = CM > 0 ? CM : g.px.M, My = g.py.M, Mz = g.pz.M, Nx = g.multi ? rhs[b].Nx : g.Nx;
+    if (g.multi) green = rhs[b].green;
     const int ZT = CM > 0 ? cZT : x_tile<T>(Mx);
     const int nzt = (Mz + ZT - 1) / ZT;
     const int y = blockIdx.x / nzt, z0 = (blockIdx.x - y * nzt) * ZT;
@@ -333,7 +342,9 @@ __global__ void __launch_bounds__(ZT * x2_radix(M, 0), MINB) k_xpass2(Geom g, co
     cx<T>* s = stw + M;  // [M][WP]
     const int b = blockIdx.y;
     const SolveState* st = rhs[b].st;
-    const int My = g.py.M, Mz = g.pz.M, Nx = g.Nx;
+    // a right-hand side of a cross-lattice batch brings its own box and spectrum
+    const int My = g.py.M, Mz = g.pz.M, Nx = g.multi ? rhs[b].Nx : g.Nx;
+    if (g.multi) green = rhs[b].green;
     const int nzt = (Mz + ZT - 1) / ZT;
     const int y = blockIdx.x / nzt, z0 = (blockIdx.x - y * nzt) * ZT;
     const int zn = min(ZT, Mz - z0);
@@ -486,20 +497,26 @@ __global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restri
     if (rhs_done(R.st)) return;
     constexpr int cLZ = CM > 0 ? z_lines<T>(CM) : 1;
     constexpr int cMzP = CM > 0 ? pad_odd(CM) : 1;
-    const int Mz = CM > 0 ? CM : g.pz.M, Nz = g.Nz;
+    // the lattice of this right-hand side (its own in a cross-lattice batch)
+    const Lat L = lattice_of<T>(g, R, cellmap);
+    const int Mz = CM > 0 ? CM : g.pz.M, Nz = L.Nz;
     const int LZ = CM > 0 ? cLZ : z_lines<T>(Mz), MzP = CM > 0 ? cMzP : pad_odd(Mz);
     cx<T>* stw = reinterpret_cast<cx<T>*>(smem_raw);
     cx<T>* s = stw + Mz;
     cx<T>* s2 = s + 3 * LZ * MzP;
-    stage_tw<T>(stw, twz, Mz);
-    const int nlines = g.Nx * g.Ny;
+    const int nlines = L.Nx * L.Ny;
     const int l0 = blockIdx.x * LZ;
-    const int nl = min(LZ, nlines - l0);
+    // a cross-lattice batch launches the grid shape's largest line count: a block past
+    // this right-hand side's lines adds zeros to its sums
+    const int nl = max(0, min(LZ, nlines - l0));
+    acc_t<T> acc[NV] = {};
+    if (nl > 0) {
+    stage_tw<T>(stw, twz, Mz);
     const cx<T>* gb = grid + (long long)b * g.sb;
     for (int e = threadIdx.x; e < 3 * nl * Mz; e += blockDim.x) {
         const int cl = e / Mz, z = e - (e / Mz) * Mz;
         const int c = cl / nl, line = cl - (cl / nl) * nl;
-        const int l = l0 + line, x = l / g.Ny, y = l - (l / g.Ny) * g.Ny;
+        const int l = l0 + line, x = l / L.Ny, y = l - (l / L.Ny) * L.Ny;
         s[(c * LZ + line) * MzP + z] = gb[c * g.sc + x * g.sx + y * g.sy + z];
     }
     __syncthreads();
@@ -509,14 +526,13 @@ __global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restri
 
     // scatter to the dipoles, fused diagonal term and dot products
     const cx<T>* vsrc = (SRC == SRC_TUPD) ? R.t : (SRC == SRC_P ? R.P : R.p);
-    acc_t<T> acc[NV] = {};
     for (int e = threadIdx.x; e < nl * Nz; e += blockDim.x) {
         const int line = e / Nz, z = e - (e / Nz) * Nz;
-        const int i = cellmap[(long long)(l0 + line) * Nz + z];
+        const int i = L.cellmap[(long long)(l0 + line) * Nz + z];
         if (i < 0) continue;
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-            const long long o = vec_index<T>(i, c, g.N);
+            const long long o = vec_index<T>(i, c, L.N);
             cx<T> val = res[(c * LZ + line) * MzP + z];
             if (SNK == SNK_OUT) {
                 R.Ap[o] = val;
@@ -554,6 +570,7 @@ __global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restri
             }
         }
     }
+    }  // nl > 0
     if (SNK == SNK_OUT || SNK == SNK_ALB) return;
     if constexpr (sizeof(T) == 4 && (SNK == SNK_AP || SNK == SNK_AT_DEF)) {
         publish_partials<NV>(acc, R.part, gridDim.x, blockIdx.x, sred);  // the next gather forms the scalars
@@ -728,8 +745,10 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
     if constexpr (!kStep32) {  // the FP32 step reads the status with its scalars
         if (rhs_done(R.st)) return;
     }
+    const Lat L = lattice_of<T>(g, R, cellmap);
     const int x = blockIdx.x / 3, c = blockIdx.x - 3 * (blockIdx.x / 3);
-    const int Ny = g.Ny, Nz = g.Nz;
+    if (x >= L.Nx) return;  // past this right-hand side's lattice (cross-lattice batches)
+    const int Ny = L.Ny, Nz = L.Nz;
     cx<T>* stwy = reinterpret_cast<cx<T>*>(smem_raw);
     cx<T>* stwz = stwy + MY;
     cx<T>* sA = stwz + MZ;     // My rows
@@ -744,7 +763,7 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
         if (SRC == SRC_PUPD_DEF) zeta = st_zeta<T>(R.st);
     }
     const cx<T>* src = SRC == SRC_IN ? R.p : R.P;
-    const int* cm = cellmap + (long long)x * Ny * Nz;
+    const int* cm = L.cellmap + (long long)x * Ny * Nz;
     const int ibase = x * Ny * Nz;
 
     // gather: consecutive threads take consecutive cells (y, z), z fastest, in
@@ -761,8 +780,8 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
             const bool cell = c0 + q < NE && e < NCELL;
             sidx[q] = cell ? y * ZP + z : -1;
             int i = -1;
-            if (cell && y < Ny && z < Nz) i = g.dense ? ibase + y * Nz + z : cm[y * Nz + z];
-            o[q] = i >= 0 ? vec_index<T>(i, c, g.N) : -1LL;
+            if (cell && y < Ny && z < Nz) i = L.dense ? ibase + y * Nz + z : cm[y * Nz + z];
+            o[q] = i >= 0 ? vec_index<T>(i, c, L.N) : -1LL;
         }
         GatherIn<T, SRC, CH> in;
         in.load(R, o, src);
@@ -855,8 +874,27 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
     __shared__ double sred[sred_size<T, NV>()];
     const int b = blockIdx.y;
     const RhsVecs<T> R = rhs[b];
+    const Lat L = lattice_of<T>(g, R, cellmap);
     const int x = blockIdx.x / 3, c = blockIdx.x - 3 * (blockIdx.x / 3);
-    const int Ny = g.Ny, Nz = g.Nz;
+    if (x >= L.Nx) {
+        // past this right-hand side's lattice (cross-lattice batches): its sums over the
+        // grid shape's blocks take zeros here, which leave them exactly as its own
+        // blocks form them
+        if (SNK == SNK_OUT || SNK == SNK_ALB) return;
+        acc_t<T> zero[NV] = {};
+        if constexpr (sizeof(T) == 4 && (SNK == SNK_AP || SNK == SNK_AT_DEF)) {
+            publish_partials<NV>(zero, R.part, gridDim.x, blockIdx.x, sred);
+        } else {
+            tot_t<T> tot[NV];
+            const int slot = SNK == SNK_AP ? 0 : (SNK == SNK_AT || SNK == SNK_AT_DEF ? 1 : 2);
+            if (last_block_total<NV>(zero, R.part, gridDim.x, blockIdx.x, R.cnt + slot, sred, tot) &&
+                threadIdx.x == 0)
+                finalize_sink<T, SNK, NV>(R.st, tot);
+        }
+        return;
+    }
+    const int nblk = gridDim.x;
+    const int Ny = L.Ny, Nz = L.Nz;
     cx<T>* stwy = reinterpret_cast<cx<T>*>(smem_raw);
     cx<T>* stwz = stwy + MY;
     cx<T>* sA = stwz + MZ;     // My rows
@@ -938,7 +976,7 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
     __syncthreads();
     // scatter component c: consecutive threads take consecutive cells (y, z),
     // in chunks of CH whose loads are issued before their stores
-    const int* cm = cellmap + (long long)x * Ny * Nz;
+    const int* cm = L.cellmap + (long long)x * Ny * Nz;
     const int ibase = x * Ny * Nz;
     acc_t<T> acc[NV] = {};
     // the sink's operand loads of all the thread's cells at once, up to 9 cells
@@ -954,20 +992,20 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
             const int y = e / LZ, z = e - (e / LZ) * LZ;
             const bool cell = c0 + q < NE && e < NCELL && y < Ny && z < Nz;
             int i = -1;
-            if (cell) i = g.dense ? ibase + y * Nz + z : cm[y * Nz + z];
-            o[q] = i >= 0 ? vec_index<T>(i, c, g.N) : -1LL;
+            if (cell) i = L.dense ? ibase + y * Nz + z : cm[y * Nz + z];
+            o[q] = i >= 0 ? vec_index<T>(i, c, L.N) : -1LL;
             vo[q] = i >= 0 ? sB[y * ZP + z] : czero<T>();
         }
         scatter_chunk<T, SRC, SNK, CH, NV>(R, o, vo, acc);
     }
     if (SNK == SNK_OUT || SNK == SNK_ALB) return;
     if constexpr (sizeof(T) == 4 && (SNK == SNK_AP || SNK == SNK_AT_DEF)) {
-        publish_partials<NV>(acc, R.part, gridDim.x, blockIdx.x, sred);  // the next gather forms the scalars
+        publish_partials<NV>(acc, R.part, nblk, blockIdx.x, sred);  // the next gather forms the scalars
         return;
     }
     tot_t<T> tot[NV];
     const int slot = SNK == SNK_AP ? 0 : (SNK == SNK_AT || SNK == SNK_AT_DEF ? 1 : 2);
-    if (!last_block_total<NV>(acc, R.part, gridDim.x, blockIdx.x, R.cnt + slot, sred, tot)) return;
+    if (!last_block_total<NV>(acc, R.part, nblk, blockIdx.x, R.cnt + slot, sred, tot)) return;
     if (threadIdx.x != 0) return;
     finalize_sink<T, SNK, NV>(R.st, tot);
 }

@@ -45,7 +45,7 @@ EXPORTS = [
     "tdda_model_initialize_P", "tdda_model_aproduct_with_alb", "tdda_model_bicgstab", "tdda_model_solve_mixed",
     "tdda_model_update_E_in_structure", "tdda_model_get", "tdda_model_iterations", "tdda_model_field_at",
     "tdda_model_density_gradient",
-    "tdda_solve_batch",
+    "tdda_solve_batch", "tdda_solve_multi",
     "tdda_fft3d", "tdda_core_stream", "tdda_kernel_launches", "tdda_profile_aproduct", "tdda_core_pass_count",
     "tdda_core_pass_name", "tdda_core_set_xpass", "tdda_core_autotune",
     "tdda_aproduct_noalloc", "tdda_server_create", "tdda_server_submit", "tdda_server_result",
@@ -146,6 +146,7 @@ def load() -> ctypes.CDLL:
         "tdda_core_interaction": (i, [vp, d, d, d, dp]),
         "tdda_model_density_gradient": (i, [vp, i, vp, vp, i, vp, vp, vp]),
         "tdda_solve_batch": (i, [ctypes.POINTER(vp), i, i, i, d, ctypes.POINTER(SolveInfo)]),
+        "tdda_solve_multi": (i, [ctypes.POINTER(vp), i, i, d, ctypes.POINTER(SolveInfo)]),
         "tdda_fft3d": (i, [vp, i, i, i, i]),
         "tdda_core_stream": (i, [vp, ctypes.POINTER(vp)]),
         "tdda_kernel_launches": (ctypes.c_ulonglong, []),
@@ -462,6 +463,20 @@ def solve_batch(models, precision: int = FP64, max_it: int = 10000, tol: float =
     st = load().tdda_solve_batch(arr, n, int(precision), int(max_it), float(tol), infos)
     # a right-hand side that stops without converging reports it in its own info
     _check(st, "tdda_solve_batch", allowed=(OK, NOT_CONVERGED, BREAKDOWN, ERR_NAN))
+    out = [infos[k].as_dict() for k in range(n)]
+    for m, o in zip(models, out):
+        m.last_info = o
+    return out
+
+
+def solve_multi(models, max_it: int = 10000, tol: float = 1e-5) -> list:
+    """FP32+refine solves of models on different cores that share one FFT grid shape, with
+    the inner solves of all of them in one launch per pass (tdda_solve_multi)."""
+    n = len(models)
+    arr = (ctypes.c_void_p * n)(*[m.h.value for m in models])
+    infos = (SolveInfo * n)()
+    st = load().tdda_solve_multi(arr, n, int(max_it), float(tol), infos)
+    _check(st, "tdda_solve_multi", allowed=(OK, NOT_CONVERGED, BREAKDOWN, ERR_NAN))
     out = [infos[k].as_dict() for k in range(n)]
     for m, o in zip(models, out):
         m.last_info = o
