@@ -196,13 +196,19 @@ tdda_status tdda_solve_multi(tdda_model* const* models, int n, int max_it, doubl
                              tdda_solve_info* infos);
 
 /* serving loop: continuous batching of solve requests ------------------- */
-/* Requests queue in arrival order.  A worker takes the first request whose
- * device memory fits the HBM budget that the requests in flight leave free,
- * together with queued requests that share its operator (lattice, spacing,
- * wavelength, material, nback) up to max_group right-hand sides, and solves
- * them in one batched solve on its own CUDA stream while other workers solve
- * theirs.  No counterpart in the reference, which solves one structure at a
- * time (main.cpp:577-598); each result equals the same request solved alone. */
+/* Requests queue in arrival order; workers run concurrently on their own CUDA
+ * streams.  Operators (lattice, spacing, wavelength, material, nback: the core
+ * and its Green spectrum) stay resident after their requests, with a pool of
+ * their models, and later requests of the same operator reuse them; idle ones
+ * are evicted least recently used first when admission needs the memory.
+ * FP32+refine: a worker runs a session of max_group slots for lattices of one
+ * FFT grid shape (tdda_solve_multi's batching) and, between rounds of at most
+ * 32 inner steps, frees finished slots and admits queued requests of that
+ * shape (continuous batching).  FP64: a worker solves the first request that
+ * fits with the queued requests of its operator in one batched solve.
+ * Admission is first fit under the HBM budget.  No counterpart in the
+ * reference, which solves one structure at a time (main.cpp:577-598); each
+ * result equals the same request solved alone. */
 typedef enum tdda_request_state {
     TDDA_REQ_QUEUED = 0,
     TDDA_REQ_RUNNING = 1,
@@ -217,7 +223,8 @@ typedef struct tdda_server_desc {
     int precision;            /* TDDA_FP64 or TDDA_FP32_REFINE */
     int max_it;
     double tol;
-    int max_group;            /* right-hand sides of one batched solve (<= 64) */
+    int max_group;            /* right-hand sides of one batched solve, or the slots of one
+                                 FP32+refine session (<= 64) */
     int dry_run;              /* scheduler only: no device work, a request takes dry_run_ms */
     double dry_run_ms;
 } tdda_server_desc;
@@ -242,7 +249,7 @@ typedef struct tdda_request_info {
     int iterations;           /* largest iteration count over the right-hand sides */
     double error;             /* largest final relative residual */
     double bytes;             /* device bytes admitted for the request */
-    int group;                /* right-hand sides of the batched solve that carried it */
+    int group;                /* right-hand sides sharing its launches when it was admitted */
 } tdda_request_info;
 
 typedef struct tdda_server_s tdda_server;
@@ -258,7 +265,21 @@ tdda_status tdda_server_result(tdda_server* server, unsigned long long id, int w
 tdda_status tdda_server_stats(tdda_server* server, int* queued, int* running, double* bytes, double* peak_bytes);
 /* seconds since the server was created */
 double tdda_server_clock(const tdda_server* server);
-/* finishes every submitted request, then stops the workers */
+/* what the server has done so far: residency and continuous batching */
+typedef struct tdda_server_counters {
+    unsigned long long operators_built;    /* cores built (each builds its Green spectrum) */
+    unsigned long long operator_hits;      /* requests whose operator was resident */
+    unsigned long long operators_evicted;  /* idle resident operators freed for admission */
+    unsigned long long shapes_built;       /* FP32+refine: grid-shape sessions created */
+    unsigned long long joined_running;     /* FP32+refine: requests admitted while others ran */
+    unsigned long long rounds;             /* FP32+refine: session rounds (one launch of the steps each) */
+    int max_slots_in_use;                  /* most right-hand sides sharing one launch */
+    int max_lattices_in_use;               /* most different lattices sharing one launch */
+    int resident_operators;                /* operators resident now */
+} tdda_server_counters;
+tdda_status tdda_server_counters_get(tdda_server* server, tdda_server_counters* out);
+/* finishes every submitted request, then stops the workers and frees the
+ * resident operators */
 tdda_status tdda_server_destroy(tdda_server* server);
 /* device bytes a request of nrhs right-hand sides holds while it is solved */
 double tdda_request_bytes(int Nx, int Ny, int Nz, int N, int nrhs, int precision);

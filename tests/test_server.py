@@ -98,3 +98,105 @@ def test_each_result_equals_the_request_alone(precision):
         tdda.solve_batch(models, precision, 10000, 1e-5)
         for k, m in enumerate(models):
             assert np.array_equal(P[k], m.get_P())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [tdda.FP64, tdda.FP32_REFINE])
+def test_operators_stay_resident(precision):
+    """Requests of one operator (lattice, spacing, wavelength, material) after one another:
+    the core and its models are built once and reused; results equal the request alone."""
+    if tdda.device_count() < 1:
+        pytest.skip("no CUDA device")
+    n = 9
+    R = lattice.bulk(n, n, n)
+    s = tdda.Server(hbm_budget_bytes=150e9, workers=1, precision=precision, max_group=4)
+    outs = []
+    for k in range(4):
+        rng = np.random.Generator(np.random.PCG64(60 + k))
+        diel = np.repeat(rng.random(n ** 3), 3)  # new densities: same operator, new models' al
+        rid = s.submit(n, n, n, R, 10.0, 500.0, MAT, diel, [XPOL, YPOL][: 1 + k % 2])
+        outs.append((diel, k, s.result(rid)))
+    c = s.counters()
+    s.close()
+    assert c["operators_built"] == 1 and c["operator_hits"] == 3 and c["resident_operators"] == 1
+    core = tdda.AProductCore(n, n, n, R, 10.0, 500.0, MAT, max_rhs=2)
+    for diel, k, (info, P) in outs:
+        assert info["state"] == tdda.REQ_DONE
+        incs = [XPOL, YPOL][: 1 + k % 2]
+        ms = [tdda.DDAModel(core, i[0], i[2], i[1], diel) for i in incs]
+        tdda.solve_batch(ms, precision, 10000, 1e-5)
+        for j, m in enumerate(ms):
+            assert np.array_equal(P[j], m.get_P())
+            m.close()
+    core.close()
+
+
+@pytest.mark.gpu
+def test_requests_join_running_work_across_lattices():
+    """FP32+refine continuous batching: one worker, a session of 4 slots.  A slow request
+    (a 14^3 lattice at a high contrast) is running when requests of other lattices of the
+    same FFT grid shape arrive; they join its launches as slots are free, and every result
+    equals its request alone."""
+    if tdda.device_count() < 1:
+        pytest.skip("no CUDA device")
+    rng = np.random.Generator(np.random.PCG64(77))
+    boxes = [(14, 14, 14), (15, 14, 16), (16, 15, 14), (14, 16, 15), (15, 15, 15)]
+    grids = {tuple(lattice.fft_length(b[a], a == 2) for a in range(3)) for b in boxes}
+    assert len(grids) == 1
+    reqs = []
+    for k, b in enumerate(boxes):
+        mat = np.array([1.0, 12.0 + 0.05j]) if k == 0 else np.array([1.0, [2.25, 4.0 + 0.1j][k % 2]])
+        reqs.append((b, 10.0 - k, float(rng.uniform(450, 650)), mat, np.repeat(rng.random(int(np.prod(b))), 3)))
+    s = tdda.Server(hbm_budget_bytes=150e9, workers=1, precision=tdda.FP32_REFINE, max_group=4)
+    ids = []
+    for k, (b, d, lam, mat, diel) in enumerate(reqs):
+        ids.append(s.submit(*b, lattice.bulk(*b), d, lam, mat, diel, [XPOL]))
+        if k == 0:
+            time.sleep(0.05)  # the first request is running when the others arrive
+    out = [s.result(i) for i in ids]
+    c = s.counters()
+    s.close()
+    assert c["joined_running"] >= 1 and c["max_lattices_in_use"] >= 2, c
+    for (b, d, lam, mat, diel), (info, P) in zip(reqs, out):
+        assert info["state"] == tdda.REQ_DONE, info
+        core = tdda.AProductCore(*b, lattice.bulk(*b), d, lam, mat)
+        m = tdda.DDAModel(core, XPOL[0], XPOL[2], XPOL[1], diel)
+        m.solve_mixed(10000, 1e-5)
+        assert np.array_equal(P[0], m.get_P())
+        m.close()
+        core.close()
+
+
+@pytest.mark.gpu
+def test_request_bytes_bound_the_device_memory_a_request_takes():
+    """tdda_request_bytes against the device memory a core and its models take (the drop in
+    free memory while they exist, in a fresh process so the memory pool starts empty)."""
+    if tdda.device_count() < 1:
+        pytest.skip("no CUDA device")
+    import subprocess
+    import sys
+    code = (
+        "import sys, numpy as np; sys.path.insert(0, 'topo-dda-forwin64_gb300'); import tdda, torch\n"
+        "from tdda import lattice\n"
+        "torch.cuda.init(); torch.zeros(1, device='cuda'); torch.cuda.synchronize()\n"
+        "out = []\n"
+        "for (nx, ny, nz, nrhs) in ((40, 40, 20, 1), (48, 40, 24, 2)):\n"
+        "    f0 = torch.cuda.mem_get_info()[0]\n"
+        "    R = lattice.bulk(nx, ny, nz)\n"
+        "    c = tdda.AProductCore(nx, ny, nz, R, 10.0, 500.0, np.array([1.0, 4.0 + 0.1j]), max_rhs=nrhs)\n"
+        "    ms = [tdda.DDAModel(c, [0, 0, 1], 1.0, [1, 0, 0], np.full(R.size, 0.5)) for _ in range(nrhs)]\n"
+        "    tdda.solve_batch(ms, tdda.FP32_REFINE, 10000, 1e-5)\n"
+        "    torch.cuda.synchronize()\n"
+        "    f1 = torch.cuda.mem_get_info()[0]\n"
+        "    out.append((f0 - f1, tdda.request_bytes(nx, ny, nz, R.size // 3, nrhs)))\n"
+        "print(out)\n")
+    import os
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, cwd=root, timeout=300)
+    assert r.returncode == 0, r.stderr
+    pairs = eval(r.stdout.strip().splitlines()[-1])
+    for used, est in pairs:
+        print(f"\ndevice memory taken {used / 1e6:.1f} MB, tdda_request_bytes {est / 1e6:.1f} MB")
+        # the estimate bounds what a request takes (pool granularity: up to 64 MB more per request)
+        assert used <= est + 64e6
+        assert est <= 3 * used + 64e6

@@ -901,6 +901,11 @@ void core_grid(const tdda_core* c, int grid[3]) {
     grid[2] = c->g.pz.M;
 }
 int core_device(const tdda_core* c) { return c->device; }
+void grid_of_box(int Nx, int Ny, int Nz, int grid[3]) {
+    grid[0] = fft_length(Nx, false);
+    grid[1] = fft_length(Ny, false);
+    grid[2] = fft_length(Nz, true);
+}
 
 namespace {
 // The largest lattice a grid shape holds on each axis: M >= 2N - 1
@@ -1003,6 +1008,26 @@ tdda_status upload_subset(Shape* s, const std::vector<int>& ks) {
     return TDDA_OK;
 }
 }  // namespace
+
+double core_bytes(int Nx, int Ny, int Nz, int N, int max_rhs) {
+    const double Mx = fft_length(Nx, false), My = fft_length(Ny, false), Mz = fft_length(Nz, true);
+    const double H = (Mx / 2 + 1) * (My / 2 + 1) * (Mz / 2 + 1);
+    const double n3 = 3.0 * N;
+    const double grid = 3.0 * Nx * My * Mz * max_rhs;  // FFT work grid entries
+    return (double)Nx * Ny * Nz * 4 + n3 * 4           // cellmap, R
+           + 6 * H * (16 + 8 + 16)                     // Green spectra (FP64, FP32, double-float)
+           + grid * (16 + 8)                           // FP64 and FP32 grids
+           + n3 * 2 * (16 + 8)                         // product staging
+           + 6 * Mx * My * Mz * 16                     // full Green grid while the core is built
+           + 1e6;                                      // reduction partials, states, twiddles
+}
+
+double model_bytes(int N, int precision) {
+    const double n3 = 3.0 * N;
+    double model = n3 * (12 * 16 + 8);  // FP64 vectors and densities
+    if (precision == TDDA_FP32_REFINE) model += n3 * 10 * 8;
+    return model;
+}
 
 double shape_bytes(const int grid[3], int cap) {
     Geom g;
@@ -1200,23 +1225,26 @@ tdda_status shape_step(Shape* s, std::vector<Done>* done) {
         TDDA_CK(aprod<float>(c, tdda::SRC_IN, tdda::SNK_AP, n, s->rhs32c, nullptr, 1));
         TDDA_CK(aprod<float>(c, tdda::SRC_TUPD, tdda::SNK_AT_DEF, n, s->rhs32c, nullptr, 1));
     }
-    bool any_inner = false;
-    for (const Slot& sl : s->slots) any_inner |= sl.phase == kInner;
-    if (!any_inner) return TDDA_OK;
-    // 3. one launch of the steps of every slot (the device-side loop: at most
+    // the launch covers the slots up to the last one in an inner solve (slots are
+    // taken lowest first, so a lightly loaded shape launches few right-hand sides)
+    int width = 0;
+    for (int k = 0; k < s->cap; k++)
+        if (s->slots[k].phase == kInner) width = k + 1;
+    if (width == 0) return TDDA_OK;
+    // 3. one launch of the steps of those slots (the device-side loop: at most
     // kLoopChunks chunks of kChunk steps, or one host-launched chunk); the chunk
     // count of the launch restarts in the first slot's state
     const int zero_limit[2] = {0, 1 << 30};
     TDDA_CK(cudaMemcpyAsync(&c->st32[0].chunks, zero_limit, sizeof(zero_limit), cudaMemcpyHostToDevice, c->stream));
     cudaGraphExec_t ex;
-    TDDA_TRY(get_iteration_graph<float>(c, s->cap, &ex));
+    TDDA_TRY(get_iteration_graph<float>(c, width, &ex));
     TDDA_CK(cudaGraphLaunch(ex, c->stream));
-    TDDA_CK(cudaMemcpyAsync(c->hst, c->st32, sizeof(SolveState) * s->cap, cudaMemcpyDeviceToHost, c->stream));
+    TDDA_CK(cudaMemcpyAsync(c->hst, c->st32, sizeof(SolveState) * width, cudaMemcpyDeviceToHost, c->stream));
     TDDA_CK(cudaStreamSynchronize(c->stream));
     count_launches(std::max(1, c->hst[0].chunks) * chunk_kernels<float>(c));
     // 4. inner solves that stopped: the pending update, then P += the correction
     std::vector<int> stopped;
-    for (int k = 0; k < s->cap; k++)
+    for (int k = 0; k < width; k++)
         if (s->slots[k].phase == kInner && c->hst[k].status != tdda::ST_RUNNING) stopped.push_back(k);
     if (stopped.empty()) return TDDA_OK;
     TDDA_TRY(upload_subset(s, stopped));
@@ -2213,19 +2241,7 @@ tdda_status tdda_aproduct_noalloc(tdda_core* c, const double* b, double* y) {
 
 double tdda_request_bytes(int Nx, int Ny, int Nz, int N, int nrhs, int precision) {
     if (Nx < 1 || Ny < 1 || Nz < 1 || N < 1 || nrhs < 1) return 0.0;
-    const double Mx = fft_length(Nx, false), My = fft_length(Ny, false), Mz = fft_length(Nz, true);
-    const double H = (Mx / 2 + 1) * (My / 2 + 1) * (Mz / 2 + 1);
-    const double n3 = 3.0 * N;
-    const double grid = 3.0 * Nx * My * Mz * nrhs;  // FFT work grid entries
-    double core = (double)Nx * Ny * Nz * 4 + n3 * 4    // cellmap, R
-                  + 6 * H * (16 + 8)                    // Green spectra
-                  + grid * (16 + 8)                     // FP64 and FP32 grids
-                  + n3 * 2 * (16 + 8)                   // product staging
-                  + 6 * Mx * My * Mz * 16               // full Green grid while the core is built
-                  + 1e6;                                // reduction partials, states, twiddles
-    double model = n3 * (12 * 16 + 8);                  // FP64 vectors and densities
-    if (precision == TDDA_FP32_REFINE) model += n3 * 10 * 8;
-    return core + nrhs * model;
+    return tdda_session::core_bytes(Nx, Ny, Nz, N, nrhs) + nrhs * tdda_session::model_bytes(N, precision);
 }
 
 }  // extern "C"

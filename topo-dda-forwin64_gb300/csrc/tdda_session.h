@@ -28,10 +28,15 @@ struct Done {
     tdda_solve_info info;
 };
 
-// the FFT grid of a core, and the device memory of a shape of `cap` slots
+// the FFT grid of a core; the device memory of a core of max_rhs right-hand
+// sides, of one model, and of a shape of `cap` slots (upper estimates)
 void core_grid(const tdda_core* c, int grid[3]);
 int core_device(const tdda_core* c);
+double core_bytes(int Nx, int Ny, int Nz, int N, int max_rhs);
+double model_bytes(int N, int precision);
 double shape_bytes(const int grid[3], int cap);
+// the FFT grid a lattice box gets (tdda_core_create's choice)
+void grid_of_box(int Nx, int Ny, int Nz, int grid[3]);
 
 tdda_status shape_create(int device, const int grid[3], int cap, Shape** out);
 void shape_destroy(Shape* s);

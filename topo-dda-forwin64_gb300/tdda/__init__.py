@@ -49,7 +49,8 @@ EXPORTS = [
     "tdda_fft3d", "tdda_core_stream", "tdda_kernel_launches", "tdda_profile_aproduct", "tdda_core_pass_count",
     "tdda_core_pass_name", "tdda_core_set_xpass", "tdda_core_autotune",
     "tdda_aproduct_noalloc", "tdda_server_create", "tdda_server_submit", "tdda_server_result",
-    "tdda_server_stats", "tdda_server_clock", "tdda_server_destroy", "tdda_request_bytes",
+    "tdda_server_stats", "tdda_server_counters_get", "tdda_server_clock", "tdda_server_destroy",
+    "tdda_request_bytes",
 ]
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 
@@ -95,6 +96,14 @@ class RequestDesc(ctypes.Structure):
                 ("diel_old", ctypes.POINTER(ctypes.c_double)), ("nrhs", ctypes.c_int),
                 ("nK", ctypes.POINTER(ctypes.c_double)), ("nE0", ctypes.POINTER(ctypes.c_double)),
                 ("E0", ctypes.POINTER(ctypes.c_double))]
+
+
+class ServerCounters(ctypes.Structure):
+    _fields_ = [("operators_built", ctypes.c_ulonglong), ("operator_hits", ctypes.c_ulonglong),
+                ("operators_evicted", ctypes.c_ulonglong), ("shapes_built", ctypes.c_ulonglong),
+                ("joined_running", ctypes.c_ulonglong), ("rounds", ctypes.c_ulonglong),
+                ("max_slots_in_use", ctypes.c_int), ("max_lattices_in_use", ctypes.c_int),
+                ("resident_operators", ctypes.c_int)]
 
 
 class RequestInfo(ctypes.Structure):
@@ -160,6 +169,7 @@ def load() -> ctypes.CDLL:
         "tdda_server_submit": (i, [vp, ctypes.POINTER(RequestDesc), ctypes.POINTER(ctypes.c_ulonglong)]),
         "tdda_server_result": (i, [vp, ctypes.c_ulonglong, i, ctypes.POINTER(RequestInfo), vp]),
         "tdda_server_stats": (i, [vp, ip, ip, dp, dp]),
+        "tdda_server_counters_get": (i, [vp, ctypes.POINTER(ServerCounters)]),
         "tdda_server_clock": (d, [vp]),
         "tdda_server_destroy": (i, [vp]),
         "tdda_request_bytes": (d, [i, i, i, i, i, i]),
@@ -553,6 +563,12 @@ class Server:
         _check(load().tdda_server_stats(self.h, ctypes.byref(q), ctypes.byref(r), ctypes.byref(b), ctypes.byref(pk)),
                "tdda_server_stats")
         return {"queued": q.value, "running": r.value, "bytes": b.value, "peak_bytes": pk.value}
+
+    def counters(self) -> dict:
+        """Residency and continuous-batching counters (tdda_server_counters_get)."""
+        c = ServerCounters()
+        _check(load().tdda_server_counters_get(self.h, ctypes.byref(c)), "tdda_server_counters_get")
+        return {f: getattr(c, f) for f, _ in ServerCounters._fields_}
 
     def clock(self) -> float:
         return load().tdda_server_clock(self.h)
