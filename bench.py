@@ -12,9 +12,12 @@ ours       FP32 FFT convolution + Krylov vectors, double-float dot sums, the res
            (value); the plain FP64 solve of the same lattice is
            timed beside it (fp64).  Inputs are resident in HBM in the device-timed region;
            `e2e` is the same solve through the C ABI with host buffers.
-reference  the reference's solve path run on the host cores (the oracle port of
-           AProductCore::Aproduct + DDAModel::bicgstab, all host threads, one full converged
-           solve per thread per step), solves/s.
+reference  the reference's solve path run on the host cores: its own AProductCore.cpp /
+           DDAModel.cpp sources (oracle/_ref/ref_timer, built from the reference's sources
+           with CPU stand-ins for cuFFT), one process per core, one full converged solve in
+           each; beside it the reference's own GPU build with cuFFT on this GPU
+           (oracle/_ref/ref_cufft).  Where the reference's sources were not built, the
+           oracle port of AProductCore::Aproduct + DDAModel::bicgstab, all host threads.
 
 Multi-GPU: the solve does not shard; N ranks run N independent replicas (weak scaling).
 """
@@ -271,12 +274,82 @@ class CpuBaseline:
                 "sample_wall_s": wall, "iterations": its}
 
 
+def run_reference_code(args, w, threads: int) -> dict:
+    """The reference's own code (oracle/_ref/ref_timer: its AProductCore.cpp, DDAModel.cpp, ...
+    compiled unchanged against the CPU stand-ins for cuFFT and the CUDA runtime), timed on
+    the host cores with one independent process per core.  Each warm-up and timed step runs,
+    in every process, the constructor and one A-product of the workload; a last step runs,
+    in every process, the constructor and one full BiCGSTAB solve to tol 1e-5 from P = 0.
+    The line's value is that full step's: processes / median solve time (measured, not
+    extrapolated).  The product steps give the extrapolated rate beside it, processes /
+    (median product time x the 2 its + 3 products of the reference's solve).  Then, where
+    it was built, the reference's GPU build (oracle/_ref/ref_cufft: kernel.cu for sm_103a
+    with cuFFT) runs the same constructor, products and solve on the GPU."""
+    import ref_timing as RT
+
+    inc = w.incidences[0]
+    for _ in range(args.warmup):
+        RT.run_many(RT.TIMER, w, inc, MAX_IT, TOL, 1, False, threads)
+    prods, step_s = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        rs = RT.run_many(RT.TIMER, w, inc, MAX_IT, TOL, 1, False, threads)
+        step_s.append(time.perf_counter() - t0)
+        prods += [r["aprod_s"][0] for r in rs]
+    t0 = time.perf_counter()
+    full = RT.run_many(RT.TIMER, w, inc, MAX_IT, TOL, 0, True, threads)
+    full_wall = time.perf_counter() - t0
+    its = full[0]["iterations"]
+    solve_s = statistics.median(r["solve_s"] for r in full)
+    value = threads / solve_s
+    extrap = threads / (statistics.median(prods) * (2 * its + 3))
+    sample = (f"reference's own AProductCore/DDAModel sources (oracle/_ref/ref_timer, CPU stand-ins for cuFFT "
+              f"with Bluestein on its {2 * w.Nx - 1}x{2 * w.Ny - 1}x{2 * w.Nz - 1} grid), {threads} processes, one per "
+              f"core: one full BiCGSTAB solve each to tol {TOL:g} from P = 0 ({its} iterations, median "
+              f"{solve_s:.1f} s, {full_wall:.1f} s wall); {args.steps} steps of one A-product per process "
+              f"(median {1e3 * statistics.median(prods):.0f} ms) give {extrap:.3f} solves/s extrapolated")
+    out = {"value": value, "kind": "reference", "cores": threads, "cpu_model": cpu_model(), "sample": sample,
+           "iterations": its, "error": full[0]["error"], "solve_s_median": solve_s,
+           "aprod_ms_median": 1e3 * statistics.median(prods), "extrapolated_value": extrap,
+           "ms_per_step": 1e3 * statistics.median(step_s)}
+    import torch
+    if RT.available(RT.CUFFT) and torch.cuda.is_available():
+        g = RT.run_many(RT.CUFFT, w, inc, MAX_IT, TOL, 20, True, 1)[0]
+        out["gpu_cufft_build"] = {
+            "what": "the reference's AProductCore.cpp + DDAModel.cpp + kernel.cu built for sm_103a with cuFFT "
+                    "(oracle/_ref/ref_cufft), one solve on this GPU; host<->device copies per product included "
+                    "(its design)",
+            "value": 1.0 / g["solve_s"], "unit": UNIT, "solve_s": g["solve_s"], "iterations": g["iterations"],
+            "error": g["error"], "aprod_ms_median": 1e3 * statistics.median(g["aprod_s"][1:]),
+            "ctor_s": g["ctor_s"]}
+    return out
+
+
 def run_reference(args, dist: Dist):
-    """The reference's CPU solve path timed on the host cores (rank 0 only)."""
+    """The reference's CPU solve path timed on the host cores (rank 0 only): the reference's
+    own code where it was built on this host (run_reference_code), else the oracle port."""
     if dist.rank != 0:
         return
     w = lattice.config(2)
     threads = os.cpu_count() or 1
+    import ref_timing as RT
+    if RT.available(RT.TIMER):
+        r = run_reference_code(args, w, threads)
+        line = {"impl": "reference", "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+                "data": "synthetic (seeded)",
+                "config": {"workload": WORKLOAD, "lattice": [w.Nx, w.Ny, w.Nz], "dipoles": w.N, "tol": TOL,
+                           "grid": [2 * n - 1 for n in (w.Nx, w.Ny, w.Nz)]},
+                "cpu_baseline": {k: r[k] for k in ("value", "kind", "cores", "cpu_model", "sample")},
+                "reference_solve": {k: r[k] for k in ("iterations", "error", "solve_s_median", "aprod_ms_median",
+                                                      "extrapolated_value")},
+                "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        line["cpu_baseline"]["unit"] = UNIT
+        if "gpu_cufft_build" in r:
+            line["gpu_cufft_build"] = r["gpu_cufft_build"]
+        print(json.dumps(line), flush=True)
+        return
     iters = max(1, args.cpu_iters)
     cpu = CpuBaseline(w, threads)
     for _ in range(args.warmup):
@@ -426,6 +499,7 @@ def run_serving(tdda, stream, precision, workers, budget, dev):
                               np.array([1.0, r.eps_m]), diel, r.incidences))
     infos = [srv.result(i, with_P=False)[0] for i in ids]
     peak = srv.stats()["peak_bytes"]
+    counters = srv.counters()
     srv.close()
     ok = [i["state"] == tdda.REQ_DONE for i in infos]
     lat = np.array([(i["t_done"] - i["t_submit"]) * 1e3 for i in infos])
@@ -439,8 +513,18 @@ def run_serving(tdda, stream, precision, workers, budget, dev):
         if sel:
             per[name] = {"requests": len(sel), "p50_ms": float(np.percentile(sel, 50)),
                          "p99_ms": float(np.percentile(sel, 99))}
+    # steady state: right-hand sides completed between the 10th and the 90th percentile of the
+    # completion times, over that window (the ramp-up and the tail of slow requests excluded)
+    done = sorted((i["t_done"], len(r.incidences)) for i, r in zip(infos, stream))
+    lo, hi = done[len(done) // 10], done[(9 * len(done)) // 10]
+    window = hi[0] - lo[0]
+    mid = sum(n for t, n in done if lo[0] < t <= hi[0])
+    shared = sum(1 for i, r in zip(infos, stream) if i["group"] > len(r.incidences))
     return {"requests": len(stream), "failed": int(len(ok) - sum(ok)), "rhs_solves": rhs,
             "value": rhs / span, "unit": UNIT, "requests_per_s": len(stream) / span, "makespan_s": span,
+            "steady_state": {"value": mid / window if window > 0 else None, "unit": UNIT,
+                             "window_s": window, "rhs_solves": mid},
+            "requests_sharing_launches": shared, "counters": counters,
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
             "latency_by_size": per, "peak_admitted_bytes": peak,
             "max_iterations": max(i["iterations"] for i in infos)}
@@ -626,11 +710,12 @@ def run_ours(args, dist: Dist):
     if args.serve_requests > 0:
         stream = lattice.serving_stream(n=args.serve_requests, rate=200.0, seed=5)
         s32 = run_serving(tdda, stream, tdda.FP32_REFINE, args.serve_workers, 150e9, dev)
-        s64 = run_serving(tdda, stream, tdda.FP64, args.serve_workers, 150e9, dev)
+        n64 = min(args.serve_requests, args.serve_fp64_requests or args.serve_requests)
+        s64 = run_serving(tdda, stream[:n64], tdda.FP64, args.serve_workers, 150e9, dev) if n64 > 0 else None
         serving = {"workload": f"serving stream {args.serve_requests} requests, Poisson 200/s, dims 16-128 "
                                "log-uniform (z<=32), 1-4 RHS (cfg 5)", "hbm_budget_bytes": 150e9,
                    "workers": args.serve_workers, "fp32_refine": s32, "fp64": s64,
-                   "speedup_fp32_refine": s32["value"] / s64["value"]}
+                   "speedup_fp32_refine": s32["value"] / s64["value"] if s64 and n64 == len(stream) else None}
 
     # topology optimisation: forward + adjoint solves batched per iteration
     topo_line = None
@@ -728,6 +813,8 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-workers", type=int, default=4)
+    ap.add_argument("--serve-fp64-requests", type=int, default=0,
+                    help="replay only the first n requests with plain FP64 (0: all of them)")
     ap.add_argument("--topo-iters", type=int, default=200)
     ap.add_argument("--aprod-only", type=int, default=0)
     ap.add_argument("--aprod-precision", choices=["fp32", "fp64"], default="fp32")

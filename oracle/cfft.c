@@ -170,3 +170,153 @@ int oc_fft3d(int n0, int n1, int n2, oc_cplx* data, int sign) {
     free(work);
     return 0;
 }
+
+/* ------------------------------------------------------------------------
+ * Lengths with a large prime factor, for timing the reference's CPU path.
+ *
+ * oc_fft3d_fast gives the same transform as oc_fft3d (to rounding) but runs a
+ * line whose length has a prime factor above 7 through Bluestein's chirp-z
+ * algorithm (L. I. Bluestein, "A linear filtering approach to the
+ * computation of the discrete Fourier transform", 1970): with
+ * k q = (k^2 + q^2 - (q - k)^2) / 2 and c_k = exp(sign pi i k^2 / n),
+ *     X_q = c_q sum_k (x_k c_k) conj(c_{q - k}),
+ * a circular convolution of length L >= 2n - 1 (a power of two) evaluated
+ * with the radix-4/2 FFT above.  The reference's 2N - 1 grids (127, 31, 191,
+ * ...) are such lengths; the direct O(p^2) prime DFT of oc_fft3d is kept for
+ * the checker itself, whose outputs are pinned to fixtures.
+ */
+typedef struct {
+    int n, L;
+    oc_plan1d* sub;   /* length L */
+    oc_cplx* chirp;   /* c_k for sign -1, k < n (sign +1 is the conjugate) */
+    oc_cplx* bhat[2]; /* FFT_L of the conjugate chirp, for sign -1 and +1 */
+} oc_blue;
+
+static int largest_prime_factor(int n) {
+    int p = 1;
+    for (int f = 2; (long long)f * f <= n; f++)
+        while (n % f == 0) { p = f; n /= f; }
+    return n > 1 ? n : p;
+}
+
+static void blue_destroy(oc_blue* b) {
+    if (!b) return;
+    oc_plan1d_destroy(b->sub);
+    free(b->chirp);
+    free(b->bhat[0]);
+    free(b->bhat[1]);
+    free(b);
+}
+
+static oc_blue* blue_create(int n) {
+    oc_blue* b = (oc_blue*)calloc(1, sizeof(oc_blue));
+    if (!b) return NULL;
+    b->n = n;
+    b->L = 1;
+    while (b->L < 2 * n - 1) b->L *= 2;
+    const int L = b->L;
+    b->sub = oc_plan1d_create(L);
+    b->chirp = (oc_cplx*)malloc(sizeof(oc_cplx) * (size_t)n);
+    b->bhat[0] = (oc_cplx*)calloc((size_t)L, sizeof(oc_cplx));
+    b->bhat[1] = (oc_cplx*)calloc((size_t)L, sizeof(oc_cplx));
+    oc_cplx* work = (oc_cplx*)malloc(sizeof(oc_cplx) * 2 * (size_t)L);
+    if (!b->sub || !b->chirp || !b->bhat[0] || !b->bhat[1] || !work) {
+        free(work);
+        blue_destroy(b);
+        return NULL;
+    }
+    const double pi = 3.14159265358979323846264338327950288;
+    for (int k = 0; k < n; k++) {
+        /* k^2 mod 2n keeps the angle's argument small and exact */
+        const long long e = ((long long)k * k) % (2LL * n);
+        const double a = pi * (double)e / (double)n;
+        b->chirp[k].re = cos(a);
+        b->chirp[k].im = -sin(a);
+    }
+    for (int s = 0; s < 2; s++) {
+        const double sg = s == 0 ? -1.0 : 1.0; /* the transform's sign */
+        oc_cplx* h = b->bhat[s];
+        for (int k = 0; k < n; k++) {
+            /* conj(c_k) of that sign: c_k(sign) = (re, sign * |im|) */
+            oc_cplx c = b->chirp[k];
+            if (sg > 0) c.im = -c.im;
+            oc_cplx cc = {c.re, -c.im};
+            h[k] = cc;
+            if (k > 0) h[L - k] = cc;
+        }
+        oc_fft1d(b->sub, h, 1, -1, work);
+    }
+    free(work);
+    return b;
+}
+
+/* one line through the chirp-z convolution; scratch holds 3 L elements */
+static void blue_line(const oc_blue* b, oc_cplx* data, ptrdiff_t stride, int sign, oc_cplx* scratch) {
+    const int n = b->n, L = b->L;
+    oc_cplx* a = scratch;
+    oc_cplx* work = scratch + L;
+    for (int k = 0; k < n; k++) {
+        oc_cplx c = b->chirp[k];
+        if (sign > 0) c.im = -c.im;
+        a[k] = cmul(data[(ptrdiff_t)k * stride], c);
+    }
+    for (int k = n; k < L; k++) a[k].re = a[k].im = 0.0;
+    oc_fft1d(b->sub, a, 1, -1, work);
+    const oc_cplx* h = b->bhat[sign > 0 ? 1 : 0];
+    for (int k = 0; k < L; k++) a[k] = cmul(a[k], h[k]);
+    oc_fft1d(b->sub, a, 1, 1, work);
+    const double inv = 1.0 / (double)L;
+    for (int q = 0; q < n; q++) {
+        oc_cplx c = b->chirp[q];
+        if (sign > 0) c.im = -c.im;
+        oc_cplx v = cmul(a[q], c);
+        v.re *= inv;
+        v.im *= inv;
+        data[(ptrdiff_t)q * stride] = v;
+    }
+}
+
+typedef struct {
+    oc_plan1d* p;
+    oc_blue* b;
+} oc_axis;
+
+static int axis_create(oc_axis* ax, int n) {
+    ax->p = NULL;
+    ax->b = NULL;
+    if (largest_prime_factor(n) > 7) ax->b = blue_create(n);
+    else ax->p = oc_plan1d_create(n);
+    return ax->p || ax->b ? 0 : 1;
+}
+
+static void axis_line(const oc_axis* ax, oc_cplx* data, ptrdiff_t stride, int sign, oc_cplx* scratch) {
+    if (ax->b) blue_line(ax->b, data, stride, sign, scratch);
+    else oc_fft1d(ax->p, data, stride, sign, scratch);
+}
+
+static int axis_scratch(const oc_axis* ax) { return ax->b ? 3 * ax->b->L : 2 * oc_plan1d_len(ax->p); }
+
+int oc_fft3d_fast(int n0, int n1, int n2, oc_cplx* data, int sign) {
+    oc_axis a0, a1, a2;
+    int err = axis_create(&a0, n0);
+    err |= axis_create(&a1, n1);
+    err |= axis_create(&a2, n2);
+    int ns = axis_scratch(&a0);
+    if (axis_scratch(&a1) > ns) ns = axis_scratch(&a1);
+    if (axis_scratch(&a2) > ns) ns = axis_scratch(&a2);
+    oc_cplx* scratch = err ? NULL : (oc_cplx*)malloc(sizeof(oc_cplx) * (size_t)ns);
+    if (!scratch) err = 1;
+    if (!err) {
+        const ptrdiff_t s1 = n2, s0 = (ptrdiff_t)n1 * n2;
+        for (int i = 0; i < n0; i++)
+            for (int j = 0; j < n1; j++) axis_line(&a2, data + i * s0 + j * s1, 1, sign, scratch);
+        for (int i = 0; i < n0; i++)
+            for (int k = 0; k < n2; k++) axis_line(&a1, data + i * s0 + k, s1, sign, scratch);
+        for (int j = 0; j < n1; j++)
+            for (int k = 0; k < n2; k++) axis_line(&a0, data + j * s1 + k, s0, sign, scratch);
+    }
+    free(scratch);
+    oc_plan1d_destroy(a0.p); oc_plan1d_destroy(a1.p); oc_plan1d_destroy(a2.p);
+    blue_destroy(a0.b); blue_destroy(a1.b); blue_destroy(a2.b);
+    return err;
+}

@@ -38,6 +38,11 @@ void oc_fft1d(const oc_plan1d* p, oc_cplx* data, ptrdiff_t stride, int sign, oc_
  * then axis 1, then axis 0.  Returns 0 on success. */
 int oc_fft3d(int n0, int n1, int n2, oc_cplx* data, int sign);
 
+/* The same 3-D transform, with Bluestein's chirp-z algorithm for a line
+ * length that has a prime factor above 7 (the reference's 2N - 1 grids).
+ * Used to time the reference's CPU path; the checker keeps oc_fft3d. */
+int oc_fft3d_fast(int n0, int n1, int n2, oc_cplx* data, int sign);
+
 #ifdef __cplusplus
 }
 #endif

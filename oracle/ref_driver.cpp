@@ -23,9 +23,21 @@
  *        directory: CoreStructure::output_to_file (CoreStructure.cpp:155-185,
  *        both modes), DDAModel::output_to_file (DDAModel.cpp:589-697) and the
  *        commondata.txt lines of main.cpp:282-289
+ *        mode 7: timing.  Appends int32 reps, int32 solve (0/1).  Times the
+ *        constructor AProductCore(...) + DDAModel(...), then `reps`
+ *        Aproduct(vec[0]) calls, then (solve = 1) one bicgstab(max_it,
+ *        max_err) from P = 0.  Writes f64 ctor_s, f64 aprod_s[reps],
+ *        int32 iterations, f64 solve_s (the final error is on stdout).  Built against the CPU
+ *        stand-ins (oracle/_ref/ref_timer) or against the CUDA runtime and
+ *        cuFFT with kernel.cu for the GPU (oracle/_ref/ref_cufft): the
+ *        reference's host<->device copies per product are part of its design
+ *        and are inside the timed calls.  The process ends without running
+ *        the destructors (AProductCore.cpp:540-541 frees ADev twice).
  *   out: see the per-mode writers below.
  */
+#include <chrono>
 #include <cstdio>
+#include <cstdlib>
 #include <fstream>
 #include <cstdint>
 #include <iostream>
@@ -76,6 +88,14 @@ int main(int argc, char** argv) {
         std::fprintf(stderr, "usage: ref_driver in.bin out.bin\n");
         return 2;
     }
+#ifdef REF_GPU_BUILD
+    // the reference checks no CUDA call: without a device it would run on garbage
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        std::fprintf(stderr, "ref_driver: no CUDA device\n");
+        return 3;
+    }
+#endif
     FILE* fi = std::fopen(argv[1], "rb");
     if (!fi) return 2;
     Reader rd{fi};
@@ -107,6 +127,11 @@ int main(int argc, char** argv) {
         Lm = rd.get<double>();
         Ln = rd.get<double>();
     }
+    int reps = 0, do_solve = 0;
+    if (mode == 7) {
+        reps = rd.get<int32_t>();
+        do_solve = rd.get<int32_t>();
+    }
     std::vector<double> pts;
     if (mode == 3) {
         int npts = rd.get<int32_t>();
@@ -133,6 +158,8 @@ int main(int argc, char** argv) {
 
     VectorXcd material(nmat);
     for (int i = 0; i < nmat; i++) material(i) = std::complex<double>(mat[2 * i], mat[2 * i + 1]);
+    using clk = std::chrono::steady_clock;
+    const auto t_ctor = clk::now();
     AProductCore Core = mode == 4 ? AProductCore(&CStr, lam, material, nback, MAXm, MAXn, Lm, Ln, "LDR")
                                   : AProductCore(&CStr, lam, material, nback, mode == 5 ? "FCD" : "LDR");
 
@@ -155,6 +182,39 @@ int main(int argc, char** argv) {
     }
 
     DDAModel Model(&Core, nK, E0, nE0, true);
+    if (mode == 7) {
+        const double ctor_s = std::chrono::duration<double>(clk::now() - t_ctor).count();
+        std::fwrite(&ctor_s, 8, 1, fo);
+        VectorXcd b = to_cvec(vecs, 0, 3 * N);
+        for (int k = 0; k < reps; k++) {
+            const auto t0 = clk::now();
+            VectorXcd y = Core.Aproduct(b);
+            const double s = std::chrono::duration<double>(clk::now() - t0).count();
+            std::fwrite(&s, 8, 1, fo);
+        }
+        int32_t it = 0;
+        double solve_s = 0;
+        if (do_solve) {  // the reference prints the final Error on stdout (DDAModel.cpp:236-255)
+            const auto t0 = clk::now();
+            Model.bicgstab(max_it, max_err);
+            solve_s = std::chrono::duration<double>(clk::now() - t0).count();
+            it = Model.get_ITERATION();
+        }
+        std::fwrite(&it, 4, 1, fo);
+        std::fwrite(&solve_s, 8, 1, fo);
+        std::fclose(fo);
+#ifdef REF_GPU_BUILD
+        const cudaError_t e = cudaDeviceSynchronize();
+        const cudaError_t e2 = cudaGetLastError();
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+            std::fprintf(stderr, "ref_driver: CUDA error %d / %d in the reference's calls\n", (int)e, (int)e2);
+            std::fflush(stdout);
+            std::_Exit(4);
+        }
+#endif
+        std::fflush(stdout);
+        std::_Exit(0);
+    }
     VectorXi* Rs = CStr.get_R();
     for (int i = 0; i < 3 * N; i++) {
         int32_t r = (*Rs)(i);

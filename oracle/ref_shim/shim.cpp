@@ -65,7 +65,13 @@ cufftResult cufftExecZ2Z(cufftHandle plan, cufftDoubleComplex* idata, cufftDoubl
     }
     size_t n = (size_t)p.n0 * p.n1 * p.n2;
     if (odata != idata) std::memmove(odata, idata, n * sizeof(cufftDoubleComplex));
+#ifdef SHIM_FAST_FFT
+    // timing build (oracle/_ref/ref_timer): Bluestein for the prime lengths of the 2N - 1 grid
+    if (oc_fft3d_fast(p.n0, p.n1, p.n2, reinterpret_cast<oc_cplx*>(odata), direction < 0 ? -1 : 1))
+        return CUFFT_ALLOC_FAILED;
+#else
     if (oc_fft3d(p.n0, p.n1, p.n2, reinterpret_cast<oc_cplx*>(odata), direction < 0 ? -1 : 1)) return CUFFT_ALLOC_FAILED;
+#endif
     return CUFFT_SUCCESS;
 }
 

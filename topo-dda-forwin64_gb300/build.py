@@ -26,7 +26,7 @@ UNITS = ["tdda_kernels.cu", "tdda_api.cu", "tdda_pass_generic.cu", "tdda_pass_z.
          "tdda_pass_zy.cu", "tdda_server.cu", "tdda_pass_xy2.cu", "tdda_pass_dd.cu", "tdda_pass_dd_128.cu", "tdda_pass_dd_192.cu",
          "tdda_pass_dd_160.cu", "tdda_pass_dd_40.cu"]
 HEADERS = ["tdda_fft.cuh", "tdda_fft_ct.cuh", "tdda_internal.cuh", "tdda_device.cuh", "tdda_passes.cuh",
-           "tdda_tensor.cuh"]
+           "tdda_tensor.cuh", "tdda_session.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
