@@ -94,6 +94,44 @@ template <int SIGN, typename T> __device__ __forceinline__ cx<T> cmul_i(cx<T> a)
 }
 template <typename T> __device__ __forceinline__ cx<T> czero() { return mk<T>(T(0), T(0)); }
 
+// Butterfly arithmetic.  For FP32 the real and imaginary parts of a complex
+// value are one 64-bit register pair, and sm_100-family GPUs add, subtract and
+// fused-multiply-add such pairs in one instruction (PTX add / sub / fma.rn.f32x2):
+// each is exactly two rn operations, so the results are those of the scalar
+// forms, at half the instruction count.  Other types use the scalar forms.
+__device__ __forceinline__ unsigned long long f2_pack(float2 a) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+    return r;
+}
+__device__ __forceinline__ float2 f2_unpack(unsigned long long r) {
+    float2 a;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+    return a;
+}
+template <typename T> __device__ __forceinline__ cx<T> badd(cx<T> a, cx<T> b) { return cadd<T>(a, b); }
+template <typename T> __device__ __forceinline__ cx<T> bsub(cx<T> a, cx<T> b) { return csub<T>(a, b); }
+// acc + c a for a real constant c
+template <typename T> __device__ __forceinline__ cx<T> bfma(cx<T> a, T c, cx<T> acc) {
+    return mk<T>(acc.x + c * a.x, acc.y + c * a.y);
+}
+template <> __device__ __forceinline__ float2 badd<float>(float2 a, float2 b) {
+    unsigned long long r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_pack(a)), "l"(f2_pack(b)));
+    return f2_unpack(r);
+}
+template <> __device__ __forceinline__ float2 bsub<float>(float2 a, float2 b) {
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_pack(a)), "l"(f2_pack(b)));
+    return f2_unpack(r);
+}
+template <> __device__ __forceinline__ float2 bfma<float>(float2 a, float c, float2 acc) {
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(f2_pack(a)), "l"(f2_pack(make_float2(c, c))),
+        "l"(f2_pack(acc)));
+    return f2_unpack(r);
+}
+
 // Up to 8 radix stages per axis (M <= 8^8 is far beyond any lattice here).
 constexpr int kMaxStages = 8;
 
@@ -126,21 +164,21 @@ template <int R, int SIGN, typename T> struct Bfly;
 template <int SIGN, typename T> struct Bfly<2, SIGN, T> {
     static __device__ __forceinline__ void run(cx<T>* v) {
         cx<T> a = v[0], b = v[1];
-        v[0] = cadd<T>(a, b);
-        v[1] = csub<T>(a, b);
+        v[0] = badd<T>(a, b);
+        v[1] = bsub<T>(a, b);
     }
 };
 
 template <int SIGN, typename T> struct Bfly<4, SIGN, T> {
     static __device__ __forceinline__ void run(cx<T>* v) {
-        cx<T> t0 = cadd<T>(v[0], v[2]);
-        cx<T> t1 = csub<T>(v[0], v[2]);
-        cx<T> t2 = cadd<T>(v[1], v[3]);
-        cx<T> t3 = cmul_i<SIGN, T>(csub<T>(v[1], v[3]));
-        v[0] = cadd<T>(t0, t2);
-        v[2] = csub<T>(t0, t2);
-        v[1] = cadd<T>(t1, t3);
-        v[3] = csub<T>(t1, t3);
+        cx<T> t0 = badd<T>(v[0], v[2]);
+        cx<T> t1 = bsub<T>(v[0], v[2]);
+        cx<T> t2 = badd<T>(v[1], v[3]);
+        cx<T> t3 = cmul_i<SIGN, T>(bsub<T>(v[1], v[3]));
+        v[0] = badd<T>(t0, t2);
+        v[2] = bsub<T>(t0, t2);
+        v[1] = badd<T>(t1, t3);
+        v[3] = bsub<T>(t1, t3);
     }
 };
 
@@ -162,10 +200,10 @@ template <int SIGN, typename T> struct BflyIn<4, SIGN, T, 2> {
     // v[0] + W^q v[1], W = exp(SIGN i pi / 2)
     static __device__ __forceinline__ void run(cx<T>* v) {
         const cx<T> a = v[0], b = v[1], wb = cmul_i<SIGN, T>(b);
-        v[0] = cadd<T>(a, b);
-        v[1] = cadd<T>(a, wb);
-        v[2] = csub<T>(a, b);
-        v[3] = csub<T>(a, wb);
+        v[0] = badd<T>(a, b);
+        v[1] = badd<T>(a, wb);
+        v[2] = bsub<T>(a, b);
+        v[3] = bsub<T>(a, wb);
     }
 };
 
@@ -183,14 +221,14 @@ template <int SIGN, typename T, int NIN4> struct Bfly8 {
         cx<T> o1 = mk<T>((o[1].x - T(SIGN) * o[1].y) * h, (o[1].y + T(SIGN) * o[1].x) * h);
         cx<T> o2 = cmul_i<SIGN, T>(o[2]);
         cx<T> o3 = mk<T>((-o[3].x - T(SIGN) * o[3].y) * h, (-o[3].y + T(SIGN) * o[3].x) * h);
-        v[0] = cadd<T>(e[0], o[0]);
-        v[4] = csub<T>(e[0], o[0]);
-        v[1] = cadd<T>(e[1], o1);
-        v[5] = csub<T>(e[1], o1);
-        v[2] = cadd<T>(e[2], o2);
-        v[6] = csub<T>(e[2], o2);
-        v[3] = cadd<T>(e[3], o3);
-        v[7] = csub<T>(e[3], o3);
+        v[0] = badd<T>(e[0], o[0]);
+        v[4] = bsub<T>(e[0], o[0]);
+        v[1] = badd<T>(e[1], o1);
+        v[5] = bsub<T>(e[1], o1);
+        v[2] = badd<T>(e[2], o2);
+        v[6] = bsub<T>(e[2], o2);
+        v[3] = badd<T>(e[3], o3);
+        v[7] = bsub<T>(e[3], o3);
     }
 };
 template <int SIGN, typename T> struct Bfly<8, SIGN, T> : Bfly8<SIGN, T, 4> {};
@@ -237,13 +275,13 @@ template <int R, int SIGN, typename T> struct BflyOdd {
         cx<T> sp[H], sm[H];
 #pragma unroll
         for (int r = 1; r <= H; r++) {
-            sp[r - 1] = cadd<T>(v[r], v[R - r]);
-            sm[r - 1] = csub<T>(v[r], v[R - r]);
+            sp[r - 1] = badd<T>(v[r], v[R - r]);
+            sm[r - 1] = bsub<T>(v[r], v[R - r]);
         }
         cx<T> out[R];
         cx<T> s0 = v[0];
 #pragma unroll
-        for (int r = 0; r < H; r++) s0 = cadd<T>(s0, sp[r]);
+        for (int r = 0; r < H; r++) s0 = badd<T>(s0, sp[r]);
         out[0] = s0;
 #pragma unroll
         for (int q = 1; q <= H; q++) {
@@ -253,12 +291,12 @@ template <int R, int SIGN, typename T> struct BflyOdd {
             for (int r = 1; r <= H; r++) {
                 const T c = T(OddConst<R>::c(r * q));
                 const T s = T(OddConst<R>::s(r * q));
-                re = mk<T>(re.x + c * sp[r - 1].x, re.y + c * sp[r - 1].y);
-                im = mk<T>(im.x + s * sm[r - 1].x, im.y + s * sm[r - 1].y);
+                re = bfma<T>(sp[r - 1], c, re);
+                im = bfma<T>(sm[r - 1], s, im);
             }
             cx<T> rot = cmul_i<SIGN, T>(im);  // SIGN i * im
-            out[q] = cadd<T>(re, rot);
-            out[R - q] = csub<T>(re, rot);
+            out[q] = badd<T>(re, rot);
+            out[R - q] = bsub<T>(re, rot);
         }
 #pragma unroll
         for (int q = 0; q < R; q++) v[q] = out[q];

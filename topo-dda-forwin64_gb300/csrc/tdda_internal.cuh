@@ -4,7 +4,8 @@
 // HBM layout of one core (one lattice at one wavelength):
 //   cellmap   int32 [Nx][Ny][Nz]          dipole index of each cell, -1 if empty
 //   green64   double2 [Hy][Hx][Hz][6]     folded Green spectrum / (Mx My Mz)
-//   green32   float2  [Hy][Hx][Hz][6]     the same rounded to FP32 (mixed path)
+//   green32   float2  [Hy][Hx][3][Hz][2]  the same rounded to FP32 (mixed path), as
+//                                         planes of component pairs (xx|xy, xz|yy, yz|zz)
 //   tw{x,y,z} double2/float2 [M]          exp(-2 pi i m / M)
 //   grid      cx<T> [nrhs][3][Nx][My][Mz]  FFT work grid (x kept to the lattice)
 // with H = M/2 + 1 per axis (the tensor components are even or odd in each

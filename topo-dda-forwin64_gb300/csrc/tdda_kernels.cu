@@ -319,7 +319,9 @@ __global__ void k_green_fold(Geom g, const double2* __restrict__ full6, double2*
         const double2 v = full6[l * M + ((long long)fx * My + fy) * Mz + fz];
         const double2 w = make_double2(v.x * inv, v.y * inv);
         green64[e] = w;
-        green32[e] = make_float2((float)w.x, (float)w.y);
+        // FP32: planes of component pairs, [fy][fx][l / 2][fz][l % 2]
+        green32[((((long long)fy * g.Hx + fx) * 3 + l / 2) * g.Hz + fz) * 2 + (l & 1)] =
+            make_float2((float)w.x, (float)w.y);
     }
 }
 

@@ -251,6 +251,25 @@ __device__ __forceinline__ void load_green6(const cx<T>* gg, cx<T>& a0, cx<T>& a
     }
 }
 
+// The six components at folded point (fy, fx, fz).  FP64 and double-float
+// tables hold the six contiguously ([Hy][Hx][Hz][6]).  The FP32 table holds
+// them as three planes of component pairs ([Hy][Hx][3][Hz] float4: xx|xy,
+// xz|yy, yz|zz), so the threads of a warp that walk z read whole 128-byte
+// lines with each 16-byte load instead of a third of three lines each.
+template <typename T>
+__device__ __forceinline__ void load_green(const cx<T>* green, const Geom& g, int fy, int fx, int fz, cx<T>& a0,
+                                           cx<T>& a1, cx<T>& a2, cx<T>& a3, cx<T>& a4, cx<T>& a5) {
+    if constexpr (sizeof(cx<T>) == 8) {
+        const float4* q = reinterpret_cast<const float4*>(green) + ((long long)fy * g.Hx + fx) * 3 * g.Hz + fz;
+        const float4 u = __ldg(q), v = __ldg(q + g.Hz), w = __ldg(q + 2 * g.Hz);
+        a0 = mk<T>(u.x, u.y); a1 = mk<T>(u.z, u.w);
+        a2 = mk<T>(v.x, v.y); a3 = mk<T>(v.z, v.w);
+        a4 = mk<T>(w.x, w.y); a5 = mk<T>(w.z, w.w);
+    } else {
+        load_green6<T>(green + (((long long)fy * g.Hx + fx) * g.Hz + fz) * 6, a0, a1, a2, a3, a4, a5);
+    }
+}
+
 template <typename T, int CM>
 __global__ void __launch_bounds__(kNT) k_xpass(Geom g, const RhsVecs<T>* __restrict__ rhs,
                                                const cx<T>* __restrict__ green, const cx<T>* __restrict__ twx,
@@ -293,9 +312,8 @@ __global__ void __launch_bounds__(kNT) k_xpass(Geom g, const RhsVecs<T>* __restr
         if (zl >= zn) continue;
         const int fx = fold(kx, Mx), fz = fold(z, Mz);
         const bool ux = 2 * kx > Mx, uz = 2 * z > Mz;
-        const cx<T>* gg = green + (((long long)fy * g.Hx + fx) * g.Hz + fz) * 6;
         cx<T> a0, a1, a2, a3, a4, a5;
-        load_green6<T>(gg, a0, a1, a2, a3, a4, a5);
+        load_green<T>(green, g, fy, fx, fz, a0, a1, a2, a3, a4, a5);
         if (ux != uy) a1 = mk<T>(-a1.x, -a1.y);  // xy: odd in x and y
         if (ux != uz) a2 = mk<T>(-a2.x, -a2.y);  // xz: odd in x and z
         if (uy != uz) a4 = mk<T>(-a4.x, -a4.y);  // yz: odd in y and z
@@ -336,10 +354,17 @@ __global__ void __launch_bounds__(ZT * x2_radix(M, 0), MINB) k_xpass2(Geom g, co
                                                                    cx<T>* __restrict__ grid) {
     constexpr int R1 = x2_radix(M, 0), R2 = x2_radix(M, 1);
     static_assert(R1 * R2 == M, "two-stage plan");
-    constexpr int NT = ZT * R1, W = 3 * ZT, WP = W + 1;
+    constexpr int NT = ZT * R1, W = 3 * ZT;
+    // Shared rows of W lines.  With 8 z-columns (W = 24) a half warp's 8-byte
+    // accesses span two rows, whose banks must differ by 8: the rows of the
+    // first exchange (stage 1 -> stage 2) shift by 8 entries every R1 rows,
+    // those of the second every R2 rows (R2 even), so that each of the four
+    // access patterns takes the minimum two wavefronts per warp.  With 16
+    // z-columns a half warp stays in one row and no shift is needed.
+    constexpr int SA = ZT == 8 ? 8 : 0, SB = (ZT == 8 && R2 % 2 == 0) ? 8 : 0;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<T>* stw = reinterpret_cast<cx<T>*>(smem_raw);
-    cx<T>* s = stw + M;  // [M][WP]
+    cx<T>* s = stw + M;  // M rows of W, plus the row shifts
     const int b = blockIdx.y;
     const SolveState* st = rhs[b].st;
     // a right-hand side of a cross-lattice batch brings its own box and spectrum
@@ -372,8 +397,9 @@ __global__ void __launch_bounds__(ZT * x2_radix(M, 0), MINB) k_xpass2(Geom g, co
             v[r] = (zl < zn && xx < Nx) ? src[(long long)xx * g.sx] : czero<T>();
         }
         BflyIn<R1, -1, T, RH>::run(v);
+        cx<T>* d = s + j * (R1 * W + SA) + l;  // row j R1 + q, shifted SA j
 #pragma unroll
-        for (int q = 0; q < R1; q++) s[(j * R1 + q) * WP + l] = v[q];
+        for (int q = 0; q < R1; q++) d[q * W] = v[q];
     }
     // a stopped solve is checked here, after the first loads are issued: nothing
     // has been written to global memory yet
@@ -387,7 +413,7 @@ __global__ void __launch_bounds__(ZT * x2_radix(M, 0), MINB) k_xpass2(Geom g, co
     for (int c = 0; c < 3; c++) {
 #pragma unroll
         for (int r = 0; r < R2; r++) {
-            cx<T> t = s[(j + R1 * r) * WP + c * ZT + zl];
+            cx<T> t = s[(j + R1 * r) * W + SA * r + c * ZT + zl];  // row j + R1 r
             if (r > 0) t = cmul<T>(t, stw[r * j]);
             X[c][r] = t;
         }
@@ -403,7 +429,7 @@ __global__ void __launch_bounds__(ZT * x2_radix(M, 0), MINB) k_xpass2(Geom g, co
             const int fx = fold(kx, M);
             const bool ux = 2 * kx > M;
             cx<T> a0, a1, a2, a3, a4, a5;
-            load_green6<T>(green + (((long long)fy * g.Hx + fx) * g.Hz + fz) * 6, a0, a1, a2, a3, a4, a5);
+            load_green<T>(green, g, fy, fx, fz, a0, a1, a2, a3, a4, a5);
             if (ux != uy) a1 = mk<T>(-a1.x, -a1.y);  // xy: odd in x and y
             if (ux != uz) a2 = mk<T>(-a2.x, -a2.y);  // xz: odd in x and z
             if (uy != uz) a4 = mk<T>(-a4.x, -a4.y);  // yz: odd in y and z
@@ -419,7 +445,7 @@ __global__ void __launch_bounds__(ZT * x2_radix(M, 0), MINB) k_xpass2(Geom g, co
 #pragma unroll
     for (int c = 0; c < 3; c++)
 #pragma unroll
-        for (int q = 0; q < R2; q++) s[(j * R2 + q) * WP + c * ZT + zl] = X[c][q];
+        for (int q = 0; q < R2; q++) s[(j * R2 + q) * W + SB * j + c * ZT + zl] = X[c][q];  // row j R2 + q
     __syncthreads();
 
     // inverse stage 2: radix R1, butterfly j < R2, twiddles conj(w^(r j)), outputs x = j + R2 q < Nx
@@ -429,7 +455,7 @@ __global__ void __launch_bounds__(ZT * x2_radix(M, 0), MINB) k_xpass2(Geom g, co
         cx<T> v[R1];
 #pragma unroll
         for (int r = 0; r < R1; r++) {
-            cx<T> t = s[(jj + R2 * r) * WP + l];
+            cx<T> t = s[(jj + R2 * r) * W + SB * r + l];  // row jj + R2 r
             if (r > 0) {
                 cx<T> tw = stw[r * jj];
                 tw.y = -tw.y;
@@ -449,7 +475,10 @@ __global__ void __launch_bounds__(ZT * x2_radix(M, 0), MINB) k_xpass2(Geom g, co
 
 template <typename T, int M, int ZT, int MINB = 1> struct XLaunch2 {
     static constexpr int NT = ZT * x2_radix(M, 0);
-    static constexpr size_t smem = sizeof(cx<T>) * (size_t)(M + M * (3 * ZT + 1));
+    // twiddles, M rows of 3 ZT lines, the row shifts (at most 8 max(R1, R2))
+    static constexpr size_t smem =
+        sizeof(cx<T>) * (size_t)(M + M * 3 * ZT + 8 * (x2_radix(M, 0) > x2_radix(M, 1) ? x2_radix(M, 0)
+                                                                                         : x2_radix(M, 1)));
     static cudaError_t run(const PassArgs<T>& a) {
         const Geom& g = a.g;
         const dim3 grid(g.py.M * ((g.pz.M + ZT - 1) / ZT), a.nrhs);
