@@ -389,6 +389,8 @@ def time_batch(tdda, torch, w, incs, precision, steps, dev, flush_l2, keep_P=Fal
     (keep_P: the result's polarisations in out["P"])."""
     core = tdda.AProductCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material, w.nback, max_rhs=len(incs), device=dev)
     tune = core.autotune(nrhs=len(incs), reps=10) if precision == tdda.FP32_REFINE else None
+    # the batch schedule (right-hand sides per launch), timed on this core's FP32 products
+    btune = core.autotune_batch(nrhs=len(incs), reps=5) if precision == tdda.FP32_REFINE else None
     models = [tdda.DDAModel(core, inc.nK, inc.E0, inc.nE0, w.diel_old) for inc in incs]
     stream = torch.cuda.ExternalStream(core.stream(), device=dev)
     zero = pinned_c128(3 * w.N)
@@ -418,6 +420,8 @@ def time_batch(tdda, torch, w, incs, precision, steps, dev, flush_l2, keep_P=Fal
            "pass_ms": prof, "kernels": pass_names(core, precision), "grid": list(core.grid)}
     if tune:
         out["x_pass_autotune"] = tune
+    if btune:
+        out["batch_schedule_autotune"] = btune
     if keep_P:
         out["P"] = [m.get_P() for m in models]
     for m in models:

@@ -357,6 +357,26 @@ typedef struct {
  * every candidate form and tile, and sets the fastest on the core. */
 tdda_status tdda_core_autotune(tdda_core* core, int nrhs, int reps, tdda_xpass_tune* out);
 
+/* Batch schedule of the FP32 products of a batched solve (no counterpart in the
+ * reference, which solves one right-hand side at a time): `group` right-hand
+ * sides per launch, 0 for the whole batch in one launch per pass.  With groups,
+ * each group runs through all of its passes before the next one starts, so the
+ * FFT work grid of a group that fits in L2 stays there between the passes.
+ * Results do not change (every right-hand side is computed independently).
+ * Captured FP32 solve steps of the core are dropped and captured again on next
+ * use; the call waits for the core's stream first.  0 <= group <= max_rhs. */
+tdda_status tdda_core_set_batch_group(tdda_core* core, int group);
+typedef struct {
+    int group;           /* the chosen right-hand sides per launch (0: all; now set on the core) */
+    int ncand;           /* candidates timed: 0, nrhs / 2, nrhs / 4, ... (at most 4) */
+    int groups[4];
+    double ms[4];        /* average ms of one FP32 A-product of nrhs right-hand sides, per candidate */
+} tdda_batch_tune;
+/* Autotuner of the batch schedule: times `reps` plain FP32 A-products of nrhs
+ * right-hand sides (CUDA events, after one warm-up) for each candidate group
+ * size and sets the fastest on the core. */
+tdda_status tdda_core_autotune_batch(tdda_core* core, int nrhs, int reps, tdda_batch_tune* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -50,6 +50,9 @@ def test_xpass_tuning_rejects_bad_arguments_before_touching_a_device():
     assert L.tdda_core_set_xpass(None, 0, 0) == tdda.ERR_INVALID_ARGUMENT
     assert L.tdda_core_autotune(None, 1, 1, ctypes.byref(t)) == tdda.ERR_INVALID_ARGUMENT
     assert b"invalid" in L.tdda_last_error()
+    bt = tdda.BatchTune()
+    assert L.tdda_core_set_batch_group(None, 0) == tdda.ERR_INVALID_ARGUMENT
+    assert L.tdda_core_autotune_batch(None, 2, 1, ctypes.byref(bt)) == tdda.ERR_INVALID_ARGUMENT
 
 
 def test_fcd_needs_the_spacing_inside_the_sici_tables():

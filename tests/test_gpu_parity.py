@@ -170,6 +170,38 @@ def test_xpass_tile_and_form_and_the_autotuner():
     assert [(k["form"], k["tile"]) for k in t2["candidates"]] == [(1, 0)] and t2["x_form"] == 1
 
 
+def test_batch_schedule_groups_and_its_autotuner():
+    """Right-hand sides per launch (the batch schedule) change no result: a batched FP32+refine
+    solve of 6 incidences run as one launch per pass, as groups of 4 (with a ragged last group)
+    and of 1 gives bit-identical P and iteration counts; the tuner keeps its fastest candidate."""
+    w = tdda.lattice.config(1)
+    incs = tdda.lattice.config(3).incidences[:6]
+    c = tdda.AProductCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material, w.nback, max_rhs=6)
+    ms = [tdda.DDAModel(c, i.nK, i.E0, i.nE0, w.diel_old) for i in incs]
+    zero = np.zeros(3 * w.N, np.complex128)
+    out = {}
+    for group in (0, 4, 1):
+        c.set_batch_group(group)
+        for m in ms:
+            m.InitializeP(zero)
+        infos = tdda.solve_batch(ms, tdda.FP32_REFINE, 10000, 1e-5)
+        assert all(i["status"] == tdda.OK and i["true_residual"] <= 1e-5 for i in infos)
+        out[group] = ([m.get_P() for m in ms], [i["inner_iterations"] for i in infos])
+    for group in (4, 1):
+        assert out[group][1] == out[0][1]
+        for a, b in zip(out[group][0], out[0][0]):
+            assert np.array_equal(a, b)
+    t = c.autotune_batch(nrhs=6, reps=2)
+    assert [k["group"] for k in t["candidates"]] == [0, 3, 1]
+    assert all(k["ms"] > 0 for k in t["candidates"])
+    assert t["group"] == min(t["candidates"], key=lambda k: k["ms"])["group"]
+    with pytest.raises(tdda.TddaError):
+        c.set_batch_group(7)
+    for m in ms:
+        m.close()
+    c.close()
+
+
 def _model(g, core):
     m = tdda.DDAModel(core, g["nK"], float(g["E0"]), g["nE0"], g["diel_old"])
     if "P0" in g:

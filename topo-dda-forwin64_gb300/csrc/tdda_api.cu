@@ -181,6 +181,10 @@ struct tdda_core_s {
     // environment makes the host launch each chunk instead (profilers see the kernels of a
     // host-launched graph, not those of a device-side loop's body)
     bool device_loop = true;
+    // batch schedule of the FP32 products: right-hand sides per launch (0: all of a
+    // batch in one launch per pass).  Groups run one after another, each through all
+    // of its passes, so a group's FFT work grid can stay in L2 between the passes.
+    int group = 0;
     dd2* green_dd = nullptr;            // double-float copies for the residual product (on first use)
     dd2* tw_dd[3] = {nullptr, nullptr, nullptr};
     float2* green32 = nullptr;
@@ -430,12 +434,31 @@ template <> struct Prec<float> {
 // kernels of one A-product at precision T: 3 with the fused z+y passes, else 5
 template <typename T> int product_kernels(const tdda_core* c) { return tdda::zy_fused(c->g, sizeof(T) == 4) ? 3 : 5; }
 
+// right-hand sides per launch of a batch of n: the core's FP32 batch schedule
+template <typename T> int group_size(const tdda_core* c, int n) {
+    return (sizeof(T) == 4 && c->group > 0 && c->group < n) ? c->group : n;
+}
+template <typename T> int group_count(const tdda_core* c, int n) {
+    const int gs = group_size<T>(c, n);
+    return (n + gs - 1) / gs;
+}
+
+// One A-product of n right-hand sides: one launch per pass, or, with an FP32
+// batch schedule of groups, each group through all of its passes in turn (the
+// group's right-hand sides use the first slices of the work grid).  ev (the
+// six pass events) is recorded for an ungrouped product only.
 template <typename T>
 cudaError_t aprod(tdda_core* c, int src, int snk, int n, const RhsVecs<T>* rhs, cudaEvent_t* ev = nullptr,
                   int slot = 0) {
-    count_launches(product_kernels<T>(c));
-    return tdda::launch_aproduct<T>(c->g, src, snk, n, rhs, Prec<T>::green(c), Prec<T>::tw(c, 0), Prec<T>::tw(c, 1),
-                                    Prec<T>::tw(c, 2), c->cellmap, Prec<T>::grid(c), c->stream, ev, slot);
+    const int gs = group_size<T>(c, n);
+    for (int g0 = 0; g0 < n; g0 += gs) {
+        count_launches(product_kernels<T>(c));
+        const cudaError_t e = tdda::launch_aproduct<T>(
+            c->g, src, snk, std::min(gs, n - g0), rhs + g0, Prec<T>::green(c), Prec<T>::tw(c, 0), Prec<T>::tw(c, 1),
+            Prec<T>::tw(c, 2), c->cellmap, Prec<T>::grid(c), c->stream, gs == n ? ev : nullptr, slot);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 // One BiCGSTAB step.  FP64 (the drop-in): the reference's recurrence with its
@@ -448,7 +471,9 @@ cudaError_t aprod(tdda_core* c, int src, int snk, int n, const RhsVecs<T>* rhs, 
 // them in the state slots of the step's parity `slot`.
 template <typename T> constexpr bool kDeferred = sizeof(T) == 4;
 
-template <typename T> int step_kernels(const tdda_core* c) { return 2 * product_kernels<T>(c) + (kDeferred<T> ? 0 : 1); }
+template <typename T> int step_kernels(const tdda_core* c, int n) {
+    return 2 * product_kernels<T>(c) * group_count<T>(c, n) + (kDeferred<T> ? 0 : 1);
+}
 
 template <typename T> cudaError_t enqueue_iteration(tdda_core* c, int n, int slot) {
     const RhsVecs<T>* rhs = Prec<T>::rhs(c);
@@ -476,7 +501,9 @@ cudaError_t enqueue_chunk(tdda_core* c, int n, cudaGraphConditionalHandle loop, 
     if constexpr (kDeferred<T>) return tdda::launch_chunk_end(c->g, n, Prec<T>::rhs(c), 0, loop, in_loop, c->stream);
     return cudaSuccess;
 }
-template <typename T> int chunk_kernels(const tdda_core* c) { return kChunk * step_kernels<T>(c) + (kDeferred<T> ? 1 : 0); }
+template <typename T> int chunk_kernels(const tdda_core* c, int n) {
+    return kChunk * step_kernels<T>(c, n) + (kDeferred<T> ? 1 : 0);
+}
 
 // The graph of the steps.  FP64: one chunk, launched by the host until the
 // states it reads stop.  FP32: a conditional WHILE node whose body is one
@@ -582,7 +609,7 @@ template <typename T> tdda_status krylov(tdda_core* c, int n, bool p_zero, int m
             for (int i = 0; i < n; i++) running |= c->hst[i].status == tdda::ST_RUNNING;
             if (!running || c->hst[0].chunks >= c->hst[0].chunk_limit) break;
         }
-        count_launches(c->hst[0].chunks * chunk_kernels<T>(c));
+        count_launches(c->hst[0].chunks * chunk_kernels<T>(c, n));
         TDDA_CK1(tdda::launch_finish<T>(c->g, n, rhs, c->stream));  // the last step's update
         return TDDA_OK;
     }
@@ -593,7 +620,7 @@ template <typename T> tdda_status krylov(tdda_core* c, int n, bool p_zero, int m
         bool running = false;
         for (int i = 0; i < n; i++) running |= c->hst[i].status == tdda::ST_RUNNING;
         if (!running || done_it > max_it) break;
-        count_launches(chunk_kernels<T>(c));
+        count_launches(chunk_kernels<T>(c, n));
         TDDA_CK(cudaGraphLaunch(ex, c->stream));
         done_it += kChunk;
     }
@@ -1241,7 +1268,7 @@ tdda_status shape_step(Shape* s, std::vector<Done>* done) {
     TDDA_CK(cudaGraphLaunch(ex, c->stream));
     TDDA_CK(cudaMemcpyAsync(c->hst, c->st32, sizeof(SolveState) * width, cudaMemcpyDeviceToHost, c->stream));
     TDDA_CK(cudaStreamSynchronize(c->stream));
-    count_launches(std::max(1, c->hst[0].chunks) * chunk_kernels<float>(c));
+    count_launches(std::max(1, c->hst[0].chunks) * chunk_kernels<float>(c, width));
     // 4. inner solves that stopped: the pending update, then P += the correction
     std::vector<int> stopped;
     for (int k = 0; k < width; k++)
@@ -2128,18 +2155,31 @@ tdda_status profile_products(tdda_core* c, int precision, int nrhs, int reps, do
     for (auto& e : ev) TDDA_CK(cudaEventCreate(&e));
     double acc[5] = {0, 0, 0, 0, 0};
     tdda_status st = TDDA_OK;
+    // an FP32 batch schedule of groups: each group's passes are timed and the
+    // groups' times of a pass added
+    const int gs = precision == TDDA_FP64 ? nrhs : group_size<float>(c, nrhs);
     for (int r = 0; r < reps + 1 && st == TDDA_OK; r++) {  // the first run is a warm-up
-        cudaError_t e = precision == TDDA_FP64 ? aprod<double>(c, tdda::SRC_IN, tdda::SNK_OUT, nrhs, c->rhs64, ev)
-                                               : aprod<float>(c, tdda::SRC_IN, tdda::SNK_OUT, nrhs, c->rhs32, ev);
-        if (e == cudaSuccess) e = cudaEventSynchronize(ev[5]);
-        if (e != cudaSuccess) {
-            st = cuda_fail(e, "profiled A-product");
-            break;
-        }
-        for (int k = 0; k < 5 && r > 0; k++) {
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
-            acc[k] += ms;
+        for (int g0 = 0; g0 < nrhs && st == TDDA_OK; g0 += gs) {
+            const int n = std::min(gs, nrhs - g0);
+            count_launches(precision == TDDA_FP64 ? product_kernels<double>(c) : product_kernels<float>(c));
+            cudaError_t e =
+                precision == TDDA_FP64
+                    ? tdda::launch_aproduct<double>(c->g, tdda::SRC_IN, tdda::SNK_OUT, n, c->rhs64 + g0, c->green64,
+                                                    c->tw64[0], c->tw64[1], c->tw64[2], c->cellmap, c->grid64,
+                                                    c->stream, ev, 0)
+                    : tdda::launch_aproduct<float>(c->g, tdda::SRC_IN, tdda::SNK_OUT, n, c->rhs32 + g0, c->green32,
+                                                   c->tw32[0], c->tw32[1], c->tw32[2], c->cellmap, c->grid32,
+                                                   c->stream, ev, 0);
+            if (e == cudaSuccess) e = cudaEventSynchronize(ev[5]);
+            if (e != cudaSuccess) {
+                st = cuda_fail(e, "profiled A-product");
+                break;
+            }
+            for (int k = 0; k < 5 && r > 0; k++) {
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+                acc[k] += ms;
+            }
         }
     }
     for (auto& e : ev) cudaEventDestroy(e);
@@ -2156,6 +2196,16 @@ tdda_status set_xpass(tdda_core* c, int form, int tile) {
         if (e) cudaGraphExecDestroy(e), e = nullptr;
     c->g.x_form = form;
     c->g.x_tile = tile;
+    return TDDA_OK;
+}
+
+// The batch schedule is part of the captured FP32 steps: a new one drops them.
+tdda_status set_batch_group(tdda_core* c, int group) {
+    if (c->group == group) return TDDA_OK;
+    TDDA_CK(cudaStreamSynchronize(c->stream));
+    for (auto& e : c->g32.iter)
+        if (e) cudaGraphExecDestroy(e), e = nullptr;
+    c->group = group;
     return TDDA_OK;
 }
 }  // namespace
@@ -2211,6 +2261,45 @@ tdda_status tdda_core_autotune(tdda_core* c, int nrhs, int reps, tdda_xpass_tune
     out->x_form = out->form[best];
     out->x_tile = out->tile[best];
     return set_xpass(c, out->x_form, out->x_tile);
+}
+
+tdda_status tdda_core_set_batch_group(tdda_core* c, int group) {
+    if (!c || group < 0 || group > c->max_rhs) {
+        set_err("invalid argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    TDDA_TRY(set_device(c->device));
+    return set_batch_group(c, group);
+}
+
+tdda_status tdda_core_autotune_batch(tdda_core* c, int nrhs, int reps, tdda_batch_tune* out) {
+    if (!c || !out || reps < 1 || nrhs < 1 || nrhs > c->max_rhs) {
+        set_err("invalid argument");
+        return TDDA_ERR_INVALID_ARGUMENT;
+    }
+    TDDA_TRY(set_device(c->device));
+    *out = tdda_batch_tune{};
+    // candidates: the whole batch in one launch per pass (0), then halves of it
+    int nc = 0;
+    out->groups[nc++] = 0;
+    for (int g = nrhs / 2; g >= 1 && nc < 4; g /= 2)
+        if (g < nrhs) out->groups[nc++] = g;
+    out->ncand = nc;
+    const int group0 = c->group;
+    int best = -1;
+    for (int k = 0; k < nc; k++) {
+        double ms5[5];
+        tdda_status st = set_batch_group(c, out->groups[k]);
+        if (st == TDDA_OK) st = profile_products(c, TDDA_FP32_REFINE, nrhs, reps, ms5);
+        if (st != TDDA_OK) {
+            set_batch_group(c, group0);
+            return st;
+        }
+        out->ms[k] = ms5[0] + ms5[1] + ms5[2] + ms5[3] + ms5[4];
+        if (best < 0 || out->ms[k] < out->ms[best]) best = k;
+    }
+    out->group = out->groups[best];
+    return set_batch_group(c, out->group);
 }
 
 tdda_status tdda_aproduct_noalloc(tdda_core* c, const double* b, double* y) {

@@ -48,7 +48,7 @@ EXPORTS = [
     "tdda_solve_batch", "tdda_solve_multi",
     "tdda_fft3d", "tdda_core_stream", "tdda_kernel_launches", "tdda_profile_aproduct", "tdda_core_pass_count",
     "tdda_core_pass_name", "tdda_core_set_xpass", "tdda_core_autotune",
-    "tdda_aproduct_noalloc", "tdda_server_create", "tdda_server_submit", "tdda_server_result",
+    "tdda_core_set_batch_group", "tdda_core_autotune_batch", "tdda_aproduct_noalloc", "tdda_server_create", "tdda_server_submit", "tdda_server_result",
     "tdda_server_stats", "tdda_server_counters_get", "tdda_server_clock", "tdda_server_destroy",
     "tdda_request_bytes",
 ]
@@ -72,6 +72,11 @@ class CoreDesc(ctypes.Structure):
 class XpassTune(ctypes.Structure):
     _fields_ = [("x_form", ctypes.c_int), ("x_tile", ctypes.c_int), ("ncand", ctypes.c_int),
                 ("form", ctypes.c_int * 4), ("tile", ctypes.c_int * 4), ("ms", ctypes.c_double * 4)]
+
+
+class BatchTune(ctypes.Structure):
+    _fields_ = [("group", ctypes.c_int), ("ncand", ctypes.c_int), ("groups", ctypes.c_int * 4),
+                ("ms", ctypes.c_double * 4)]
 
 
 class SolveInfo(ctypes.Structure):
@@ -164,6 +169,8 @@ def load() -> ctypes.CDLL:
         "tdda_core_pass_name": (ctypes.c_char_p, [vp, i, i]),
         "tdda_core_set_xpass": (i, [vp, i, i]),
         "tdda_core_autotune": (i, [vp, i, i, ctypes.POINTER(XpassTune)]),
+        "tdda_core_set_batch_group": (i, [vp, i]),
+        "tdda_core_autotune_batch": (i, [vp, i, i, ctypes.POINTER(BatchTune)]),
         "tdda_aproduct_noalloc": (i, [vp, vp, vp]),
         "tdda_server_create": (i, [ctypes.POINTER(ServerDesc), ctypes.POINTER(vp)]),
         "tdda_server_submit": (i, [vp, ctypes.POINTER(RequestDesc), ctypes.POINTER(ctypes.c_ulonglong)]),
@@ -305,6 +312,17 @@ class AProductCore:
         _check(load().tdda_core_autotune(self.h, int(nrhs), int(reps), ctypes.byref(t)), "tdda_core_autotune")
         return {"x_form": t.x_form, "x_tile": t.x_tile,
                 "candidates": [{"form": t.form[k], "tile": t.tile[k], "ms": t.ms[k]} for k in range(t.ncand)]}
+
+    def set_batch_group(self, group: int) -> None:
+        """Right-hand sides per launch of the FP32 products of batched solves (0: all)."""
+        _check(load().tdda_core_set_batch_group(self.h, int(group)), "tdda_core_set_batch_group")
+
+    def autotune_batch(self, nrhs: int, reps: int = 5) -> dict:
+        """Time the batch-schedule candidates on this core's FP32 A-product and keep the fastest."""
+        t = BatchTune()
+        _check(load().tdda_core_autotune_batch(self.h, int(nrhs), int(reps), ctypes.byref(t)),
+               "tdda_core_autotune_batch")
+        return {"group": t.group, "candidates": [{"group": t.groups[k], "ms": t.ms[k]} for k in range(t.ncand)]}
 
     def profile_aproduct(self, precision: int = FP32_REFINE, nrhs: int = 1, reps: int = 10) -> list:
         """Average ms of the five passes of one A-product (CUDA events on the core stream)."""
