@@ -729,10 +729,27 @@ def run_ours(args, dist: Dist):
 
     cpu = None
     if dist.rank == 0:
-        base = CpuBaseline(w, args.cpu_threads or (os.cpu_count() or 1))
-        base.sample(1)  # warm-up
-        cpu = base.sample(0)
-        cpu.pop("sample_wall_s", None)
+        threads = args.cpu_threads or (os.cpu_count() or 1)
+        import ref_timing as RT
+        if RT.available(RT.TIMER) and not args.cpu_port:
+            # the reference's own code (its sources with the CPU stand-ins for cuFFT): one full
+            # converged solve per process, one process per core
+            t0 = time.perf_counter()
+            rs = RT.run_many(RT.TIMER, w, inc, MAX_IT, TOL, 0, True, threads)
+            wall = time.perf_counter() - t0
+            solve_s = statistics.median(r["solve_s"] for r in rs)
+            cpu = {"value": threads / solve_s, "unit": UNIT, "cores": threads, "kind": "reference",
+                   "cpu_model": cpu_model(), "iterations": rs[0]["iterations"],
+                   "sample": (f"{threads} processes, one per core, of the reference's own AProductCore/DDAModel "
+                              f"sources (oracle/_ref/ref_timer: CPU stand-ins for cuFFT, Bluestein on its "
+                              f"{2 * w.Nx - 1}x{2 * w.Ny - 1}x{2 * w.Nz - 1} grid): one full FP64 BiCGSTAB solve "
+                              f"each to tol {TOL:g} ({rs[0]['iterations']} iterations, median {solve_s:.1f} s, "
+                              f"{wall:.1f} s wall)")}
+        else:
+            base = CpuBaseline(w, threads)
+            base.sample(1)  # warm-up
+            cpu = base.sample(0)
+            cpu.pop("sample_wall_s", None)
     clocks = ck.summary()
     if dist.rank == 0:
         line = {
@@ -813,9 +830,11 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=5)
     ap.add_argument("--cpu-iters", type=int, default=4)
     ap.add_argument("--cpu-threads", type=int, default=0)
+    ap.add_argument("--cpu-port", action="store_true",
+                    help="time the oracle port for cpu_baseline even where the reference's own code was built")
     ap.add_argument("--batched-steps", type=int, default=3)
     ap.add_argument("--no-batched", action="store_true")
-    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-requests", type=int, default=64)
     ap.add_argument("--serve-workers", type=int, default=4)
     ap.add_argument("--serve-fp64-requests", type=int, default=0,
                     help="replay only the first n requests with plain FP64 (0: all of them)")
