@@ -835,7 +835,7 @@ def main():
     ap.add_argument("--batched-steps", type=int, default=3)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=64)
-    ap.add_argument("--serve-workers", type=int, default=4)
+    ap.add_argument("--serve-workers", type=int, default=8)
     ap.add_argument("--serve-fp64-requests", type=int, default=0,
                     help="replay only the first n requests with plain FP64 (0: all of them)")
     ap.add_argument("--topo-iters", type=int, default=200)

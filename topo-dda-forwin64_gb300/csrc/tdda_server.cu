@@ -472,6 +472,7 @@ void tdda_server_s::run_fp32(int me) {
         if (!sh) st = tdda_session::shape_create(desc.device, grid, desc.max_group, &sh);
         // request of each slot's model, and its right-hand side index
         std::vector<std::pair<Request*, int>> slot_of(desc.max_group, {nullptr, 0});
+        std::vector<tdda_model*> slot_model(desc.max_group, nullptr);
         auto fail_request = [&](Request* r, tdda_status s2) {
             std::lock_guard<std::mutex> lk(mu);
             r->info.status = s2;
@@ -486,7 +487,7 @@ void tdda_server_s::run_fp32(int me) {
             for (size_t k = 0; k < ms.size() && s2 == TDDA_OK; k++) {
                 int slot = -1;
                 s2 = tdda_session::shape_admit(sh, ms[k], desc.max_it, desc.tol, &slot);
-                if (s2 == TDDA_OK) slot_of[slot] = {r, (int)k}, used++;
+                if (s2 == TDDA_OK) slot_of[slot] = {r, (int)k}, slot_model[slot] = ms[k], used++;
             }
             if (s2 != TDDA_OK) {
                 {
@@ -552,9 +553,20 @@ void tdda_server_s::run_fp32(int me) {
             std::vector<tdda_session::Done> done;
             st = tdda_session::shape_step(sh, &done);
             if (st != TDDA_OK) {
-                // a device error: fail every request holding a slot, drop the shape
+                // a device error: fail every request holding a slot, free the slots'
+                // models (their state is unknown) and drop the shape
                 std::lock_guard<std::mutex> lk(mu);
                 const double t = now();
+                for (size_t k = 0; k < slot_of.size(); k++) {  // the models first: finishing clears r->op
+                    Request* r = slot_of[k].first;
+                    if (!r || !slot_model[k]) continue;
+                    tdda_model_destroy(slot_model[k]);
+                    slot_model[k] = nullptr;
+                    if (r->op) {
+                        r->op->nmodels--;
+                        bytes -= r->op->model_bytes;
+                    }
+                }
                 for (auto& so : slot_of) {
                     Request* r = so.first;
                     if (!r || r->info.state != TDDA_REQ_RUNNING) continue;
@@ -568,6 +580,7 @@ void tdda_server_s::run_fp32(int me) {
                 Request* r = slot_of[dn.slot].first;
                 const int k = slot_of[dn.slot].second;
                 slot_of[dn.slot] = {nullptr, 0};
+                slot_model[dn.slot] = nullptr;
                 const size_t n6 = 6 * (size_t)r->d.N;
                 tdda_status gs = tdda_model_get(dn.model, TDDA_FIELD_P, r->P.data() + k * n6, TDDA_MEM_HOST);
                 const tdda_status ss = gs != TDDA_OK ? gs : (tdda_status)dn.info.status;
