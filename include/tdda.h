@@ -42,10 +42,17 @@ typedef enum tdda_method { TDDA_METHOD_LDR = 0, TDDA_METHOD_FCD = 1 } tdda_metho
 typedef enum tdda_memory { TDDA_MEM_HOST = 0, TDDA_MEM_DEVICE = 1 } tdda_memory;
 typedef enum tdda_precision {
     TDDA_FP64 = 0,       /* complex128 FFT convolution and Krylov vectors */
-    TDDA_FP32_REFINE = 1 /* complex64 FFT and Krylov vectors, double-float dot sums, and an
+    TDDA_FP32_REFINE = 1, /* complex64 FFT and Krylov vectors, double-float dot sums, and an
                             outer residual of the FP64 vectors (double-float product, ~44 bits,
                             on the compiled grids; FP64 product elsewhere) with iterative
                             refinement */
+    TDDA_FP32_JACOBI = 2  /* TDDA_FP32_REFINE whose inner BiCGSTAB is right-preconditioned by
+                            the diagonal al (Jacobi): it solves (A D^-1) y = r with D = diag(al)
+                            and corrects P by D^-1 y.  The outer FP64 residual check is the same,
+                            so results meet the same tolerance; the inner iterates differ from
+                            the reference's recurrence.  No counterpart in the reference.  For
+                            the solves (tdda_solve_batch, tdda_solve_multi_precision, the server),
+                            not for single products */
 } tdda_precision;
 typedef enum tdda_field {
     TDDA_FIELD_P = 0,
@@ -194,6 +201,10 @@ tdda_status tdda_solve_batch(tdda_model* const* models, int n, int precision, in
  * model's tdda_model_solve_mixed alone.  1 <= n <= 64; infos may be NULL. */
 tdda_status tdda_solve_multi(tdda_model* const* models, int n, int max_it, double max_err,
                              tdda_solve_info* infos);
+/* tdda_solve_multi with the inner solves' precision: TDDA_FP32_REFINE (the same
+ * as tdda_solve_multi) or TDDA_FP32_JACOBI. */
+tdda_status tdda_solve_multi_precision(tdda_model* const* models, int n, int precision, int max_it,
+                                       double max_err, tdda_solve_info* infos);
 
 /* serving loop: continuous batching of solve requests ------------------- */
 /* Requests queue in arrival order; workers run concurrently on their own CUDA
@@ -220,7 +231,7 @@ typedef struct tdda_server_desc {
     int device;
     double hbm_budget_bytes;  /* device memory the requests in flight may hold */
     int workers;              /* requests solved concurrently (one stream each) */
-    int precision;            /* TDDA_FP64 or TDDA_FP32_REFINE */
+    int precision;            /* TDDA_FP64, TDDA_FP32_REFINE or TDDA_FP32_JACOBI */
     int max_it;
     double tol;
     int max_group;            /* right-hand sides of one batched solve, or the slots of one

@@ -181,6 +181,7 @@ struct tdda_core_s {
     // environment makes the host launch each chunk instead (profilers see the kernels of a
     // host-launched graph, not those of a device-side loop's body)
     bool device_loop = true;
+    float2* ones32 = nullptr;  // 3N entries of 1 (the sinks' diagonal of a Jacobi-preconditioned solve)
     // batch schedule of the FP32 products: right-hand sides per launch (0: all of a
     // batch in one launch per pass).  Groups run one after another, each through all
     // of its passes, so a group's FFT work grid can stay in L2 between the passes.
@@ -222,6 +223,10 @@ struct tdda_model_s {
     // FP32 Krylov vectors of the mixed solve (allocated on first use)
     float2 *fP = nullptr, *fE = nullptr, *fal = nullptr, *fr = nullptr, *fr0 = nullptr, *fp = nullptr, *fu = nullptr,
            *ft = nullptr, *fAp = nullptr, *fAt = nullptr;
+    // Jacobi right preconditioning of the FP32 inner solve (TDDA_FP32_JACOBI):
+    // whether the model's current solve uses it, and 1 / al as FP32 SoA
+    bool jacobi = false;
+    float2* fpre = nullptr;
     std::vector<void*> allocs;
     bool P_zero = true;
     int ITERATION = 0;
@@ -335,6 +340,10 @@ RhsVecs<float> vecs32(tdda_core* c, tdda_model* m, int slot) {
     RhsVecs<float> v{};
     v.P = m->fP; v.E = m->fE; v.r = m->fr; v.r0 = m->fr0; v.p = m->fp; v.u = m->fu; v.t = m->ft;
     v.Ap = m->fAp; v.At = m->fAt; v.al = m->fal;
+    if (m->jacobi) {  // products A D^-1 v: the gathers scale by 1 / al, the sinks add 1 v
+        v.pre = m->fpre;
+        v.al = m->core->ones32;
+    }
     v.st = c->st32 + slot;
     v.part = c->part + (size_t)slot * tdda::kPartSlots * c->maxblk;
     v.cnt = c->cnt + (size_t)slot * tdda::kCounters;
@@ -410,6 +419,29 @@ tdda_status model_alloc_f32(tdda_model* m) {
     float2** v[] = {&m->fP, &m->fE, &m->fal, &m->fr, &m->fr0, &m->fp, &m->fu, &m->ft, &m->fAp, &m->fAt};
     for (float2** q : v) TDDA_TRY(dalloc(m->allocs, q, n3, m->core->stream));
     TDDA_CK1(tdda::launch_to_f32((int)n3, m->al, m->fal, m->core->stream));
+    return TDDA_OK;
+}
+
+// The state of a Jacobi-preconditioned FP32 solve of model m: 1 / al of its
+// current polarisabilities and its core's vector of ones (on the model's core
+// stream, before the solve's first product).
+tdda_status prepare_jacobi(tdda_model* m) {
+    tdda_core* c = m->core;
+    const size_t n3 = 3 * (size_t)c->N;
+    if (!m->fpre) TDDA_TRY(dalloc(m->allocs, &m->fpre, n3, c->stream));
+    if (!c->ones32) {
+        TDDA_TRY(dalloc_c(c, &c->ones32, n3));
+        TDDA_CK1(tdda::launch_fill_ones(n3, c->ones32, c->stream));
+    }
+    TDDA_CK1(tdda::launch_recip_f32((int)n3, m->al, m->fpre, c->stream));
+    return TDDA_OK;
+}
+
+// P (FP64) += the inner solve's correction: d, or D^-1 d for a Jacobi-preconditioned solve
+tdda_status accumulate_correction(tdda_model* m, cudaStream_t stream) {
+    const int n3 = 3 * m->core->N;
+    if (m->jacobi) TDDA_CK1(tdda::launch_accumulate_scaled(n3, m->fP, m->al, m->P, stream));
+    else TDDA_CK1(tdda::launch_accumulate(n3, m->fP, m->P, stream));
     return TDDA_OK;
 }
 
@@ -723,9 +755,14 @@ tdda_status solve_fp64(tdda_model* const* ms, int n, int max_it, double tol, tdd
 
 // Mixed precision: FP32 BiCGSTAB on the FP64 residual, FP64 accumulation of
 // the correction, FP64 residual check, until |E - A P| / |E| <= tol.
-tdda_status solve_mixed(tdda_model* const* ms, int n, int max_it, double tol, tdda_solve_info* infos) {
+tdda_status solve_mixed(tdda_model* const* ms, int n, int max_it, double tol, tdda_solve_info* infos,
+                        bool jacobi = false) {
     tdda_core* c = ms[0]->core;
-    for (int i = 0; i < n; i++) TDDA_TRY(model_alloc_f32(ms[i]));
+    for (int i = 0; i < n; i++) {
+        TDDA_TRY(model_alloc_f32(ms[i]));
+        ms[i]->jacobi = jacobi;
+        if (jacobi) TDDA_TRY(prepare_jacobi(ms[i]));
+    }
     std::vector<RhsVecs<double>> h64(n);
     std::vector<RhsVecs<float>> h32(n);
     std::vector<int> done(n, 0), inner(n, 0), outer(n, 0);
@@ -811,7 +848,7 @@ tdda_status solve_mixed(tdda_model* const* ms, int n, int max_it, double tol, td
                 stat[i] = TDDA_ERR_NAN;
                 continue;
             }
-            TDDA_CK1(tdda::launch_accumulate(3 * c->N, ms[i]->fP, ms[i]->P, c->stream));
+            TDDA_TRY(accumulate_correction(ms[i], c->stream));
         }
     }
     TDDA_CK(cudaStreamSynchronize(c->stream));
@@ -1053,6 +1090,7 @@ double model_bytes(int N, int precision) {
     const double n3 = 3.0 * N;
     double model = n3 * (12 * 16 + 8);  // FP64 vectors and densities
     if (precision == TDDA_FP32_REFINE) model += n3 * 10 * 8;
+    if (precision == TDDA_FP32_JACOBI) model += n3 * 11 * 8;  // and 1 / al
     return model;
 }
 
@@ -1167,7 +1205,7 @@ int shape_active(const Shape* s) {
     return n;
 }
 
-tdda_status shape_admit(Shape* s, tdda_model* m, int max_it, double tol, int* slot) {
+tdda_status shape_admit(Shape* s, tdda_model* m, int max_it, double tol, int* slot, bool jacobi) {
     if (!shape_accepts(s, m)) {
         set_err("the model's core does not share the shape's FFT grid");
         return TDDA_ERR_INVALID_ARGUMENT;
@@ -1180,6 +1218,8 @@ tdda_status shape_admit(Shape* s, tdda_model* m, int max_it, double tol, int* sl
     }
     TDDA_TRY(set_device(s->c->device));
     TDDA_TRY(model_alloc_f32(m));
+    m->jacobi = jacobi;
+    if (jacobi) TDDA_TRY(prepare_jacobi(m));
     TDDA_CK(cudaStreamSynchronize(m->core->stream));
     Slot& sl = s->slots[k];
     sl = Slot{};
@@ -1285,7 +1325,7 @@ tdda_status shape_step(Shape* s, std::vector<Done>* done) {
             finish_slot(s, k, TDDA_ERR_NAN, done);
             continue;
         }
-        TDDA_CK1(tdda::launch_accumulate(3 * sl.m->core->N, sl.m->fP, sl.m->P, c->stream));
+        TDDA_TRY(accumulate_correction(sl.m, c->stream));
         sl.m->P_zero = false;
         sl.phase = kResidual;
     }
@@ -1845,13 +1885,14 @@ tdda_status tdda_solve_batch(tdda_model* const* ms, int n, int precision, int ma
                              tdda_solve_info* infos) {
     g_err.clear();
     TDDA_TRY(check_batch(ms, n));
-    if (!(max_err >= 0) || (precision != TDDA_FP64 && precision != TDDA_FP32_REFINE)) {
+    if (!(max_err >= 0) ||
+        (precision != TDDA_FP64 && precision != TDDA_FP32_REFINE && precision != TDDA_FP32_JACOBI)) {
         set_err("invalid tolerance or precision");
         return TDDA_ERR_INVALID_ARGUMENT;
     }
     TDDA_TRY(set_device(ms[0]->core->device));
     if (precision == TDDA_FP64) return solve_fp64(ms, n, max_it, max_err, infos);
-    return solve_mixed(ms, n, max_it, max_err, infos);
+    return solve_mixed(ms, n, max_it, max_err, infos, precision == TDDA_FP32_JACOBI);
 }
 
 namespace {
@@ -1867,9 +1908,15 @@ std::vector<std::pair<ShapeKey, tdda_session::Shape*>> g_shapes;  // idle shapes
 }  // namespace
 
 tdda_status tdda_solve_multi(tdda_model* const* ms, int n, int max_it, double max_err, tdda_solve_info* infos) {
+    return tdda_solve_multi_precision(ms, n, TDDA_FP32_REFINE, max_it, max_err, infos);
+}
+
+tdda_status tdda_solve_multi_precision(tdda_model* const* ms, int n, int precision, int max_it, double max_err,
+                                       tdda_solve_info* infos) {
     g_err.clear();
-    if (!ms || n < 1 || n > 64 || !(max_err >= 0)) {
-        set_err("invalid batch, tolerance or size (1..64 right-hand sides)");
+    if (!ms || n < 1 || n > 64 || !(max_err >= 0) ||
+        (precision != TDDA_FP32_REFINE && precision != TDDA_FP32_JACOBI)) {
+        set_err("invalid batch, precision, tolerance or size (1..64 right-hand sides)");
         return TDDA_ERR_INVALID_ARGUMENT;
     }
     for (int i = 0; i < n; i++) {
@@ -1909,7 +1956,8 @@ tdda_status tdda_solve_multi(tdda_model* const* ms, int n, int max_it, double ma
     if (!sh) TDDA_TRY(tdda_session::shape_create(device, grid, n, &sh));
     tdda_status worst = TDDA_OK;
     tdda_status st = TDDA_OK;
-    for (int i = 0; i < n && st == TDDA_OK; i++) st = tdda_session::shape_admit(sh, ms[i], max_it, max_err, nullptr);
+    for (int i = 0; i < n && st == TDDA_OK; i++)
+        st = tdda_session::shape_admit(sh, ms[i], max_it, max_err, nullptr, precision == TDDA_FP32_JACOBI);
     std::vector<tdda_session::Done> done;
     while (st == TDDA_OK && tdda_session::shape_active(sh) > 0) st = tdda_session::shape_step(sh, &done);
     if (st != TDDA_OK) {

@@ -85,6 +85,11 @@ template <typename T> struct RhsVecs {
     cx<T>* Ap;
     cx<T>* At;
     const cx<T>* al;
+    // FP32 inner solve with Jacobi right preconditioning (TDDA_FP32_JACOBI): the
+    // gathers scatter pre v = v / al onto the grid and the sinks add 1 v (al
+    // then points to ones), so every product is A D^-1 v with D = diag(al);
+    // the correction is D^-1 of the inner solution.  nullptr otherwise.
+    const cx<T>* pre;
     SolveState* st;
     double* part;        // reduction partials, kPartSlots x maxblk doubles
     unsigned int* cnt;   // last-block counters, kCounters
@@ -306,6 +311,10 @@ cudaError_t launch_to_f32(int n3, const double2* src, float2* dst, cudaStream_t 
 // [0, hi) or is NaN (mode 1); else 0
 cudaError_t launch_scan(long long n, const double* v, int mode, double hi, unsigned int* flag, cudaStream_t stream);
 cudaError_t launch_accumulate(int n3, const float2* d, double2* P, cudaStream_t stream);
+// Jacobi preconditioning: pre = 1 / al (FP32 SoA), P += d / al, v = 1
+cudaError_t launch_recip_f32(int n3, const double2* al, float2* pre, cudaStream_t stream);
+cudaError_t launch_accumulate_scaled(int n3, const float2* d, const double2* al, double2* P, cudaStream_t stream);
+cudaError_t launch_fill_ones(long long n, float2* v, cudaStream_t stream);
 template <typename T> cudaError_t launch_zero(long long n, cx<T>* v, cudaStream_t stream);
 
 // generic in-place 3-D FFT of a contiguous (n0, n1, n2) double2 array

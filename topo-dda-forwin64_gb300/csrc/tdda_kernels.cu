@@ -517,6 +517,33 @@ __global__ void k_accumulate(int n3, const float2* d, double2* P) {
         P[e] = make_double2(P[e].x + (double)v.x, P[e].y + (double)v.y);
     }
 }
+// Jacobi preconditioning of the FP32 inner solve: pre = 1 / al (FP64 AoS ->
+// FP32 SoA, the division in FP64), P += d / al, and a vector of ones
+__global__ void k_recip_f32(int n3, const double2* al, float2* pre) {
+    const int n = n3 / 3;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x) {
+        const int c = e / n, i = e - c * n;
+        const double2 a = al[3LL * i + c];
+        const double m = a.x * a.x + a.y * a.y;
+        pre[e] = make_float2((float)(a.x / m), (float)(-a.y / m));
+    }
+}
+__global__ void k_accumulate_scaled(int n3, const float2* d, const double2* al, double2* P) {
+    const int n = n3 / 3;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x) {
+        const int i = e / 3, c = e - 3 * i;
+        const float2 v = d[(long long)c * n + i];
+        const double2 a = al[e];
+        const double m = a.x * a.x + a.y * a.y;
+        const double vx = v.x, vy = v.y;
+        // (vx + i vy) / (ax + i ay) = (vx ax + vy ay + i (vy ax - vx ay)) / |a|^2
+        P[e] = make_double2(P[e].x + (vx * a.x + vy * a.y) / m, P[e].y + (vy * a.x - vx * a.y) / m);
+    }
+}
+__global__ void k_fill_ones(long long n, float2* v) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        v[e] = make_float2(1.f, 0.f);
+}
 template <typename T> __global__ void k_zero(long long n, cx<T>* v) {
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
         v[e] = czero<T>();
@@ -775,6 +802,18 @@ cudaError_t launch_to_dd(long long n, const double2* src, dd2* dst, cudaStream_t
 }
 cudaError_t launch_to_f32(int n3, const double2* src, float2* dst, cudaStream_t stream) {
     k_to_f32<<<grid1d(n3, kNT), kNT, 0, stream>>>(n3, src, dst);
+    return cudaGetLastError();
+}
+cudaError_t launch_recip_f32(int n3, const double2* al, float2* pre, cudaStream_t stream) {
+    k_recip_f32<<<grid1d(n3, kNT), kNT, 0, stream>>>(n3, al, pre);
+    return cudaGetLastError();
+}
+cudaError_t launch_accumulate_scaled(int n3, const float2* d, const double2* al, double2* P, cudaStream_t stream) {
+    k_accumulate_scaled<<<grid1d(n3, kNT), kNT, 0, stream>>>(n3, d, al, P);
+    return cudaGetLastError();
+}
+cudaError_t launch_fill_ones(long long n, float2* v, cudaStream_t stream) {
+    k_fill_ones<<<grid1d(n, kNT), kNT, 0, stream>>>(n, v);
     return cudaGetLastError();
 }
 cudaError_t launch_accumulate(int n3, const float2* d, double2* P, cudaStream_t stream) {

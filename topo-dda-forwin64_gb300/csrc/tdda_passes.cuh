@@ -166,6 +166,9 @@ __global__ void __launch_bounds__(kNT) k_zfwd(Geom g, const RhsVecs<T>* __restri
                 } else {
                     v[c] = ldv<T>(src, o);
                 }
+                if constexpr (sizeof(T) == 4) {  // Jacobi preconditioning: the grid gets D^-1 v
+                    if (SRC != SRC_P && R.pre) v[c] = cmul<T>(v[c], R.pre[o]);
+                }
             }
         } else {
             v[0] = v[1] = v[2] = czero<T>();
@@ -630,6 +633,9 @@ __global__ void __launch_bounds__(kNT) k_zinv(Geom g, const RhsVecs<T>* __restri
 // first store.
 template <typename T, int SRC, int CH> struct GatherIn {
     static constexpr int NL = SRC == SRC_PUPD_DEF ? 6 : (SRC == SRC_PUPD ? 3 : (SRC == SRC_TUPD ? 2 : 1));
+    // FP32 gathers of a Jacobi-preconditioned solve scale the grid values by pre
+    static constexpr bool kPre = sizeof(T) == 4 && (SRC == SRC_IN || SRC == SRC_PUPD || SRC == SRC_TUPD ||
+                                                    SRC == SRC_PUPD_DEF);
     cx<T> a[NL][CH];
     __device__ __forceinline__ void load(const RhsVecs<T>& R, const long long (&o)[CH], const cx<T>* src) {
 #pragma unroll
@@ -673,6 +679,9 @@ template <typename T, int SRC, int CH> struct GatherIn {
                 R.t[i] = v[q];
             } else {
                 v[q] = a[0][q];
+            }
+            if constexpr (kPre) {  // the stored vectors stay unscaled; the grid gets D^-1 v
+                if (R.pre) v[q] = cmul<T>(v[q], R.pre[i]);
             }
         }
     }

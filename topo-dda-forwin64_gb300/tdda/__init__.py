@@ -30,7 +30,7 @@ OK, ERR_INVALID_ARGUMENT, ERR_CUDA, ERR_OUT_OF_MEMORY, ERR_UNSUPPORTED = 0, 1, 2
 NOT_CONVERGED, BREAKDOWN, ERR_NAN, ERR_NO_DEVICE = 5, 6, 7, 8
 STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "cuda error", 3: "out of memory", 4: "unsupported",
                 5: "not converged", 6: "breakdown", 7: "nan", 8: "no device"}
-FP64, FP32_REFINE = 0, 1
+FP64, FP32_REFINE, FP32_JACOBI = 0, 1, 2
 MEM_HOST, MEM_DEVICE = 0, 1
 FIELD_P, FIELD_E, FIELD_AL, FIELD_DIEL, FIELD_EINTERNAL = 0, 1, 2, 3, 4
 METHODS = {"LDR": 0, "FCD": 1}
@@ -48,7 +48,7 @@ EXPORTS = [
     "tdda_solve_batch", "tdda_solve_multi",
     "tdda_fft3d", "tdda_core_stream", "tdda_kernel_launches", "tdda_profile_aproduct", "tdda_core_pass_count",
     "tdda_core_pass_name", "tdda_core_set_xpass", "tdda_core_autotune",
-    "tdda_core_set_batch_group", "tdda_core_autotune_batch", "tdda_aproduct_noalloc", "tdda_server_create", "tdda_server_submit", "tdda_server_result",
+    "tdda_core_set_batch_group", "tdda_core_autotune_batch", "tdda_solve_multi_precision", "tdda_aproduct_noalloc", "tdda_server_create", "tdda_server_submit", "tdda_server_result",
     "tdda_server_stats", "tdda_server_counters_get", "tdda_server_clock", "tdda_server_destroy",
     "tdda_request_bytes",
 ]
@@ -161,6 +161,7 @@ def load() -> ctypes.CDLL:
         "tdda_model_density_gradient": (i, [vp, i, vp, vp, i, vp, vp, vp]),
         "tdda_solve_batch": (i, [ctypes.POINTER(vp), i, i, i, d, ctypes.POINTER(SolveInfo)]),
         "tdda_solve_multi": (i, [ctypes.POINTER(vp), i, i, d, ctypes.POINTER(SolveInfo)]),
+        "tdda_solve_multi_precision": (i, [ctypes.POINTER(vp), i, i, i, d, ctypes.POINTER(SolveInfo)]),
         "tdda_fft3d": (i, [vp, i, i, i, i]),
         "tdda_core_stream": (i, [vp, ctypes.POINTER(vp)]),
         "tdda_kernel_launches": (ctypes.c_ulonglong, []),
@@ -497,13 +498,14 @@ def solve_batch(models, precision: int = FP64, max_it: int = 10000, tol: float =
     return out
 
 
-def solve_multi(models, max_it: int = 10000, tol: float = 1e-5) -> list:
-    """FP32+refine solves of models on different cores that share one FFT grid shape, with
-    the inner solves of all of them in one launch per pass (tdda_solve_multi)."""
+def solve_multi(models, max_it: int = 10000, tol: float = 1e-5, precision: int = FP32_REFINE) -> list:
+    """FP32+refine solves (precision FP32_REFINE or FP32_JACOBI) of models on different cores
+    that share one FFT grid shape, with the inner solves of all of them in one launch per pass
+    (tdda_solve_multi_precision)."""
     n = len(models)
     arr = (ctypes.c_void_p * n)(*[m.h.value for m in models])
     infos = (SolveInfo * n)()
-    st = load().tdda_solve_multi(arr, n, int(max_it), float(tol), infos)
+    st = load().tdda_solve_multi_precision(arr, n, int(precision), int(max_it), float(tol), infos)
     _check(st, "tdda_solve_multi", allowed=(OK, NOT_CONVERGED, BREAKDOWN, ERR_NAN))
     out = [infos[k].as_dict() for k in range(n)]
     for m, o in zip(models, out):
