@@ -388,9 +388,10 @@ def time_batch(tdda, torch, w, incs, precision, steps, dev, flush_l2, keep_P=Fal
     """Solve len(incs) right-hand sides of one lattice in one batched solve per step
     (keep_P: the result's polarisations in out["P"])."""
     core = tdda.AProductCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material, w.nback, max_rhs=len(incs), device=dev)
-    tune = core.autotune(nrhs=len(incs), reps=10) if precision == tdda.FP32_REFINE else None
+    fp32 = precision in (tdda.FP32_REFINE, tdda.FP32_JACOBI)
+    tune = core.autotune(nrhs=len(incs), reps=10) if fp32 else None
     # the batch schedule (right-hand sides per launch), timed on this core's FP32 products
-    btune = core.autotune_batch(nrhs=len(incs), reps=5) if precision == tdda.FP32_REFINE else None
+    btune = core.autotune_batch(nrhs=len(incs), reps=5) if fp32 else None
     models = [tdda.DDAModel(core, inc.nK, inc.E0, inc.nE0, w.diel_old) for inc in incs]
     stream = torch.cuda.ExternalStream(core.stream(), device=dev)
     zero = pinned_c128(3 * w.N)
@@ -414,10 +415,11 @@ def time_batch(tdda, torch, w, incs, precision, steps, dev, flush_l2, keep_P=Fal
     ms = [r[0] for r in runs]
     infos = runs[-1][1]
     n32 = 2 * max(i["inner_iterations"] for i in infos) + 2 * max(i["outer_iterations"] for i in infos)
-    prof = core.profile_aproduct(precision, len(incs), 5)
+    prof = core.profile_aproduct(tdda.FP32_REFINE if fp32 else tdda.FP64, len(incs), 5)
     out = {"rhs": len(incs), "value": len(incs) * steps / (sum(ms) / 1000.0), "unit": UNIT, "steps": steps,
            "ms_per_batch": sum(ms) / steps, "iterations": [i["iterations"] for i in infos],
-           "pass_ms": prof, "kernels": pass_names(core, precision), "grid": list(core.grid)}
+           "pass_ms": prof, "kernels": pass_names(core, tdda.FP32_REFINE if fp32 else tdda.FP64),
+           "grid": list(core.grid)}
     if tune:
         out["x_pass_autotune"] = tune
     if btune:
@@ -534,6 +536,34 @@ def run_serving(tdda, stream, precision, workers, budget, dev):
             "max_iterations": max(i["iterations"] for i in infos)}
 
 
+def run_cfg1(tdda, torch, dev, steps=10):
+    """The plain FP64 single-solve workload (20x20x10, rho ~ U[0,1]), solved with each
+    precision: solves/s over `steps` solves after 3 warm-up solves (CUDA events)."""
+    w = lattice.config(1)
+    inc = w.incidences[0]
+    core = tdda.AProductCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material, w.nback, device=dev)
+    m = tdda.DDAModel(core, inc.nK, inc.E0, inc.nE0, w.diel_old)
+    stream = torch.cuda.ExternalStream(core.stream(), device=dev)
+    zero = np.zeros(3 * w.N, np.complex128)
+    out = {"workload": "plain single solve 20x20x10 (cfg 1)", "dipoles": w.N}
+    for name, prec in (("fp64", tdda.FP64), ("fp32_refine", tdda.FP32_REFINE), ("fp32_jacobi", tdda.FP32_JACOBI)):
+        ms = []
+        for k in range(3 + steps):
+            m.InitializeP(zero)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            [info] = tdda.solve_batch([m], prec, MAX_IT, TOL)
+            e1.record(stream)
+            e1.synchronize()
+            if k >= 3:
+                ms.append(e0.elapsed_time(e1))
+        out[name] = {"value": 1000.0 * steps / sum(ms), "unit": UNIT, "ms_p50": float(np.percentile(ms, 50)),
+                     "iterations": info["iterations"], "true_residual": info.get("true_residual")}
+    m.close()
+    core.close()
+    return out
+
+
 def run_topo(tdda, iters):
     """The topology-optimisation workload: 80x80x20, forward + 3 adjoint solves batched per
     iteration, point |E|^2 objective 100 nm above the top centre, gradient ascent.  The loop
@@ -555,8 +585,16 @@ def run_topo(tdda, iters):
         f.append(r.objective)
         its.append(r.iterations)
     dt = time.perf_counter() - t0
+    # the same loop with the Jacobi-preconditioned inner solves, from the same start
+    jloop = topo.TopoLoop(w.Nx, w.Ny, w.Nz, w.d, w.lam, w.material, th0, r_obs, precision=tdda.FP32_JACOBI, tol=TOL)
+    t0 = time.perf_counter()
+    fj = []
+    for _ in range(iters):
+        fj.append(jloop.step().objective)
+    dtj = time.perf_counter() - t0
+    jloop.close()
     final = {}
-    for name, prec in (("fp32_refine", tdda.FP32_REFINE), ("fp64", tdda.FP64)):
+    for name, prec in (("fp32_refine", tdda.FP32_REFINE), ("fp32_jacobi", tdda.FP32_JACOBI), ("fp64", tdda.FP64)):
         loop.precision = prec
         loop.evaluate()  # warm-up: graphs and buffers of this precision
         t1 = time.perf_counter()
@@ -567,7 +605,9 @@ def run_topo(tdda, iters):
     return {"steps": iters, "s_per_step": dt / iters, "solves_per_s": 4 * iters / dt,
             "objective_first": f[0], "objective_last": f[-1], "bicgstab_iterations_last": its[-1],
             "final_design": final,
-            "speedup_fp32_refine": final["fp64"]["evaluate_s"] / final["fp32_refine"]["evaluate_s"]}
+            "fp32_jacobi_loop": {"s_per_step": dtj / iters, "solves_per_s": 4 * iters / dtj, "objective_last": fj[-1]},
+            "speedup_fp32_refine": final["fp64"]["evaluate_s"] / final["fp32_refine"]["evaluate_s"],
+            "speedup_fp32_jacobi": final["fp64"]["evaluate_s"] / final["fp32_jacobi"]["evaluate_s"]}
 
 
 def run_ours(args, dist: Dist):
@@ -693,33 +733,42 @@ def run_ours(args, dist: Dist):
                                     keep_P=True)
         b32["roofline"] = batched_roofline(w3, tuple(b32["grid"]), prof_b, len(w3.incidences), 8, peaks["hbm_gbs"],
                                            b32["kernels"][2], b32["kernels"])
+        j32, _, _ = time_batch(tdda, torch, w3, w3.incidences, tdda.FP32_JACOBI, args.batched_steps, dev, flush_l2,
+                               keep_P=True)
         b64, _, _ = time_batch(tdda, torch, w3, w3.incidences, tdda.FP64, 1, dev, flush_l2)
         # error of each FP32+refine result against the FP64 solution to 1e-10 (untimed)
         c3 = tdda.AProductCore(w3.Nx, w3.Ny, w3.Nz, w3.R, w3.d, w3.lam, w3.material, w3.nback,
                                max_rhs=len(w3.incidences), device=dev)
         m3 = [tdda.DDAModel(c3, i.nK, i.E0, i.nE0, w3.diel_old) for i in w3.incidences]
         tdda.solve_batch(m3, tdda.FP64, MAX_IT, 1e-10)
-        b32["error_vs_fp64"] = [float(np.linalg.norm(p32 - m.get_P()) / np.linalg.norm(m.get_P()))
-                                for p32, m in zip(b32.pop("P"), m3)]
+        for bx in (b32, j32):
+            bx["error_vs_fp64"] = [float(np.linalg.norm(p32 - m.get_P()) / np.linalg.norm(m.get_P()))
+                                   for p32, m in zip(bx.pop("P"), m3)]
         for m in m3:
             m.close()
         c3.close()
         batched = {"workload": "batched 8 RHS 96x96x24 (cfg 3)", "dipoles": w3.N, "fp32_refine": b32,
                    "fp64": {"value": b64["value"], "unit": UNIT, "iterations": b64["iterations"],
                             "ms_per_batch": b64["ms_per_batch"]},
-                   "speedup_fp32_refine": b32["value"] / b64["value"]}
+                   "speedup_fp32_refine": b32["value"] / b64["value"],
+                   "fp32_jacobi": {k: j32[k] for k in ("value", "unit", "ms_per_batch", "iterations", "error_vs_fp64")},
+                   "speedup_fp32_jacobi": j32["value"] / b64["value"]}
 
     # serving: the request stream through the continuous-batching loop
     serving = None
     if args.serve_requests > 0:
         stream = lattice.serving_stream(n=args.serve_requests, rate=200.0, seed=5)
         s32 = run_serving(tdda, stream, tdda.FP32_REFINE, args.serve_workers, 150e9, dev)
+        sj = run_serving(tdda, stream, tdda.FP32_JACOBI, args.serve_workers, 150e9, dev)
         n64 = min(args.serve_requests, args.serve_fp64_requests or args.serve_requests)
         s64 = run_serving(tdda, stream[:n64], tdda.FP64, args.serve_workers, 150e9, dev) if n64 > 0 else None
         serving = {"workload": f"serving stream {args.serve_requests} requests, Poisson 200/s, dims 16-128 "
                                "log-uniform (z<=32), 1-4 RHS (cfg 5)", "hbm_budget_bytes": 150e9,
-                   "workers": args.serve_workers, "fp32_refine": s32, "fp64": s64,
-                   "speedup_fp32_refine": s32["value"] / s64["value"] if s64 and n64 == len(stream) else None}
+                   "workers": args.serve_workers, "fp32_refine": s32, "fp32_jacobi": sj, "fp64": s64,
+                   "speedup_fp32_refine": s32["value"] / s64["value"] if s64 and n64 == len(stream) else None,
+                   "speedup_fp32_jacobi": sj["value"] / s64["value"] if s64 and n64 == len(stream) else None}
+
+    cfg1 = run_cfg1(tdda, torch, dev)
 
     # topology optimisation: forward + adjoint solves batched per iteration
     topo_line = None
@@ -778,6 +827,7 @@ def run_ours(args, dist: Dist):
                          "passes_fp32": passes32, "aproduct_fp32": whole32, "x_pass_autotune": tune},
             "batched": batched,
             "serving": serving,
+            "cfg1": cfg1,
             "topo": topo_line,
             "gpu_launches": launches,
             "clocks": clocks,

@@ -532,7 +532,12 @@ def solve_workload(w, precision: int = FP64, inc=None, tol=None, max_it=None) ->
     model = DDAModel(core, inc.nK, inc.E0, inc.nE0, w.diel_old)
     tol = w.tol if tol is None else tol
     max_it = w.max_it if max_it is None else max_it
-    info = model.bicgstab(max_it, tol) if precision == FP64 else model.solve_mixed(max_it, tol)
+    if precision == FP64:
+        info = model.bicgstab(max_it, tol)
+    elif precision == FP32_JACOBI:
+        [info] = solve_batch([model], FP32_JACOBI, max_it, tol)
+    else:
+        info = model.solve_mixed(max_it, tol)
     model.update_E_in_structure()
     out = Solved(model.get_P(), model.get_Einternal(), info)
     model.close()
