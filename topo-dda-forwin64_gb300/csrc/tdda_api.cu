@@ -227,6 +227,10 @@ struct tdda_model_s {
     // whether the model's current solve uses it, and 1 / al as FP32 SoA
     bool jacobi = false;
     float2* fpre = nullptr;
+    // UpdateAlpha keeps the previous densities on the device (restored when the new
+    // ones are refused) and leaves the host copy diel_old stale until it is needed
+    double* dold_bak = nullptr;
+    bool dold_host_stale = false;
     std::vector<void*> allocs;
     bool P_zero = true;
     int ITERATION = 0;
@@ -1351,6 +1355,7 @@ tdda_status model_reinit(tdda_model* m, const double* nK, double E0, const doubl
     }
     m->E0 = E0;
     m->diel_old.assign(diel_old, diel_old + 3 * (size_t)c->N);
+    m->dold_host_stale = false;
     const size_t n3 = 3 * (size_t)c->N;
     TDDA_CK(cudaMemsetAsync(m->P, 0, sizeof(double2) * n3, c->stream));
     TDDA_CK(cudaMemsetAsync(m->Ein, 0, sizeof(double2) * n3, c->stream));
@@ -1786,8 +1791,11 @@ tdda_status tdda_model_update_alpha(tdda_model* m, const double* diel_old) {
     TDDA_TRY(set_device(m->core->device));
     tdda_core* c = m->core;
     const size_t n3 = 3 * (size_t)c->N;
-    // upload, then check the range on the device before anything that depends
-    // on the densities changes (the host scan below only names the entry)
+    if (!m->dold_bak) TDDA_TRY(dalloc(m->allocs, &m->dold_bak, n3, c->stream));
+    // keep the current densities, upload, then check the range on the device
+    // before anything that depends on the densities changes (the host scan below
+    // only names the entry)
+    TDDA_CK(cudaMemcpyAsync(m->dold_bak, m->dold, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->stream));
     TDDA_CK(cudaMemcpyAsync(m->dold, diel_old, sizeof(double) * n3, cudaMemcpyHostToDevice, c->stream));
     TDDA_CK1(tdda::launch_scan((long long)n3, m->dold, 1, (double)c->nmat, c->flag, c->stream));
     TDDA_CK(cudaMemcpyAsync(c->hflag, c->flag, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
@@ -1795,14 +1803,25 @@ tdda_status tdda_model_update_alpha(tdda_model* m, const double* diel_old) {
     if (*c->hflag || c->nmat < 2) {
         size_t bad = 0;
         densities_in_table(diel_old, n3, c->nmat, &bad);
-        TDDA_CK(cudaMemcpyAsync(m->dold, m->diel_old.data(), sizeof(double) * n3, cudaMemcpyHostToDevice, c->stream));
+        TDDA_CK(cudaMemcpyAsync(m->dold, m->dold_bak, sizeof(double) * n3, cudaMemcpyDeviceToDevice, c->stream));
         TDDA_CK(cudaStreamSynchronize(c->stream));  // the model keeps its densities
         set_err("density %g of entry %zu is outside the material table", diel_old[bad], bad);
         return TDDA_ERR_INVALID_ARGUMENT;
     }
     TDDA_CK1(tdda::launch_model_alpha((int)n3, m->dold, alpha_params(m), m->diel, m->al, m->fal, c->stream));
-    m->diel_old.assign(diel_old, diel_old + n3);  // while the kernel runs
+    m->dold_host_stale = true;  // the device holds the densities; the host copy follows on demand
     TDDA_CK(cudaStreamSynchronize(c->stream));
+    return TDDA_OK;
+}
+
+// the host copy of the densities, refreshed from the device after UpdateAlpha
+static tdda_status host_densities(tdda_model* m) {
+    if (!m->dold_host_stale) return TDDA_OK;
+    tdda_core* c = m->core;
+    TDDA_CK(cudaMemcpyAsync(m->diel_old.data(), m->dold, sizeof(double) * 3 * (size_t)c->N, cudaMemcpyDeviceToHost,
+                            c->stream));
+    TDDA_CK(cudaStreamSynchronize(c->stream));
+    m->dold_host_stale = false;
     return TDDA_OK;
 }
 
@@ -1811,6 +1830,8 @@ tdda_status tdda_model_update_alpha_single(tdda_model* m, int idx, double value)
         set_err("invalid argument");
         return TDDA_ERR_INVALID_ARGUMENT;
     }
+    TDDA_TRY(set_device(m->core->device));
+    TDDA_TRY(host_densities(m));
     std::vector<double> d = m->diel_old;
     d[3 * (size_t)idx] = d[3 * (size_t)idx + 1] = d[3 * (size_t)idx + 2] = value;
     return tdda_model_update_alpha(m, d.data());
