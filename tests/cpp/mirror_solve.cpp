@@ -4,7 +4,7 @@
 // Einternal and EResult to a file for tests/test_cpp_mirror.py to check
 // against the oracle.
 //
-//   mirror_solve Nx Ny Nz d lam eps_re eps_im tol precision(0|1) out.bin
+//   mirror_solve Nx Ny Nz d lam eps_re eps_im tol precision(0 FP64, 1 FP32+refine, 2 Jacobi) out.bin
 // densities: rho_i = 0.5 + 0.5 sin(0.37 i), the same in the Python test.
 #include <cmath>
 #include <cstdio>
@@ -74,6 +74,8 @@ int main(int argc, char** argv) {
     tdda::DDAModel TestModel(&Core, nK, 1.0, nE0, &RResult, false);
     if (precision == 0)
         TestModel.bicgstab(100000, tol);
+    else if (precision == 2)
+        TestModel.bicgstab_jacobi(100000, tol);
     else
         TestModel.bicgstab_mixed(100000, tol);
     TestModel.update_E_in_structure();

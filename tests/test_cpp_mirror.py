@@ -54,7 +54,7 @@ def test_reference_callers_compile_against_the_dropin():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision,tol,bound", [(0, 1e-10, 1e-9), (1, 1e-5, 1e-4)])
+@pytest.mark.parametrize("precision,tol,bound", [(0, 1e-10, 1e-9), (1, 1e-5, 1e-4), (2, 1e-5, 1e-4)])
 def test_mirror_solve_matches_oracle(tmp_path, precision, tol, bound):
     if tdda.device_count() < 1:
         pytest.skip("no CUDA device")

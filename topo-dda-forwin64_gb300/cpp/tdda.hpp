@@ -299,6 +299,8 @@ template <class VectorXcd = std::vector<cplx>> class DDAModelT {
     void bicgstab(int MAX_ITERATION, double MAX_ERROR, int /*EVOITERATION*/) { bicgstab(MAX_ITERATION, MAX_ERROR); }
     // the same solve with the FP32 convolution and FP64 refinement
     void bicgstab_mixed(int MAX_ITERATION, double MAX_ERROR) { solve(MAX_ITERATION, MAX_ERROR, TDDA_FP32_REFINE); }
+    // the same with the inner solve right-preconditioned by diag(al) (TDDA_FP32_JACOBI)
+    void bicgstab_jacobi(int MAX_ITERATION, double MAX_ERROR) { solve(MAX_ITERATION, MAX_ERROR, TDDA_FP32_JACOBI); }
 
     void change_E(const VectorXcd& E) { check(tdda_model_change_E(h_, dptr(E), TDDA_MEM_HOST), "change_E"); }
     void reset_E() { check(tdda_model_reset_E(h_), "reset_E"); }
@@ -394,8 +396,11 @@ template <class VectorXcd = std::vector<cplx>> class DDAModelT {
     }
     void solve(int max_it, double max_err, int precision) {
         if (verbose_) std::cout << "--------------Calculation start. Iterative method used: BICGSTAB---------------\n\n";
-        const tdda_status st = precision == TDDA_FP64 ? tdda_model_bicgstab(h_, max_it, max_err, &info_)
-                                                      : tdda_model_solve_mixed(h_, max_it, max_err, &info_);
+        tdda_model* one[1] = {h_};
+        const tdda_status st = precision == TDDA_FP64          ? tdda_model_bicgstab(h_, max_it, max_err, &info_)
+                               : precision == TDDA_FP32_JACOBI ? tdda_solve_batch(one, 1, TDDA_FP32_JACOBI, max_it,
+                                                                                  max_err, &info_)
+                                                               : tdda_model_solve_mixed(h_, max_it, max_err, &info_);
         if (st != TDDA_OK && st != TDDA_NOT_CONVERGED && st != TDDA_BREAKDOWN) check(st, "bicgstab");
         fetch(TDDA_FIELD_P, P_);
         if (st == TDDA_NOT_CONVERGED) {
