@@ -427,7 +427,8 @@ tdda_status model_alloc_f32(tdda_model* m) {
 }
 
 // The state of a Jacobi-preconditioned FP32 solve of model m: 1 / al of its
-// current polarisabilities and its core's vector of ones (on the model's core
+// current polarisabilities (from the FP32 al, which model_alloc_f32 and every
+// UpdateAlpha keep current) and its core's vector of ones (on the model's core
 // stream, before the solve's first product).
 tdda_status prepare_jacobi(tdda_model* m) {
     tdda_core* c = m->core;
@@ -437,14 +438,14 @@ tdda_status prepare_jacobi(tdda_model* m) {
         TDDA_TRY(dalloc_c(c, &c->ones32, n3));
         TDDA_CK1(tdda::launch_fill_ones(n3, c->ones32, c->stream));
     }
-    TDDA_CK1(tdda::launch_recip_f32((int)n3, m->al, m->fpre, c->stream));
+    TDDA_CK1(tdda::launch_recip_f32((int)n3, m->fal, m->fpre, c->stream));
     return TDDA_OK;
 }
 
 // P (FP64) += the inner solve's correction: d, or D^-1 d for a Jacobi-preconditioned solve
 tdda_status accumulate_correction(tdda_model* m, cudaStream_t stream) {
     const int n3 = 3 * m->core->N;
-    if (m->jacobi) TDDA_CK1(tdda::launch_accumulate_scaled(n3, m->fP, m->al, m->P, stream));
+    if (m->jacobi) TDDA_CK1(tdda::launch_accumulate_scaled(n3, m->fP, m->fpre, m->P, stream));
     else TDDA_CK1(tdda::launch_accumulate(n3, m->fP, m->P, stream));
     return TDDA_OK;
 }

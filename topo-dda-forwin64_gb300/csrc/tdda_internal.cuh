@@ -311,9 +311,9 @@ cudaError_t launch_to_f32(int n3, const double2* src, float2* dst, cudaStream_t 
 // [0, hi) or is NaN (mode 1); else 0
 cudaError_t launch_scan(long long n, const double* v, int mode, double hi, unsigned int* flag, cudaStream_t stream);
 cudaError_t launch_accumulate(int n3, const float2* d, double2* P, cudaStream_t stream);
-// Jacobi preconditioning: pre = 1 / al (FP32 SoA), P += d / al, v = 1
-cudaError_t launch_recip_f32(int n3, const double2* al, float2* pre, cudaStream_t stream);
-cudaError_t launch_accumulate_scaled(int n3, const float2* d, const double2* al, double2* P, cudaStream_t stream);
+// Jacobi preconditioning: pre = 1 / al (FP32 SoA from the FP32 al), P += d pre, v = 1
+cudaError_t launch_recip_f32(int n3, const float2* al, float2* pre, cudaStream_t stream);
+cudaError_t launch_accumulate_scaled(int n3, const float2* d, const float2* pre, double2* P, cudaStream_t stream);
 cudaError_t launch_fill_ones(long long n, float2* v, cudaStream_t stream);
 template <typename T> cudaError_t launch_zero(long long n, cx<T>* v, cudaStream_t stream);
 

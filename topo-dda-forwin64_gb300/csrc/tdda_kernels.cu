@@ -517,27 +517,25 @@ __global__ void k_accumulate(int n3, const float2* d, double2* P) {
         P[e] = make_double2(P[e].x + (double)v.x, P[e].y + (double)v.y);
     }
 }
-// Jacobi preconditioning of the FP32 inner solve: pre = 1 / al (FP64 AoS ->
-// FP32 SoA, the division in FP64), P += d / al, and a vector of ones
-__global__ void k_recip_f32(int n3, const double2* al, float2* pre) {
-    const int n = n3 / 3;
+// Jacobi preconditioning of the FP32 inner solve: pre = 1 / al from the FP32
+// al (SoA; al is well away from 0, so FP32 is enough for a preconditioner), and
+// P += d pre (the correction's product in FP32, like the correction itself,
+// accumulated in FP64), and a vector of ones
+__global__ void k_recip_f32(int n3, const float2* al, float2* pre) {
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x) {
-        const int c = e / n, i = e - c * n;
-        const double2 a = al[3LL * i + c];
-        const double m = a.x * a.x + a.y * a.y;
-        pre[e] = make_float2((float)(a.x / m), (float)(-a.y / m));
+        const float2 a = al[e];
+        const float m = a.x * a.x + a.y * a.y;
+        pre[e] = make_float2(a.x / m, -a.y / m);
     }
 }
-__global__ void k_accumulate_scaled(int n3, const float2* d, const double2* al, double2* P) {
+__global__ void k_accumulate_scaled(int n3, const float2* d, const float2* pre, double2* P) {
     const int n = n3 / 3;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x) {
         const int i = e / 3, c = e - 3 * i;
-        const float2 v = d[(long long)c * n + i];
-        const double2 a = al[e];
-        const double m = a.x * a.x + a.y * a.y;
-        const double vx = v.x, vy = v.y;
-        // (vx + i vy) / (ax + i ay) = (vx ax + vy ay + i (vy ax - vx ay)) / |a|^2
-        P[e] = make_double2(P[e].x + (vx * a.x + vy * a.y) / m, P[e].y + (vy * a.x - vx * a.y) / m);
+        const long long s = (long long)c * n + i;
+        const float2 v = d[s], q = pre[s];
+        const float vx = v.x * q.x - v.y * q.y, vy = v.x * q.y + v.y * q.x;
+        P[e] = make_double2(P[e].x + (double)vx, P[e].y + (double)vy);
     }
 }
 __global__ void k_fill_ones(long long n, float2* v) {
@@ -804,12 +802,12 @@ cudaError_t launch_to_f32(int n3, const double2* src, float2* dst, cudaStream_t 
     k_to_f32<<<grid1d(n3, kNT), kNT, 0, stream>>>(n3, src, dst);
     return cudaGetLastError();
 }
-cudaError_t launch_recip_f32(int n3, const double2* al, float2* pre, cudaStream_t stream) {
+cudaError_t launch_recip_f32(int n3, const float2* al, float2* pre, cudaStream_t stream) {
     k_recip_f32<<<grid1d(n3, kNT), kNT, 0, stream>>>(n3, al, pre);
     return cudaGetLastError();
 }
-cudaError_t launch_accumulate_scaled(int n3, const float2* d, const double2* al, double2* P, cudaStream_t stream) {
-    k_accumulate_scaled<<<grid1d(n3, kNT), kNT, 0, stream>>>(n3, d, al, P);
+cudaError_t launch_accumulate_scaled(int n3, const float2* d, const float2* pre, double2* P, cudaStream_t stream) {
+    k_accumulate_scaled<<<grid1d(n3, kNT), kNT, 0, stream>>>(n3, d, pre, P);
     return cudaGetLastError();
 }
 cudaError_t launch_fill_ones(long long n, float2* v, cudaStream_t stream) {
