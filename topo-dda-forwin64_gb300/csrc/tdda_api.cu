@@ -825,12 +825,12 @@ tdda_status solve_mixed(tdda_model* const* ms, int n, int max_it, double tol, td
         }
         if (!open) break;
         // FP32 correction: A d = r, d0 = 0, to a relative tolerance that brings
-        // the true residual under tol with margin (0.8 tol: the FP32 recurrence
+        // the true residual under tol with margin (0.9 tol: the FP32 recurrence
         // residual tracks the true one to ~1e-8 of |E| at these tolerances; the
         // outer check catches the rest)
         for (int i = 0; i < n; i++) {
             tdda_model* m = ms[i];
-            double tin = std::min(0.5, std::max(2e-6, 0.8 * tol / std::max(res[i], 1e-300)));
+            double tin = std::min(0.5, std::max(2e-6, 0.9 * tol / std::max(res[i], 1e-300)));
             c->hst[i] = fresh_state(tin, max_it - inner[i], 0);
             if (done[i]) {
                 c->hst[i].status = tdda::ST_CONVERGED;
@@ -1271,7 +1271,7 @@ tdda_status shape_step(Shape* s, std::vector<Done>* done) {
         }
         // 2. the inner solve's start: FP32 right-hand side r, correction 0, a fresh state
         tdda_model* m = sl.m;
-        const double tin = std::min(0.5, std::max(2e-6, 0.8 * sl.tol / std::max(sl.res, 1e-300)));
+        const double tin = std::min(0.5, std::max(2e-6, 0.9 * sl.tol / std::max(sl.res, 1e-300)));
         c->hst[k] = fresh_state(tin, sl.max_it - sl.inner, 0);
         TDDA_CK(cudaMemcpyAsync(c->st32 + k, &c->hst[k], sizeof(SolveState), cudaMemcpyHostToDevice, c->stream));
         TDDA_CK1(tdda::launch_to_f32(3 * m->core->N, m->r, m->fE, c->stream));
