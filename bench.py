@@ -585,14 +585,22 @@ def run_topo(tdda, iters):
         f.append(r.objective)
         its.append(r.iterations)
     dt = time.perf_counter() - t0
-    # the same loop with the Jacobi-preconditioned inner solves, from the same start
-    jloop = topo.TopoLoop(w.Nx, w.Ny, w.Nz, w.d, w.lam, w.material, th0, r_obs, precision=tdda.FP32_JACOBI, tol=TOL)
-    t0 = time.perf_counter()
-    fj = []
-    for _ in range(iters):
-        fj.append(jloop.step().objective)
-    dtj = time.perf_counter() - t0
-    jloop.close()
+    # the same loop with the Jacobi-preconditioned inner solves, from the same start, cold
+    # and with the reference's heritage option (each step's solves start from the last ones)
+    loops = {}
+    for name, her in (("fp32_jacobi_loop", False), ("fp32_jacobi_heritage_loop", True)):
+        jloop = topo.TopoLoop(w.Nx, w.Ny, w.Nz, w.d, w.lam, w.material, th0, r_obs, precision=tdda.FP32_JACOBI,
+                              tol=TOL, origin_heritage=her, adjoint_heritage=her)
+        t0 = time.perf_counter()
+        fj, itj = [], []
+        for _ in range(iters):
+            rj = jloop.step()
+            fj.append(rj.objective)
+            itj.append(rj.iterations)
+        dtj = time.perf_counter() - t0
+        jloop.close()
+        loops[name] = {"s_per_step": dtj / iters, "solves_per_s": 4 * iters / dtj, "objective_last": fj[-1],
+                       "bicgstab_iterations_last": itj[-1]}
     final = {}
     for name, prec in (("fp32_refine", tdda.FP32_REFINE), ("fp32_jacobi", tdda.FP32_JACOBI), ("fp64", tdda.FP64)):
         loop.precision = prec
@@ -605,7 +613,7 @@ def run_topo(tdda, iters):
     return {"steps": iters, "s_per_step": dt / iters, "solves_per_s": 4 * iters / dt,
             "objective_first": f[0], "objective_last": f[-1], "bicgstab_iterations_last": its[-1],
             "final_design": final,
-            "fp32_jacobi_loop": {"s_per_step": dtj / iters, "solves_per_s": 4 * iters / dtj, "objective_last": fj[-1]},
+            **loops,
             "speedup_fp32_refine": final["fp64"]["evaluate_s"] / final["fp32_refine"]["evaluate_s"],
             "speedup_fp32_jacobi": final["fp64"]["evaluate_s"] / final["fp32_jacobi"]["evaluate_s"]}
 

@@ -90,6 +90,31 @@ def test_gradient_ascent_raises_the_objective():
     assert f[-1] > f[0]
 
 
+@pytest.mark.gpu
+def test_heritage_starts_from_the_last_solutions():
+    """origin_heritage / adjoint_heritage (EvoDDAModel.cpp:435-440, 598-604): each step's solves
+    start from the previous step's solutions.  The objectives follow the cold-started loop's to
+    the solves' tolerance, and the warm-started solves take fewer BiCGSTAB steps."""
+    if tdda.device_count() < 1:
+        pytest.skip("no CUDA device")
+    Nx, Ny, Nz, d = 12, 12, 4, 10.0
+    rng = np.random.Generator(np.random.PCG64(19))
+    th0 = 0.4 + 0.2 * rng.random((6, 6))
+    r_obs = (d * (Nx - 1) / 2, d * (Ny - 1) / 2, d * (Nz - 1) + 100.0)
+    out = {}
+    for her in (False, True):
+        loop = topo.TopoLoop(Nx, Ny, Nz, d, 500.0, np.array([1.0, 4.0 + 0.1j]), th0, r_obs, precision=tdda.FP64,
+                             tol=1e-8, origin_heritage=her, adjoint_heritage=her)
+        rs = [loop.step() for _ in range(5)]
+        loop.close()
+        out[her] = ([r.objective for r in rs], [sum(r.iterations) for r in rs])
+    (f0, i0), (f1, i1) = out[False], out[True]
+    assert i1[0] == i0[0]  # the first step starts from P = 0 in both
+    assert sum(i1[1:]) < sum(i0[1:])
+    for a, b in zip(f0, f1):
+        assert abs(a - b) <= 1e-6 * abs(a)
+
+
 def test_adam_moments_follow_the_reference():
     """EvoDDAModel.cpp:673-690: bias correction inside the moving averages, beta2 = 1 - (1-beta1)^2."""
     st = SimpleNamespace(iteration=0, method="Adam", epsilon=0.05, V=None, S_ad=None, gsq=None)

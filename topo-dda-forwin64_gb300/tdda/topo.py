@@ -215,8 +215,13 @@ class TopoLoop:
 
     def __init__(self, Nx, Ny, Nz, d, lam, material, theta0, r_obs, precision=FP32_REFINE, tol=1e-5,
                  max_it=10000, nK=(0.0, 0.0, 1.0), nE0=(1.0, 0.0, 0.0), E0=1.0, filter_r=2.0, epsilon=0.1,
-                 method="grad", projection: Projection = None, max_steps: int = 200, chain: str = "exact"):
-        """projection: the smooth Heaviside applied after the filter, its beta scheduled over
+                 method="grad", projection: Projection = None, max_steps: int = 200, chain: str = "exact",
+                 origin_heritage: bool = False, adjoint_heritage: bool = False):
+        """origin_heritage / adjoint_heritage: start each step's forward / adjoint solves from
+        the previous step's solutions instead of P = 0 (the reference's HaveOriginHeritage and
+        HaveAdjointHeritage, EvoDDAModel.cpp:435-440, 598-604; its main.cpp sets both false,
+        the default here).
+        projection: the smooth Heaviside applied after the filter, its beta scheduled over
         max_steps steps (the reference's MAX_ITERATION_EVO); chain "exact" (the transposed
         chain rule through filter and projection, checked against finite differences) or
         "reference" (the reference's diagonal form of gradients_filtered,
@@ -232,6 +237,7 @@ class TopoLoop:
         if chain not in ("exact", "reference"):
             raise ValueError(f"unknown chain rule {chain!r}")
         self.projection, self.max_steps, self.chain = projection, int(max_steps), chain
+        self.origin_heritage, self.adjoint_heritage = bool(origin_heritage), bool(adjoint_heritage)
         self.iteration = 0
         self.core = AProductCore(Nx, Ny, Nz, self.R, d, lam, material, max_rhs=4)
         self.K = self.core.K
@@ -282,9 +288,11 @@ class TopoLoop:
         """Solve forward + adjoints at the current theta; return f and df/dtheta."""
         diel = self._diel()
         models = [self.fwd] + self.adj
-        for m in models:
+        for k, m in enumerate(models):
             m.UpdateAlpha(diel)
-            m.InitializeP()
+            # a model keeps its last solution on the device: heritage starts from it
+            if not (self.origin_heritage if k == 0 else self.adjoint_heritage):
+                m.InitializeP()
         infos = solve_batch(models, self.precision, self.max_it, self.tol)
         E_obs = self.fwd.field_at(self.r_obs[None, :])[0]  # E_inc(r_obs) - sum_j A(r_obs - r_j) P_j
         f = float(np.sum(np.abs(E_obs) ** 2))
