@@ -457,8 +457,12 @@ class DDAModel:
         self.last_info = info.as_dict()
         return self.last_info
 
-    def solve_mixed(self, MAX_ITERATION: int, MAX_ERROR: float) -> dict:
-        """FP32 BiCGSTAB with FP64 refinement to MAX_ERROR."""
+    def solve_mixed(self, MAX_ITERATION: int, MAX_ERROR: float, jacobi: bool = False) -> dict:
+        """FP32 BiCGSTAB with FP64 refinement to MAX_ERROR; jacobi: the inner solve
+        right-preconditioned by diag(al) (TDDA_FP32_JACOBI)."""
+        if jacobi:
+            [info] = solve_batch([self], FP32_JACOBI, MAX_ITERATION, MAX_ERROR)
+            return info
         info = SolveInfo()
         load().tdda_model_solve_mixed(self.h, int(MAX_ITERATION), float(MAX_ERROR), ctypes.byref(info))
         _check(info.status, "solve_mixed", allowed=(OK, NOT_CONVERGED, BREAKDOWN))
