@@ -52,7 +52,11 @@ typedef enum tdda_precision {
                             so results meet the same tolerance; the inner iterates differ from
                             the reference's recurrence.  No counterpart in the reference.  For
                             the solves (tdda_solve_batch, tdda_solve_multi_precision, the server),
-                            not for single products */
+                            not for single products */,
+    TDDA_FP32_AUTO = 3    /* per right-hand side, TDDA_FP32_JACOBI where its |al| varies by more
+                            than 4x over the dipoles (densities that mix near-vacuum and dense
+                            dipoles), else TDDA_FP32_REFINE; one small reduction per solve.  No
+                            counterpart in the reference */
 } tdda_precision;
 typedef enum tdda_field {
     TDDA_FIELD_P = 0,
@@ -202,7 +206,7 @@ tdda_status tdda_solve_batch(tdda_model* const* models, int n, int precision, in
 tdda_status tdda_solve_multi(tdda_model* const* models, int n, int max_it, double max_err,
                              tdda_solve_info* infos);
 /* tdda_solve_multi with the inner solves' precision: TDDA_FP32_REFINE (the same
- * as tdda_solve_multi) or TDDA_FP32_JACOBI. */
+ * as tdda_solve_multi), TDDA_FP32_JACOBI or TDDA_FP32_AUTO. */
 tdda_status tdda_solve_multi_precision(tdda_model* const* models, int n, int precision, int max_it,
                                        double max_err, tdda_solve_info* infos);
 
@@ -231,7 +235,7 @@ typedef struct tdda_server_desc {
     int device;
     double hbm_budget_bytes;  /* device memory the requests in flight may hold */
     int workers;              /* requests solved concurrently (one stream each) */
-    int precision;            /* TDDA_FP64, TDDA_FP32_REFINE or TDDA_FP32_JACOBI */
+    int precision;            /* TDDA_FP64, TDDA_FP32_REFINE, TDDA_FP32_JACOBI or TDDA_FP32_AUTO */
     int max_it;
     double tol;
     int max_group;            /* right-hand sides of one batched solve, or the slots of one

@@ -139,3 +139,23 @@ def test_served_jacobi_requests_equal_each_request_alone():
             assert np.array_equal(P[k], m.get_P())
             m.close()
         core.close()
+
+
+def test_auto_takes_jacobi_where_al_varies():
+    """TDDA_FP32_AUTO per right-hand side: Jacobi on cfg 1's random densities (|al| over two
+    decades), plain FP32+refine on cfg 2's box-filtered ones (|al| within 2x); each result is
+    bit-identical to the solve with the explicit choice."""
+    for cfg, expect in ((1, tdda.FP32_JACOBI), (2, tdda.FP32_REFINE)):
+        w = lattice.config(cfg)
+        inc = w.incidences[0]
+        c = tdda.AProductCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material, w.nback)
+        out = {}
+        for prec in (tdda.FP32_AUTO, expect):
+            m = tdda.DDAModel(c, inc.nK, inc.E0, inc.nE0, w.diel_old)
+            [info] = tdda.solve_batch([m], prec, 10000, 1e-5)
+            assert info["status"] == tdda.OK and info["true_residual"] <= 1e-5
+            out[prec] = (m.get_P(), info["inner_iterations"])
+            m.close()
+        assert out[tdda.FP32_AUTO][1] == out[expect][1]
+        assert np.array_equal(out[tdda.FP32_AUTO][0], out[expect][0]), cfg
+        c.close()

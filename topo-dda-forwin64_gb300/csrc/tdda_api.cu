@@ -182,6 +182,7 @@ struct tdda_core_s {
     // host-launched graph, not those of a device-side loop's body)
     bool device_loop = true;
     float2* ones32 = nullptr;  // 3N entries of 1 (the sinks' diagonal of a Jacobi-preconditioned solve)
+    unsigned int* alr = nullptr;  // max and min |al|^2 of a model (TDDA_FP32_AUTO's choice)
     // batch schedule of the FP32 products: right-hand sides per launch (0: all of a
     // batch in one launch per pass).  Groups run one after another, each through all
     // of its passes, so a group's FFT work grid can stay in L2 between the passes.
@@ -440,6 +441,38 @@ tdda_status prepare_jacobi(tdda_model* m) {
     }
     TDDA_CK1(tdda::launch_recip_f32((int)n3, m->fal, m->fpre, c->stream));
     return TDDA_OK;
+}
+
+// TDDA_FP32_AUTO: precondition when |al| varies by more than kJacobiSpread
+// over the model's dipoles (the preconditioner pays its extra load where al is
+// nearly constant, and cuts the steps 5-10x where low- and high-density dipoles
+// mix).  Reads the FP32 al, so after model_alloc_f32.
+constexpr float kJacobiSpread = 4.f;
+tdda_status wants_jacobi(tdda_model* m, bool* out) {
+    tdda_core* c = m->core;
+    if (!c->alr) TDDA_TRY(dalloc_c(c, &c->alr, 2));
+    TDDA_CK1(tdda::launch_al_range(3 * c->N, m->fal, c->alr, c->stream));
+    unsigned int h[2] = {0u, 0u};
+    TDDA_CK(cudaMemcpyAsync(h, c->alr, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    TDDA_CK(cudaStreamSynchronize(c->stream));
+    float hi, lo;
+    std::memcpy(&hi, &h[0], sizeof(float));
+    std::memcpy(&lo, &h[1], sizeof(float));
+    *out = hi > kJacobiSpread * kJacobiSpread * lo;
+    return TDDA_OK;
+}
+
+// the preconditioning of a model's FP32 inner solves: mode 0 none, 1 Jacobi,
+// 2 chosen by wants_jacobi (TDDA_FP32_REFINE, _JACOBI, _AUTO)
+tdda_status set_preconditioner(tdda_model* m, int mode) {
+    bool j = mode == 1;
+    if (mode == 2) TDDA_TRY(wants_jacobi(m, &j));
+    m->jacobi = j;
+    if (j) TDDA_TRY(prepare_jacobi(m));
+    return TDDA_OK;
+}
+int precond_mode(int precision) {
+    return precision == TDDA_FP32_JACOBI ? 1 : precision == TDDA_FP32_AUTO ? 2 : 0;
 }
 
 // P (FP64) += the inner solve's correction: d, or D^-1 d for a Jacobi-preconditioned solve
@@ -761,12 +794,11 @@ tdda_status solve_fp64(tdda_model* const* ms, int n, int max_it, double tol, tdd
 // Mixed precision: FP32 BiCGSTAB on the FP64 residual, FP64 accumulation of
 // the correction, FP64 residual check, until |E - A P| / |E| <= tol.
 tdda_status solve_mixed(tdda_model* const* ms, int n, int max_it, double tol, tdda_solve_info* infos,
-                        bool jacobi = false) {
+                        int precond = 0) {
     tdda_core* c = ms[0]->core;
     for (int i = 0; i < n; i++) {
         TDDA_TRY(model_alloc_f32(ms[i]));
-        ms[i]->jacobi = jacobi;
-        if (jacobi) TDDA_TRY(prepare_jacobi(ms[i]));
+        TDDA_TRY(set_preconditioner(ms[i], precond));
     }
     std::vector<RhsVecs<double>> h64(n);
     std::vector<RhsVecs<float>> h32(n);
@@ -1095,7 +1127,7 @@ double model_bytes(int N, int precision) {
     const double n3 = 3.0 * N;
     double model = n3 * (12 * 16 + 8);  // FP64 vectors and densities
     if (precision == TDDA_FP32_REFINE) model += n3 * 10 * 8;
-    if (precision == TDDA_FP32_JACOBI) model += n3 * 11 * 8;  // and 1 / al
+    if (precision == TDDA_FP32_JACOBI || precision == TDDA_FP32_AUTO) model += n3 * 11 * 8;  // and 1 / al
     return model;
 }
 
@@ -1210,7 +1242,7 @@ int shape_active(const Shape* s) {
     return n;
 }
 
-tdda_status shape_admit(Shape* s, tdda_model* m, int max_it, double tol, int* slot, bool jacobi) {
+tdda_status shape_admit(Shape* s, tdda_model* m, int max_it, double tol, int* slot, int precond) {
     if (!shape_accepts(s, m)) {
         set_err("the model's core does not share the shape's FFT grid");
         return TDDA_ERR_INVALID_ARGUMENT;
@@ -1223,8 +1255,7 @@ tdda_status shape_admit(Shape* s, tdda_model* m, int max_it, double tol, int* sl
     }
     TDDA_TRY(set_device(s->c->device));
     TDDA_TRY(model_alloc_f32(m));
-    m->jacobi = jacobi;
-    if (jacobi) TDDA_TRY(prepare_jacobi(m));
+    TDDA_TRY(set_preconditioner(m, precond));
     TDDA_CK(cudaStreamSynchronize(m->core->stream));
     Slot& sl = s->slots[k];
     sl = Slot{};
@@ -1907,14 +1938,14 @@ tdda_status tdda_solve_batch(tdda_model* const* ms, int n, int precision, int ma
                              tdda_solve_info* infos) {
     g_err.clear();
     TDDA_TRY(check_batch(ms, n));
-    if (!(max_err >= 0) ||
-        (precision != TDDA_FP64 && precision != TDDA_FP32_REFINE && precision != TDDA_FP32_JACOBI)) {
+    if (!(max_err >= 0) || (precision != TDDA_FP64 && precision != TDDA_FP32_REFINE &&
+                            precision != TDDA_FP32_JACOBI && precision != TDDA_FP32_AUTO)) {
         set_err("invalid tolerance or precision");
         return TDDA_ERR_INVALID_ARGUMENT;
     }
     TDDA_TRY(set_device(ms[0]->core->device));
     if (precision == TDDA_FP64) return solve_fp64(ms, n, max_it, max_err, infos);
-    return solve_mixed(ms, n, max_it, max_err, infos, precision == TDDA_FP32_JACOBI);
+    return solve_mixed(ms, n, max_it, max_err, infos, precond_mode(precision));
 }
 
 namespace {
@@ -1937,7 +1968,7 @@ tdda_status tdda_solve_multi_precision(tdda_model* const* ms, int n, int precisi
                                        tdda_solve_info* infos) {
     g_err.clear();
     if (!ms || n < 1 || n > 64 || !(max_err >= 0) ||
-        (precision != TDDA_FP32_REFINE && precision != TDDA_FP32_JACOBI)) {
+        (precision != TDDA_FP32_REFINE && precision != TDDA_FP32_JACOBI && precision != TDDA_FP32_AUTO)) {
         set_err("invalid batch, precision, tolerance or size (1..64 right-hand sides)");
         return TDDA_ERR_INVALID_ARGUMENT;
     }
@@ -1979,7 +2010,7 @@ tdda_status tdda_solve_multi_precision(tdda_model* const* ms, int n, int precisi
     tdda_status worst = TDDA_OK;
     tdda_status st = TDDA_OK;
     for (int i = 0; i < n && st == TDDA_OK; i++)
-        st = tdda_session::shape_admit(sh, ms[i], max_it, max_err, nullptr, precision == TDDA_FP32_JACOBI);
+        st = tdda_session::shape_admit(sh, ms[i], max_it, max_err, nullptr, precond_mode(precision));
     std::vector<tdda_session::Done> done;
     while (st == TDDA_OK && tdda_session::shape_active(sh) > 0) st = tdda_session::shape_step(sh, &done);
     if (st != TDDA_OK) {

@@ -315,6 +315,8 @@ cudaError_t launch_accumulate(int n3, const float2* d, double2* P, cudaStream_t 
 cudaError_t launch_recip_f32(int n3, const float2* al, float2* pre, cudaStream_t stream);
 cudaError_t launch_accumulate_scaled(int n3, const float2* d, const float2* pre, double2* P, cudaStream_t stream);
 cudaError_t launch_fill_ones(long long n, float2* v, cudaStream_t stream);
+// max and min |al|^2 of a model's FP32 al (as float bits) into out[0], out[1]
+cudaError_t launch_al_range(int n3, const float2* al, unsigned int* out, cudaStream_t stream);
 template <typename T> cudaError_t launch_zero(long long n, cx<T>* v, cudaStream_t stream);
 
 // generic in-place 3-D FFT of a contiguous (n0, n1, n2) double2 array

@@ -538,6 +538,25 @@ __global__ void k_accumulate_scaled(int n3, const float2* d, const float2* pre, 
         P[e] = make_double2(P[e].x + (double)vx, P[e].y + (double)vy);
     }
 }
+// the largest and smallest |al|^2 of a model (positive floats compare as their
+// bit patterns): out[0] max, out[1] min, set to 0 and ~0 before the launch
+__global__ void k_al_range(int n3, const float2* __restrict__ al, unsigned int* __restrict__ out) {
+    float hi = 0.f, lo = 3.0e38f;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n3; e += gridDim.x * blockDim.x) {
+        const float2 a = al[e];
+        const float m = a.x * a.x + a.y * a.y;
+        hi = fmaxf(hi, m);
+        lo = fminf(lo, m);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        hi = fmaxf(hi, __shfl_down_sync(0xffffffffu, hi, o));
+        lo = fminf(lo, __shfl_down_sync(0xffffffffu, lo, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(out, __float_as_uint(hi));
+        atomicMin(out + 1, __float_as_uint(lo));
+    }
+}
 __global__ void k_fill_ones(long long n, float2* v) {
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
         v[e] = make_float2(1.f, 0.f);
@@ -808,6 +827,13 @@ cudaError_t launch_recip_f32(int n3, const float2* al, float2* pre, cudaStream_t
 }
 cudaError_t launch_accumulate_scaled(int n3, const float2* d, const float2* pre, double2* P, cudaStream_t stream) {
     k_accumulate_scaled<<<grid1d(n3, kNT), kNT, 0, stream>>>(n3, d, pre, P);
+    return cudaGetLastError();
+}
+cudaError_t launch_al_range(int n3, const float2* al, unsigned int* out, cudaStream_t stream) {
+    const unsigned int init[2] = {0u, 0xffffffffu};
+    cudaError_t e = cudaMemcpyAsync(out, init, sizeof(init), cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return e;
+    k_al_range<<<std::min(grid1d(n3, kNT), 152 * 8), kNT, 0, stream>>>(n3, al, out);
     return cudaGetLastError();
 }
 cudaError_t launch_fill_ones(long long n, float2* v, cudaStream_t stream) {

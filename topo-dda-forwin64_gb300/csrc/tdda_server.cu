@@ -487,7 +487,9 @@ void tdda_server_s::run_fp32(int me) {
             for (size_t k = 0; k < ms.size() && s2 == TDDA_OK; k++) {
                 int slot = -1;
                 s2 = tdda_session::shape_admit(sh, ms[k], desc.max_it, desc.tol, &slot,
-                                               desc.precision == TDDA_FP32_JACOBI);
+                                               desc.precision == TDDA_FP32_JACOBI ? 1
+                                               : desc.precision == TDDA_FP32_AUTO ? 2
+                                                                                  : 0);
                 if (s2 == TDDA_OK) slot_of[slot] = {r, (int)k}, slot_model[slot] = ms[k], used++;
             }
             if (s2 != TDDA_OK) {
@@ -614,7 +616,8 @@ extern "C" {
 tdda_status tdda_server_create(const tdda_server_desc* desc, tdda_server** out) {
     if (!desc || !out || desc->workers < 1 || desc->workers > 64 || !(desc->hbm_budget_bytes > 0) ||
         desc->max_group < 1 || desc->max_group > 64 ||
-        (desc->precision != TDDA_FP64 && desc->precision != TDDA_FP32_REFINE && desc->precision != TDDA_FP32_JACOBI))
+        (desc->precision != TDDA_FP64 && desc->precision != TDDA_FP32_REFINE && desc->precision != TDDA_FP32_JACOBI &&
+         desc->precision != TDDA_FP32_AUTO))
         return TDDA_ERR_INVALID_ARGUMENT;
     if (!desc->dry_run && tdda_device_count() < 1) return TDDA_ERR_NO_DEVICE;
     tdda_server* s = new tdda_server_s();

@@ -45,8 +45,9 @@ bool shape_accepts(const Shape* s, const tdda_model* m);
 int shape_cap(const Shape* s);
 int shape_active(const Shape* s);
 // takes a free slot for model m (P as the model holds it: zero or a warm start);
-// jacobi: its inner solves are right-preconditioned by diag(al) (TDDA_FP32_JACOBI)
-tdda_status shape_admit(Shape* s, tdda_model* m, int max_it, double tol, int* slot, bool jacobi = false);
+// precond: its inner solves' preconditioning, 0 none, 1 Jacobi (TDDA_FP32_JACOBI),
+// 2 chosen from the model's al (TDDA_FP32_AUTO)
+tdda_status shape_admit(Shape* s, tdda_model* m, int max_it, double tol, int* slot, int precond = 0);
 // One round: the refinement residual of every slot that needs one (on its own
 // core), the start of the inner solves that follow, one launch of the
 // device-side loop of the inner solves (at most 8 chunks of 4 steps), and the

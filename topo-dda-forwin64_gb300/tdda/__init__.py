@@ -30,7 +30,7 @@ OK, ERR_INVALID_ARGUMENT, ERR_CUDA, ERR_OUT_OF_MEMORY, ERR_UNSUPPORTED = 0, 1, 2
 NOT_CONVERGED, BREAKDOWN, ERR_NAN, ERR_NO_DEVICE = 5, 6, 7, 8
 STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "cuda error", 3: "out of memory", 4: "unsupported",
                 5: "not converged", 6: "breakdown", 7: "nan", 8: "no device"}
-FP64, FP32_REFINE, FP32_JACOBI = 0, 1, 2
+FP64, FP32_REFINE, FP32_JACOBI, FP32_AUTO = 0, 1, 2, 3
 MEM_HOST, MEM_DEVICE = 0, 1
 FIELD_P, FIELD_E, FIELD_AL, FIELD_DIEL, FIELD_EINTERNAL = 0, 1, 2, 3, 4
 METHODS = {"LDR": 0, "FCD": 1}
