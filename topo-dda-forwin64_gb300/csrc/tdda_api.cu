@@ -373,7 +373,7 @@ tdda::AlphaParams alpha_params(const tdda_model* m) {
     return ap;
 }
 
-tdda_status model_upload_fields(tdda_model* m, bool field_E, bool field_al) {
+tdda_status model_upload_fields(tdda_model* m, bool field_E, bool field_al, const double* diel_old = nullptr) {
     tdda_core* c = m->core;
     const int N = c->N;
     if (field_E) {
@@ -387,8 +387,8 @@ tdda_status model_upload_fields(tdda_model* m, bool field_E, bool field_al) {
         // eps and al on the device (DDAModel.cpp:54-63, tools.cpp:617-630) from
         // the densities the caller checked with densities_in_table
         const tdda::AlphaParams ap = alpha_params(m);
-        TDDA_CK(cudaMemcpyAsync(m->dold, m->diel_old.data(), sizeof(double) * 3 * (size_t)N, cudaMemcpyHostToDevice,
-                                c->stream));
+        TDDA_CK(cudaMemcpyAsync(m->dold, diel_old ? diel_old : m->diel_old.data(), sizeof(double) * 3 * (size_t)N,
+                                cudaMemcpyHostToDevice, c->stream));
         TDDA_CK1(tdda::launch_model_alpha(3 * N, m->dold, ap, m->diel, m->al, m->fal, c->stream));
         TDDA_CK(cudaStreamSynchronize(c->stream));
     }
@@ -1386,12 +1386,11 @@ tdda_status model_reinit(tdda_model* m, const double* nK, double E0, const doubl
         m->nE0[j] = nE0[j];
     }
     m->E0 = E0;
-    m->diel_old.assign(diel_old, diel_old + 3 * (size_t)c->N);
-    m->dold_host_stale = false;
+    m->dold_host_stale = true;  // uploaded straight from the caller; the host copy follows on demand
     const size_t n3 = 3 * (size_t)c->N;
     TDDA_CK(cudaMemsetAsync(m->P, 0, sizeof(double2) * n3, c->stream));
     TDDA_CK(cudaMemsetAsync(m->Ein, 0, sizeof(double2) * n3, c->stream));
-    TDDA_TRY(model_upload_fields(m, true, true));
+    TDDA_TRY(model_upload_fields(m, true, true, diel_old));
     m->P_zero = true;
     m->ITERATION = 0;
     m->Error = 0.0;
@@ -1775,7 +1774,7 @@ tdda_status tdda_model_create(tdda_core* c, const double* nK, double E0, const d
     }
     m->E0 = E0;
     const size_t n3 = 3 * (size_t)c->N;
-    m->diel_old.assign(diel_old, diel_old + n3);
+    m->dold_host_stale = true;  // uploaded straight from the caller; the host copy follows on demand
     double2** v[] = {&m->P, &m->E, &m->al, &m->diel, &m->Ein, &m->r, &m->r0, &m->p, &m->u, &m->t, &m->Ap, &m->At};
     for (double2** q : v) {
         tdda_status s = dalloc(m->allocs, q, n3, c->stream);
@@ -1797,7 +1796,7 @@ tdda_status tdda_model_create(tdda_core* c, const double* nK, double E0, const d
         tdda_model_destroy(m);
         return cuda_fail(e, "cudaMemsetAsync");
     }
-    tdda_status s = model_upload_fields(m, true, true);
+    tdda_status s = model_upload_fields(m, true, true, diel_old);
     if (s != TDDA_OK) {
         tdda_model_destroy(m);
         return s;
@@ -1850,6 +1849,7 @@ tdda_status tdda_model_update_alpha(tdda_model* m, const double* diel_old) {
 static tdda_status host_densities(tdda_model* m) {
     if (!m->dold_host_stale) return TDDA_OK;
     tdda_core* c = m->core;
+    m->diel_old.resize(3 * (size_t)c->N);
     TDDA_CK(cudaMemcpyAsync(m->diel_old.data(), m->dold, sizeof(double) * 3 * (size_t)c->N, cudaMemcpyDeviceToHost,
                             c->stream));
     TDDA_CK(cudaStreamSynchronize(c->stream));
