@@ -327,8 +327,10 @@ __global__ void k_green_fold(Geom g, const double2* __restrict__ full6, double2*
 
 // ------------------------------------------------------- generic FFT passes
 // rows: nrows contiguous lines of length M
+// nout: outputs m >= nout are neither formed in the last stage nor stored (the
+// Green spectrum keeps only the octant k <= M / 2 of each axis)
 __global__ void __launch_bounds__(kNT) k_fft_rows(double2* __restrict__ data, long long nrows, AxisPlan p,
-                                                  const double2* __restrict__ tw, int sign) {
+                                                  const double2* __restrict__ tw, int sign, int nout) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int M = p.M;
     const int L = row_lines(p);
@@ -344,11 +346,11 @@ __global__ void __launch_bounds__(kNT) k_fft_rows(double2* __restrict__ data, lo
         s[line * MP + m] = data[(r0 + line) * M + m];
     }
     __syncthreads();
-    const double2* res = sign < 0 ? smem_fft<-1, double>(s, s2, L, MP, 1, p, stw, M, M)
-                                  : smem_fft<+1, double>(s, s2, L, MP, 1, p, stw, M, M);
+    const double2* res = sign < 0 ? smem_fft<-1, double>(s, s2, L, MP, 1, p, stw, M, nout)
+                                  : smem_fft<+1, double>(s, s2, L, MP, 1, p, stw, M, nout);
     for (int e = threadIdx.x; e < nl * M; e += blockDim.x) {
         const int line = e / M, m = e - (e / M) * M;
-        data[(r0 + line) * M + m] = res[line * MP + m];
+        if (m < nout) data[(r0 + line) * M + m] = res[line * MP + m];
     }
 }
 
@@ -356,7 +358,7 @@ __global__ void __launch_bounds__(kNT) k_fft_rows(double2* __restrict__ data, lo
 // contiguous; off(o) = (o / o1) * s1 + (o % o1) * s2
 __global__ void __launch_bounds__(kNT) k_fft_cols(double2* __restrict__ data, int nouter, int o1, long long s1,
                                                   long long s2, long long ms, int ninner, AxisPlan p,
-                                                  const double2* __restrict__ tw, int sign) {
+                                                  const double2* __restrict__ tw, int sign, int nout) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int M = p.M;
     const int ZT = col_tile(p);
@@ -373,9 +375,9 @@ __global__ void __launch_bounds__(kNT) k_fft_cols(double2* __restrict__ data, in
         s[e] = zl < zn ? base[m * ms + zl] : make_double2(0.0, 0.0);
     }
     __syncthreads();
-    const double2* res = sign < 0 ? smem_fft<-1, double>(s, sb2, ZT, 1, ZT, p, stw, M, M)
-                                  : smem_fft<+1, double>(s, sb2, ZT, 1, ZT, p, stw, M, M);
-    for (int e = threadIdx.x; e < M * ZT; e += blockDim.x) {
+    const double2* res = sign < 0 ? smem_fft<-1, double>(s, sb2, ZT, 1, ZT, p, stw, M, nout)
+                                  : smem_fft<+1, double>(s, sb2, ZT, 1, ZT, p, stw, M, nout);
+    for (int e = threadIdx.x; e < nout * ZT; e += blockDim.x) {
         const int m = e / ZT, zl = e - (e / ZT) * ZT;
         if (zl < zn) base[m * ms + zl] = res[e];
     }
@@ -630,17 +632,18 @@ int max_blocks_per_rhs(const Geom& g) {
 // ------------------------------------------------------------------ launchers
 namespace {
 cudaError_t fft_rows(double2* data, long long nrows, const AxisPlan& p, const double2* tw, int sign,
-                     cudaStream_t stream) {
+                     cudaStream_t stream, int nout = 0) {
     const int L = row_lines(p);
-    k_fft_rows<<<(unsigned)((nrows + L - 1) / L), kNT, rowsmem(p), stream>>>(data, nrows, p, tw, sign);
+    k_fft_rows<<<(unsigned)((nrows + L - 1) / L), kNT, rowsmem(p), stream>>>(data, nrows, p, tw, sign,
+                                                                              nout > 0 ? nout : p.M);
     return cudaGetLastError();
 }
 cudaError_t fft_cols(double2* data, int nouter, int o1, long long s1, long long s2, long long ms, int ninner,
-                     const AxisPlan& p, const double2* tw, int sign, cudaStream_t stream) {
+                     const AxisPlan& p, const double2* tw, int sign, cudaStream_t stream, int nout = 0) {
     const int ZT = col_tile(p);
     const int nt = (ninner + ZT - 1) / ZT;
     k_fft_cols<<<(unsigned)(nouter * nt), kNT, colsmem(p), stream>>>(data, nouter, o1, s1, s2, ms, ninner, p, tw,
-                                                                      sign);
+                                                                      sign, nout > 0 ? nout : p.M);
     return cudaGetLastError();
 }
 }  // namespace
@@ -663,10 +666,13 @@ cudaError_t launch_green(const Geom& g, double K, double d, const double2* twx, 
         err = cudaGetLastError();
     }
     // the six components form a (6 Mx, My, Mz) array for the z and y axes;
-    // the x axis runs over the outer pairs (component, y)
-    if (!err) err = fft_rows(full6, 6LL * Mx * My, g.pz, twz, -1, stream);
-    if (!err) err = fft_cols(full6, 6 * Mx, 6 * Mx, 0, (long long)My * Mz, Mz, Mz, g.py, twy, -1, stream);
-    if (!err) err = fft_cols(full6, 6 * My, My, M, Mz, (long long)My * Mz, Mz, g.px, twx, -1, stream);
+    // the x axis runs over the outer pairs (component, y).  Only the octant
+    // k <= M / 2 of each axis is folded, so each axis forms only those outputs,
+    // and the later axes transform only the lines of the kept indices: the y
+    // pass the columns kz < Hz, the x pass the columns ky < Hy, kz < Hz.
+    if (!err) err = fft_rows(full6, 6LL * Mx * My, g.pz, twz, -1, stream, g.Hz);
+    if (!err) err = fft_cols(full6, 6 * Mx, 6 * Mx, 0, (long long)My * Mz, Mz, g.Hz, g.py, twy, -1, stream, g.Hy);
+    if (!err) err = fft_cols(full6, 6 * g.Hy, g.Hy, M, Mz, (long long)My * Mz, g.Hz, g.px, twx, -1, stream, g.Hx);
     if (err) return err;
     const long long H6 = 6LL * g.Hx * g.Hy * g.Hz;
     k_green_fold<<<grid1d(H6, kNT), kNT, 0, stream>>>(g, full6, green64, green32);
