@@ -1648,8 +1648,9 @@ tdda_status core_create(const tdda_core_desc* desc, const tdda::PeriodicImages* 
     double2* full6 = nullptr;
     double2* oct = nullptr;
     TDDA_CORE_CK(cudaMallocAsync((void**)&full6, sizeof(double2) * 6 * (size_t)Mfull, c->stream));
-    if (pi) TDDA_CORE_CK(cudaMallocAsync((void**)&oct, sizeof(double2) * 6 * (size_t)g.Nx * g.Ny * g.Nz, c->stream));
-    count_launches(pi ? 6 : 5);
+    // the octant of lattice offsets (both forms: the tensor is even or odd in each axis)
+    TDDA_CORE_CK(cudaMallocAsync((void**)&oct, sizeof(double2) * 6 * (size_t)g.Nx * g.Ny * g.Nz, c->stream));
+    count_launches(6);
     cudaError_t ge = tdda::launch_green(g, c->K, c->d, c->tw64[0], c->tw64[1], c->tw64[2], full6, c->green64,
                                         c->green32, c->stream, c->inter, pi, oct);
     cudaError_t fe = cudaFreeAsync(full6, c->stream);

@@ -156,28 +156,6 @@ __global__ void __launch_bounds__(kNT) k_chunk_end(const RhsVecs<float>* __restr
 }
 
 // ================================================================ K0 green
-__global__ void k_green_real(Geom g, double K, double d, Interaction it, double2* __restrict__ full6) {
-    const int Mx = g.px.M, My = g.py.M, Mz = g.pz.M;
-    const long long M = (long long)Mx * My * Mz;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < M; e += (long long)gridDim.x * blockDim.x) {
-        const int k = (int)(e % Mz);
-        const int j = (int)((e / Mz) % My);
-        const int i = (int)(e / ((long long)Mz * My));
-        // signed lattice offset of each grid index (AProductCore.cpp:53-194)
-        int ox = i < g.Nx ? i : (i > Mx - g.Nx ? i - Mx : INT32_MIN);
-        int oy = j < g.Ny ? j : (j > My - g.Ny ? j - My : INT32_MIN);
-        int oz = k < g.Nz ? k : (k > Mz - g.Nz ? k - Mz : INT32_MIN);
-        double2 t[6];
-        if (ox != INT32_MIN && oy != INT32_MIN && oz != INT32_MIN) {
-            interaction_tensor(it, K, d, d * ox, d * oy, d * oz, t);
-        } else {
-#pragma unroll
-            for (int l = 0; l < 6; l++) t[l] = make_double2(0.0, 0.0);
-        }
-#pragma unroll
-        for (int l = 0; l < 6; l++) full6[l * M + e] = t[l];
-    }
-}
 
 // ================================================================ field at points
 // E(r_p) = E_ext(r_p) - sum_i A(r_p - d R_i) P_i (ObjDDAModel.cpp:42-96,
@@ -271,6 +249,23 @@ __global__ void __launch_bounds__(kNT) k_green_periodic_octant(Geom g, double K,
 
 // the full padded grid from the octant: xx, yy, zz even in every axis; xy odd
 // in x and y, xz in x and z, yz in y and z
+// The tensor at the octant of lattice offsets (0 <= o < N on each axis), one
+// thread per offset: every other offset differs only by the sign of the odd
+// components (xy odd in x and y, xz in x and z, yz in y and z), which
+// k_green_expand applies, so the FP64 tensor is evaluated Nx Ny Nz times
+// instead of once per grid point.
+__global__ void k_green_octant(Geom g, double K, double d, Interaction it, double2* __restrict__ oct) {
+    const long long n = (long long)g.Nx * g.Ny * g.Nz;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int oz = (int)(e % g.Nz);
+        const int oy = (int)((e / g.Nz) % g.Ny);
+        const int ox = (int)(e / ((long long)g.Nz * g.Ny));
+        double2 t[6];
+        interaction_tensor(it, K, d, d * ox, d * oy, d * oz, t);
+#pragma unroll
+        for (int l = 0; l < 6; l++) oct[e * 6 + l] = t[l];
+    }
+}
 __global__ void k_green_expand(Geom g, const double2* __restrict__ oct, double2* __restrict__ full6) {
     const int Mx = g.px.M, My = g.py.M, Mz = g.pz.M;
     const long long M = (long long)Mx * My * Mz;
@@ -662,8 +657,13 @@ cudaError_t launch_green(const Geom& g, double K, double d, const double2* twx, 
             err = cudaGetLastError();
         }
     } else {
-        k_green_real<<<grid1d(M, kNT), kNT, 0, stream>>>(g, K, d, it, full6);
+        const long long n = (long long)g.Nx * g.Ny * g.Nz;
+        k_green_octant<<<grid1d(n, kNT), kNT, 0, stream>>>(g, K, d, it, oct);
         err = cudaGetLastError();
+        if (!err) {
+            k_green_expand<<<grid1d(M, kNT), kNT, 0, stream>>>(g, oct, full6);
+            err = cudaGetLastError();
+        }
     }
     // the six components form a (6 Mx, My, Mz) array for the z and y axes;
     // the x axis runs over the outer pairs (component, y).  Only the octant
