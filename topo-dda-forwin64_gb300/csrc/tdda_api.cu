@@ -182,7 +182,6 @@ struct tdda_core_s {
     // host-launched graph, not those of a device-side loop's body)
     bool device_loop = true;
     float2* ones32 = nullptr;  // 3N entries of 1 (the sinks' diagonal of a Jacobi-preconditioned solve)
-    unsigned int* alr = nullptr;  // max and min |al|^2 of a model (TDDA_FP32_AUTO's choice)
     // batch schedule of the FP32 products: right-hand sides per launch (0: all of a
     // batch in one launch per pass).  Groups run one after another, each through all
     // of its passes, so a group's FFT work grid can stay in L2 between the passes.
@@ -450,14 +449,12 @@ tdda_status prepare_jacobi(tdda_model* m) {
 constexpr float kJacobiSpread = 4.f;
 tdda_status wants_jacobi(tdda_model* m, bool* out) {
     tdda_core* c = m->core;
-    if (!c->alr) TDDA_TRY(dalloc_c(c, &c->alr, 2));
-    TDDA_CK1(tdda::launch_al_range(3 * c->N, m->fal, c->alr, c->stream));
-    unsigned int h[2] = {0u, 0u};
-    TDDA_CK(cudaMemcpyAsync(h, c->alr, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    TDDA_CK1(tdda::launch_al_range(3 * c->N, m->fal, c->flag + 1, c->stream));
+    TDDA_CK(cudaMemcpyAsync(c->hflag + 1, c->flag + 1, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
     TDDA_CK(cudaStreamSynchronize(c->stream));
     float hi, lo;
-    std::memcpy(&hi, &h[0], sizeof(float));
-    std::memcpy(&lo, &h[1], sizeof(float));
+    std::memcpy(&hi, &c->hflag[1], sizeof(float));
+    std::memcpy(&lo, &c->hflag[2], sizeof(float));
     *out = hi > kJacobiSpread * kJacobiSpread * lo;
     return TDDA_OK;
 }
@@ -1616,8 +1613,9 @@ tdda_status core_create(const tdda_core_desc* desc, const tdda::PeriodicImages* 
     TDDA_CORE_TRY(dalloc_c(c, &c->part, (size_t)c->max_rhs * tdda::kPartSlots * c->maxblk));
     TDDA_CORE_TRY(dalloc_c(c, &c->cnt, (size_t)c->max_rhs * tdda::kCounters));
     TDDA_CORE_CK(pinned_get((void**)&c->hst, sizeof(SolveState) * c->max_rhs));
-    TDDA_CORE_TRY(dalloc_c(c, &c->flag, 1));
-    TDDA_CORE_CK(pinned_get((void**)&c->hflag, sizeof(unsigned int)));
+    // flag[0]: launch_scan's result; flag[1..2]: the |al|^2 range of TDDA_FP32_AUTO
+    TDDA_CORE_TRY(dalloc_c(c, &c->flag, 3));
+    TDDA_CORE_CK(pinned_get((void**)&c->hflag, 3 * sizeof(unsigned int)));
     TDDA_CORE_CK(cudaMemsetAsync(c->cnt, 0, sizeof(unsigned int) * c->max_rhs * tdda::kCounters, c->stream));
     TDDA_CORE_CK(cudaMemcpyAsync(c->cellmap, cellmap.data(), sizeof(int) * cellmap.size(), cudaMemcpyHostToDevice,
                                  c->stream));
@@ -1677,7 +1675,7 @@ tdda_status tdda_core_destroy(tdda_core* c) {
     free_all(c->allocs, c->stream);
     if (c->stream) cudaStreamSynchronize(c->stream);
     pinned_put(c->hst, sizeof(SolveState) * c->max_rhs);
-    pinned_put(c->hflag, sizeof(unsigned int));
+    pinned_put(c->hflag, 3 * sizeof(unsigned int));
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return TDDA_OK;

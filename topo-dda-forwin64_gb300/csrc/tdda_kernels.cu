@@ -836,8 +836,9 @@ cudaError_t launch_accumulate_scaled(int n3, const float2* d, const float2* pre,
     return cudaGetLastError();
 }
 cudaError_t launch_al_range(int n3, const float2* al, unsigned int* out, cudaStream_t stream) {
-    const unsigned int init[2] = {0u, 0xffffffffu};
-    cudaError_t e = cudaMemcpyAsync(out, init, sizeof(init), cudaMemcpyHostToDevice, stream);
+    // out[0] = 0 (max), out[1] = ~0 (min), without a host buffer
+    cudaError_t e = cudaMemsetAsync(out, 0, sizeof(unsigned int), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(out + 1, 0xff, sizeof(unsigned int), stream);
     if (e != cudaSuccess) return e;
     k_al_range<<<std::min(grid1d(n3, kNT), 152 * 8), kNT, 0, stream>>>(n3, al, out);
     return cudaGetLastError();
