@@ -1182,6 +1182,10 @@ tdda_status shape_create(int device, const int grid[3], int cap, Shape** out) {
     {
         const char* v = std::getenv("TDDA_DEVICE_LOOP");
         c->device_loop = !(v && v[0] == '0');
+        // early launch of the fused FP32 pass kernels (Geom::early; 0: every kernel the ordinary way)
+        const char* el = std::getenv("TDDA_EARLY_LAUNCH");
+        c->g.early = el ? std::atoi(el) : 3;
+        if (cudaDeviceGetAttribute(&c->g.sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess) c->g.sms = 0;
     }
     for (int a = 0; a < 3; a++) TDDA_SHAPE_TRY(dalloc_c(c, &c->tw32[a], (size_t)grid[a]));
     TDDA_SHAPE_TRY(dalloc_c(c, &c->grid32, (size_t)(g.sb * cap)));
@@ -1587,6 +1591,10 @@ tdda_status core_create(const tdda_core_desc* desc, const tdda::PeriodicImages* 
     {
         const char* v = std::getenv("TDDA_DEVICE_LOOP");
         c->device_loop = !(v && v[0] == '0');
+        // early launch of the fused FP32 pass kernels (Geom::early; 0: every kernel the ordinary way)
+        const char* el = std::getenv("TDDA_EARLY_LAUNCH");
+        c->g.early = el ? std::atoi(el) : 3;
+        if (cudaDeviceGetAttribute(&c->g.sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess) c->g.sms = 0;
     }
     const size_t n3 = 3 * (size_t)g.N;
     const long long H6 = 6LL * g.Hx * g.Hy * g.Hz;

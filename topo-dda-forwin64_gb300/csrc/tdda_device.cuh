@@ -470,6 +470,14 @@ __device__ __forceinline__ bool rhs_done(const SolveState* st) {
     return st != nullptr && *((volatile const int*)&st->status) != ST_RUNNING;
 }
 
+// Programmatic dependent launch (launch_early): grid_dep_wait() returns once the
+// previous kernel of the stream has completed and its writes are visible;
+// grid_dep_release() lets the stream's next kernel start launching its blocks
+// (they wait in their own grid_dep_wait).  Both do nothing in a kernel launched
+// the ordinary way.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 template <typename T> __device__ __forceinline__ void stage_tw(cx<T>* stw, const cx<T>* tw, int M) {
     for (int i = threadIdx.x; i < M; i += blockDim.x) stw[i] = tw[i];
 }

@@ -35,7 +35,43 @@ struct Geom {
     int multi;         // 1: a cross-lattice batch -- every right-hand side brings its own
                        // lattice (RhsVecs::Nx ... green); Nx, Ny, Nz, N above are the
                        // largest the grid shape holds (the strides follow them)
+    int early;         // the fused FP32 pass kernels launched early (launch_early): 0 no;
+                       // 1 the next kernel released after the wait; 2 before the last
+                       // stage; 3 per launch: 1 for at most `sms` blocks, else 2
+    int sms;           // streaming multiprocessors of the core's device
 };
+
+// The release point of an early launch of `blocks` blocks.  Released right after
+// its wait, a kernel of more blocks than SMs had the next kernel's blocks stack
+// up on the SMs its own blocks left free first (64x64x16 solve: -6%); released
+// before its last stage, it keeps the ordinary placement.
+inline Geom early_geom(Geom g, long long blocks) {
+    if (g.early == 3) g.early = blocks <= g.sms ? 1 : 2;
+    return g;
+}
+
+// A launch that lets the kernel's blocks start while the previous kernel of the
+// stream is still running (programmatic dependent launch), when `early` is set:
+// the blocks stage their constants (twiddles, the lattice), then wait in
+// grid_dep_wait() for the previous kernel's completion and memory before they
+// touch anything another kernel writes.  Only kernels that call grid_dep_wait
+// on every path that reads or writes such memory may be launched this way.
+// Inside a stream capture the dependency becomes a programmatic graph edge.
+template <typename... P, typename... A>
+cudaError_t launch_early(bool early, void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                         A... args) {
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cfg.attrs = at;
+    cfg.numAttrs = early ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k, args...);
+}
 
 // solver status values (mirrored in include/tdda.h)
 enum : int { ST_RUNNING = 0, ST_CONVERGED = 1, ST_BREAKDOWN = 2, ST_MAXITER = 3, ST_NAN = 4 };

@@ -130,6 +130,7 @@ __global__ void __launch_bounds__(kNT) k_chunk_end(const RhsVecs<float>* __restr
                                                    int prod_nblk, cudaGraphConditionalHandle loop, int in_loop) {
     __shared__ float2 sred[8];
     __shared__ int s_running;
+    grid_dep_wait();  // the partials and states are the previous kernel's
     if (threadIdx.x == 0) s_running = 0;
     for (int b = 0; b < nrhs; b++) {
         const RhsVecs<float> R = rhs[b];
@@ -731,8 +732,9 @@ template <typename T> int sink_blocks(const Geom& g) {
 
 cudaError_t launch_chunk_end(const Geom& g, int nrhs, const RhsVecs<float>* rhs, int slot,
                              cudaGraphConditionalHandle loop, bool in_loop, cudaStream_t stream) {
-    k_chunk_end<<<1, kNT, 0, stream>>>(rhs, nrhs, slot, sink_blocks<float>(g), loop, in_loop ? 1 : 0);
-    return cudaGetLastError();
+    const cudaError_t e = launch_early(g.early != 0, k_chunk_end, dim3(1), dim3(kNT), 0, stream, rhs, nrhs, slot,
+                                       sink_blocks<float>(g), loop, in_loop ? 1 : 0);
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 template <typename T>

@@ -378,6 +378,8 @@ __global__ void __launch_bounds__(ZT * x2_radix(M, 0), MINB) k_xpass2(Geom g, co
     const int zn = min(ZT, Mz - z0);
     stage_tw<T>(stw, twx, M);
     cx<T>* gp = grid + (long long)b * g.sb + (long long)y * g.sy + z0;
+    grid_dep_wait();  // the grid and the solve's state are the previous kernel's
+    if (g.early == 1) grid_dep_release();
 
     // forward stage 1: radix R1 over x = j + R2 r < Nx, grid -> s[j R1 + q][line].
     // Nx <= M / 2, so the inputs r >= R1 / 2 are zero padding: not read, not added.
@@ -451,6 +453,7 @@ __global__ void __launch_bounds__(ZT * x2_radix(M, 0), MINB) k_xpass2(Geom g, co
         for (int q = 0; q < R2; q++) s[(j * R2 + q) * W + SB * j + c * ZT + zl] = X[c][q];  // row j R2 + q
     __syncthreads();
 
+    if (g.early == 2) grid_dep_release();  // the next kernel's blocks start during the last stage
     // inverse stage 2: radix R1, butterfly j < R2, twiddles conj(w^(r j)), outputs x = j + R2 q < Nx
     for (int w = threadIdx.x; w < W * R2; w += NT) {
         const int l = w % W, jj = w / W;
@@ -483,10 +486,11 @@ template <typename T, int M, int ZT, int MINB = 1> struct XLaunch2 {
         sizeof(cx<T>) * (size_t)(M + M * 3 * ZT + 8 * (x2_radix(M, 0) > x2_radix(M, 1) ? x2_radix(M, 0)
                                                                                          : x2_radix(M, 1)));
     static cudaError_t run(const PassArgs<T>& a) {
-        const Geom& g = a.g;
-        const dim3 grid(g.py.M * ((g.pz.M + ZT - 1) / ZT), a.nrhs);
-        k_xpass2<T, M, ZT, MINB><<<grid, NT, smem, a.stream>>>(g, a.rhs, a.green, a.twx, a.grid);
-        return cudaGetLastError();
+        const dim3 grid(a.g.py.M * ((a.g.pz.M + ZT - 1) / ZT), a.nrhs);
+        const Geom g = early_geom(a.g, (long long)grid.x * grid.y);
+        const cudaError_t e =
+            launch_early(g.early, k_xpass2<T, M, ZT, MINB>, grid, dim3(NT), smem, a.stream, g, a.rhs, a.green, a.twx, a.grid);
+        return e != cudaSuccess ? e : cudaGetLastError();
     }
     static cudaError_t configure() {
         return cudaFuncSetAttribute((const void*)k_xpass2<T, M, ZT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -780,9 +784,6 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int b = blockIdx.y;
     const RhsVecs<T> R = rhs[b];
-    if constexpr (!kStep32) {  // the FP32 step reads the status with its scalars
-        if (rhs_done(R.st)) return;
-    }
     const Lat L = lattice_of<T>(g, R, cellmap);
     const int x = blockIdx.x / 3, c = blockIdx.x - 3 * (blockIdx.x / 3);
     if (x >= L.Nx) return;  // past this right-hand side's lattice (cross-lattice batches)
@@ -793,6 +794,11 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
     cx<T>* sB = sA + MY * ZP;  // LY rows
     stage_tw<T>(stwy, twy, MY);
     stage_tw<T>(stwz, twz, MZ);
+    grid_dep_wait();  // the vectors, partials and states are the previous kernels'
+    if (g.early == 1) grid_dep_release();
+    if constexpr (!kStep32) {  // the FP32 step reads the status with its scalars
+        if (rhs_done(R.st)) return;
+    }
 
     cx<T> beta, alpha, zeta;
     if constexpr (!kStep32) {
@@ -881,6 +887,7 @@ __global__ void __launch_bounds__(kNT) k_zyfwd(Geom g, const RhsVecs<T>* __restr
         for (int q = 0; q < B1; q++) sA[(j * B1 + q) * ZP + kz] = v[q];
     }
     __syncthreads();
+    if (g.early == 2) grid_dep_release();  // the next kernel's blocks start during the last stage
     // y stage 2 to the grid plane [y][z]: task (kz, j < B1), rows j + B1 q
     cx<T>* gp = grid + (long long)b * g.sb + c * g.sc + (long long)x * g.sx;
     for (int w = threadIdx.x; w < MZ * B1; w += kNT) {
@@ -919,6 +926,7 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
         // grid shape's blocks take zeros here, which leave them exactly as its own
         // blocks form them
         if (SNK == SNK_OUT || SNK == SNK_ALB) return;
+        grid_dep_wait();
         acc_t<T> zero[NV] = {};
         if constexpr (sizeof(T) == 4 && (SNK == SNK_AP || SNK == SNK_AT_DEF)) {
             publish_partials<NV>(zero, R.part, gridDim.x, blockIdx.x, sred);
@@ -940,6 +948,8 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
     stage_tw<T>(stwy, twy, MY);
     stage_tw<T>(stwz, twz, MZ);
     const cx<T>* gp = grid + (long long)b * g.sb + c * g.sc + (long long)x * g.sx;
+    grid_dep_wait();  // the grid and the solve's state are the previous kernel's
+    if (g.early == 1) grid_dep_release();
 
     // y stage 1 on the grid plane: task (kz < Mz, j < B2) reads rows j + B2 r
     for (int w = threadIdx.x; w < MZ * B2; w += kNT) {
@@ -990,6 +1000,7 @@ __global__ void __launch_bounds__(kNT) k_yzinv(Geom g, const RhsVecs<T>* __restr
         for (int q = 0; q < A1; q++) sA[y * ZP + j * A1 + q] = v[q];
     }
     __syncthreads();
+    if (g.early == 2) grid_dep_release();  // the next kernel's blocks start during the last stage
     // z stage 2: task (y, j < A1), twiddles conj(w^(r j)), outputs z = j + A1 q < LZ
     constexpr int LZ = PL::LZ, QV = (LZ + A1 - 1) / A1;
     for (int w = threadIdx.x; w < LY * A1; w += kNT) {
@@ -1053,26 +1064,27 @@ template <typename T, int MY, int MZ> struct ZyLaunch {
     static cudaError_t run(int pass, int mode, const PassArgs<T>& a) {
         const dim3 grid(3 * a.g.Nx, a.nrhs);
         const size_t sm = ZyPlane<T, MY, MZ>::smem;
-        const Geom& g = a.g;
+        const Geom g = early_geom(a.g, (long long)grid.x * grid.y);
+        cudaError_t e = cudaSuccess;
         if (pass == PASS_ZFWD) {
             switch (mode) {
-                case SRC_IN: k_zyfwd<T, SRC_IN, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid, a.slot, a.prod_nblk); break;
-                case SRC_PUPD: k_zyfwd<T, SRC_PUPD, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid, a.slot, a.prod_nblk); break;
-                case SRC_TUPD: k_zyfwd<T, SRC_TUPD, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid, a.slot, a.prod_nblk); break;
-                case SRC_PUPD_DEF: k_zyfwd<T, SRC_PUPD_DEF, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid, a.slot, a.prod_nblk); break;
-                default: k_zyfwd<T, SRC_P, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid, a.slot, a.prod_nblk); break;
+                case SRC_IN: e = launch_early(g.early, k_zyfwd<T, SRC_IN, MY, MZ>, grid, dim3(kNT), sm, a.stream, g, a.rhs, a.twy, a.twz, a.cellmap, a.grid, a.slot, a.prod_nblk); break;
+                case SRC_PUPD: e = launch_early(g.early, k_zyfwd<T, SRC_PUPD, MY, MZ>, grid, dim3(kNT), sm, a.stream, g, a.rhs, a.twy, a.twz, a.cellmap, a.grid, a.slot, a.prod_nblk); break;
+                case SRC_TUPD: e = launch_early(g.early, k_zyfwd<T, SRC_TUPD, MY, MZ>, grid, dim3(kNT), sm, a.stream, g, a.rhs, a.twy, a.twz, a.cellmap, a.grid, a.slot, a.prod_nblk); break;
+                case SRC_PUPD_DEF: e = launch_early(g.early, k_zyfwd<T, SRC_PUPD_DEF, MY, MZ>, grid, dim3(kNT), sm, a.stream, g, a.rhs, a.twy, a.twz, a.cellmap, a.grid, a.slot, a.prod_nblk); break;
+                default: e = launch_early(g.early, k_zyfwd<T, SRC_P, MY, MZ>, grid, dim3(kNT), sm, a.stream, g, a.rhs, a.twy, a.twz, a.cellmap, a.grid, a.slot, a.prod_nblk); break;
             }
         } else {
             switch (mode) {
-                case SNK_OUT: k_yzinv<T, SRC_IN, SNK_OUT, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
-                case SNK_ALB: k_yzinv<T, SRC_IN, SNK_ALB, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
-                case SNK_AP: k_yzinv<T, SRC_PUPD, SNK_AP, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
-                case SNK_AT: k_yzinv<T, SRC_TUPD, SNK_AT, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
-                case SNK_AT_DEF: k_yzinv<T, SRC_TUPD, SNK_AT_DEF, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
-                default: k_yzinv<T, SRC_P, SNK_RES, MY, MZ><<<grid, kNT, sm, a.stream>>>(g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
+                case SNK_OUT: e = launch_early(g.early, k_yzinv<T, SRC_IN, SNK_OUT, MY, MZ>, grid, dim3(kNT), sm, a.stream, g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
+                case SNK_ALB: e = launch_early(g.early, k_yzinv<T, SRC_IN, SNK_ALB, MY, MZ>, grid, dim3(kNT), sm, a.stream, g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
+                case SNK_AP: e = launch_early(g.early, k_yzinv<T, SRC_PUPD, SNK_AP, MY, MZ>, grid, dim3(kNT), sm, a.stream, g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
+                case SNK_AT: e = launch_early(g.early, k_yzinv<T, SRC_TUPD, SNK_AT, MY, MZ>, grid, dim3(kNT), sm, a.stream, g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
+                case SNK_AT_DEF: e = launch_early(g.early, k_yzinv<T, SRC_TUPD, SNK_AT_DEF, MY, MZ>, grid, dim3(kNT), sm, a.stream, g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
+                default: e = launch_early(g.early, k_yzinv<T, SRC_P, SNK_RES, MY, MZ>, grid, dim3(kNT), sm, a.stream, g, a.rhs, a.twy, a.twz, a.cellmap, a.grid); break;
             }
         }
-        return cudaGetLastError();
+        return e != cudaSuccess ? e : cudaGetLastError();
     }
     static cudaError_t configure() {
         const void* ks[] = {(const void*)k_zyfwd<T, SRC_IN, MY, MZ>, (const void*)k_zyfwd<T, SRC_PUPD, MY, MZ>,
