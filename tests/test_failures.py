@@ -61,6 +61,37 @@ def test_nan_right_hand_side_is_isolated_in_a_batch(precision):
     core.close()
 
 
+@pytest.mark.parametrize("precision", [tdda.FP32_REFINE, tdda.FP32_JACOBI])
+def test_zero_right_hand_side_in_a_mixed_batch(precision):
+    """E = 0 in one right-hand side of a mixed-precision batch started from P = 0: the first
+    inner solve starts before the first residual is read back, so the zero right-hand side
+    must still end as converged with P = 0 and no steps, and the others must equal their solves
+    alone, bit for bit."""
+    w = lattice.config(1)
+    core = tdda.AProductCore(w.Nx, w.Ny, w.Nz, w.R, w.d, w.lam, w.material, max_rhs=3)
+    alone = []
+    for inc in INCS:
+        m = tdda.DDAModel(core, inc.nK, 1.0, inc.nE0, w.diel_old)
+        tdda.solve_batch([m], precision, 10000, 1e-5)
+        alone.append((m.get_P(), m.last_info))
+        m.close()
+    ms = [tdda.DDAModel(core, inc.nK, 1.0, inc.nE0, w.diel_old) for inc in INCS]
+    ms[1].change_E(np.zeros(3 * core.N, np.complex128))
+    infos = tdda.solve_batch(ms, precision, 10000, 1e-5)
+    assert infos[1]["status"] == tdda.OK, infos[1]
+    assert infos[1]["inner_iterations"] == 0 and infos[1]["outer_iterations"] == 0
+    assert infos[1]["error"] == 0.0
+    assert not np.any(ms[1].get_P())
+    for k in (0, 2):
+        P, ia = alone[k]
+        assert infos[k]["status"] == tdda.OK
+        assert infos[k]["inner_iterations"] == ia["inner_iterations"]
+        assert np.array_equal(ms[k].get_P(), P)
+    for m in ms:
+        m.close()
+    core.close()
+
+
 @pytest.mark.parametrize("precision", [tdda.FP64, tdda.FP32_REFINE])
 def test_server_fails_the_nan_request_and_completes_the_others(precision):
     rng = np.random.Generator(np.random.PCG64(9))

@@ -200,6 +200,7 @@ struct tdda_core_s {
     SolveState* st64 = nullptr;        // device, max_rhs
     SolveState* st32 = nullptr;
     SolveState* hst = nullptr;         // pinned host, max_rhs
+    SolveState* hst_first = nullptr;   // pinned host, max_rhs: the first residual's states (solve_mixed)
     unsigned int* flag = nullptr;      // device: result of launch_scan
     unsigned int* hflag = nullptr;     // pinned host copy of it
     double* part = nullptr;
@@ -810,13 +811,22 @@ tdda_status solve_mixed(tdda_model* const* ms, int n, int max_it, double tol, td
     }
     TDDA_CK(cudaMemcpyAsync(c->rhs64, h64.data(), sizeof(RhsVecs<double>) * n, cudaMemcpyHostToDevice, c->stream));
     TDDA_CK(cudaMemcpyAsync(c->rhs32, h32.data(), sizeof(RhsVecs<float>) * n, cudaMemcpyHostToDevice, c->stream));
+    // With every P zero the first residual is E itself, |r| / |E| = 1 exactly for a finite,
+    // nonzero E, so the first inner solve starts without the host reading that residual back
+    // (one host round trip less).  The first residual's states land in hst_first and are
+    // checked with the inner solve's: a right-hand side whose E is zero or not finite ends
+    // as the check would have ended it, and its inner result is dropped.
+    const bool ahead = all_p_zero && max_it > 0 && tol < 1.0;
+    if (ahead && !c->hst_first) TDDA_CK(pinned_get((void**)&c->hst_first, sizeof(SolveState) * c->max_rhs));
     for (int outer_it = 0; outer_it <= kMaxOuter; outer_it++) {
+        const bool first_ahead = ahead && outer_it == 0;
+        SolveState* hs = first_ahead ? c->hst_first : c->hst;
         // FP64 residual r = E - (A P + al P) of the right-hand sides still open
         for (int i = 0; i < n; i++) {
-            c->hst[i] = fresh_state(tol, 0, 0);
-            if (done[i]) c->hst[i].status = tdda::ST_CONVERGED;
+            hs[i] = fresh_state(tol, 0, 0);
+            if (done[i]) hs[i].status = tdda::ST_CONVERGED;
         }
-        TDDA_CK(cudaMemcpyAsync(c->st64, c->hst, sizeof(SolveState) * n, cudaMemcpyHostToDevice, c->stream));
+        TDDA_CK(cudaMemcpyAsync(c->st64, hs, sizeof(SolveState) * n, cudaMemcpyHostToDevice, c->stream));
         if (outer_it == 0 && all_p_zero) {
             // P = 0: the residual is E exactly (A 0 = 0), no product needed
             TDDA_CK1(tdda::launch_residual_is_rhs<double>(c->g, n, c->rhs64, c->stream));
@@ -824,10 +834,15 @@ tdda_status solve_mixed(tdda_model* const* ms, int n, int max_it, double tol, td
             TDDA_CK1(tdda::launch_solve_begin<double>(c->g, n, c->rhs64, c->stream));
             TDDA_TRY(residual_product(c, n));
         }
-        TDDA_CK(cudaMemcpyAsync(c->hst, c->st64, sizeof(SolveState) * n, cudaMemcpyDeviceToHost, c->stream));
-        TDDA_CK(cudaStreamSynchronize(c->stream));
+        TDDA_CK(cudaMemcpyAsync(hs, c->st64, sizeof(SolveState) * n, cudaMemcpyDeviceToHost, c->stream));
         bool open = false;
-        for (int i = 0; i < n; i++) {
+        if (first_ahead) {
+            for (int i = 0; i < n; i++) res[i] = prev_res[i] = 1.0;
+            open = true;
+        } else {
+            TDDA_CK(cudaStreamSynchronize(c->stream));
+        }
+        for (int i = 0; i < n && !first_ahead; i++) {
             if (done[i]) continue;
             const SolveState& s = c->hst[i];
             if (s.status == tdda::ST_NAN) {
@@ -871,7 +886,24 @@ tdda_status solve_mixed(tdda_model* const* ms, int n, int max_it, double tol, td
         // the device-side loop reads its limit from the first state: the largest of the batch
         for (int i = 1; i < n; i++) c->hst[0].chunk_limit = std::max(c->hst[0].chunk_limit, c->hst[i].chunk_limit);
         TDDA_CK(cudaMemcpyAsync(c->st32, c->hst, sizeof(SolveState) * n, cudaMemcpyHostToDevice, c->stream));
-        TDDA_TRY(krylov<float>(c, n, true, max_it));
+        TDDA_TRY(krylov<float>(c, n, true, max_it));  // ends with the stream synchronised
+        for (int i = 0; i < n && first_ahead; i++) {
+            // the first residual's check, as above for r = E
+            const SolveState& s = c->hst_first[i];
+            Enorm[i] = s.Enorm;
+            if (s.status == tdda::ST_NAN) {
+                done[i] = 1;
+                stat[i] = TDDA_ERR_NAN;
+            } else if (!std::isfinite(s.Enorm)) {
+                done[i] = 1;
+                stat[i] = TDDA_ERR_NAN;
+                res[i] = s.Enorm;
+            } else if (!(s.Enorm > 0)) {
+                done[i] = 1;
+                stat[i] = TDDA_OK;
+                res[i] = 0.0;
+            }
+        }
         for (int i = 0; i < n; i++) {
             if (done[i]) continue;
             const SolveState& s = c->hst[i];
@@ -1683,6 +1715,7 @@ tdda_status tdda_core_destroy(tdda_core* c) {
     free_all(c->allocs, c->stream);
     if (c->stream) cudaStreamSynchronize(c->stream);
     pinned_put(c->hst, sizeof(SolveState) * c->max_rhs);
+    if (c->hst_first) pinned_put(c->hst_first, sizeof(SolveState) * c->max_rhs);
     pinned_put(c->hflag, 3 * sizeof(unsigned int));
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;

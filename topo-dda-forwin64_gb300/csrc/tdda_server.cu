@@ -87,6 +87,22 @@ struct IdleShape {
     double last_used;
 };
 
+// An evicted operator (its core and pooled models) or shape, destroyed outside
+// the server's lock
+struct Evicted {
+    tdda_core* core = nullptr;
+    std::vector<tdda_model*> models;
+    tdda_session::Shape* shape = nullptr;
+};
+
+// Idle operators and shapes kept resident beyond what the budget forces out.
+// Hundreds of cores alive at once (their allocations, streams and pinned state)
+// slowed every later request of the process by about a third, also after they
+// were destroyed, while a stream of requests rarely returns to an operator
+// long after its last use.
+constexpr int kMaxIdleOperators = 32;
+constexpr int kMaxIdleShapes = 16;
+
 }  // namespace
 
 struct tdda_server_s {
@@ -104,6 +120,9 @@ struct tdda_server_s {
     bool stop = false;
     std::vector<std::thread> workers;
     tdda_server_counters counters{};
+    // evicted operators and shapes not yet destroyed: a core's teardown waits for
+    // graph operations of other streams, so workers destroy them after leaving mu
+    std::vector<Evicted> graveyard;
 
     double now() const {
         return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -144,20 +163,68 @@ struct tdda_server_s {
             for (size_t i = 0; i < idle_shapes.size(); i++)
                 if (idle_shapes[i].last_used < t) t = idle_shapes[i].last_used, best = (int)i, kind = 1;
             if (best < 0) return false;
-            if (kind == 0) {
-                Operator* o = ops[best].get();
-                for (tdda_model* m : o->pool) tdda_model_destroy(m);
-                tdda_core_destroy(o->core);
-                bytes -= o->bytes();
-                counters.operators_evicted++;
-                ops.erase(ops.begin() + best);
-            } else {
-                tdda_session::shape_destroy(idle_shapes[best].s);
-                bytes -= idle_shapes[best].bytes;
-                idle_shapes.erase(idle_shapes.begin() + best);
-            }
+            if (kind == 0) evict_operator(best);
+            else evict_shape(best);
         }
         return true;
+    }
+
+    // move an idle operator or shape to the graveyard (mu held); its bytes are
+    // counted free now, and the worker that evicted it destroys it (drain) before
+    // it allocates anything
+    void evict_operator(int i) {
+        Operator* o = ops[i].get();
+        Evicted e;
+        e.core = o->core;
+        e.models = std::move(o->pool);
+        graveyard.push_back(std::move(e));
+        bytes -= o->bytes();
+        counters.operators_evicted++;
+        ops.erase(ops.begin() + i);
+    }
+    void evict_shape(int i) {
+        Evicted e;
+        e.shape = idle_shapes[i].s;
+        graveyard.push_back(std::move(e));
+        bytes -= idle_shapes[i].bytes;
+        idle_shapes.erase(idle_shapes.begin() + i);
+    }
+
+    // keep at most kMaxIdleOperators idle operators and kMaxIdleShapes idle
+    // shapes, least recently used out first (mu held)
+    void trim_idle() {
+        for (;;) {
+            int idle = 0, best = -1;
+            double t = 1e300;
+            for (size_t i = 0; i < ops.size(); i++) {
+                const Operator* o = ops[i].get();
+                if (o->owner >= 0 || o->active > 0 || !o->core) continue;
+                idle++;
+                if (o->last_used < t) t = o->last_used, best = (int)i;
+            }
+            if (idle <= kMaxIdleOperators) break;
+            evict_operator(best);
+        }
+        while ((int)idle_shapes.size() > kMaxIdleShapes) {
+            int best = 0;
+            for (size_t i = 1; i < idle_shapes.size(); i++)
+                if (idle_shapes[i].last_used < idle_shapes[best].last_used) best = (int)i;
+            evict_shape(best);
+        }
+    }
+
+    // destroy what was evicted (outside mu)
+    void drain() {
+        std::vector<Evicted> g;
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            g.swap(graveyard);
+        }
+        for (Evicted& e : g) {
+            for (tdda_model* m : e.models) tdda_model_destroy(m);
+            if (e.core) tdda_core_destroy(e.core);
+            if (e.shape) tdda_session::shape_destroy(e.shape);
+        }
     }
 
     // reserve the operator entry and the memory of request r for worker `me`
@@ -393,6 +460,7 @@ void tdda_server_s::run_fp64(int me) {
                 cv.wait(lk);
             }
         }
+        drain();
         std::vector<tdda_model*> models;
         std::vector<std::pair<Request*, int>> owner;
         tdda_status st = TDDA_OK;
@@ -433,7 +501,9 @@ void tdda_server_s::run_fp64(int me) {
             Operator* op = g[0]->op;
             for (Request* r : g) finish_request(r, t);
             if (op && op->active == 0) op->owner = -1;
+            trim_idle();
         }
+        drain();
         cv.notify_all();
     }
 }
@@ -468,6 +538,7 @@ void tdda_server_s::run_fp32(int me) {
                 counters.shapes_built++;
             }
         }
+        drain();
         tdda_status st = TDDA_OK;
         if (!sh) st = tdda_session::shape_create(desc.device, grid, desc.max_group, &sh);
         // request of each slot's model, and its right-hand side index
@@ -533,6 +604,7 @@ void tdda_server_s::run_fp32(int me) {
                     }
                 }
             }
+            drain();
             const int before = tdda_session::shape_active(sh);
             for (Request* r : joined) {
                 r->info.group = before + r->d.nrhs;
@@ -601,12 +673,16 @@ void tdda_server_s::run_fp32(int me) {
             if (st == TDDA_OK) {
                 idle_shapes.push_back(IdleShape{{grid[0], grid[1], grid[2]}, sh, sh_bytes, now()});
             } else {
-                tdda_session::shape_destroy(sh);
+                Evicted e;
+                e.shape = sh;
+                graveyard.push_back(std::move(e));
                 bytes -= sh_bytes;
             }
             for (auto& o : ops)
                 if (o->owner == me && o->active == 0) o->owner = -1;
+            trim_idle();
         }
+        drain();
         cv.notify_all();
     }
 }
@@ -698,6 +774,7 @@ tdda_status tdda_server_destroy(tdda_server* s) {
     }
     s->cv.notify_all();
     for (auto& t : s->workers) t.join();
+    s->drain();
     for (auto& is : s->idle_shapes) tdda_session::shape_destroy(is.s);
     for (auto& o : s->ops) {
         for (tdda_model* m : o->pool) tdda_model_destroy(m);
