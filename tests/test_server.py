@@ -132,6 +132,25 @@ def test_operators_stay_resident(precision):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("precision", [tdda.FP64, tdda.FP32_JACOBI])
+def test_idle_operators_are_capped(precision):
+    """A stream of 44 operators that never return: at most 32 idle operators stay resident
+    (hundreds of idle cores alive at once slowed every later request of the process), the
+    rest are evicted least recently used first, and every request still completes."""
+    if tdda.device_count() < 1:
+        pytest.skip("no CUDA device")
+    s = tdda.Server(hbm_budget_bytes=150e9, workers=2, precision=precision, max_group=4)
+    ids = [_req(s, 6, lam=450.0 + 5.0 * k, seed=k) for k in range(44)]
+    infos = [s.result(i, with_P=False)[0] for i in ids]
+    c = s.counters()
+    s.close()
+    assert all(i["state"] == tdda.REQ_DONE for i in infos)
+    assert c["operators_built"] == 44
+    assert c["resident_operators"] <= 32
+    assert c["operators_evicted"] >= 12
+
+
+@pytest.mark.gpu
 def test_requests_join_running_work_across_lattices():
     """FP32+refine continuous batching: one worker, a session of 4 slots.  A slow request
     (a 14^3 lattice at a high contrast) is running when requests of other lattices of the

@@ -101,7 +101,7 @@ struct Evicted {
 // were destroyed, while a stream of requests rarely returns to an operator
 // long after its last use.
 constexpr int kMaxIdleOperators = 32;
-constexpr int kMaxIdleShapes = 16;
+constexpr int kMaxIdleShapes = 48;
 
 }  // namespace
 
