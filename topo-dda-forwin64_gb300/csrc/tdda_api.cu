@@ -1879,9 +1879,11 @@ tdda_status tdda_model_update_alpha(tdda_model* m, const double* diel_old) {
         set_err("density %g of entry %zu is outside the material table", diel_old[bad], bad);
         return TDDA_ERR_INVALID_ARGUMENT;
     }
+    // no wait for the alpha kernel: the caller's densities were read before the scan's
+    // synchronisation, and everything that reads al runs on the core's stream or waits
+    // for it (the cross-lattice sessions synchronise a model's stream at admission)
     TDDA_CK1(tdda::launch_model_alpha((int)n3, m->dold, alpha_params(m), m->diel, m->al, m->fal, c->stream));
     m->dold_host_stale = true;  // the device holds the densities; the host copy follows on demand
-    TDDA_CK(cudaStreamSynchronize(c->stream));
     return TDDA_OK;
 }
 
